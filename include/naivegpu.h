@@ -1,0 +1,268 @@
+/*
+ * naivegpu.h -- C ABI of libnaivegpu, the GB300 (sm_103a) implementation of the
+ * NaiveDynamics.jl per-step hot path:
+ *
+ *   LBVH neighbour search   (src/Neighbors/BVHTraverse.jl)
+ *   LJ + Coulomb forces     (src/Forces.jl)
+ *   velocity-Verlet update  (src/Simulator.jl)
+ *
+ * It replaces the package-extension backends ext/NaiveKA.jl and ext/NaiveCUDA.jl
+ * behind the extension seam of src/PkgExtensions.jl.  Every entry point cites
+ * the reference function it replaces.
+ *
+ * Conventions
+ *   - Every function returns an nd_status (0 = ND_OK) and never throws or aborts.
+ *   - Plain pointers are HOST pointers unless the function name ends in _dev,
+ *     in which case they are device pointers on the context's device and the
+ *     work is enqueued on the context's stream.
+ *   - Atom indices written to pair lists are 1-based ORIGINAL indices and tree
+ *     node indices (left, skip) are 1-based with 0 as the sentinel, exactly as in
+ *     the reference (Julia) data structures.
+ *   - Positions for neighbour search are Float32, x y z interleaved (N x 3), the
+ *     memory layout of Vector{MVector{3,Float32}} (src/MDInput.jl:29).
+ *   - One context = one device = one stream; a context is not thread-safe.
+ */
+#ifndef NAIVEGPU_H
+#define NAIVEGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t nd_status;
+
+#define ND_OK              0
+#define ND_NEED_REALLOC    1  /* output buffer too small; the needed count is returned */
+#define ND_ERR_ARG        -1  /* bad argument (NULL pointer, negative size, ...)       */
+#define ND_ERR_SPEC       -2  /* SpheresBVHSpecs checks (BVHTraverse.jl:74-80)           */
+#define ND_ERR_NONFINITE  -3  /* NaN/Inf coordinate: InexactError of round(Int32, ...) */
+#define ND_ERR_RANGE      -4  /* p/binwidth outside Int32 (BVHTraverse.jl:266)         */
+#define ND_ERR_CUDA       -5  /* CUDA runtime error; nd_last_error() has the message    */
+#define ND_ERR_NOMEM      -6  /* device allocation failed                               */
+#define ND_ERR_INTERNAL   -7  /* device-side consistency check failed (error flag)      */
+#define ND_ERR_OVERFLOW   -8  /* neighbour list capacity exceeded during a run          */
+#define ND_ERR_NODEVICE   -9  /* no CUDA device / device index out of range             */
+
+/* Atom ordering before the tree build. */
+#define ND_ORDER_REFERENCE 0  /* mortoncodes! bit-select code, bit-exact with the reference */
+#define ND_ORDER_SPATIAL   1  /* interleaved 10-bit/axis Morton code over the bounding box  */
+
+/* Leaf boxes. */
+#define ND_BOX_LEAF 0  /* leafcluster_primitives: p -/+ r/2 (BVHTraverse.jl:376-410) */
+#define ND_BOX_ATOM 1  /* cluster_primitives:     p -/+ r   (BVHTraverse.jl:341-375) */
+
+/* Pair-list emission order. */
+#define ND_PAIRS_ORDERED   0  /* exactly the reference's single-thread emission order */
+#define ND_PAIRS_UNORDERED 1  /* same multiset, order decided at run time (one pass)  */
+
+typedef struct nd_ctx nd_ctx;
+typedef struct nd_md nd_md;
+
+/* SpheresBVHSpecs{Float32,Int32} (BVHTraverse.jl:63-69). */
+typedef struct {
+    float neighbor_distance;
+    int32_t atom_count;
+    int32_t leaves_count;
+    int32_t branches_count;
+    int32_t atomsperleaf;
+} nd_bvh_spec;
+
+/* GridKey{Float32,Int32} (BVHTraverse.jl:102-109), 32 bytes. */
+typedef struct {
+    float min[3];
+    float max[3];
+    int32_t left;
+    int32_t skip;
+} nd_gridkey;
+
+/* Force model and integrator parameters: the keywords the reference hard-codes
+ * (Forces.jl:17-19,57) plus SimSpec.stepwidth (Simulator.jl:30-49) and the
+ * GenericRandomCollector walls minDim/maxDim (MDInput.jl:67-84). */
+typedef struct {
+    double sigma;
+    double epsilon;
+    double coulomb_k;      /* 0 disables Coulomb */
+    double cutoff;         /* force cutoff r_c */
+    double skin;           /* neighbour list radius = cutoff + skin */
+    double dt;             /* stepwidth */
+    double box_lo[3];      /* reflecting walls (boundary_reflect!, Simulator.jl:81-111) */
+    double box_hi[3];
+    int32_t atomsperleaf;  /* leaf size of the tree used for the neighbour list */
+    int32_t rebuild_every; /* steps between neighbour-list rebuilds */
+    int32_t order;         /* ND_ORDER_* used for the rebuilds */
+    int32_t max_neighbors; /* per-atom list capacity, 0 = sized from the first build */
+} nd_md_params;
+
+/* ----------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device`; allocates its stream and error word. */
+nd_status nd_ctx_create(nd_ctx** out, int32_t device);
+nd_status nd_ctx_destroy(nd_ctx* ctx);
+/* Human-readable text of the last failure on this context (never NULL). */
+const char* nd_last_error(const nd_ctx* ctx);
+const char* nd_status_string(nd_status st);
+/* The context's cudaStream_t, for callers that enqueue their own work. */
+void* nd_ctx_stream(nd_ctx* ctx);
+nd_status nd_ctx_synchronize(nd_ctx* ctx);
+/* Number of kernels this library has launched on the context (diagnostics). */
+int64_t nd_ctx_launch_count(const nd_ctx* ctx);
+
+/* ------------------------------------------------------------ neighbour search */
+
+/* SpheresBVHSpecs(; neighbor_distance, atom_count, floattype=Float32, atomsperleaf)
+ * (BVHTraverse.jl:71-94): ND_ERR_SPEC unless apl divides N and N/apl >= 2. */
+nd_status nd_bvh_spec_init(nd_bvh_spec* out, float neighbor_distance, int32_t atom_count,
+                           int32_t atomsperleaf);
+
+/* mortoncodes! (BVHTraverse.jl:237-288) on the device: codes[i] for positions
+ * xyz (N x 3 Float32).  order selects the reference code or the spatial code. */
+nd_status nd_morton_codes_dev(nd_ctx* ctx, const float* xyz, int32_t n, int32_t order,
+                              int32_t* codes);
+
+/* Stable ascending sortperm (BVHTraverse.jl:570-573) of non-negative 30-bit
+ * codes on the device: codes are sorted in place and perm (0-based) returned. */
+nd_status nd_sortperm_dev(nd_ctx* ctx, int32_t* codes, int32_t n, int32_t* perm);
+
+/*
+ * leafTreeData(position, spec) (BVHTraverse.jl:544-597) when boxes == ND_BOX_LEAF,
+ * TreeData(position, spec) (BVHTraverse.jl:500-543) when boxes == ND_BOX_ATOM.
+ * Outputs (each may be NULL): keys (nkeys entries; N-1 for ND_BOX_LEAF, 2nL-1
+ * for ND_BOX_ATOM -- extra entries are zero), the sorted APointPrimitive fields
+ * index (1-based), morton_code and position (N x 3), and perm (1-based
+ * sortperm, the `mortsort` of the reference).  The root box is overwritten with
+ * [0,1]^3 as bounding_volume_hierarchy! does (BVHTraverse.jl:856-858).
+ * ND_BOX_LEAF with atomsperleaf == 1 returns ND_ERR_SPEC (the reference indexes
+ * past its N-1 key array there).
+ */
+nd_status nd_tree(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, int32_t order,
+                  int32_t boxes, nd_gridkey* keys, int64_t nkeys, int32_t* index,
+                  int32_t* morton_code, float* position, int32_t* perm);
+
+/*
+ * leafbuild_traverse_bvh(position, spec) (BVHTraverse.jl:1423-1428) =
+ * leafTreeData + leafneighbor_traverse (:1236-1323); also the pair list of
+ * gpubvh_neighborlist (ext/NaiveKA.jl:470-558).  Writes the half pair list
+ * (i, j, d) -- every unordered pair with d^2 < r^2 once -- into pi/pj/pd.
+ * *count receives the number of pairs; if it exceeds capacity nothing is written
+ * and ND_NEED_REALLOC is returned (call again with capacity >= *count, or with
+ * capacity 0 to only count).  mode: ND_PAIRS_ORDERED / ND_PAIRS_UNORDERED.
+ */
+nd_status nd_leaf_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, int32_t order,
+                        int32_t mode, int32_t* pi, int32_t* pj, float* pd, int64_t capacity,
+                        int64_t* count);
+
+/* Same, device pointers, enqueued on the context stream; *count is a host
+ * pointer and the call synchronises once to read it. */
+nd_status nd_leaf_pairs_dev(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec,
+                            int32_t order, int32_t mode, int32_t* pi, int32_t* pj, float* pd,
+                            int64_t capacity, int64_t* count);
+
+/*
+ * build_traverse_bvh(position, spec) (BVHTraverse.jl:1416-1421) = TreeData +
+ * neighbor_traverse (:1125-1183), the per-atom traversal (and the per-atom
+ * kernel gpuneighbor_traverse!, ext/NaiveKA.jl:352-453).  The reference's
+ * neighbor_traverse indexes APointPrimitive values that define no getindex at
+ * HEAD; this is the traversal it describes: queries 1..N-1 in sorted order
+ * start at their own leaf, strict point-in-box tests against +/- r leaf boxes,
+ * emit subjects later in sorted order with d^2 < r^2.  Same buffer protocol as
+ * nd_leaf_pairs.
+ */
+nd_status nd_atom_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, int32_t order,
+                        int32_t* pi, int32_t* pj, float* pd, int64_t capacity, int64_t* count);
+
+/* Order-free 128-bit hash of canonical (min(i,j), max(i,j), bits(d)) triples of
+ * a device pair list (for verifying lists too large to copy to the host). */
+nd_status nd_pair_hash_dev(nd_ctx* ctx, const int32_t* pi, const int32_t* pj, const float* pd,
+                           int64_t npairs, uint64_t hash[2]);
+
+/* ------------------------------------------------------------------ forces */
+
+/*
+ * force_lennardjones!(force, pairslist, position) (Forces.jl:15-45) +
+ * force_coulomb!(force, pairslist, charge) (Forces.jl:56-66) + sum_forces!
+ * (Forces.jl:68-75), fused, with the intended physics: for every listed pair
+ * (1-based i, j) with r < cutoff,
+ *   F_ij = [24 eps/r^2 (2 (sigma/r)^12 - (sigma/r)^6) + k q_i q_j / r^3] r_ij,
+ *   F_i += F_ij, F_j -= F_ij,  U += 4 eps((sigma/r)^12 - (sigma/r)^6) + k q_i q_j / r.
+ * x: N x 3 FP64 positions, q: N charges (NULL = no Coulomb), force: N x 3 FP32
+ * out (zeroed first), energy: FP64 out (NULL to skip).  The distances in the
+ * list are not used; directions need positions.
+ */
+nd_status nd_forces_pairs(nd_ctx* ctx, const nd_md_params* p, int32_t n, const double* x,
+                          const double* q, const int32_t* pi, const int32_t* pj, int64_t npairs,
+                          float* force, double* energy);
+
+/*
+ * Forces and energy of a configuration with the library's own neighbour search
+ * (spatial-order leaf BVH at radius p->cutoff): the fused hot-path force kernel
+ * run once.  Same physics and outputs as nd_forces_pairs.
+ */
+nd_status nd_forces(nd_ctx* ctx, const nd_md_params* p, int32_t n, const double* x,
+                    const double* q, float* force, double* energy);
+
+/* ---------------------------------------------------------------- dynamics */
+
+/*
+ * Device-resident simulation (the GPU form of simulate!, Simulator.jl:154-256,
+ * with kick-drift-kick velocity Verlet):
+ *   v += dt/2 F/m;  x += dt v;  boundary_reflect!;  [rebuild every R steps];
+ *   F = F(x);  v += dt/2 F/m.
+ * x, v: N x 3 FP64 host arrays; q (charges) and m (masses) may be NULL (q = 0
+ * disables Coulomb, m = 1).  The state is copied to the device once.
+ */
+nd_status nd_md_create(nd_ctx* ctx, const nd_md_params* p, int32_t n, const double* x,
+                       const double* v, const double* q, const double* m, nd_md** out);
+/* Same, from device arrays (x, v: N x 3 FP64; q, m: N FP64 or NULL). */
+nd_status nd_md_create_dev(nd_ctx* ctx, const nd_md_params* p, int32_t n, const double* x,
+                           const double* v, const double* q, const double* m, nd_md** out);
+nd_status nd_md_destroy(nd_md* md);
+/* Advance `steps` steps; enqueued on the context stream (captured CUDA graphs of
+ * one rebuild window).  Does not synchronise. */
+nd_status nd_md_run(nd_md* md, int64_t steps);
+/* Synchronise and check the device error word (overflow, non-finite, ...). */
+nd_status nd_md_sync(nd_md* md);
+/* Copy the state back in the caller's original atom order (each may be NULL):
+ * x, v (N x 3 FP64), f (N x 3 FP32 forces at the current positions). */
+nd_status nd_md_get(nd_md* md, double* x, double* v, float* f);
+/* Same into device buffers. */
+nd_status nd_md_get_dev(nd_md* md, double* x, double* v, float* f);
+/* Potential and kinetic energy (FP64 reductions) at the current step. */
+nd_status nd_md_energy(nd_md* md, double* potential, double* kinetic);
+/* Steps taken, rebuilds done, pairs in the current list, list capacity. */
+nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* list_pairs,
+                      int32_t* capacity);
+/* Number of kernel launches one nd_md_run(steps) enqueues (for diagnostics). */
+int64_t nd_md_launches_per_run(nd_md* md, int64_t steps);
+
+/*
+ * simulate!(sys, spec, clct) (Simulator.jl:154-256) with host arrays in and out:
+ * x, v (N x 3 FP64) are advanced `steps` steps in place and f (N x 3 FP32,
+ * may be NULL) receives the forces at the final positions.
+ */
+nd_status nd_simulate(nd_ctx* ctx, const nd_md_params* p, int32_t n, double* x, double* v,
+                      float* f, const double* q, const double* m, int64_t steps);
+
+/* ------------------------------------------------------------ synthetic inputs */
+
+/* Seeded host-side generators for benchmark and test inputs (splitmix64). */
+/* Uniform Float32 positions in [lo, lo + side)^3. */
+nd_status nd_synth_uniform(uint64_t seed, int32_t n, double lo, double side, float* xyz);
+/* Uniform positions in [0, side)^3 with no two atoms closer than dmin (random
+ * sequential addition; MDInput.jl's GenericRandomCollector.minimumdistance). */
+nd_status nd_synth_uniform_mindist(uint64_t seed, int32_t n, double side, double dmin,
+                                   double* xyz);
+/* nclusters isotropic Gaussian clusters of n/nclusters points, centres uniform in
+ * [0, side)^3, per-cluster sigma uniform in [smin, smax]. */
+nd_status nd_synth_clusters(uint64_t seed, int32_t n, int32_t nclusters, double side,
+                            double smin, double smax, float* xyz);
+/* N(0, s^2) per component. */
+nd_status nd_synth_normal(uint64_t seed, int64_t count, double s, double* out);
+/* +/-1 charges, exactly half each, random assignment (n even). */
+nd_status nd_synth_charges(uint64_t seed, int32_t n, double* q);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

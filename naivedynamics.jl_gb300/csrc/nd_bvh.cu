@@ -1,0 +1,932 @@
+// nd_bvh.cu -- LBVH neighbour search for sm_103a.
+//
+// Reference: src/Neighbors/BVHTraverse.jl (NaiveDynamics.jl).  The pipeline is
+//   Morton codes (mortoncodes!, :237-288)  -> stable radix sort (sortperm, :570)
+//   -> gather + leaf boxes (leafcluster_primitives :376-410 / cluster_primitives :341-375)
+//   -> Apetrei bottom-up build with CAS (bvh_interior!, :704-846)
+//   -> stackless rope traversal (leafneighbor_traverse :1236-1323,
+//      neighbor_traverse :1125-1183) with pair emission.
+// Everything that decides which pairs exist is computed with the reference's
+// exact single-precision operation order (no FMA contraction, IEEE division and
+// square root) so that codes, order, tree and pair list are bit-identical.
+#include <algorithm>
+#include <cstring>
+#include <utility>
+
+#include "nd_internal.cuh"
+
+namespace nd {
+
+// =================================================================== Morton
+
+// mortoncodes! with K = Int32 (BVHTraverse.jl:259-284).
+__global__ void k_morton_reference(const float* __restrict__ xyz, int32_t n, float binwidth,
+                                   int32_t* __restrict__ codes, int32_t* __restrict__ iota,
+                                   int32_t* err) {
+    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t magic[3] = {153391689, 306783378, 613566756};
+    int32_t code = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float p = xyz[3 * (int64_t)i + d];
+        if (!isfinite(p)) { set_error(err, ND_ERR_NONFINITE, i); code = 0; break; }
+        float q = floorf(__fdiv_rn(p, binwidth));
+        // trunc(Int32, ::Float32) accepts -2^31 <= q < 2^31 (Julia Base float.jl)
+        if (!(q >= -2147483648.0f && q < 2147483648.0f)) { set_error(err, ND_ERR_RANGE, i); code = 0; break; }
+        int32_t qi = (int32_t)q;
+        int32_t yin = qi & magic[d];
+        int32_t yang = qi | ~magic[d];
+        code |= (yin & yang);
+    }
+    codes[i] = code;
+    if (iota) iota[i] = i;
+}
+
+// Bounding box of the positions (order-preserving uint atomics), used by the
+// spatial code.  bbox[0..2] = min keys, bbox[3..5] = max keys.
+__global__ void k_bbox(const float* __restrict__ xyz, int32_t n, uint32_t* bbox, int32_t* err) {
+    uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
+    uint32_t mx[3] = {0u, 0u, 0u};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float p = xyz[3 * i + d];
+            if (!isfinite(p)) { set_error(err, ND_ERR_NONFINITE, (int32_t)i); continue; }
+            uint32_t o = f2o(p);
+            mn[d] = min(mn[d], o);
+            mx[d] = max(mx[d], o);
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        for (int s = 16; s > 0; s >>= 1) {
+            mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], s));
+            mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], s));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            atomicMin(&bbox[d], mn[d]);
+            atomicMax(&bbox[3 + d], mx[d]);
+        }
+    }
+}
+
+__global__ void k_bbox_init(uint32_t* bbox) {
+    if (threadIdx.x < 6) bbox[threadIdx.x] = threadIdx.x < 3 ? 0xffffffffu : 0u;
+}
+
+// Interleaved Morton code over the bounding box, 1024 bins per axis.
+__global__ void k_morton_spatial(const float* __restrict__ xyz, int32_t n,
+                                 const uint32_t* __restrict__ bbox, int32_t* __restrict__ codes,
+                                 int32_t* __restrict__ iota) {
+    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t q[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float lo = o2f(bbox[d]), hi = o2f(bbox[3 + d]);
+        float ext = __fsub_rn(hi, lo);
+        float s = ext > 0.0f ? __fdiv_rn(1024.0f, ext) : 0.0f;
+        float t = floorf(__fmul_rn(__fsub_rn(xyz[3 * (int64_t)i + d], lo), s));
+        int32_t qi = (t < 0.0f) ? 0 : (t > 1023.0f ? 1023 : (int32_t)t);
+        q[d] = (uint32_t)qi;
+    }
+    codes[i] = (int32_t)(spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2));
+    if (iota) iota[i] = i;
+}
+
+nd_status morton_codes(Ctx* c, const float* xyz, int32_t n, int32_t order, int32_t* codes,
+                       int32_t* iota) {
+    if (n <= 0) return ND_OK;
+    const int T = 256;
+    if (order == ND_ORDER_SPATIAL) {
+        nd_status st = ensure(c, c->misc, 64);
+        if (st) return st;
+        k_bbox_init<<<1, 32, 0, c->stream>>>((uint32_t*)c->misc.p);
+        c->launches++;
+        int blocks = (int)std::min<int64_t>(cdiv(n, T), 152 * 8);
+        k_bbox<<<blocks, T, 0, c->stream>>>(xyz, n, (uint32_t*)c->misc.p, c->d_err);
+        c->launches++;
+        k_morton_spatial<<<(int)cdiv(n, T), T, 0, c->stream>>>(xyz, n, (const uint32_t*)c->misc.p,
+                                                              codes, iota);
+        c->launches++;
+    } else {
+        const float binwidth = (float)(1.0 / 1023.0);  // Float32(1/1023), BVHTraverse.jl:184
+        k_morton_reference<<<(int)cdiv(n, T), T, 0, c->stream>>>(xyz, n, binwidth, codes, iota,
+                                                                c->d_err);
+        c->launches++;
+    }
+    return check_launch(c, "morton");
+}
+
+// ================================================================ radix sort
+// Stable LSD radix sort, 8-bit digits, reduce-then-scan (no inter-CTA waiting):
+//   upsweep: per-tile digit histograms, digit-major;
+//   scan:    per-digit exclusive scan over tiles + digit totals;
+//   scatter: stable in-tile ranks (warp match + per-warp prefix) -> global slot.
+
+constexpr int RS_BINS = 256;
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+static_assert(RS_THREADS == RS_BINS, "scatter maps one thread per digit");
+
+__global__ void __launch_bounds__(RS_THREADS)
+    k_rs_upsweep(const uint32_t* __restrict__ keys, int32_t n, int shift,
+                 uint32_t* __restrict__ hist, int32_t ntiles) {
+    __shared__ uint32_t sh[RS_BINS];
+    sh[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; ++k) {
+        int64_t idx = base + k * RS_THREADS + threadIdx.x;
+        bool valid = idx < n;
+        uint32_t dg = valid ? ((keys[idx] >> shift) & 0xffu) : 0x100u;
+        unsigned peers = __match_any_sync(0xffffffffu, dg);
+        if (valid && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&sh[dg], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = sh[threadIdx.x];
+}
+
+__device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_warp,
+                                                        uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, s);
+        if (lane >= s) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, s);
+            if (lane >= s) w += y;
+        }
+        if (lane < (int)(blockDim.x >> 5)) s_warp[lane] = w;  // inclusive warp prefix
+    }
+    __syncthreads();
+    uint32_t wp = warp ? s_warp[warp - 1] : 0u;
+    if (total) *total = s_warp[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return wp + x - v;
+}
+
+// One CTA per digit: exclusive scan of that digit's per-tile counts.
+__global__ void __launch_bounds__(RS_THREADS)
+    k_rs_scan(uint32_t* __restrict__ hist, int32_t ntiles, uint32_t* __restrict__ totals) {
+    __shared__ uint32_t s_warp[32];
+    uint32_t* h = hist + (int64_t)blockIdx.x * ntiles;
+    uint32_t carry = 0;
+    for (int32_t b = 0; b < ntiles; b += RS_THREADS) {
+        int32_t i = b + threadIdx.x;
+        uint32_t v = i < ntiles ? h[i] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_excl_scan_256(v, s_warp, &tot);
+        if (i < ntiles) h[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(RS_THREADS)
+    k_rs_scatter(const uint32_t* __restrict__ kin, const int32_t* __restrict__ vin,
+                 uint32_t* __restrict__ kout, int32_t* __restrict__ vout, int32_t n, int shift,
+                 const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals,
+                 int32_t ntiles) {
+    constexpr int W = RS_THREADS / 32;
+    __shared__ uint32_t s_base[RS_BINS];
+    __shared__ uint32_t s_run[RS_BINS];
+    __shared__ uint32_t s_wh[W][RS_BINS];
+    __shared__ uint32_t s_warp[32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t ex = block_excl_scan_256(totals[t], s_warp, nullptr);
+    s_base[t] = ex + hist[(int64_t)t * ntiles + blockIdx.x];
+    s_run[t] = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    for (int k = 0; k < RS_ITEMS; ++k) {
+#pragma unroll
+        for (int w = 0; w < W; ++w) s_wh[w][t] = 0;
+        __syncthreads();
+        int64_t idx = base + k * RS_THREADS + t;
+        bool valid = idx < n;
+        uint32_t key = valid ? kin[idx] : 0u;
+        int32_t val = valid ? vin[idx] : 0;
+        uint32_t dg = valid ? ((key >> shift) & 0xffu) : 0x100u;
+        unsigned peers = __match_any_sync(0xffffffffu, dg);
+        int rank = __popc(peers & lt);
+        if (valid && lane == __ffs(peers) - 1) s_wh[warp][dg] = (uint32_t)__popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = s_run[t];
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                uint32_t cnt = s_wh[w][t];
+                s_wh[w][t] = run;
+                run += cnt;
+            }
+            s_run[t] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = s_base[dg] + s_wh[warp][dg] + (uint32_t)rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+nd_status radix_sort_pairs(Ctx* c, uint32_t* keys, int32_t* vals, int32_t n, int bits) {
+    if (n <= 1) return ND_OK;
+    int32_t ntiles = (int32_t)cdiv(n, RS_TILE);
+    nd_status st;
+    if ((st = ensure(c, c->codes_alt, sizeof(uint32_t) * (size_t)n))) return st;
+    if ((st = ensure(c, c->perm_alt, sizeof(int32_t) * (size_t)n))) return st;
+    if ((st = ensure(c, c->hist, sizeof(uint32_t) * ((size_t)RS_BINS * ntiles + RS_BINS))))
+        return st;
+    uint32_t* hist = (uint32_t*)c->hist.p;
+    uint32_t* totals = hist + (size_t)RS_BINS * ntiles;
+    uint32_t* ka = keys;
+    int32_t* va = vals;
+    uint32_t* kb = (uint32_t*)c->codes_alt.p;
+    int32_t* vb = (int32_t*)c->perm_alt.p;
+    int passes = (bits + 7) / 8;
+    for (int p = 0; p < passes; ++p) {
+        int shift = 8 * p;
+        k_rs_upsweep<<<ntiles, RS_THREADS, 0, c->stream>>>(ka, n, shift, hist, ntiles);
+        k_rs_scan<<<RS_BINS, RS_THREADS, 0, c->stream>>>(hist, ntiles, totals);
+        k_rs_scatter<<<ntiles, RS_THREADS, 0, c->stream>>>(ka, va, kb, vb, n, shift, hist, totals,
+                                                          ntiles);
+        c->launches += 3;
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    if (ka != keys) {
+        cudaMemcpyAsync(keys, ka, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(vals, va, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream);
+    }
+    return check_launch(c, "radix sort");
+}
+
+// ============================================================== leaf boxes
+
+// Gather sorted positions and build leaf boxes: leafcluster_primitives
+// (BVHTraverse.jl:376-410, h = r/2) or cluster_primitives (:341-375, h = r).
+// pos4.w carries the 1-based original index (bit pattern).
+__global__ void k_leaf_boxes(const float* __restrict__ xyz, const int32_t* __restrict__ perm,
+                             int32_t nL, int32_t apl, float h, float4* __restrict__ pos4,
+                             int32_t* __restrict__ idx, float4* __restrict__ keys) {
+    int32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= nL) return;
+    int64_t bird = (int64_t)leaf * apl;
+    float mn[3], mx[3];
+    for (int32_t a = 0; a < apl; ++a) {
+        int32_t o = perm[bird + a];
+        float p[3] = {xyz[3 * (int64_t)o], xyz[3 * (int64_t)o + 1], xyz[3 * (int64_t)o + 2]};
+        pos4[bird + a] = make_float4(p[0], p[1], p[2], __int_as_float(o + 1));
+        idx[bird + a] = o + 1;
+        if (a == 0) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) { mn[d] = __fsub_rn(p[d], h); mx[d] = __fadd_rn(p[d], h); }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = jl_min(mn[d], __fsub_rn(p[d], h));
+            mx[d] = jl_max(mx[d], __fadd_rn(p[d], h));
+        }
+    }
+    keys[2 * (int64_t)leaf] = make_float4(mn[0], mn[1], mn[2], mx[0]);
+    keys[2 * (int64_t)leaf + 1] = make_float4(mx[1], mx[2], __int_as_float(0), __int_as_float(0));
+}
+
+// ==================================================================== build
+
+// exptdelta (BVHTraverse.jl:677-696), 1-based leaf index, Int32 wrap-around.
+__device__ __forceinline__ int32_t delta_ref(int32_t i, const int32_t* __restrict__ code,
+                                             int32_t nL, int32_t apl) {
+    if (i >= nL || i < 1) return INT32_MAX;
+    int32_t a = __ldg(&code[(int64_t)(i - 1) * apl]);
+    int32_t b = __ldg(&code[(int64_t)i * apl]);
+    uint32_t x = (uint32_t)(a ^ b);
+    uint32_t add = (x == 0u) ? (0x80000000u + (uint32_t)(i ^ (i + 1))) : 0u;
+    return (int32_t)(x + add - 1u);
+}
+
+__device__ __forceinline__ void load_box_cg(const float4* keys, int32_t node /*1-based*/,
+                                            float mn[3], float mx[3]) {
+    float4 a = __ldcg(&keys[2 * (int64_t)(node - 1)]);
+    float4 b = __ldcg(&keys[2 * (int64_t)(node - 1) + 1]);
+    mn[0] = a.x; mn[1] = a.y; mn[2] = a.z;
+    mx[0] = a.w; mx[1] = b.x; mx[2] = b.y;
+}
+
+// bvh_interior! (BVHTraverse.jl:704-846), one thread per leaf.  The second
+// thread to reach an internal node (the CAS on store[split] returns non-zero)
+// merges the sibling box and continues upward.  __threadfence() before the CAS
+// publishes this thread's node writes; the fence after a successful read of a
+// non-zero slot orders the sibling-box loads, which bypass L1 (ld.cg).  No
+// thread ever waits on another, so the kernel cannot hang; a climb longer than
+// nL levels flags ND_ERR_INTERNAL.
+__global__ void k_bvh_build(float4* keys, int32_t* store, const int32_t* __restrict__ code,
+                            int32_t nL, int32_t apl, int32_t* err) {
+    int32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i > nL) return;
+    int32_t rangel = i, ranger = i;
+    int32_t dell = delta_ref(rangel - 1, code, nL, apl);
+    int32_t delr = delta_ref(ranger, code, nL, apl);
+    float bmin[3], bmax[3];
+    load_box_cg(keys, i, bmin, bmax);
+    int32_t lskip;
+    if (i == nL) {
+        lskip = 0;
+    } else {
+        int32_t ir = i + 1;
+        lskip = (delr < delta_ref(ir, code, nL, apl)) ? ir : nL + ir;
+    }
+    reinterpret_cast<int32_t*>(&keys[2 * (int64_t)(i - 1) + 1])[3] = lskip;
+
+    for (int32_t guard = 0; guard <= nL + 1; ++guard) {
+        int32_t leftChild;
+        int32_t sib;
+        if (delr < dell) {
+            leftChild = i;
+            int32_t split = ranger;
+            __threadfence();
+            ranger = atomicCAS(&store[split - 1], 0, rangel);
+            if (ranger == 0) return;
+            __threadfence();
+            delr = delta_ref(ranger, code, nL, apl);
+            sib = split + 1;
+            if (sib != ranger) sib = nL + sib;
+        } else {
+            int32_t split = rangel - 1;
+            __threadfence();
+            rangel = atomicCAS(&store[split - 1], 0, ranger);
+            if (rangel == 0) return;
+            __threadfence();
+            dell = delta_ref(rangel - 1, code, nL, apl);
+            leftChild = split;
+            if (leftChild != rangel) leftChild = nL + leftChild;
+            sib = leftChild;
+        }
+        float smin[3], smax[3];
+        load_box_cg(keys, sib, smin, smax);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            bmax[d] = jl_max(smax[d], bmax[d]);
+            bmin[d] = jl_min(smin[d], bmin[d]);
+        }
+        int32_t q = (delr < dell) ? ranger : rangel;
+        int32_t parent = nL + q;
+        int32_t skip;
+        if (ranger == nL) {
+            skip = 0;
+        } else {
+            int32_t r = ranger + 1;
+            skip = (delr < delta_ref(r, code, nL, apl)) ? r : nL + r;
+        }
+        __stcg(&keys[2 * (int64_t)(parent - 1)], make_float4(bmin[0], bmin[1], bmin[2], bmax[0]));
+        __stcg(&keys[2 * (int64_t)(parent - 1) + 1],
+               make_float4(bmax[1], bmax[2], __int_as_float(leftChild), __int_as_float(skip)));
+        i = parent;
+        if (i == nL + 1) return;
+    }
+    set_error(err, ND_ERR_INTERNAL, i);
+}
+
+__global__ void k_root_overwrite(float4* keys, int32_t nL) {
+    // bounding_volume_hierarchy! (BVHTraverse.jl:856-858) forces the root box to [0,1]^3.
+    float4 b = keys[2 * (int64_t)nL + 1];
+    keys[2 * (int64_t)nL] = make_float4(0.f, 0.f, 0.f, 1.f);
+    keys[2 * (int64_t)nL + 1] = make_float4(1.f, 1.f, b.z, b.w);
+}
+
+nd_status build_internal_nodes(Ctx* c, float4* keys, int32_t* store, const int32_t* codes,
+                               int32_t nL, int32_t apl) {
+    cudaError_t e = cudaMemsetAsync(store, 0, sizeof(int32_t) * (size_t)(nL - 1), c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "store reset");
+    k_bvh_build<<<(int)cdiv(nL, 256), 256, 0, c->stream>>>(keys, store, codes, nL, apl, c->d_err);
+    c->launches++;
+    return check_launch(c, "bvh build");
+}
+
+nd_status build_tree(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t apl,
+                     int32_t order, int32_t boxes, int64_t nkeys, bool overwrite_root,
+                     TreeBuffers* out) {
+    int32_t nL = n / apl;
+    nd_status st;
+    if ((st = ensure(c, c->codes, sizeof(int32_t) * (size_t)n))) return st;
+    if ((st = ensure(c, c->perm, sizeof(int32_t) * (size_t)n))) return st;
+    if ((st = ensure(c, c->pos4, sizeof(float4) * (size_t)n))) return st;
+    if ((st = ensure(c, c->idx, sizeof(int32_t) * (size_t)n))) return st;
+    if ((st = ensure(c, c->keys, 32 * (size_t)nkeys))) return st;
+    if ((st = ensure(c, c->store, sizeof(int32_t) * (size_t)std::max(nL - 1, 1)))) return st;
+    int32_t* codes = (int32_t*)c->codes.p;
+    int32_t* perm = (int32_t*)c->perm.p;
+    if ((st = morton_codes(c, xyz_dev, n, order, codes, perm))) return st;
+    if ((st = radix_sort_pairs(c, (uint32_t*)codes, perm, n, 30))) return st;
+    float4* keys = (float4*)c->keys.p;
+    cudaError_t e = cudaMemsetAsync(keys, 0, 32 * (size_t)nkeys, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "keys reset");
+    float h = (boxes == ND_BOX_LEAF) ? r / 2.0f : r;
+    k_leaf_boxes<<<(int)cdiv(nL, 128), 128, 0, c->stream>>>(xyz_dev, perm, nL, apl, h,
+                                                           (float4*)c->pos4.p,
+                                                           (int32_t*)c->idx.p, keys);
+    c->launches++;
+    if ((st = check_launch(c, "leaf boxes"))) return st;
+    if ((st = build_internal_nodes(c, keys, (int32_t*)c->store.p, codes, nL, apl))) return st;
+    if (overwrite_root) {
+        k_root_overwrite<<<1, 1, 0, c->stream>>>(keys, nL);
+        c->launches++;
+    }
+    out->n = n;
+    out->nL = nL;
+    out->apl = apl;
+    out->codes = codes;
+    out->perm = perm;
+    out->pos4 = (const float4*)c->pos4.p;
+    out->idx = (const int32_t*)c->idx.p;
+    out->keys = keys;
+    out->nkeys = nkeys;
+    return check_launch(c, "tree");
+}
+
+// ==================================================================== scan
+
+constexpr int SC_THREADS = 1024;
+constexpr int SC_ITEMS = 4;
+constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
+
+__global__ void __launch_bounds__(SC_THREADS)
+    k_scan_tile(const int64_t* __restrict__ in, int64_t* __restrict__ out, int64_t n,
+                int64_t* __restrict__ partial) {
+    __shared__ int64_t s_warp[32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int64_t base = (int64_t)blockIdx.x * SC_TILE + (int64_t)t * SC_ITEMS;
+    int64_t v[SC_ITEMS];
+    int64_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < SC_ITEMS; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        sum += v[k];
+    }
+    int64_t x = sum;
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1) {
+        int64_t y = __shfl_up_sync(0xffffffffu, x, s);
+        if (lane >= s) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int64_t w = s_warp[lane];
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            int64_t y = __shfl_up_sync(0xffffffffu, w, s);
+            if (lane >= s) w += y;
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    int64_t run = (warp ? s_warp[warp - 1] : 0) + x - sum;
+#pragma unroll
+    for (int k = 0; k < SC_ITEMS; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (t == SC_THREADS - 1 && partial) partial[blockIdx.x] = s_warp[31];
+}
+
+__global__ void k_scan_add(int64_t* __restrict__ out, int64_t n, const int64_t* __restrict__ add) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += add[i / SC_TILE];
+}
+
+__global__ void k_scan_total(const int64_t* in, const int64_t* out, int64_t n, int64_t* total) {
+    *total = n > 0 ? in[n - 1] + out[n - 1] : 0;
+}
+
+static nd_status scan_rec(Ctx* c, const int64_t* in, int64_t* out, int64_t n, int64_t* scratch,
+                          size_t scratch_elems) {
+    int64_t nb = cdiv(n, SC_TILE);
+    if (nb <= 1) {
+        k_scan_tile<<<1, SC_THREADS, 0, c->stream>>>(in, out, n, nullptr);
+        c->launches++;
+        return check_launch(c, "scan");
+    }
+    if ((size_t)(2 * nb) > scratch_elems) return ND_ERR_INTERNAL;
+    int64_t* part = scratch;
+    int64_t* part_scan = scratch + nb;
+    k_scan_tile<<<(unsigned)nb, SC_THREADS, 0, c->stream>>>(in, out, n, part);
+    c->launches++;
+    nd_status st = scan_rec(c, part, part_scan, nb, scratch + 2 * nb, scratch_elems - 2 * nb);
+    if (st) return st;
+    k_scan_add<<<(unsigned)cdiv(n, 256), 256, 0, c->stream>>>(out, n, part_scan);
+    c->launches++;
+    return check_launch(c, "scan add");
+}
+
+nd_status scan_exclusive(Ctx* c, const int64_t* in, int64_t* out, int64_t n, int64_t* total_dev) {
+    if (n <= 0) {
+        cudaMemsetAsync(total_dev, 0, sizeof(int64_t), c->stream);
+        return ND_OK;
+    }
+    size_t need = 4 * (size_t)cdiv(n, SC_TILE) + 64;
+    nd_status st = ensure(c, c->partial, sizeof(int64_t) * need);
+    if (st) return st;
+    st = scan_rec(c, in, out, n, (int64_t*)c->partial.p, need);
+    if (st) return st;
+    k_scan_total<<<1, 1, 0, c->stream>>>(in, out, n, total_dev);
+    c->launches++;
+    return check_launch(c, "scan total");
+}
+
+// =============================================================== traversal
+
+struct Node {
+    float mnx, mny, mnz, mxx, mxy, mxz;
+    int32_t left, skip;
+};
+
+__device__ __forceinline__ Node load_node(const float4* __restrict__ keys, int32_t k /*1-based*/) {
+    float4 a = __ldg(&keys[2 * (int64_t)(k - 1)]);
+    float4 b = __ldg(&keys[2 * (int64_t)(k - 1) + 1]);
+    Node nd_;
+    nd_.mnx = a.x; nd_.mny = a.y; nd_.mnz = a.z; nd_.mxx = a.w; nd_.mxy = b.x; nd_.mxz = b.y;
+    nd_.left = __float_as_int(b.z);
+    nd_.skip = __float_as_int(b.w);
+    return nd_;
+}
+
+// aabb_overlap_test (BVHTraverse.jl:1094-1098), strict on all three axes.
+__device__ __forceinline__ bool overlap(const Node& a, const Node& b) {
+    return (a.mnx < b.mxx) & (a.mxx > b.mnx) & (a.mny < b.mxy) & (a.mxy > b.mny) &
+           (a.mnz < b.mxz) & (a.mxz > b.mnz);
+}
+
+// Emission sinks.  COUNT counts; WRITE writes at a running cursor; ATOMIC
+// reserves chunks of a global cursor (warp-aggregated) as pairs appear.
+struct SinkCount {
+    int64_t n = 0;
+    __device__ __forceinline__ void push(int32_t, int32_t, float) { ++n; }
+};
+struct SinkWrite {
+    int32_t* pi; int32_t* pj; float* pd;
+    int64_t cur;
+    __device__ __forceinline__ void push(int32_t i, int32_t j, float d) {
+        pi[cur] = i; pj[cur] = j; pd[cur] = d; ++cur;
+    }
+};
+
+// Test query atoms qa[0..na) against target atoms tb[0..nb): every (a, b) with
+// d^2 < r^2 in the reference's order (a outer, b inner), or, when `tri`, the
+// intra-leaf pairs a < b (onecluster_proximitytest!, BVHTraverse.jl:1021-1040).
+template <class Sink>
+__device__ __forceinline__ void leaf_pairs_generic(const float4* __restrict__ pos, int64_t A,
+                                                   int64_t B, int32_t apl, float r2, bool tri,
+                                                   Sink& s) {
+    for (int32_t i = 0; i < apl; ++i) {
+        float4 a = __ldg(&pos[A + i]);
+        for (int32_t j = tri ? i + 1 : 0; j < apl; ++j) {
+            float4 b = __ldg(&pos[B + j]);
+            float d2 = dist2_ref(a.x, a.y, a.z, b.x, b.y, b.z);
+            if (d2 < r2) s.push(__float_as_int(a.w), __float_as_int(b.w), __fsqrt_rn(d2));
+        }
+    }
+}
+
+template <int APL, class Sink>
+__device__ __forceinline__ void leaf_pairs_fixed(const float4 (&qa)[APL],
+                                                 const float4* __restrict__ pos, int64_t B,
+                                                 float r2, Sink& s) {
+    float4 tb[APL];
+#pragma unroll
+    for (int j = 0; j < APL; ++j) tb[j] = __ldg(&pos[B + j]);
+#pragma unroll
+    for (int i = 0; i < APL; ++i)
+#pragma unroll
+        for (int j = 0; j < APL; ++j) {
+            float d2 = dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z);
+            if (d2 < r2) s.push(__float_as_int(qa[i].w), __float_as_int(tb[j].w), __fsqrt_rn(d2));
+        }
+}
+
+// leafneighbor_traverse (BVHTraverse.jl:1236-1323) for one query leaf q (1-based).
+template <int APL, class Sink>
+__device__ __forceinline__ void leaf_query(int32_t q, const float4* __restrict__ keys,
+                                           const float4* __restrict__ pos, int32_t apl, float r2,
+                                           Sink& s) {
+    Node ql = load_node(keys, q);
+    int64_t A = (int64_t)(q - 1) * apl;
+    if constexpr (APL > 0) {
+        float4 qa[APL];
+#pragma unroll
+        for (int i = 0; i < APL; ++i) qa[i] = __ldg(&pos[A + i]);
+#pragma unroll
+        for (int i = 0; i < APL - 1; ++i)
+#pragma unroll
+            for (int j = i + 1; j < APL; ++j) {
+                float d2 = dist2_ref(qa[i].x, qa[i].y, qa[i].z, qa[j].x, qa[j].y, qa[j].z);
+                if (d2 < r2) s.push(__float_as_int(qa[i].w), __float_as_int(qa[j].w), __fsqrt_rn(d2));
+            }
+        int32_t t = ql.skip;
+        while (t != 0) {
+            Node nd_ = load_node(keys, t);
+            if (overlap(ql, nd_)) {
+                if (nd_.left == 0) {
+                    leaf_pairs_fixed<APL>(qa, pos, (int64_t)(t - 1) * APL, r2, s);
+                    t = nd_.skip;
+                } else {
+                    t = nd_.left;
+                }
+            } else {
+                t = nd_.skip;
+            }
+        }
+    } else {
+        leaf_pairs_generic(pos, A, A, apl, r2, true, s);
+        int32_t t = ql.skip;
+        while (t != 0) {
+            Node nd_ = load_node(keys, t);
+            if (overlap(ql, nd_)) {
+                if (nd_.left == 0) {
+                    leaf_pairs_generic(pos, A, (int64_t)(t - 1) * apl, apl, r2, false, s);
+                    t = nd_.skip;
+                } else {
+                    t = nd_.left;
+                }
+            } else {
+                t = nd_.skip;
+            }
+        }
+    }
+}
+
+// neighbor_traverse (BVHTraverse.jl:1143-1181) for one query atom qi (1-based, sorted).
+template <class Sink>
+__device__ __forceinline__ void atom_query(int32_t qi, const float4* __restrict__ keys,
+                                           const float4* __restrict__ pos, int32_t apl, float r2,
+                                           Sink& s) {
+    float4 p = __ldg(&pos[qi - 1]);
+    int32_t t = (qi + apl - 1) / apl;
+    while (t != 0) {
+        Node nd_ = load_node(keys, t);
+        bool in = (nd_.mnx < p.x) & (p.x < nd_.mxx) & (nd_.mny < p.y) & (p.y < nd_.mxy) &
+                  (nd_.mnz < p.z) & (p.z < nd_.mxz);
+        if (in) {
+            if (nd_.left == 0) {
+                int32_t low = (t - 1) * apl + 1;
+                for (int32_t e = 1; e <= apl; ++e) {
+                    int32_t sidx = low + e - 1;
+                    if (qi < e + low) {
+                        float4 b = __ldg(&pos[sidx - 1]);
+                        if (__float_as_int(p.w) != __float_as_int(b.w)) {
+                            float d2 = dist2_ref(p.x, p.y, p.z, b.x, b.y, b.z);
+                            if (d2 < r2) s.push(__float_as_int(p.w), __float_as_int(b.w), __fsqrt_rn(d2));
+                        }
+                    }
+                }
+                t = nd_.skip;
+            } else {
+                t = nd_.left;
+            }
+        } else {
+            t = nd_.skip;
+        }
+    }
+}
+
+template <int APL>
+__global__ void __launch_bounds__(128)
+    k_leaf_count(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
+                 int32_t apl, float r2, int64_t* __restrict__ counts) {
+    int32_t q = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (q > nL) return;
+    SinkCount s;
+    leaf_query<APL>(q, keys, pos, apl, r2, s);
+    counts[q - 1] = s.n;
+}
+
+template <int APL>
+__global__ void __launch_bounds__(128)
+    k_leaf_write(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
+                 int32_t apl, float r2, const int64_t* __restrict__ offsets, int32_t* pi,
+                 int32_t* pj, float* pd) {
+    int32_t q = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (q > nL) return;
+    SinkWrite s{pi, pj, pd, offsets[q - 1]};
+    leaf_query<APL>(q, keys, pos, apl, r2, s);
+}
+
+// One-pass emission: pairs of one leaf-vs-leaf test are staged in registers
+// and a warp-aggregated atomicAdd reserves their slots.
+struct SinkStage {
+    int32_t i[16], j[16];
+    float d[16];
+    int n = 0;
+    __device__ __forceinline__ void push(int32_t a, int32_t b, float dd) {
+        i[n] = a; j[n] = b; d[n] = dd; ++n;
+    }
+};
+
+__device__ __forceinline__ void flush_stage(SinkStage& s, unsigned long long* cursor,
+                                            int64_t cap, int32_t* pi, int32_t* pj, float* pd) {
+    // Counts are <= 16, so the exclusive prefix over the active lanes is the sum
+    // of five ballot bit-planes; valid for any set of converged lanes.
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const unsigned below = m & ((1u << lane) - 1u);
+    const unsigned cnt = (unsigned)s.n;
+    unsigned pre = 0, total = 0;
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+        unsigned plane = __ballot_sync(m, (cnt >> b) & 1u);
+        pre += (unsigned)__popc(plane & below) << b;
+        total += (unsigned)__popc(plane) << b;
+    }
+    const int leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader && total) base = atomicAdd(cursor, (unsigned long long)total);
+    base = __shfl_sync(m, base, leader);
+    unsigned long long w = base + pre;
+    for (int k = 0; k < s.n; ++k, ++w) {
+        if ((int64_t)w < cap) { pi[w] = s.i[k]; pj[w] = s.j[k]; pd[w] = s.d[k]; }
+    }
+    s.n = 0;
+}
+
+__global__ void __launch_bounds__(128)
+    k_leaf_unordered4(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
+                      float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
+                      float* pd) {
+    int32_t q = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (q > nL) return;
+    constexpr int APL = 4;
+    Node ql = load_node(keys, q);
+    int64_t A = (int64_t)(q - 1) * APL;
+    float4 qa[APL];
+#pragma unroll
+    for (int i = 0; i < APL; ++i) qa[i] = __ldg(&pos[A + i]);
+    SinkStage s;
+#pragma unroll
+    for (int i = 0; i < APL - 1; ++i)
+#pragma unroll
+        for (int j = i + 1; j < APL; ++j) {
+            float d2 = dist2_ref(qa[i].x, qa[i].y, qa[i].z, qa[j].x, qa[j].y, qa[j].z);
+            if (d2 < r2) s.push(__float_as_int(qa[i].w), __float_as_int(qa[j].w), __fsqrt_rn(d2));
+        }
+    flush_stage(s, cursor, cap, pi, pj, pd);
+    int32_t t = ql.skip;
+    while (t != 0) {
+        Node nd_ = load_node(keys, t);
+        if (overlap(ql, nd_)) {
+            if (nd_.left == 0) {
+                leaf_pairs_fixed<APL>(qa, pos, (int64_t)(t - 1) * APL, r2, s);
+                flush_stage(s, cursor, cap, pi, pj, pd);
+                t = nd_.skip;
+            } else {
+                t = nd_.left;
+            }
+        } else {
+            t = nd_.skip;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128)
+    k_atom_count(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t n,
+                 int32_t apl, float r2, int64_t* __restrict__ counts) {
+    int32_t qi = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (qi > n) return;
+    SinkCount s;
+    if (qi <= n - 1) atom_query(qi, keys, pos, apl, r2, s);
+    counts[qi - 1] = s.n;
+}
+
+__global__ void __launch_bounds__(128)
+    k_atom_write(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t n,
+                 int32_t apl, float r2, const int64_t* __restrict__ offsets, int32_t* pi,
+                 int32_t* pj, float* pd) {
+    int32_t qi = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (qi > n - 1) return;
+    SinkWrite s{pi, pj, pd, offsets[qi - 1]};
+    atom_query(qi, keys, pos, apl, r2, s);
+}
+
+nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int32_t* pj,
+                         float* pd, int64_t capacity, int64_t* total) {
+    const float r2 = r * r;  // (neighbor_distance)^2 in Float32
+    if (t.apl != 4) return ND_ERR_ARG;
+    nd_status st;
+    if ((st = ensure(c, c->misc, 64))) return st;
+    unsigned long long* cursor = (unsigned long long*)c->misc.p;
+    cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
+    k_leaf_unordered4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
+        t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd);
+    c->launches++;
+    if ((st = check_launch(c, "leaf pairs (unordered)"))) return st;
+    unsigned long long tot = 0;
+    cudaError_t e = cudaMemcpyAsync(&tot, cursor, sizeof(tot), cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "pair count");
+    if ((st = sync_and_check(c, "leaf pairs (unordered)"))) return st;
+    *total = (int64_t)tot;
+    return ND_OK;
+}
+
+nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int64_t* total) {
+    const float r2 = r * r;
+    nd_status st;
+    int64_t nq = (kind == 0) ? t.nL : t.n;
+    if ((st = ensure(c, c->counts, sizeof(int64_t) * (size_t)(nq + 1)))) return st;
+    if ((st = ensure(c, c->offsets, sizeof(int64_t) * (size_t)(nq + 2)))) return st;
+    int64_t* counts = (int64_t*)c->counts.p;
+    int64_t* offsets = (int64_t*)c->offsets.p;
+    unsigned grid = (unsigned)cdiv(nq, 128);
+    if (kind == 0) {
+        if (t.apl == 4)
+            k_leaf_count<4><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, counts);
+        else
+            k_leaf_count<0><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, counts);
+    } else {
+        k_atom_count<<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.n, t.apl, r2, counts);
+    }
+    c->launches++;
+    if ((st = check_launch(c, "pair count"))) return st;
+    if ((st = scan_exclusive(c, counts, offsets, nq, offsets + nq))) return st;
+    int64_t tot = 0;
+    cudaError_t e = cudaMemcpyAsync(&tot, offsets + nq, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                    c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "pair total");
+    if ((st = sync_and_check(c, "pair count"))) return st;
+    *total = tot;
+    return ND_OK;
+}
+
+nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int32_t* pi, int32_t* pj,
+                      float* pd) {
+    const float r2 = r * r;
+    int64_t nq = (kind == 0) ? t.nL : t.n;
+    const int64_t* offsets = (const int64_t*)c->offsets.p;
+    unsigned grid = (unsigned)cdiv(nq, 128);
+    if (kind == 0) {
+        if (t.apl == 4)
+            k_leaf_write<4><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, offsets,
+                                                        pi, pj, pd);
+        else
+            k_leaf_write<0><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, offsets,
+                                                        pi, pj, pd);
+    } else {
+        k_atom_write<<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.n, t.apl, r2, offsets, pi, pj,
+                                                  pd);
+    }
+    c->launches++;
+    return check_launch(c, "pair write");
+}
+
+// ================================================================ pair hash
+
+__global__ void k_pair_hash(const int32_t* __restrict__ pi, const int32_t* __restrict__ pj,
+                            const float* __restrict__ pd, int64_t np,
+                            unsigned long long* out) {
+    uint64_t h0 = 0, h1 = 0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < np;
+         k += (int64_t)gridDim.x * blockDim.x)
+        pair_hash_one(pi[k], pj[k], pd[k], h0, h1);
+    for (int s = 16; s > 0; s >>= 1) {
+        h0 += __shfl_xor_sync(0xffffffffu, h0, s);
+        h1 += __shfl_xor_sync(0xffffffffu, h1, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out[0], (unsigned long long)h0);
+        atomicAdd(&out[1], (unsigned long long)h1);
+    }
+}
+
+nd_status pair_hash(Ctx* c, const int32_t* pi, const int32_t* pj, const float* pd, int64_t np,
+                    uint64_t out[2]) {
+    nd_status st = ensure(c, c->hash, 16);
+    if (st) return st;
+    cudaMemsetAsync(c->hash.p, 0, 16, c->stream);
+    if (np > 0) {
+        int blocks = (int)std::min<int64_t>(cdiv(np, 256), 152 * 16);
+        k_pair_hash<<<blocks, 256, 0, c->stream>>>(pi, pj, pd, np, (unsigned long long*)c->hash.p);
+        c->launches++;
+    }
+    cudaError_t e = cudaMemcpyAsync(out, c->hash.p, 16, cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "hash copy");
+    return sync_and_check(c, "pair hash");
+}
+
+}  // namespace nd

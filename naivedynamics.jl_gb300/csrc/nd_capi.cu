@@ -1,0 +1,610 @@
+// nd_capi.cu -- the extern "C" boundary of libnaivegpu (declared in
+// include/naivegpu.h): contexts, buffer management, status codes, the
+// reference-shaped entry points and the seeded synthetic-input generators.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "nd_internal.cuh"
+
+struct nd_ctx {
+    nd::Ctx c;
+};
+
+struct nd_md {
+    nd_ctx* ctx;
+    nd::MDEngine* e;
+};
+
+namespace nd {
+
+nd_status cuda_fail(Ctx* c, cudaError_t e, const char* what) {
+    c->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();  // clear a sticky-free error so later calls can proceed
+    return e == cudaErrorMemoryAllocation ? ND_ERR_NOMEM : ND_ERR_CUDA;
+}
+
+nd_status check_launch(Ctx* c, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, what);
+    return ND_OK;
+}
+
+nd_status ensure(Ctx* c, DevBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.p && b.bytes >= bytes) return ND_OK;
+    if (b.p) {
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        char msg[128];
+        snprintf(msg, sizeof(msg), "cudaMalloc of %zu bytes", bytes);
+        c->last_error = std::string(msg) + ": " + cudaGetErrorString(e);
+        return ND_ERR_NOMEM;
+    }
+    b.bytes = bytes;
+    return ND_OK;
+}
+
+static const char* status_text(nd_status st) {
+    switch (st) {
+        case ND_OK: return "ok";
+        case ND_NEED_REALLOC: return "output buffer too small";
+        case ND_ERR_ARG: return "invalid argument";
+        case ND_ERR_SPEC: return "invalid BVH specification";
+        case ND_ERR_NONFINITE: return "non-finite coordinate";
+        case ND_ERR_RANGE: return "coordinate out of Int32 range after quantisation";
+        case ND_ERR_CUDA: return "CUDA runtime error";
+        case ND_ERR_NOMEM: return "device allocation failed";
+        case ND_ERR_INTERNAL: return "device consistency check failed";
+        case ND_ERR_OVERFLOW: return "neighbour list capacity exceeded";
+        case ND_ERR_NODEVICE: return "no such CUDA device";
+        default: return "unknown status";
+    }
+}
+
+nd_status sync_and_check(Ctx* c, const char* what) {
+    cudaError_t e = cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int32_t) * kErrWords,
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, what);
+    if (c->h_err[0] != 0) {
+        nd_status st = c->h_err[0];
+        char msg[256];
+        snprintf(msg, sizeof(msg), "%s: %s (item %d)", what, status_text(st), c->h_err[1]);
+        c->last_error = msg;
+        cudaMemsetAsync(c->d_err, 0, sizeof(int32_t) * kErrWords, c->stream);
+        cudaStreamSynchronize(c->stream);
+        return st;
+    }
+    return ND_OK;
+}
+
+static nd_status set_device(Ctx* c) {
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+    return ND_OK;
+}
+
+static void free_buf(DevBuf& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+static nd_status spec_ok(const nd_bvh_spec* s) {
+    if (!s) return ND_ERR_ARG;
+    if (s->atomsperleaf <= 0 || s->atom_count <= 0) return ND_ERR_SPEC;
+    if (s->atom_count % s->atomsperleaf != 0) return ND_ERR_SPEC;
+    int32_t nl = s->atom_count / s->atomsperleaf;
+    if (nl < 2 || s->leaves_count != nl || s->branches_count != nl - 1) return ND_ERR_SPEC;
+    return ND_OK;
+}
+
+// Upload host positions and build the tree on the context's scratch buffers.
+static nd_status tree_from_host(Ctx* c, const float* xyz, const nd_bvh_spec* s, int32_t order,
+                                int32_t boxes, int64_t nkeys, bool overwrite_root,
+                                TreeBuffers* t) {
+    const int32_t n = s->atom_count;
+    nd_status st = ensure(c, c->xyz, 3 * sizeof(float) * (size_t)n);
+    if (st) return st;
+    cudaError_t e = cudaMemcpyAsync(c->xyz.p, xyz, 3 * sizeof(float) * (size_t)n,
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "position upload");
+    return build_tree(c, (const float*)c->xyz.p, n, s->neighbor_distance, s->atomsperleaf, order,
+                      boxes, nkeys, overwrite_root, t);
+}
+
+static nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode,
+                              int kind, const float* xyz, bool host, int32_t* pi, int32_t* pj,
+                              float* pd, int64_t capacity, int64_t* count) {
+    nd_status st = spec_ok(s);
+    if (st) return st;
+    if (!xyz || !count || capacity < 0) return ND_ERR_ARG;
+    if (capacity > 0 && (!pi || !pj || !pd)) return ND_ERR_ARG;
+    if (order != ND_ORDER_REFERENCE && order != ND_ORDER_SPATIAL) return ND_ERR_ARG;
+    if ((st = set_device(c))) return st;
+    const int32_t n = s->atom_count, nL = s->leaves_count;
+    const int32_t boxes = (kind == 0) ? ND_BOX_LEAF : ND_BOX_ATOM;
+    if (kind == 0 && n - 1 < 2 * nL - 1) return ND_ERR_SPEC;  // leafTreeData needs apl >= 2
+    TreeBuffers t;
+    if (host) {
+        st = tree_from_host(c, xyz, s, order, boxes, 2LL * nL - 1, false, &t);
+    } else {
+        st = build_tree(c, xyz, n, s->neighbor_distance, s->atomsperleaf, order, boxes,
+                        2LL * nL - 1, false, &t);
+    }
+    if (st) return st;
+    const float r = s->neighbor_distance;
+    int64_t total = 0;
+    if (kind == 0 && mode == ND_PAIRS_UNORDERED && s->atomsperleaf == 4) {
+        if (host) {
+            int64_t devcap = (int64_t)(c->pairs_i.bytes / sizeof(int32_t));
+            devcap = std::min(devcap, (int64_t)(c->pairs_d.bytes / sizeof(float)));
+            if ((st = emit_unordered(c, t, r, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
+                                     (float*)c->pairs_d.p, devcap, &total)))
+                return st;
+            *count = total;
+            if (total > capacity) return ND_NEED_REALLOC;
+            if (total > devcap) {
+                if ((st = ensure(c, c->pairs_i, sizeof(int32_t) * (size_t)total))) return st;
+                if ((st = ensure(c, c->pairs_j, sizeof(int32_t) * (size_t)total))) return st;
+                if ((st = ensure(c, c->pairs_d, sizeof(float) * (size_t)total))) return st;
+                int64_t again = 0;
+                if ((st = emit_unordered(c, t, r, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
+                                         (float*)c->pairs_d.p, total, &again)))
+                    return st;
+            }
+        } else {
+            if ((st = emit_unordered(c, t, r, pi, pj, pd, capacity, &total))) return st;
+            *count = total;
+            return total > capacity ? ND_NEED_REALLOC : ND_OK;
+        }
+    } else {
+        if ((st = count_pairs(c, t, r, kind, &total))) return st;
+        *count = total;
+        if (total > capacity) return ND_NEED_REALLOC;
+        if (total == 0) return ND_OK;
+        if (host) {
+            if ((st = ensure(c, c->pairs_i, sizeof(int32_t) * (size_t)total))) return st;
+            if ((st = ensure(c, c->pairs_j, sizeof(int32_t) * (size_t)total))) return st;
+            if ((st = ensure(c, c->pairs_d, sizeof(float) * (size_t)total))) return st;
+            if ((st = write_pairs(c, t, r, kind, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
+                                  (float*)c->pairs_d.p)))
+                return st;
+        } else {
+            if ((st = write_pairs(c, t, r, kind, pi, pj, pd))) return st;
+            return sync_and_check(c, "pair write");
+        }
+    }
+    // host copy-out
+    if (total > 0) {
+        cudaError_t e = cudaMemcpyAsync(pi, c->pairs_i.p, sizeof(int32_t) * (size_t)total,
+                                        cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(pj, c->pairs_j.p, sizeof(int32_t) * (size_t)total,
+                                cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(pd, c->pairs_d.p, sizeof(float) * (size_t)total,
+                                cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "pair download");
+    }
+    return sync_and_check(c, "pairs");
+}
+
+// ------------------------------------------------------- synthetic inputs
+
+struct SplitMix {
+    uint64_t s;
+    explicit SplitMix(uint64_t seed) : s(seed) {}
+    uint64_t next() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return (double)(next() >> 11) * 0x1.0p-53; }  // [0, 1)
+    double normal() {
+        // Box-Muller, one value per call (the partner is discarded for simplicity)
+        double u1 = uniform();
+        double u2 = uniform();
+        if (u1 < 1e-300) u1 = 1e-300;
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    }
+};
+
+}  // namespace nd
+
+using nd::Ctx;
+
+extern "C" {
+
+nd_status nd_ctx_create(nd_ctx** out, int32_t device) {
+    if (!out) return ND_ERR_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return ND_ERR_NODEVICE;
+    }
+    if (device < 0 || device >= count) return ND_ERR_NODEVICE;
+    nd_ctx* h = new (std::nothrow) nd_ctx();
+    if (!h) return ND_ERR_NOMEM;
+    Ctx* c = &h->c;
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int32_t) * nd::kErrWords);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, sizeof(int32_t) * nd::kErrWords);
+    if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int32_t) * nd::kErrWords);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        nd_ctx_destroy(h);
+        return e == cudaErrorMemoryAllocation ? ND_ERR_NOMEM : ND_ERR_CUDA;
+    }
+    *out = h;
+    return ND_OK;
+}
+
+nd_status nd_ctx_destroy(nd_ctx* h) {
+    if (!h) return ND_OK;
+    Ctx* c = &h->c;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    nd::DevBuf* bufs[] = {&c->xyz, &c->codes, &c->codes_alt, &c->perm, &c->perm_alt, &c->pos4,
+                          &c->idx, &c->keys, &c->store, &c->hist, &c->counts, &c->offsets,
+                          &c->partial, &c->pairs_i, &c->pairs_j, &c->pairs_d, &c->misc, &c->hash};
+    for (nd::DevBuf* b : bufs) nd::free_buf(*b);
+    if (c->d_err) cudaFree(c->d_err);
+    if (c->h_err) cudaFreeHost(c->h_err);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete h;
+    return ND_OK;
+}
+
+const char* nd_last_error(const nd_ctx* h) { return h ? h->c.last_error.c_str() : "no context"; }
+
+const char* nd_status_string(nd_status st) { return nd::status_text(st); }
+
+void* nd_ctx_stream(nd_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+
+nd_status nd_ctx_synchronize(nd_ctx* h) {
+    if (!h) return ND_ERR_ARG;
+    return nd::sync_and_check(&h->c, "synchronize");
+}
+
+int64_t nd_ctx_launch_count(const nd_ctx* h) { return h ? h->c.launches : 0; }
+
+nd_status nd_bvh_spec_init(nd_bvh_spec* out, float r, int32_t n, int32_t apl) {
+    if (!out) return ND_ERR_ARG;
+    if (apl <= 0 || n <= 0 || n % apl != 0) return ND_ERR_SPEC;
+    int32_t nl = n / apl;
+    if (nl < 2) return ND_ERR_SPEC;
+    out->neighbor_distance = r;
+    out->atom_count = n;
+    out->leaves_count = nl;
+    out->branches_count = nl - 1;
+    out->atomsperleaf = apl;
+    return ND_OK;
+}
+
+nd_status nd_morton_codes_dev(nd_ctx* h, const float* xyz, int32_t n, int32_t order,
+                              int32_t* codes) {
+    if (!h || !xyz || !codes || n < 0) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::set_device(c);
+    if (st) return st;
+    if ((st = nd::morton_codes(c, xyz, n, order, codes, nullptr))) return st;
+    return nd::sync_and_check(c, "morton codes");
+}
+
+nd_status nd_sortperm_dev(nd_ctx* h, int32_t* codes, int32_t n, int32_t* perm) {
+    if (!h || !codes || !perm || n < 0) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::set_device(c);
+    if (st) return st;
+    // perm starts as the identity; the sort carries it along (stable)
+    std::vector<int32_t> iota((size_t)n);
+    for (int32_t i = 0; i < n; ++i) iota[i] = i;
+    cudaError_t e = cudaMemcpyAsync(perm, iota.data(), sizeof(int32_t) * (size_t)n,
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return nd::cuda_fail(c, e, "perm init");
+    if ((st = nd::radix_sort_pairs(c, (uint32_t*)codes, perm, n, 31))) return st;
+    return nd::sync_and_check(c, "sortperm");
+}
+
+nd_status nd_tree(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, int32_t order,
+                  int32_t boxes, nd_gridkey* keys, int64_t nkeys, int32_t* index,
+                  int32_t* morton_code, float* position, int32_t* perm) {
+    if (!h || !xyz) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::spec_ok(s);
+    if (st) return st;
+    if (order != ND_ORDER_REFERENCE && order != ND_ORDER_SPATIAL) return ND_ERR_ARG;
+    if (boxes != ND_BOX_LEAF && boxes != ND_BOX_ATOM) return ND_ERR_ARG;
+    const int32_t n = s->atom_count, nL = s->leaves_count;
+    if (boxes == ND_BOX_LEAF && n - 1 < 2 * nL - 1) return ND_ERR_SPEC;
+    if (keys && nkeys < 0) return ND_ERR_ARG;
+    if ((st = nd::set_device(c))) return st;
+    const int64_t need = std::max<int64_t>(2LL * nL - 1, boxes == ND_BOX_LEAF ? n - 1 : 0);
+    nd::TreeBuffers t;
+    if ((st = nd::tree_from_host(c, xyz, s, order, boxes, need, true, &t))) return st;
+    std::vector<float4> pos4;
+    cudaError_t e = cudaSuccess;
+    if (keys && nkeys > 0) {
+        int64_t k = std::min(nkeys, need);
+        e = cudaMemcpyAsync(keys, t.keys, 32 * (size_t)k, cudaMemcpyDeviceToHost, c->stream);
+        if (nkeys > k) memset(keys + k, 0, 32 * (size_t)(nkeys - k));
+    }
+    if (e == cudaSuccess && index)
+        e = cudaMemcpyAsync(index, t.idx, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && morton_code)
+        e = cudaMemcpyAsync(morton_code, t.codes, sizeof(int32_t) * (size_t)n,
+                            cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && perm)
+        e = cudaMemcpyAsync(perm, t.perm, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && position) {
+        pos4.resize((size_t)n);
+        e = cudaMemcpyAsync(pos4.data(), t.pos4, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost,
+                            c->stream);
+    }
+    if (e != cudaSuccess) return nd::cuda_fail(c, e, "tree download");
+    if ((st = nd::sync_and_check(c, "tree"))) return st;
+    if (perm)
+        for (int32_t i = 0; i < n; ++i) perm[i] += 1;  // 1-based, as Julia's sortperm
+    if (position)
+        for (int32_t i = 0; i < n; ++i) {
+            position[3 * (size_t)i] = pos4[i].x;
+            position[3 * (size_t)i + 1] = pos4[i].y;
+            position[3 * (size_t)i + 2] = pos4[i].z;
+        }
+    return ND_OK;
+}
+
+nd_status nd_leaf_pairs(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, int32_t order,
+                        int32_t mode, int32_t* pi, int32_t* pj, float* pd, int64_t capacity,
+                        int64_t* count) {
+    if (!h) return ND_ERR_ARG;
+    return nd::pairs_common(&h->c, s, order, mode, 0, xyz, true, pi, pj, pd, capacity, count);
+}
+
+nd_status nd_leaf_pairs_dev(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, int32_t order,
+                            int32_t mode, int32_t* pi, int32_t* pj, float* pd, int64_t capacity,
+                            int64_t* count) {
+    if (!h) return ND_ERR_ARG;
+    return nd::pairs_common(&h->c, s, order, mode, 0, xyz, false, pi, pj, pd, capacity, count);
+}
+
+nd_status nd_atom_pairs(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, int32_t order,
+                        int32_t* pi, int32_t* pj, float* pd, int64_t capacity, int64_t* count) {
+    if (!h) return ND_ERR_ARG;
+    return nd::pairs_common(&h->c, s, order, ND_PAIRS_ORDERED, 1, xyz, true, pi, pj, pd, capacity,
+                            count);
+}
+
+nd_status nd_pair_hash_dev(nd_ctx* h, const int32_t* pi, const int32_t* pj, const float* pd,
+                           int64_t np, uint64_t hash[2]) {
+    if (!h || !hash || np < 0 || (np > 0 && (!pi || !pj || !pd))) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::set_device(c);
+    if (st) return st;
+    return nd::pair_hash(c, pi, pj, pd, np, hash);
+}
+
+nd_status nd_forces_pairs(nd_ctx* h, const nd_md_params* p, int32_t n, const double* x,
+                          const double* q, const int32_t* pi, const int32_t* pj, int64_t npairs,
+                          float* force, double* energy) {
+    if (!h) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::set_device(c);
+    if (st) return st;
+    return nd::forces_pairs(c, p, n, x, q, pi, pj, npairs, force, energy);
+}
+
+nd_status nd_forces(nd_ctx* h, const nd_md_params* p, int32_t n, const double* x,
+                    const double* q, float* force, double* energy) {
+    if (!h || !p || !x || n <= 0) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::set_device(c);
+    if (st) return st;
+    nd_md_params pp = *p;
+    if (pp.rebuild_every <= 0) pp.rebuild_every = 1;
+    if (!(pp.dt > 0)) pp.dt = 1.0;
+    std::vector<double> v0(3 * (size_t)n, 0.0);
+    nd::MDEngine* m = nullptr;
+    if ((st = nd::md_create(c, &pp, n, x, v0.data(), q, nullptr, true, false, &m))) return st;
+    st = nd::md_get(m, nullptr, nullptr, force, true);
+    if (st == ND_OK && energy) {
+        double pot = 0.0;
+        st = nd::md_energy(m, &pot, nullptr);
+        *energy = pot;
+    }
+    if (st) c->last_error = nd::md_last_error(m);
+    nd::md_destroy(m);
+    return st;
+}
+
+nd_status nd_md_create(nd_ctx* h, const nd_md_params* p, int32_t n, const double* x,
+                       const double* v, const double* q, const double* m, nd_md** out) {
+    if (!h || !out) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    nd::MDEngine* e = nullptr;
+    if ((st = nd::md_create(&h->c, p, n, x, v, q, m, true, true, &e))) return st;
+    *out = new nd_md{h, e};
+    return ND_OK;
+}
+
+nd_status nd_md_create_dev(nd_ctx* h, const nd_md_params* p, int32_t n, const double* x,
+                           const double* v, const double* q, const double* m, nd_md** out) {
+    if (!h || !out) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    nd::MDEngine* e = nullptr;
+    if ((st = nd::md_create(&h->c, p, n, x, v, q, m, false, true, &e))) return st;
+    *out = new nd_md{h, e};
+    return ND_OK;
+}
+
+nd_status nd_md_destroy(nd_md* md) {
+    if (!md) return ND_OK;
+    nd::set_device(&md->ctx->c);
+    nd::md_destroy(md->e);
+    delete md;
+    return ND_OK;
+}
+
+static nd_status md_wrap(nd_md* md, nd_status st) {
+    if (st) md->ctx->c.last_error = nd::md_last_error(md->e);
+    return st;
+}
+
+nd_status nd_md_run(nd_md* md, int64_t steps) {
+    if (!md || steps < 0) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_run(md->e, steps));
+}
+
+nd_status nd_md_sync(nd_md* md) {
+    if (!md) return ND_ERR_ARG;
+    return md_wrap(md, nd::md_sync(md->e));
+}
+
+nd_status nd_md_get(nd_md* md, double* x, double* v, float* f) {
+    if (!md) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_get(md->e, x, v, f, true));
+}
+
+nd_status nd_md_get_dev(nd_md* md, double* x, double* v, float* f) {
+    if (!md) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_get(md->e, x, v, f, false));
+}
+
+nd_status nd_md_energy(nd_md* md, double* potential, double* kinetic) {
+    if (!md) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_energy(md->e, potential, kinetic));
+}
+
+nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* list_pairs,
+                      int32_t* capacity) {
+    if (!md) return ND_ERR_ARG;
+    return md_wrap(md, nd::md_stats(md->e, steps, rebuilds, list_pairs, capacity));
+}
+
+int64_t nd_md_launches_per_run(nd_md* md, int64_t steps) {
+    return md ? nd::md_launches_per_run(md->e, steps) : 0;
+}
+
+nd_status nd_simulate(nd_ctx* h, const nd_md_params* p, int32_t n, double* x, double* v,
+                      float* f, const double* q, const double* m, int64_t steps) {
+    if (!h || !p || !x || !v || steps < 0) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::set_device(c);
+    if (st) return st;
+    nd::MDEngine* e = nullptr;
+    const bool capture = steps >= 2LL * std::max(p->rebuild_every, 1);
+    if ((st = nd::md_create(c, p, n, x, v, q, m, true, capture, &e))) return st;
+    st = nd::md_run(e, steps);
+    if (st == ND_OK) st = nd::md_get(e, x, v, f, true);
+    if (st) c->last_error = nd::md_last_error(e);
+    nd::md_destroy(e);
+    return st;
+}
+
+// ------------------------------------------------------------ synthetic inputs
+
+nd_status nd_synth_uniform(uint64_t seed, int32_t n, double lo, double side, float* xyz) {
+    if (!xyz || n < 0) return ND_ERR_ARG;
+    nd::SplitMix g(seed);
+    for (int64_t k = 0; k < 3LL * n; ++k) xyz[k] = (float)(lo + side * g.uniform());
+    return ND_OK;
+}
+
+nd_status nd_synth_uniform_mindist(uint64_t seed, int32_t n, double side, double dmin,
+                                   double* xyz) {
+    if (!xyz || n < 0 || !(side > 0) || !(dmin >= 0)) return ND_ERR_ARG;
+    nd::SplitMix g(seed);
+    int nc = dmin > 0 ? (int)std::floor(side / dmin) : 1;
+    nc = std::max(1, std::min(nc, 1024));
+    const double cs = side / nc;
+    std::vector<int32_t> head((size_t)nc * nc * nc, -1), next((size_t)n, -1);
+    const double d2 = dmin * dmin;
+    for (int32_t i = 0; i < n; ++i) {
+        bool placed = false;
+        for (int attempt = 0; attempt < 100000 && !placed; ++attempt) {
+            double p[3];
+            int ci[3];
+            for (int d = 0; d < 3; ++d) {
+                p[d] = side * g.uniform();
+                ci[d] = std::min(nc - 1, (int)(p[d] / cs));
+            }
+            bool ok = true;
+            for (int oz = -1; oz <= 1 && ok; ++oz)
+                for (int oy = -1; oy <= 1 && ok; ++oy)
+                    for (int ox = -1; ox <= 1 && ok; ++ox) {
+                        int X = ci[0] + ox, Y = ci[1] + oy, Z = ci[2] + oz;
+                        if (X < 0 || Y < 0 || Z < 0 || X >= nc || Y >= nc || Z >= nc) continue;
+                        for (int32_t j = head[((size_t)Z * nc + Y) * nc + X]; j >= 0; j = next[j]) {
+                            double dx = p[0] - xyz[3 * (size_t)j], dy = p[1] - xyz[3 * (size_t)j + 1],
+                                   dz = p[2] - xyz[3 * (size_t)j + 2];
+                            if (dx * dx + dy * dy + dz * dz < d2) { ok = false; break; }
+                        }
+                    }
+            if (!ok) continue;
+            for (int d = 0; d < 3; ++d) xyz[3 * (size_t)i + d] = p[d];
+            size_t cell = ((size_t)ci[2] * nc + ci[1]) * nc + ci[0];
+            next[i] = head[cell];
+            head[cell] = i;
+            placed = true;
+        }
+        if (!placed) return ND_ERR_ARG;  // too dense for this minimum distance
+    }
+    return ND_OK;
+}
+
+nd_status nd_synth_clusters(uint64_t seed, int32_t n, int32_t nclusters, double side,
+                            double smin, double smax, float* xyz) {
+    if (!xyz || n < 0 || nclusters <= 0 || n % nclusters != 0) return ND_ERR_ARG;
+    nd::SplitMix g(seed);
+    const int32_t per = n / nclusters;
+    for (int32_t c = 0; c < nclusters; ++c) {
+        double ctr[3] = {side * g.uniform(), side * g.uniform(), side * g.uniform()};
+        double sg = smin + (smax - smin) * g.uniform();
+        for (int32_t k = 0; k < per; ++k) {
+            size_t a = (size_t)c * per + k;
+            for (int d = 0; d < 3; ++d) xyz[3 * a + d] = (float)(ctr[d] + sg * g.normal());
+        }
+    }
+    return ND_OK;
+}
+
+nd_status nd_synth_normal(uint64_t seed, int64_t count, double s, double* out) {
+    if (!out || count < 0) return ND_ERR_ARG;
+    nd::SplitMix g(seed);
+    for (int64_t k = 0; k < count; ++k) out[k] = s * g.normal();
+    return ND_OK;
+}
+
+nd_status nd_synth_charges(uint64_t seed, int32_t n, double* q) {
+    if (!q || n < 0 || (n & 1)) return ND_ERR_ARG;
+    nd::SplitMix g(seed);
+    for (int32_t i = 0; i < n; ++i) q[i] = i < n / 2 ? 1.0 : -1.0;
+    for (int32_t i = n - 1; i > 0; --i) {
+        int32_t j = (int32_t)(g.next() % (uint64_t)(i + 1));
+        std::swap(q[i], q[j]);
+    }
+    return ND_OK;
+}
+
+}  // extern "C"

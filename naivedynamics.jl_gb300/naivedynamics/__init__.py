@@ -1,0 +1,21 @@
+"""naivedynamics (GB300): Python host mirror of NaiveDynamics.jl's hot path.
+
+The compute path is libnaivegpu (CUDA, sm_103a) behind the C ABI declared in
+include/naivegpu.h; this package only marshals arguments.  Importing it loads
+the library and fails loudly if it has not been built.
+"""
+from . import _lib
+from ._lib import (Context, NDError, SpecError, InexactError, default_context,
+                   ND_ORDER_REFERENCE, ND_ORDER_SPATIAL, ND_PAIRS_ORDERED, ND_PAIRS_UNORDERED,
+                   GRIDKEY_DTYPE, PAIR_DTYPE)
+from .bvh import (SpheresBVHSpecs, APointPrimitive, leafTreeData, TreeData,
+                  leafbuild_traverse_bvh, build_traverse_bvh, gpubvh_neighborlist,
+                  neighbor_pairs_dev, pair_hash_dev)
+from .dynamics import (ForceField, md_params, force_lennardjones_, force_coulomb_, sum_forces_,
+                       forces, SimSpec, GenericObjectCollection, GenericRandomCollector,
+                       simulate_, MDEngine)
+from . import synth
+
+_lib.lib()  # load now: no CPU fallback exists
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,260 @@
+"""Forces and dynamics: the GPU mirror of src/Forces.jl and src/Simulator.jl.
+
+  force_lennardjones_  force_lennardjones!(force, pairslist, position)  Forces.jl:15-45
+  force_coulomb_       force_coulomb!(force, pairslist, charge)          Forces.jl:56-66
+  sum_forces_          sum_forces!(force, f1, f2)                        Forces.jl:68-75
+  SimSpec              SimSpec(; duration, stepwidth, ...)               Simulator.jl:30-49
+  simulate_            simulate!(sys, spec, clct)                        Simulator.jl:154-256
+  MDEngine             device-resident form of the simulate! step loop
+
+Julia's `f!` (mutates its first argument) is spelled `f_` here.  The physics
+is the intended one (truncated Lennard-Jones + cutoff Coulomb with direction,
+Newton's third law, kick-drift-kick velocity Verlet, reflecting walls), not the
+reference's scalar broadcast; sigma, epsilon, k and the cutoff are keywords
+instead of the constants hard-coded at Forces.jl:17-19,57.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import MDParams, ND_ORDER_SPATIAL, default_context, ptr
+
+__all__ = ["ForceField", "md_params", "force_lennardjones_", "force_coulomb_", "sum_forces_",
+           "forces", "SimSpec", "GenericObjectCollection", "GenericRandomCollector", "simulate_",
+           "MDEngine"]
+
+
+@dataclass
+class ForceField:
+    sigma: float = 1.0
+    epsilon: float = 1.0
+    coulomb_k: float = 1.0
+    cutoff: float = 2.5
+
+
+def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e-3,
+              box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), atomsperleaf=4, rebuild_every=10,
+              order=ND_ORDER_SPATIAL, max_neighbors=0) -> MDParams:
+    p = MDParams()
+    p.sigma, p.epsilon, p.coulomb_k, p.cutoff, p.skin, p.dt = (float(sigma), float(epsilon),
+                                                               float(coulomb_k), float(cutoff),
+                                                               float(skin), float(dt))
+    for d in range(3):
+        p.box_lo[d] = float(box_lo[d])
+        p.box_hi[d] = float(box_hi[d])
+    p.atomsperleaf, p.rebuild_every, p.order, p.max_neighbors = (int(atomsperleaf),
+                                                                 int(rebuild_every), int(order),
+                                                                 int(max_neighbors))
+    return p
+
+
+def _f64(a, shape=None):
+    x = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    return x.reshape(shape) if shape is not None else x
+
+
+def _pair_arrays(pairslist):
+    if isinstance(pairslist, np.ndarray) and pairslist.dtype.names:
+        return (np.ascontiguousarray(pairslist["i"], np.int32),
+                np.ascontiguousarray(pairslist["j"], np.int32))
+    arr = np.asarray([(p[0], p[1]) for p in pairslist], dtype=np.int32).reshape(-1, 2)
+    return np.ascontiguousarray(arr[:, 0]), np.ascontiguousarray(arr[:, 1])
+
+
+def _pair_forces(force, pairslist, position, charge, p, ctx):
+    ctx = ctx or default_context()
+    x = _f64(position, (-1, 3))
+    n = x.shape[0]
+    pi, pj = _pair_arrays(pairslist)
+    q = None if charge is None else _f64(charge)
+    f = np.empty((n, 3), np.float32)
+    e = ctypes.c_double()
+    st = _lib.lib().nd_forces_pairs(ctx.handle, ctypes.byref(p), n, ptr(x), ptr(q), ptr(pi),
+                                    ptr(pj), pi.shape[0], ptr(f), ctypes.byref(e))
+    ctx.check(st, "nd_forces_pairs")
+    if force is not None:
+        np.copyto(np.asarray(force).reshape(n, 3), f, casting="unsafe")
+    return f, e.value
+
+
+def force_lennardjones_(force, pairslist, position, sigma=1.0, epsilon=1.0, cutoff=2.5,
+                        ctx=None):
+    """force_lennardjones!(force, pairslist, position): force is overwritten.
+
+    F_ij = 24 eps / r^2 (2 (sigma/r)^12 - (sigma/r)^6) r_ij for listed pairs with
+    r < cutoff; returns the LJ potential energy."""
+    p = md_params(sigma=sigma, epsilon=epsilon, coulomb_k=0.0, cutoff=cutoff)
+    return _pair_forces(force, pairslist, position, None, p, ctx)[1]
+
+
+def force_coulomb_(force, pairslist, charge, position, k=1.0, cutoff=2.5, ctx=None):
+    """force_coulomb!(force, pairslist, charge): force is overwritten.
+
+    F_ij = k q_i q_j r_ij / r^3 for listed pairs with r < cutoff.  Unlike the
+    reference signature it needs the positions for the direction."""
+    p = md_params(sigma=1.0, epsilon=0.0, coulomb_k=k, cutoff=cutoff)
+    return _pair_forces(force, pairslist, position, charge, p, ctx)[1]
+
+
+def sum_forces_(force, force1, force2):
+    """sum_forces!(force, f1, f2) (Forces.jl:68-75)."""
+    np.add(force1, force2, out=force)
+    return force
+
+
+def forces(position, charge=None, ff: ForceField | None = None, ctx=None):
+    """Fused LJ + Coulomb forces and energy with the library's own neighbour search."""
+    ff = ff or ForceField()
+    ctx = ctx or default_context()
+    x = _f64(position, (-1, 3))
+    n = x.shape[0]
+    q = None if charge is None else _f64(charge)
+    lo, hi = x.min(0), x.max(0)
+    p = md_params(sigma=ff.sigma, epsilon=ff.epsilon, coulomb_k=ff.coulomb_k if q is not None else 0.0,
+                  cutoff=ff.cutoff, skin=0.0, box_lo=lo, box_hi=hi)
+    f = np.empty((n, 3), np.float32)
+    e = ctypes.c_double()
+    st = _lib.lib().nd_forces(ctx.handle, ctypes.byref(p), n, ptr(x), ptr(q), ptr(f), ctypes.byref(e))
+    ctx.check(st, "nd_forces")
+    return f, e.value
+
+
+@dataclass
+class SimSpec:
+    """SimSpec (Simulator.jl:30-49): duration (steps) and stepwidth (dt)."""
+    duration: int
+    stepwidth: float
+    currentstep: int = 1
+    logLength: int = 10
+    vDamp: float = 0.0
+    threshold: float = 0.0
+
+
+@dataclass
+class GenericRandomCollector:
+    """The fields of GenericRandomCollector (MDInput.jl:67-84) the step loop uses."""
+    objectnumber: int
+    minDim: tuple
+    maxDim: tuple
+    temperature: float = 0.0
+    minimumdistance: float = 0.0
+
+
+@dataclass
+class GenericObjectCollection:
+    """GenericObjectCollection (MDInput.jl:33-46), struct-of-arrays per atom."""
+    position: np.ndarray
+    velocity: np.ndarray
+    force: np.ndarray | None = None
+    mass: np.ndarray | None = None
+    charge: np.ndarray | None = None
+    index: np.ndarray | None = field(default=None)
+
+    def __post_init__(self):
+        self.position = _f64(self.position, (-1, 3)).copy()
+        self.velocity = _f64(self.velocity, (-1, 3)).copy()
+        n = self.position.shape[0]
+        if self.force is None:
+            self.force = np.zeros((n, 3), np.float32)
+        if self.index is None:
+            self.index = np.arange(1, n + 1, dtype=np.int64)
+
+
+def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCollector,
+              ff: ForceField | None = None, skin=0.3, atomsperleaf=4, rebuild_every=10,
+              order=ND_ORDER_SPATIAL, ctx=None):
+    """simulate!(sys, spec, clct) (Simulator.jl:154-256) on the GPU.
+
+    Advances sys.position / sys.velocity in place by spec.duration steps of
+    kick-drift-kick velocity Verlet with reflecting walls at clct.minDim /
+    clct.maxDim, and stores the final forces in sys.force."""
+    ff = ff or ForceField()
+    ctx = ctx or default_context()
+    n = sys.position.shape[0]
+    q = None if sys.charge is None else _f64(sys.charge)
+    m = None if sys.mass is None else _f64(sys.mass)
+    p = md_params(sigma=ff.sigma, epsilon=ff.epsilon,
+                  coulomb_k=ff.coulomb_k if q is not None else 0.0, cutoff=ff.cutoff, skin=skin,
+                  dt=spec.stepwidth, box_lo=clct.minDim, box_hi=clct.maxDim,
+                  atomsperleaf=atomsperleaf, rebuild_every=rebuild_every, order=order)
+    f = np.empty((n, 3), np.float32)
+    st = _lib.lib().nd_simulate(ctx.handle, ctypes.byref(p), n, ptr(sys.position),
+                                ptr(sys.velocity), ptr(f), ptr(q), ptr(m), int(spec.duration))
+    ctx.check(st, "nd_simulate")
+    sys.force = f
+    return sys
+
+
+class MDEngine:
+    """Device-resident simulation state (nd_md_*).
+
+    Host arrays (numpy) are copied once; with device=True, x/v/q/m are device
+    pointers (torch tensors or ints) and nothing crosses the host boundary."""
+
+    def __init__(self, params: MDParams, x, v, q=None, m=None, device=False, ctx=None):
+        self.ctx = ctx or default_context()
+        self.params = params
+        h = ctypes.c_void_p()
+        if device:
+            n = int(x.shape[0]) if hasattr(x, "shape") else None
+            st = _lib.lib().nd_md_create_dev(self.ctx.handle, ctypes.byref(params), n, ptr(x),
+                                             ptr(v), ptr(q), ptr(m), ctypes.byref(h))
+        else:
+            x = _f64(x, (-1, 3))
+            v = _f64(v, (-1, 3))
+            n = x.shape[0]
+            qq = None if q is None else _f64(q)
+            mm = None if m is None else _f64(m)
+            st = _lib.lib().nd_md_create(self.ctx.handle, ctypes.byref(params), n, ptr(x), ptr(v),
+                                         ptr(qq), ptr(mm), ctypes.byref(h))
+        self.ctx.check(st, "nd_md_create")
+        self.handle = h.value
+        self.n = n
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.lib().nd_md_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, steps: int):
+        self.ctx.check(_lib.lib().nd_md_run(self.handle, int(steps)), "nd_md_run")
+
+    def sync(self):
+        self.ctx.check(_lib.lib().nd_md_sync(self.handle), "nd_md_sync")
+
+    def get(self):
+        x = np.empty((self.n, 3), np.float64)
+        v = np.empty((self.n, 3), np.float64)
+        f = np.empty((self.n, 3), np.float32)
+        self.ctx.check(_lib.lib().nd_md_get(self.handle, ptr(x), ptr(v), ptr(f)), "nd_md_get")
+        return x, v, f
+
+    def get_dev(self, x=None, v=None, f=None):
+        self.ctx.check(_lib.lib().nd_md_get_dev(self.handle, ptr(x), ptr(v), ptr(f)),
+                       "nd_md_get_dev")
+
+    def energy(self):
+        pe, ke = ctypes.c_double(), ctypes.c_double()
+        self.ctx.check(_lib.lib().nd_md_energy(self.handle, ctypes.byref(pe), ctypes.byref(ke)),
+                       "nd_md_energy")
+        return pe.value, ke.value
+
+    def stats(self):
+        s, r, p = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        cap = ctypes.c_int32()
+        self.ctx.check(_lib.lib().nd_md_stats(self.handle, ctypes.byref(s), ctypes.byref(r),
+                                              ctypes.byref(p), ctypes.byref(cap)), "nd_md_stats")
+        return dict(steps=s.value, rebuilds=r.value, list_pairs=p.value, capacity=cap.value)
+
+    def launches_per_run(self, steps: int) -> int:
+        return int(_lib.lib().nd_md_launches_per_run(self.handle, int(steps)))

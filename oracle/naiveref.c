@@ -1,0 +1,732 @@
+/*
+ * naiveref.c -- CPU oracle (test infrastructure only, never shipped) for the
+ * NaiveDynamics.jl hot path: LBVH neighbour search (src/Neighbors/BVHTraverse.jl),
+ * brute-force pairs (src/Neighbors/AllToAll.jl) and an FP64 physics oracle for
+ * the intended LJ + Coulomb forces and velocity-Verlet integrator
+ * (src/Forces.jl, src/Simulator.jl).
+ *
+ * Build flags must keep IEEE single precision semantics exactly as Julia does:
+ * no fast-math, no FMA contraction (-ffp-contract=off).
+ */
+#include "naiveref.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int ref_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------ helpers */
+
+/* Julia's min/max on IEEE floats (Base.min / Base.max): the sign of x - y picks
+ * the argument, so -0.0 orders below +0.0 and the argument order is kept. */
+static inline float jl_min(float x, float y) {
+    float d = x - y;
+    if (isnan(x) || isnan(y)) return d;
+    return signbit(d) ? x : y;
+}
+static inline float jl_max(float x, float y) {
+    float d = x - y;
+    if (isnan(x) || isnan(y)) return d;
+    return signbit(d) ? y : x;
+}
+
+float ref_dist2(const float* a, const float* b) {
+    /* sum((a - b).^2) for SVector{3,Float32}: StaticArrays unrolls the sum
+     * left to right, Julia emits plain fmul/fadd (no contraction). */
+    float dx = a[0] - b[0];
+    float dy = a[1] - b[1];
+    float dz = a[2] - b[2];
+    float sx = dx * dx;
+    float sy = dy * dy;
+    float sz = dz * dz;
+    float s = sx + sy;
+    return s + sz;
+}
+
+/* ---------------------------------------------------------------- spec / codes */
+
+int ref_spec(int64_t atom_count, int64_t atomsperleaf, int32_t* leaves, int32_t* branches) {
+    /* SpheresBVHSpecs (BVHTraverse.jl:71-94): apl must divide N, >= 2 leaves. */
+    if (atomsperleaf <= 0 || atom_count <= 0 || atom_count > 2147483647LL) return REF_ERR_SPEC;
+    if (atom_count % atomsperleaf != 0) return REF_ERR_SPEC;
+    int64_t nl = atom_count / atomsperleaf;
+    if (nl < 2) return REF_ERR_SPEC;
+    if (leaves) *leaves = (int32_t)nl;
+    if (branches) *branches = (int32_t)(nl - 1);
+    return REF_OK;
+}
+
+int ref_morton_reference(const float* xyz, int64_t n, int32_t* codes) {
+    /* BVHTraverse.jl:241-283: q = round(Int32, p / binwidth, RoundDown);
+     * code |= (q & magic) & (q | ~magic) == q & magic, per axis. */
+    const float binwidth = (float)(1.0 / 1023.0); /* Float32(1/1023), :184 */
+    const int32_t magic[3] = {153391689, 306783378, 613566756};
+    for (int64_t a = 0; a < n; ++a) {
+        int32_t code = 0;
+        for (int d = 0; d < 3; ++d) {
+            float p = xyz[3 * a + d];
+            if (!isfinite(p)) return REF_ERR_NONFINITE;
+            float q = floorf(p / binwidth);
+            /* trunc(Int32, ::Float32) accepts -2^31 <= x < 2^31 (Base float.jl). */
+            if (!(q >= -2147483648.0f && q < 2147483648.0f)) return REF_ERR_RANGE;
+            int32_t qi = (int32_t)q;
+            int32_t yin = qi & magic[d];
+            int32_t yang = qi | ~magic[d];
+            code |= (yin & yang);
+        }
+        codes[a] = code;
+    }
+    return REF_OK;
+}
+
+static inline uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+int ref_morton_spatial(const float* xyz, int64_t n, int32_t* codes) {
+    /* Interleaved Morton code (x in bit 0, y bit 1, z bit 2 of each triple)
+     * over the Float32 bounding box, 1024 bins per axis:
+     *   s = 1024 / (hi - lo); q = clamp(floor((p - lo) * s), 0, 1023). */
+    float lo[3], hi[3], s[3];
+    for (int d = 0; d < 3; ++d) { lo[d] = INFINITY; hi[d] = -INFINITY; }
+    for (int64_t a = 0; a < n; ++a)
+        for (int d = 0; d < 3; ++d) {
+            float p = xyz[3 * a + d];
+            if (!isfinite(p)) return REF_ERR_NONFINITE;
+            lo[d] = fminf(lo[d], p);
+            hi[d] = fmaxf(hi[d], p);
+        }
+    for (int d = 0; d < 3; ++d) {
+        float ext = hi[d] - lo[d];
+        s[d] = (ext > 0.0f) ? 1024.0f / ext : 0.0f;
+    }
+    for (int64_t a = 0; a < n; ++a) {
+        uint32_t q[3];
+        for (int d = 0; d < 3; ++d) {
+            float t = (xyz[3 * a + d] - lo[d]) * s[d];
+            t = floorf(t);
+            int32_t qi = (t < 0.0f) ? 0 : (t > 1023.0f ? 1023 : (int32_t)t);
+            q[d] = (uint32_t)qi;
+        }
+        codes[a] = (int32_t)(spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2));
+    }
+    return REF_OK;
+}
+
+typedef struct { int32_t code; int32_t idx; } ci_pair;
+
+static int ci_cmp(const void* pa, const void* pb) {
+    const ci_pair* a = (const ci_pair*)pa;
+    const ci_pair* b = (const ci_pair*)pb;
+    if (a->code != b->code) return (a->code < b->code) ? -1 : 1;
+    return (a->idx < b->idx) ? -1 : (a->idx > b->idx);
+}
+
+int ref_sortperm(const int32_t* codes, int64_t n, int32_t* perm) {
+    /* sortperm is stable: equal codes keep ascending original index. */
+    ci_pair* tmp = (ci_pair*)malloc(sizeof(ci_pair) * (size_t)(n > 0 ? n : 1));
+    if (!tmp) return REF_ERR_NOMEM;
+    for (int64_t i = 0; i < n; ++i) { tmp[i].code = codes[i]; tmp[i].idx = (int32_t)i; }
+    qsort(tmp, (size_t)n, sizeof(ci_pair), ci_cmp);
+    for (int64_t i = 0; i < n; ++i) perm[i] = tmp[i].idx;
+    free(tmp);
+    return REF_OK;
+}
+
+/* ----------------------------------------------------------------- tree build */
+
+int32_t ref_delta(int32_t i, const int32_t* code_sorted, int32_t nL, int32_t apl) {
+    /* exptdelta (BVHTraverse.jl:677-696), Int32 wrap-around arithmetic. */
+    if (i >= nL || i < 1) return INT32_MAX;
+    int32_t a = code_sorted[(int64_t)(i - 1) * apl]; /* atom 1 + (i-1)*apl */
+    int32_t b = code_sorted[(int64_t)i * apl];       /* atom 1 + i*apl     */
+    uint32_t x = (uint32_t)(a ^ b);
+    uint32_t add = (x == 0u) ? (0x80000000u + (uint32_t)(i ^ (i + 1))) : 0u;
+    return (int32_t)(x + add - 1u);
+}
+
+#define KEY(k) keys[(k) - 1]
+
+static void bvh_interior(ref_key* keys, int32_t* store, int32_t i, int32_t nL,
+                         const int32_t* code, int32_t apl) {
+    /* bvh_interior! (BVHTraverse.jl:704-846); store is 1-based (store[s-1]). */
+    int32_t rangel = i, ranger = i;
+    int32_t dell = ref_delta(rangel - 1, code, nL, apl);
+    int32_t delr = ref_delta(ranger, code, nL, apl);
+    float bmin[3], bmax[3];
+    for (int d = 0; d < 3; ++d) { bmin[d] = KEY(i).min[d]; bmax[d] = KEY(i).max[d]; }
+
+    if (i == nL) {
+        KEY(i).skip = 0;
+    } else {
+        int32_t ir = i + 1;
+        KEY(i).skip = (delr < ref_delta(ir, code, nL, apl)) ? ir : nL + ir;
+    }
+
+    for (;;) {
+        int32_t leftChild;
+        if (delr < dell) {
+            leftChild = i;
+            int32_t split = ranger;
+            int32_t old = store[split - 1];
+            if (old == 0) { store[split - 1] = rangel; }
+            ranger = old;
+            if (ranger == 0) break;
+            delr = ref_delta(ranger, code, nL, apl);
+            int32_t rightChild = split + 1;
+            if (rightChild != ranger) rightChild = nL + rightChild;
+            for (int d = 0; d < 3; ++d) {
+                bmax[d] = jl_max(KEY(rightChild).max[d], bmax[d]);
+                bmin[d] = jl_min(KEY(rightChild).min[d], bmin[d]);
+            }
+        } else {
+            int32_t split = rangel - 1;
+            int32_t old = store[split - 1];
+            if (old == 0) { store[split - 1] = ranger; }
+            rangel = old;
+            if (rangel == 0) break;
+            dell = ref_delta(rangel - 1, code, nL, apl);
+            leftChild = split;
+            if (leftChild != rangel) leftChild = nL + leftChild;
+            for (int d = 0; d < 3; ++d) {
+                bmax[d] = jl_max(KEY(leftChild).max[d], bmax[d]);
+                bmin[d] = jl_min(KEY(leftChild).min[d], bmin[d]);
+            }
+        }
+        int32_t q = (delr < dell) ? ranger : rangel;
+        int32_t parent = nL + q;
+        int32_t skip;
+        if (ranger == nL) {
+            skip = 0;
+        } else {
+            int32_t r = ranger + 1;
+            skip = (delr < ref_delta(r, code, nL, apl)) ? r : nL + r;
+        }
+        for (int d = 0; d < 3; ++d) { KEY(parent).min[d] = bmin[d]; KEY(parent).max[d] = bmax[d]; }
+        KEY(parent).left = leftChild;
+        KEY(parent).skip = skip;
+        i = parent;
+        if (i == nL + 1) return;
+    }
+}
+
+int ref_tree(const float* xyz, int32_t n, float r, int32_t apl, int32_t order, int32_t boxes,
+             int32_t overwrite_root, ref_key* keys, int64_t nkeys, int32_t* idx_sorted,
+             int32_t* code_sorted, float* pos_sorted, int32_t* perm) {
+    int32_t nL = 0, nB = 0;
+    int st = ref_spec(n, apl, &nL, &nB);
+    if (st != REF_OK) return st;
+    int64_t need = 2LL * nL - 1;
+    if (boxes == REF_BOX_LEAF && (int64_t)n - 1 < need) return REF_ERR_SPEC; /* BoundsError in the reference */
+    if (nkeys < need) return REF_ERR_ARG;
+
+    int32_t* codes = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t* store = (int32_t*)calloc((size_t)nB, sizeof(int32_t));
+    if (!codes || !store) { free(codes); free(store); return REF_ERR_NOMEM; }
+    st = (order == REF_ORDER_SPATIAL) ? ref_morton_spatial(xyz, n, codes)
+                                      : ref_morton_reference(xyz, n, codes);
+    if (st == REF_OK) st = ref_sortperm(codes, n, perm);
+    if (st != REF_OK) { free(codes); free(store); return st; }
+
+    for (int32_t k = 0; k < n; ++k) {
+        int32_t o = perm[k];
+        idx_sorted[k] = o + 1;
+        code_sorted[k] = codes[o];
+        for (int d = 0; d < 3; ++d) pos_sorted[3 * k + d] = xyz[3 * o + d];
+    }
+    free(codes);
+
+    memset(keys, 0, sizeof(ref_key) * (size_t)nkeys);
+    /* leafcluster_primitives (:376-410) uses r/2, cluster_primitives (:341-375) r. */
+    float h = (boxes == REF_BOX_LEAF) ? r / 2.0f : r;
+    for (int32_t leaf = 1; leaf <= nL; ++leaf) {
+        int32_t bird = (leaf - 1) * apl; /* 0-based first atom */
+        ref_key* k = &KEY(leaf);
+        for (int d = 0; d < 3; ++d) {
+            k->min[d] = pos_sorted[3 * bird + d] - h;
+            k->max[d] = pos_sorted[3 * bird + d] + h;
+        }
+        for (int32_t i = 0; i < apl; ++i) {
+            int32_t a = bird + i;
+            for (int d = 0; d < 3; ++d) {
+                k->min[d] = jl_min(k->min[d], pos_sorted[3 * a + d] - h);
+                k->max[d] = jl_max(k->max[d], pos_sorted[3 * a + d] + h);
+            }
+        }
+        k->left = 0;
+        k->skip = 0;
+    }
+    /* bounding_volume_hierarchy! (:849-860): one task per leaf; running them in
+     * leaf order is one valid interleaving of the CAS protocol. */
+    for (int32_t i = 1; i <= nL; ++i) bvh_interior(keys, store, i, nL, code_sorted, apl);
+    if (overwrite_root) {
+        for (int d = 0; d < 3; ++d) { KEY(nL + 1).min[d] = 0.0f; KEY(nL + 1).max[d] = 1.0f; }
+    }
+    free(store);
+    return REF_OK;
+}
+
+/* ------------------------------------------------------------------ traversal */
+
+static inline int aabb_overlap(const ref_key* a, const ref_key* b) {
+    /* aabb_overlap_test (BVHTraverse.jl:1094-1098): strict, all three axes. */
+    int ok = 1;
+    for (int d = 0; d < 3; ++d) ok &= (a->min[d] < b->max[d]) & (a->max[d] > b->min[d]);
+    return ok;
+}
+
+#define EMIT(I, J, D)                                          \
+    do {                                                       \
+        if (count < cap) { pi[count] = (I); pj[count] = (J); pd[count] = (D); } \
+        ++count;                                               \
+    } while (0)
+
+int64_t ref_leaf_traverse(const ref_key* keys, const int32_t* idx, const float* pos, int32_t nL,
+                          int32_t apl, float r, int32_t* pi, int32_t* pj, float* pd, int64_t cap) {
+    const float r2 = r * r;
+    int64_t count = 0;
+    for (int32_t q = 1; q <= nL; ++q) {
+        const ref_key* ql = &KEY(q);
+        int32_t A = (q - 1) * apl;
+        /* onecluster_proximitytest! (:1021-1040) */
+        for (int32_t i = 0; i < apl - 1; ++i)
+            for (int32_t j = i + 1; j < apl; ++j) {
+                float d2 = ref_dist2(&pos[3 * (A + i)], &pos[3 * (A + j)]);
+                if (d2 < r2) EMIT(idx[A + i], idx[A + j], sqrtf(d2));
+            }
+        int32_t t = ql->skip;
+        while (t != 0) {
+            const ref_key* node = &KEY(t);
+            if (aabb_overlap(ql, node)) {
+                if (node->left == 0) {
+                    int32_t B = (t - 1) * apl;
+                    /* twocluster_proximitytest! (:1042-1055) */
+                    for (int32_t i = 0; i < apl; ++i)
+                        for (int32_t j = 0; j < apl; ++j) {
+                            float d2 = ref_dist2(&pos[3 * (A + i)], &pos[3 * (B + j)]);
+                            if (d2 < r2) EMIT(idx[A + i], idx[B + j], sqrtf(d2));
+                        }
+                    t = node->skip;
+                } else {
+                    t = node->left;
+                }
+            } else {
+                t = node->skip;
+            }
+        }
+    }
+    return count;
+}
+
+static inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static inline void hash_one(int32_t i, int32_t j, float d, uint64_t* h0, uint64_t* h1) {
+    uint32_t a = (uint32_t)(i < j ? i : j);
+    uint32_t b = (uint32_t)(i < j ? j : i);
+    uint32_t db;
+    memcpy(&db, &d, 4);
+    uint64_t k = ((uint64_t)a << 32) | (uint64_t)b;
+    uint64_t x = mix64(k ^ ((uint64_t)db * 0xD6E8FEB86659FD93ull));
+    uint64_t y = mix64(x ^ ((uint64_t)db << 21) ^ 0x5851F42D4C957F2Dull);
+    *h0 += x;
+    *h1 += y;
+}
+
+void ref_pair_hash(const int32_t* pi, const int32_t* pj, const float* pd, int64_t np,
+                   uint64_t hash_out[2]) {
+    uint64_t h0 = 0, h1 = 0;
+    for (int64_t k = 0; k < np; ++k) hash_one(pi[k], pj[k], pd[k], &h0, &h1);
+    hash_out[0] = h0;
+    hash_out[1] = h1;
+}
+
+int64_t ref_leaf_traverse_hash(const ref_key* keys, const int32_t* idx, const float* pos,
+                               int32_t nL, int32_t apl, float r, uint64_t hash_out[2]) {
+    const float r2 = r * r;
+    int64_t total = 0;
+    uint64_t H0 = 0, H1 = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total, H0, H1)
+    for (int32_t q = 1; q <= nL; ++q) {
+        const ref_key* ql = &KEY(q);
+        int32_t A = (q - 1) * apl;
+        uint64_t h0 = 0, h1 = 0;
+        int64_t c = 0;
+        for (int32_t i = 0; i < apl - 1; ++i)
+            for (int32_t j = i + 1; j < apl; ++j) {
+                float d2 = ref_dist2(&pos[3 * (A + i)], &pos[3 * (A + j)]);
+                if (d2 < r2) { hash_one(idx[A + i], idx[A + j], sqrtf(d2), &h0, &h1); ++c; }
+            }
+        int32_t t = ql->skip;
+        while (t != 0) {
+            const ref_key* node = &KEY(t);
+            if (aabb_overlap(ql, node)) {
+                if (node->left == 0) {
+                    int32_t B = (t - 1) * apl;
+                    for (int32_t i = 0; i < apl; ++i)
+                        for (int32_t j = 0; j < apl; ++j) {
+                            float d2 = ref_dist2(&pos[3 * (A + i)], &pos[3 * (B + j)]);
+                            if (d2 < r2) { hash_one(idx[A + i], idx[B + j], sqrtf(d2), &h0, &h1); ++c; }
+                        }
+                    t = node->skip;
+                } else {
+                    t = node->left;
+                }
+            } else {
+                t = node->skip;
+            }
+        }
+        total += c;
+        H0 += h0;
+        H1 += h1;
+    }
+    hash_out[0] = H0;
+    hash_out[1] = H1;
+    return total;
+}
+
+int64_t ref_atom_traverse(const ref_key* keys, const int32_t* idx, const float* pos, int32_t n,
+                          int32_t apl, float r, int32_t* pi, int32_t* pj, float* pd, int64_t cap) {
+    /* neighbor_traverse (:1125-1183): queries 1..N-1 start at their own leaf
+     * ceil(q/apl); point-in-box test overlap_test (:1089-1092); a leaf emits
+     * subjects s with q < s (proximity_test!, :1057-1086). */
+    const float r2 = r * r;
+    int64_t count = 0;
+    for (int32_t qi = 1; qi <= n - 1; ++qi) {
+        const float* p = &pos[3 * (qi - 1)];
+        int32_t t = (qi + apl - 1) / apl;
+        while (t != 0) {
+            const ref_key* node = &KEY(t);
+            int in = 1;
+            for (int d = 0; d < 3; ++d) in &= (node->min[d] < p[d]) & (p[d] < node->max[d]);
+            if (in) {
+                if (node->left == 0) {
+                    int32_t low = (t - 1) * apl + 1;
+                    for (int32_t e = 1; e <= apl; ++e) {
+                        int32_t s = low + e - 1;
+                        if (qi < e + low && idx[qi - 1] != idx[s - 1]) {
+                            float d2 = ref_dist2(p, &pos[3 * (s - 1)]);
+                            if (d2 < r2) EMIT(idx[qi - 1], idx[s - 1], sqrtf(d2));
+                        }
+                    }
+                    t = node->skip;
+                } else {
+                    t = node->left;
+                }
+            } else {
+                t = node->skip;
+            }
+        }
+    }
+    return count;
+}
+
+int64_t ref_brute_pairs(const float* xyz, int32_t n, float r, int32_t criterion, int32_t* pi,
+                        int32_t* pj, float* pd, int64_t cap) {
+    const float r2 = r * r;
+    int64_t count = 0;
+    for (int32_t i = 0; i < n - 1; ++i)
+        for (int32_t j = i + 1; j < n; ++j) {
+            float d2 = ref_dist2(&xyz[3 * i], &xyz[3 * j]);
+            float d = sqrtf(d2);
+            int hit = (criterion == 0) ? (d2 < r2) : (d < r);
+            if (hit) EMIT(i + 1, j + 1, d);
+        }
+    return count;
+}
+
+/* --------------------------------------------------------------- FP64 physics */
+
+static inline void pair_force(const ref_md_params* p, const double* xi, const double* xj,
+                              double qi, double qj, double fij[3], double* u, int* hit) {
+    double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+    double r2 = dx * dx + dy * dy + dz * dz;
+    *hit = 0;
+    if (!(r2 < p->cutoff * p->cutoff)) return;
+    *hit = 1;
+    double inv_r2 = 1.0 / r2;
+    double s2 = p->sigma * p->sigma * inv_r2;
+    double s6 = s2 * s2 * s2;
+    double fmag = 24.0 * p->epsilon * inv_r2 * (2.0 * s6 * s6 - s6);
+    double e = 4.0 * p->epsilon * (s6 * s6 - s6);
+    if (p->coulomb_k != 0.0) {
+        double inv_r = 1.0 / sqrt(r2);
+        double kqq = p->coulomb_k * qi * qj;
+        fmag += kqq * inv_r * inv_r2;
+        e += kqq * inv_r;
+    }
+    fij[0] = fmag * dx;
+    fij[1] = fmag * dy;
+    fij[2] = fmag * dz;
+    *u = e;
+}
+
+int64_t ref_forces(const ref_md_params* p, int32_t n, const double* x, const double* q,
+                   double* f, double* energy) {
+    /* Cell list with cells >= cutoff over the bounding box of x. */
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) { lo[d] = INFINITY; hi[d] = -INFINITY; }
+    for (int32_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            if (x[3 * i + d] < lo[d]) lo[d] = x[3 * i + d];
+            if (x[3 * i + d] > hi[d]) hi[d] = x[3 * i + d];
+        }
+    int nc[3];
+    double cs[3];
+    int64_t ncell = 1;
+    for (int d = 0; d < 3; ++d) {
+        double ext = hi[d] - lo[d];
+        int c = (int)floor(ext / p->cutoff);
+        if (c < 1) c = 1;
+        if (c > 1024) c = 1024;
+        nc[d] = c;
+        cs[d] = (ext > 0) ? ext / c : 1.0;
+        ncell *= c;
+    }
+    int32_t* head = (int32_t*)malloc(sizeof(int32_t) * (size_t)ncell);
+    int32_t* next = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t* cell = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    if (!head || !next || !cell) { free(head); free(next); free(cell); return REF_ERR_NOMEM; }
+    for (int64_t c = 0; c < ncell; ++c) head[c] = -1;
+    for (int32_t i = n - 1; i >= 0; --i) {
+        int ci[3];
+        for (int d = 0; d < 3; ++d) {
+            int c = (int)floor((x[3 * i + d] - lo[d]) / cs[d]);
+            if (c < 0) c = 0;
+            if (c >= nc[d]) c = nc[d] - 1;
+            ci[d] = c;
+        }
+        int32_t id = (ci[2] * nc[1] + ci[1]) * nc[0] + ci[0];
+        cell[i] = id;
+        next[i] = head[id];
+        head[id] = i;
+    }
+    memset(f, 0, sizeof(double) * 3 * (size_t)n);
+    double U = 0.0;
+    int64_t npairs = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        int32_t id = cell[i];
+        int cx = id % nc[0], cy = (id / nc[0]) % nc[1], cz = id / (nc[0] * nc[1]);
+        for (int oz = -1; oz <= 1; ++oz)
+            for (int oy = -1; oy <= 1; ++oy)
+                for (int ox = -1; ox <= 1; ++ox) {
+                    int X = cx + ox, Y = cy + oy, Z = cz + oz;
+                    if (X < 0 || Y < 0 || Z < 0 || X >= nc[0] || Y >= nc[1] || Z >= nc[2]) continue;
+                    for (int32_t j = head[(Z * nc[1] + Y) * nc[0] + X]; j >= 0; j = next[j]) {
+                        if (j <= i) continue;
+                        double fij[3], u;
+                        int hit;
+                        pair_force(p, &x[3 * i], &x[3 * j], q ? q[i] : 0.0, q ? q[j] : 0.0, fij, &u, &hit);
+                        if (!hit) continue;
+                        ++npairs;
+                        U += u;
+                        for (int d = 0; d < 3; ++d) { f[3 * i + d] += fij[d]; f[3 * j + d] -= fij[d]; }
+                    }
+                }
+    }
+    free(head); free(next); free(cell);
+    if (energy) *energy = U;
+    return npairs;
+}
+
+static void reflect(const ref_md_params* p, int32_t n, double* x, double* v) {
+    /* boundary_reflect! (Simulator.jl:81-111): clamp to the wall, flip v. */
+    for (int32_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            if (p->box_lo[d] > x[3 * i + d]) { v[3 * i + d] *= -1.0; x[3 * i + d] = p->box_lo[d]; }
+            if (p->box_hi[d] < x[3 * i + d]) { v[3 * i + d] *= -1.0; x[3 * i + d] = p->box_hi[d]; }
+        }
+}
+
+int ref_md_run(const ref_md_params* p, int32_t n, double* x, double* v, double* f,
+               const double* q, const double* m, int64_t steps) {
+    const double h = 0.5 * p->dt;
+    for (int64_t s = 0; s < steps; ++s) {
+        for (int32_t i = 0; i < n; ++i) {
+            double im = m ? 1.0 / m[i] : 1.0;
+            for (int d = 0; d < 3; ++d) {
+                v[3 * i + d] += h * f[3 * i + d] * im;
+                x[3 * i + d] += p->dt * v[3 * i + d];
+            }
+        }
+        reflect(p, n, x, v);
+        int64_t st = ref_forces(p, n, x, q, f, NULL);
+        if (st < 0) return (int)st;
+        for (int32_t i = 0; i < n; ++i) {
+            double im = m ? 1.0 / m[i] : 1.0;
+            for (int d = 0; d < 3; ++d) v[3 * i + d] += h * f[3 * i + d] * im;
+        }
+    }
+    return REF_OK;
+}
+
+/* CPU baseline: leaf BVH every `rebuild` steps + FP64 forces over the half list. */
+typedef struct { int32_t* i; int32_t* j; int64_t n, cap; } pairbuf;
+
+static int pb_push(pairbuf* b, int32_t i, int32_t j) {
+    if (b->n == b->cap) {
+        int64_t nc = b->cap ? 2 * b->cap : 1024;
+        int32_t* ni = (int32_t*)realloc(b->i, sizeof(int32_t) * (size_t)nc);
+        if (!ni) return -1;
+        b->i = ni;
+        int32_t* nj = (int32_t*)realloc(b->j, sizeof(int32_t) * (size_t)nc);
+        if (!nj) return -1;
+        b->j = nj;
+        b->cap = nc;
+    }
+    b->i[b->n] = i;
+    b->j[b->n] = j;
+    ++b->n;
+    return 0;
+}
+
+static int64_t build_half_list(const double* x, int32_t n, float rl, int32_t apl, int32_t order,
+                               pairbuf* out) {
+    int32_t nL, nB;
+    if (ref_spec(n, apl, &nL, &nB) != REF_OK) return REF_ERR_SPEC;
+    int64_t nkeys = 2LL * nL - 1;
+    float* xf = (float*)malloc(sizeof(float) * 3 * (size_t)n);
+    float* ps = (float*)malloc(sizeof(float) * 3 * (size_t)n);
+    int32_t* idx = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t* code = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t* perm = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    ref_key* keys = (ref_key*)malloc(sizeof(ref_key) * (size_t)(nkeys > n ? nkeys : n));
+    if (!xf || !ps || !idx || !code || !perm || !keys) return REF_ERR_NOMEM;
+    for (int64_t k = 0; k < 3LL * n; ++k) xf[k] = (float)x[k];
+    int st = ref_tree(xf, n, rl, apl, order, REF_BOX_LEAF, 1, keys, nkeys, idx, code, ps, perm);
+    if (st != REF_OK) return st;
+    const float r2 = rl * rl;
+    int nt = ref_num_threads();
+    pairbuf* bufs = (pairbuf*)calloc((size_t)nt, sizeof(pairbuf));
+    /* leafneighbor_traverse (:1236-1323): strided query chunks per thread. */
+#pragma omp parallel
+    {
+#ifdef _OPENMP
+        int tid = omp_get_thread_num();
+        int nth = omp_get_num_threads();
+#else
+        int tid = 0, nth = 1;
+#endif
+        pairbuf* b = &bufs[tid];
+        for (int32_t q = 1 + tid; q <= nL; q += nth) {
+            const ref_key* ql = &KEY(q);
+            int32_t A = (q - 1) * apl;
+            for (int32_t i = 0; i < apl - 1; ++i)
+                for (int32_t j = i + 1; j < apl; ++j)
+                    if (ref_dist2(&ps[3 * (A + i)], &ps[3 * (A + j)]) < r2)
+                        pb_push(b, idx[A + i] - 1, idx[A + j] - 1);
+            int32_t t = ql->skip;
+            while (t != 0) {
+                const ref_key* node = &KEY(t);
+                if (aabb_overlap(ql, node)) {
+                    if (node->left == 0) {
+                        int32_t B = (t - 1) * apl;
+                        for (int32_t i = 0; i < apl; ++i)
+                            for (int32_t j = 0; j < apl; ++j)
+                                if (ref_dist2(&ps[3 * (A + i)], &ps[3 * (B + j)]) < r2)
+                                    pb_push(b, idx[A + i] - 1, idx[B + j] - 1);
+                        t = node->skip;
+                    } else {
+                        t = node->left;
+                    }
+                } else {
+                    t = node->skip;
+                }
+            }
+        }
+    }
+    out->n = 0;
+    for (int t = 0; t < nt; ++t) {
+        for (int64_t k = 0; k < bufs[t].n; ++k) pb_push(out, bufs[t].i[k], bufs[t].j[k]);
+        free(bufs[t].i);
+        free(bufs[t].j);
+    }
+    free(bufs); free(xf); free(ps); free(idx); free(code); free(perm); free(keys);
+    return out->n;
+}
+
+static void forces_from_list(const ref_md_params* p, int32_t n, const double* x, const double* q,
+                             const pairbuf* L, double* f, double* fth, int nt) {
+#pragma omp parallel
+    {
+#ifdef _OPENMP
+        int tid = omp_get_thread_num();
+#else
+        int tid = 0;
+#endif
+        double* ft = fth + (size_t)tid * 3 * (size_t)n;
+        memset(ft, 0, sizeof(double) * 3 * (size_t)n);
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < L->n; ++k) {
+            int32_t i = L->i[k], j = L->j[k];
+            double fij[3], u;
+            int hit;
+            pair_force(p, &x[3 * i], &x[3 * j], q ? q[i] : 0.0, q ? q[j] : 0.0, fij, &u, &hit);
+            if (!hit) continue;
+            for (int d = 0; d < 3; ++d) { ft[3 * i + d] += fij[d]; ft[3 * j + d] -= fij[d]; }
+        }
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < 3LL * n; ++k) {
+            double s = 0.0;
+            for (int t = 0; t < nt; ++t) s += fth[(size_t)t * 3 * (size_t)n + (size_t)k];
+            f[k] = s;
+        }
+    }
+}
+
+int64_t ref_md_run_bvh(const ref_md_params* p, int32_t n, double* x, double* v, double* f,
+                       const double* q, const double* m, int64_t steps, int32_t rebuild,
+                       double skin, int32_t apl, int32_t order) {
+    int nt = ref_num_threads();
+    double* fth = (double*)malloc(sizeof(double) * 3 * (size_t)n * (size_t)nt);
+    if (!fth) return REF_ERR_NOMEM;
+    pairbuf L = {0};
+    const float rl = (float)(p->cutoff + skin);
+    const double h = 0.5 * p->dt;
+    int64_t st = build_half_list(x, n, rl, apl, order, &L);
+    if (st < 0) { free(fth); return st; }
+    forces_from_list(p, n, x, q, &L, f, fth, nt);
+    for (int64_t s = 0; s < steps; ++s) {
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; ++i) {
+            double im = m ? 1.0 / m[i] : 1.0;
+            for (int d = 0; d < 3; ++d) {
+                v[3 * i + d] += h * f[3 * i + d] * im;
+                x[3 * i + d] += p->dt * v[3 * i + d];
+            }
+        }
+        reflect(p, n, x, v);
+        if (rebuild > 0 && (s + 1) % rebuild == 0) {
+            st = build_half_list(x, n, rl, apl, order, &L);
+            if (st < 0) break;
+        }
+        forces_from_list(p, n, x, q, &L, f, fth, nt);
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; ++i) {
+            double im = m ? 1.0 / m[i] : 1.0;
+            for (int d = 0; d < 3; ++d) v[3 * i + d] += h * f[3 * i + d] * im;
+        }
+    }
+    int64_t np = L.n;
+    free(L.i); free(L.j); free(fth);
+    return st < 0 ? st : np;
+}

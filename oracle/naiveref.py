@@ -1,0 +1,285 @@
+"""ctypes wrapper of the CPU oracle ``libnaiveref`` (test infrastructure only).
+
+The oracle restates the NaiveDynamics.jl hot path in plain C (see naiveref.c for
+the reference file:line of every function).  It is the checker for the GPU
+library: only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module.  The product path never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libnaiveref.so")
+
+REF_ORDER_REFERENCE = 0
+REF_ORDER_SPATIAL = 1
+REF_BOX_LEAF = 0
+REF_BOX_ATOM = 1
+
+KEY_DTYPE = np.dtype([("min", np.float32, 3), ("max", np.float32, 3),
+                      ("left", np.int32), ("skip", np.int32)])
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class RefMDParams(ctypes.Structure):
+    _fields_ = [("sigma", ctypes.c_double), ("epsilon", ctypes.c_double),
+                ("coulomb_k", ctypes.c_double), ("cutoff", ctypes.c_double),
+                ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3),
+                ("dt", ctypes.c_double)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc, no fast-math, no FMA contraction)."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t)) if a is not None else None
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB_PATH)
+            i32p = ctypes.POINTER(ctypes.c_int32)
+            f32p = ctypes.POINTER(ctypes.c_float)
+            f64p = ctypes.POINTER(ctypes.c_double)
+            u64p = ctypes.POINTER(ctypes.c_uint64)
+            L.ref_spec.argtypes = [ctypes.c_int64, ctypes.c_int64, i32p, i32p]
+            L.ref_spec.restype = ctypes.c_int
+            L.ref_morton_reference.argtypes = [f32p, ctypes.c_int64, i32p]
+            L.ref_morton_reference.restype = ctypes.c_int
+            L.ref_morton_spatial.argtypes = [f32p, ctypes.c_int64, i32p]
+            L.ref_morton_spatial.restype = ctypes.c_int
+            L.ref_sortperm.argtypes = [i32p, ctypes.c_int64, i32p]
+            L.ref_sortperm.restype = ctypes.c_int
+            L.ref_delta.argtypes = [ctypes.c_int32, i32p, ctypes.c_int32, ctypes.c_int32]
+            L.ref_delta.restype = ctypes.c_int32
+            L.ref_tree.argtypes = [f32p, ctypes.c_int32, ctypes.c_float, ctypes.c_int32,
+                                   ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                   ctypes.c_int64, i32p, i32p, f32p, i32p]
+            L.ref_tree.restype = ctypes.c_int
+            for name in ("ref_leaf_traverse", "ref_atom_traverse"):
+                fn = getattr(L, name)
+                fn.argtypes = [ctypes.c_void_p, i32p, f32p, ctypes.c_int32, ctypes.c_int32,
+                               ctypes.c_float, i32p, i32p, f32p, ctypes.c_int64]
+                fn.restype = ctypes.c_int64
+            L.ref_leaf_traverse_hash.argtypes = [ctypes.c_void_p, i32p, f32p, ctypes.c_int32,
+                                                 ctypes.c_int32, ctypes.c_float, u64p]
+            L.ref_leaf_traverse_hash.restype = ctypes.c_int64
+            L.ref_brute_pairs.argtypes = [f32p, ctypes.c_int32, ctypes.c_float, ctypes.c_int32,
+                                          i32p, i32p, f32p, ctypes.c_int64]
+            L.ref_brute_pairs.restype = ctypes.c_int64
+            L.ref_pair_hash.argtypes = [i32p, i32p, f32p, ctypes.c_int64, u64p]
+            L.ref_pair_hash.restype = None
+            L.ref_forces.argtypes = [ctypes.POINTER(RefMDParams), ctypes.c_int32, f64p, f64p,
+                                     f64p, f64p]
+            L.ref_forces.restype = ctypes.c_int64
+            L.ref_md_run.argtypes = [ctypes.POINTER(RefMDParams), ctypes.c_int32, f64p, f64p,
+                                     f64p, f64p, f64p, ctypes.c_int64]
+            L.ref_md_run.restype = ctypes.c_int
+            L.ref_md_run_bvh.argtypes = [ctypes.POINTER(RefMDParams), ctypes.c_int32, f64p,
+                                         f64p, f64p, f64p, f64p, ctypes.c_int64, ctypes.c_int32,
+                                         ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
+            L.ref_md_run_bvh.restype = ctypes.c_int64
+            L.ref_num_threads.argtypes = []
+            L.ref_num_threads.restype = ctypes.c_int
+            _lib = L
+    return _lib
+
+
+def _check(st):
+    if st != 0:
+        raise OracleError(f"oracle status {st}")
+
+
+def _xyz(xyz):
+    a = np.ascontiguousarray(np.asarray(xyz, dtype=np.float32).reshape(-1, 3))
+    return a
+
+
+def spec(n, apl):
+    """SpheresBVHSpecs checks; returns (leaves, branches)."""
+    nl = ctypes.c_int32()
+    nb = ctypes.c_int32()
+    _check(lib().ref_spec(n, apl, ctypes.byref(nl), ctypes.byref(nb)))
+    return nl.value, nb.value
+
+
+def morton_reference(xyz):
+    a = _xyz(xyz)
+    out = np.empty(a.shape[0], np.int32)
+    _check(lib().ref_morton_reference(_p(a, ctypes.c_float), a.shape[0], _p(out, ctypes.c_int32)))
+    return out
+
+
+def morton_spatial(xyz):
+    a = _xyz(xyz)
+    out = np.empty(a.shape[0], np.int32)
+    _check(lib().ref_morton_spatial(_p(a, ctypes.c_float), a.shape[0], _p(out, ctypes.c_int32)))
+    return out
+
+
+def sortperm(codes):
+    c = np.ascontiguousarray(codes, dtype=np.int32)
+    out = np.empty(c.shape[0], np.int32)
+    _check(lib().ref_sortperm(_p(c, ctypes.c_int32), c.shape[0], _p(out, ctypes.c_int32)))
+    return out
+
+
+def tree(xyz, r, apl, order=REF_ORDER_REFERENCE, boxes=REF_BOX_LEAF, overwrite_root=True):
+    """leafTreeData / TreeData.  Returns dict(keys, index, code, position, perm)."""
+    a = _xyz(xyz)
+    n = a.shape[0]
+    nl, _ = spec(n, apl)
+    nkeys = (n - 1) if boxes == REF_BOX_LEAF else (2 * nl - 1)
+    nkeys = max(nkeys, 2 * nl - 1)
+    keys = np.zeros(nkeys, KEY_DTYPE)
+    idx = np.empty(n, np.int32)
+    code = np.empty(n, np.int32)
+    pos = np.empty((n, 3), np.float32)
+    perm = np.empty(n, np.int32)
+    _check(lib().ref_tree(_p(a, ctypes.c_float), n, np.float32(r), apl, order, boxes,
+                          1 if overwrite_root else 0, keys.ctypes.data, nkeys,
+                          _p(idx, ctypes.c_int32), _p(code, ctypes.c_int32),
+                          _p(pos, ctypes.c_float), _p(perm, ctypes.c_int32)))
+    if boxes == REF_BOX_LEAF:
+        keys = keys[: n - 1]
+    return dict(keys=keys, index=idx, code=code, position=pos, perm=perm, leaves=nl)
+
+
+def _pairs_call(fn, *args, cap_hint=1024):
+    cap = cap_hint
+    while True:
+        pi = np.empty(cap, np.int32)
+        pj = np.empty(cap, np.int32)
+        pd = np.empty(cap, np.float32)
+        cnt = fn(*args, _p(pi, ctypes.c_int32), _p(pj, ctypes.c_int32), _p(pd, ctypes.c_float), cap)
+        if cnt < 0:
+            raise OracleError(f"oracle status {cnt}")
+        if cnt <= cap:
+            return pi[:cnt].copy(), pj[:cnt].copy(), pd[:cnt].copy()
+        cap = int(cnt)
+
+
+def leaf_traverse(t, r, apl):
+    """leafneighbor_traverse in serial order over a tree from tree(..., boxes=LEAF)."""
+    keys = np.ascontiguousarray(t["keys"])
+    return _pairs_call(lib().ref_leaf_traverse, keys.ctypes.data, _p(t["index"], ctypes.c_int32),
+                       _p(t["position"], ctypes.c_float), t["leaves"], apl, np.float32(r))
+
+
+def leaf_traverse_hash(t, r, apl):
+    keys = np.ascontiguousarray(t["keys"])
+    h = np.zeros(2, np.uint64)
+    cnt = lib().ref_leaf_traverse_hash(keys.ctypes.data, _p(t["index"], ctypes.c_int32),
+                                       _p(t["position"], ctypes.c_float), t["leaves"], apl,
+                                       np.float32(r), _p(h, ctypes.c_uint64))
+    return int(cnt), (int(h[0]), int(h[1]))
+
+
+def atom_traverse(t, r, apl):
+    keys = np.ascontiguousarray(t["keys"])
+    n = t["index"].shape[0]
+    return _pairs_call(lib().ref_atom_traverse, keys.ctypes.data, _p(t["index"], ctypes.c_int32),
+                       _p(t["position"], ctypes.c_float), n, apl, np.float32(r))
+
+
+def leafbuild_traverse_bvh(xyz, r, apl, order=REF_ORDER_REFERENCE):
+    t = tree(xyz, r, apl, order=order, boxes=REF_BOX_LEAF)
+    return leaf_traverse(t, r, apl)
+
+
+def build_traverse_bvh(xyz, r, apl, order=REF_ORDER_REFERENCE):
+    t = tree(xyz, r, apl, order=order, boxes=REF_BOX_ATOM)
+    return atom_traverse(t, r, apl)
+
+
+def brute_pairs(xyz, r, criterion=0):
+    a = _xyz(xyz)
+    return _pairs_call(lib().ref_brute_pairs, _p(a, ctypes.c_float), a.shape[0], np.float32(r),
+                       criterion)
+
+
+def pair_hash(pi, pj, pd):
+    pi = np.ascontiguousarray(pi, np.int32)
+    pj = np.ascontiguousarray(pj, np.int32)
+    pd = np.ascontiguousarray(pd, np.float32)
+    h = np.zeros(2, np.uint64)
+    lib().ref_pair_hash(_p(pi, ctypes.c_int32), _p(pj, ctypes.c_int32), _p(pd, ctypes.c_float),
+                        pi.shape[0], _p(h, ctypes.c_uint64))
+    return int(h[0]), int(h[1])
+
+
+def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, box_lo=(0, 0, 0),
+              box_hi=(1, 1, 1), dt=1e-3):
+    p = RefMDParams()
+    p.sigma, p.epsilon, p.coulomb_k, p.cutoff, p.dt = sigma, epsilon, coulomb_k, cutoff, dt
+    for d in range(3):
+        p.box_lo[d] = box_lo[d]
+        p.box_hi[d] = box_hi[d]
+    return p
+
+
+def forces(p, x, q=None):
+    """FP64 LJ + Coulomb forces and energy (cell list).  Returns (f, energy, npairs)."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+    qq = None if q is None else np.ascontiguousarray(q, np.float64)
+    f = np.empty_like(x)
+    e = ctypes.c_double()
+    n = lib().ref_forces(ctypes.byref(p), x.shape[0], _p(x, ctypes.c_double),
+                         _p(qq, ctypes.c_double), _p(f, ctypes.c_double), ctypes.byref(e))
+    if n < 0:
+        raise OracleError(f"oracle status {n}")
+    return f, e.value, int(n)
+
+
+def md_run(p, x, v, q=None, m=None, steps=1):
+    """FP64 kick-drift-kick run from (x, v); returns (x, v, f)."""
+    x = np.array(x, np.float64).reshape(-1, 3)
+    v = np.array(v, np.float64).reshape(-1, 3)
+    qq = None if q is None else np.ascontiguousarray(q, np.float64)
+    mm = None if m is None else np.ascontiguousarray(m, np.float64)
+    f, _, _ = forces(p, x, qq)
+    _check(lib().ref_md_run(ctypes.byref(p), x.shape[0], _p(x, ctypes.c_double),
+                            _p(v, ctypes.c_double), _p(f, ctypes.c_double),
+                            _p(qq, ctypes.c_double), _p(mm, ctypes.c_double), steps))
+    return x, v, f
+
+
+def md_run_bvh(p, x, v, q=None, m=None, steps=1, rebuild=10, skin=0.3, apl=4,
+               order=REF_ORDER_REFERENCE):
+    """CPU baseline run (leaf BVH + FP64 forces, OpenMP).  Returns (x, v, f, npairs)."""
+    x = np.array(x, np.float64).reshape(-1, 3)
+    v = np.array(v, np.float64).reshape(-1, 3)
+    f = np.zeros_like(x)
+    qq = None if q is None else np.ascontiguousarray(q, np.float64)
+    mm = None if m is None else np.ascontiguousarray(m, np.float64)
+    n = lib().ref_md_run_bvh(ctypes.byref(p), x.shape[0], _p(x, ctypes.c_double),
+                             _p(v, ctypes.c_double), _p(f, ctypes.c_double),
+                             _p(qq, ctypes.c_double), _p(mm, ctypes.c_double), steps, rebuild,
+                             skin, apl, order)
+    if n < 0:
+        raise OracleError(f"oracle status {n}")
+    return x, v, f, int(n)
+
+
+def num_threads():
+    return int(lib().ref_num_threads())

@@ -1,0 +1,200 @@
+"""GPU forces and dynamics against the FP64 oracle.
+
+Tolerances (stated per result, as the contract requires):
+  * forces: relative L2 error |F32 - F64|_2 / |F64|_2 <= 1e-5, and the per-atom
+    error max_i |dF_i| / max(|F64_i|, 1e-3 rms|F64|) <= 2e-3 (the floor term is
+    dominated by FP32 rounding of individual pair terms for atoms whose net
+    force nearly cancels);
+  * energies: relative error <= 1e-6;
+  * dynamics over 100 steps (dt = 1e-3, rebuild every 10): positions within
+    1e-6 (absolute, box side 17) of the FP64 trajectory -- an FP32 force error
+    of ~1e-6 relative acts for t = 0.1 and the LJ dynamics amplify it.
+"""
+import numpy as np
+import pytest
+
+from conftest import canon
+from helpers import force_errors
+
+pytestmark = pytest.mark.gpu
+
+F_L2_TOL = 1e-5
+F_ATOM_TOL = 2e-3
+
+
+def _config1(nd, charges=False, n=4096, side=17.0, seed=0x4E440001):
+    return nd.synth.lj_system(seed, n, side, 0.8, charges)
+
+
+def test_forces_lj_vs_fp64(nd, oracle):
+    x, _, _ = _config1(nd)
+    f32, u32 = nd.forces(x, None, nd.ForceField(1.0, 1.0, 0.0, 2.5))
+    p = oracle.md_params(cutoff=2.5, box_hi=(17, 17, 17))
+    f64, u64, _ = oracle.forces(p, x)
+    per_atom, l2 = force_errors(f32, f64)
+    print(f"LJ force error: per-atom {per_atom:.3e}  L2 {l2:.3e}  energy {abs(u32-u64)/abs(u64):.3e}")
+    assert l2 <= F_L2_TOL
+    assert per_atom <= F_ATOM_TOL
+    assert abs(u32 - u64) <= 1e-6 * abs(u64)
+
+
+def test_forces_lj_coulomb_vs_fp64(nd, oracle):
+    x, _, q = _config1(nd, charges=True)
+    f32, u32 = nd.forces(x, q, nd.ForceField(1.0, 1.0, 1.0, 2.5))
+    p = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(17, 17, 17))
+    f64, u64, _ = oracle.forces(p, x, q)
+    per_atom, l2 = force_errors(f32, f64)
+    print(f"LJ+C force error: per-atom {per_atom:.3e}  L2 {l2:.3e}  energy {abs(u32-u64)/abs(u64):.3e}")
+    assert l2 <= F_L2_TOL
+    assert per_atom <= F_ATOM_TOL
+    assert abs(u32 - u64) <= 1e-6 * abs(u64)
+
+
+def test_force_calls_with_pair_list(nd, oracle):
+    # force_lennardjones!(force, pairslist, position) + force_coulomb! + sum_forces!
+    x, _, q = _config1(nd, charges=True, n=2048, side=13.5)
+    spec = nd.SpheresBVHSpecs(2.5, len(x), 4)
+    pairs = nd.leafbuild_traverse_bvh(x.astype(np.float32), spec)
+    flj = np.zeros((len(x), 3), np.float32)
+    fc = np.zeros((len(x), 3), np.float32)
+    ulj = nd.force_lennardjones_(flj, pairs, x)
+    uc = nd.force_coulomb_(fc, pairs, q, x)
+    f = nd.sum_forces_(np.zeros_like(flj), flj, fc)
+    p = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(14, 14, 14))
+    f64, u64, _ = oracle.forces(p, x, q)
+    per_atom, l2 = force_errors(f, f64)
+    assert l2 <= F_L2_TOL
+    assert abs((ulj + uc) - u64) <= 1e-6 * abs(u64)
+
+
+def _params(nd, side, coulomb=0.0, rebuild=10, order=1, **kw):
+    return nd.md_params(sigma=1.0, epsilon=1.0, coulomb_k=coulomb, cutoff=2.5, skin=0.3, dt=1e-3,
+                        box_lo=(0, 0, 0), box_hi=(side, side, side), atomsperleaf=4,
+                        rebuild_every=rebuild, order=order, **kw)
+
+
+def test_md_trajectory_vs_fp64(nd, oracle):
+    # plain LJ, 4096 atoms, side 17, 100 steps, rebuild every 10
+    x0, v0, _ = _config1(nd)
+    eng = nd.MDEngine(_params(nd, 17.0), x0, v0)
+    pe0, ke0 = eng.energy()
+    eng.run(100)
+    eng.sync()
+    x, v, f = eng.get()
+    pe1, ke1 = eng.energy()
+    p = oracle.md_params(cutoff=2.5, box_hi=(17, 17, 17), dt=1e-3)
+    xr, vr, fr = oracle.md_run(p, x0, v0, steps=100)
+    dx = np.abs(x - xr).max()
+    dv = np.abs(v - vr).max()
+    print(f"100-step trajectory: max|dx| {dx:.3e}  max|dv| {dv:.3e}")
+    assert dx < 1e-6
+    assert dv < 1e-3
+    # forces at the GPU's final positions vs FP64 forces there
+    f64, u64, _ = oracle.forces(p, x)
+    per_atom, l2 = force_errors(f, f64)
+    assert l2 <= F_L2_TOL
+    e0, e1 = pe0 + ke0, pe1 + ke1
+    print(f"energy: {e0:.6f} -> {e1:.6f} (rel drift {abs(e1-e0)/abs(e0):.2e})")
+    u0 = oracle.forces(p, x0)[1]
+    assert abs(pe0 - u0) <= 1e-6 * abs(u0)
+    assert abs(ke0 - 0.5 * (v0 ** 2).sum()) <= 1e-12 * ke0
+    st = eng.stats()
+    assert st["steps"] == 100 and st["rebuilds"] == 10
+
+
+def test_md_neighbor_list_pair_set(nd, oracle):
+    # The engine's list at a rebuild equals every pair with d^2 < r_list^2 on
+    # the Float32 positions (full list: each pair twice).
+    x0, v0, _ = _config1(nd)
+    eng = nd.MDEngine(_params(nd, 17.0), x0, v0)
+    eng.run(10)   # window 0 done, next run rebuilds
+    eng.run(1)    # rebuild at step 10 + one step
+    x10 = None
+    eng2 = nd.MDEngine(_params(nd, 17.0), x0, v0)
+    eng2.run(10)
+    x10, _, _ = eng2.get()
+    xf = x10.astype(np.float32)
+    b = oracle.brute_pairs(xf, np.float32(2.8), 0)
+    lst = eng.stats()["list_pairs"]
+    assert lst == 2 * len(b[0])
+    # reference-order pair list on the same Float32 positions, bit-exact
+    spec = nd.SpheresBVHSpecs(2.8, len(xf), 4)
+    p = nd.leafbuild_traverse_bvh(xf, spec)
+    t = oracle.tree(xf, 2.8, 4)
+    ri, rj, rd = oracle.leaf_traverse(t, 2.8, 4)
+    assert np.array_equal(p["i"], ri) and np.array_equal(p["j"], rj)
+    assert np.array_equal(p["d"].view(np.int32), rd.view(np.int32))
+    assert np.array_equal(canon(p["i"], p["j"], p["d"]), canon(*b))
+
+
+def test_md_graph_equals_eager_and_deterministic(nd):
+    x0, v0, q = _config1(nd, charges=True, n=2048, side=13.5)
+    a = nd.MDEngine(_params(nd, 13.5, coulomb=1.0), x0, v0, q)
+    a.run(40)
+    xa, va, fa = a.get()
+    b = nd.MDEngine(_params(nd, 13.5, coulomb=1.0), x0, v0, q)
+    for k in (7, 3, 11, 9, 10):
+        b.run(k)
+    xb, vb, fb = b.get()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+    c = nd.MDEngine(_params(nd, 13.5, coulomb=1.0), x0, v0, q)
+    c.run(40)
+    xc, vc, _ = c.get()
+    assert np.array_equal(xa, xc) and np.array_equal(va, vc)
+
+
+def test_md_reference_order_matches_spatial(nd):
+    # The order mode changes only the atom order, not the physics.
+    x0, v0, _ = _config1(nd, n=2048, side=13.5)
+    a = nd.MDEngine(_params(nd, 13.5, order=0), x0, v0)
+    b = nd.MDEngine(_params(nd, 13.5, order=1), x0, v0)
+    a.run(20)
+    b.run(20)
+    xa, _, _ = a.get()
+    xb, _, _ = b.get()
+    assert np.abs(xa - xb).max() < 1e-6
+
+
+def test_md_walls(nd):
+    x0, v0, _ = _config1(nd, n=512, side=8.5)
+    v0 = v0 * 50.0  # fast atoms hit the walls within a few steps
+    eng = nd.MDEngine(_params(nd, 8.5), x0, v0)
+    eng.run(50)
+    x, v, _ = eng.get()
+    assert x.min() >= 0.0 and x.max() <= 8.5
+
+
+def test_simulate_drop_in(nd, oracle):
+    x0, v0, q = _config1(nd, charges=True, n=1024, side=10.7)
+    sys_ = nd.GenericObjectCollection(position=x0, velocity=v0, charge=q)
+    clct = nd.GenericRandomCollector(1024, (0, 0, 0), (10.7, 10.7, 10.7))
+    nd.simulate_(sys_, nd.SimSpec(duration=30, stepwidth=1e-3), clct,
+                 nd.ForceField(1.0, 1.0, 1.0, 2.5))
+    p = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(10.7, 10.7, 10.7), dt=1e-3)
+    xr, vr, fr = oracle.md_run(p, x0, v0, q, steps=30)
+    assert np.abs(sys_.position - xr).max() < 1e-6
+    assert force_errors(sys_.force, fr)[1] <= F_L2_TOL
+
+
+def test_md_masses(nd, oracle):
+    x0, v0, _ = _config1(nd, n=1024, side=10.7)
+    m = 1.0 + np.arange(1024) % 3
+    eng = nd.MDEngine(_params(nd, 10.7), x0, v0, m=m)
+    eng.run(20)
+    x, v, _ = eng.get()
+    p = oracle.md_params(cutoff=2.5, box_hi=(10.7, 10.7, 10.7), dt=1e-3)
+    xr, vr, _ = oracle.md_run(p, x0, v0, m=m, steps=20)
+    assert np.abs(x - xr).max() < 1e-6
+
+
+def test_md_overflow_reported(nd):
+    x0, v0, _ = _config1(nd, n=1024, side=10.7)
+    with pytest.raises(nd.NDError) as e:
+        eng = nd.MDEngine(_params(nd, 10.7, max_neighbors=8), x0, v0)
+        eng.run(10)
+        eng.sync()
+    assert e.value.status == -8
+    # a fresh engine on the same context still works
+    eng = nd.MDEngine(_params(nd, 10.7), x0, v0)
+    eng.run(10)
+    eng.sync()

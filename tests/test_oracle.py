@@ -1,0 +1,252 @@
+"""The CPU oracle against the reference's own known answers and golden vectors.
+
+These run without a GPU.  They pin the oracle before it is trusted as the
+checker of the CUDA path:
+  * test/BVHTraverse.jl:165-220 -- the 8-point hand fixture and its invariants;
+  * test/BVHTraverse.jl:222-287 -- BVH pair list == brute-force pair list over
+    the reference's r / atomsperleaf / N families (seeded stand-ins for the
+    missing data/positions.jld2);
+  * tests/golden/bvh_golden.json -- vectors from an independent pure-Python
+    restatement (tests/golden/make_golden.py).
+"""
+import numpy as np
+import pytest
+
+from conftest import canon
+from helpers import golden_cases, uniform
+
+POSITION8 = np.array([[0.1, 0.1, 0.1], [0.2, 0.2, 0.2], [0.346, 0.98, 0.12], [0.01, 0.76, 0.99],
+                      [0.1111, 0.4, 0.31], [0.234, 0.29, 0.2], [0.11346, 0.918, 0.1276],
+                      [0.061, 0.76, 0.989]], np.float32)
+
+
+def test_position8_traversability(oracle):
+    # test/BVHTraverse.jl:170-211: neighbor_distance=10, atomsperleaf=1, TreeData
+    t = oracle.tree(POSITION8, 10.0, 1, boxes=oracle.REF_BOX_ATOM)
+    keys = t["keys"]
+    assert keys[7]["skip"] == 0                      # keys[8].skip == 0
+    assert all(keys[k]["skip"] != 0 for k in range(7))  # keys[1:7].skip != 0
+    pi, pj, pd = oracle.build_traverse_bvh(POSITION8, 10.0, 1)
+    paired = np.zeros(9, bool)
+    paired[pi] = True
+    paired[pj] = True
+    assert paired[1:].all()                          # every atom paired
+    bi, bj, bd = oracle.brute_pairs(POSITION8, 10.0, criterion=1)
+    assert len(bi) == 28
+    assert np.array_equal(canon(pi, pj, pd), canon(bi, bj, bd))
+
+
+def test_position8_root_contains_scene(oracle):
+    # test/BVHTraverse.jl:213-220 (root box overwritten to [0,1]^3)
+    t = oracle.tree(POSITION8, 10.0, 1, boxes=oracle.REF_BOX_ATOM)
+    root = t["keys"][8]
+    assert np.all(root["min"] < POSITION8) and np.all(POSITION8 < root["max"])
+
+
+def _self_consistent_tree(keys, nl):
+    # is_traversable (test/BVHTraverse.jl:87-116): no self ropes, every node reached
+    for k in range(2 * nl - 1):
+        assert keys[k]["left"] != k + 1 and keys[k]["skip"] != k + 1
+    seen = np.zeros(2 * nl, bool)
+    t = keys[nl]["left"]
+    seen[nl + 1] = True
+    steps = 0
+    while t != 0:
+        seen[t] = True
+        steps += 1
+        assert steps <= 4 * nl
+        t = keys[t - 1]["left"] if keys[t - 1]["left"] != 0 else keys[t - 1]["skip"]
+    assert seen[1:].all()
+
+
+@pytest.mark.parametrize("boxes", [0, 1])
+def test_tree_fully_traversable(oracle, boxes):
+    x = uniform(11, 400)
+    for apl in (2, 4, 5):
+        t = oracle.tree(x, 0.1, apl, boxes=boxes)
+        _self_consistent_tree(t["keys"], t["leaves"])
+
+
+@pytest.mark.parametrize("r", [1e-4, 1e-3, 1e-2, 1e-1, 1.0])
+def test_family_neighbor_distance(oracle, r):
+    # test/BVHTraverse.jl:225-243 (pos5000 -> 2000 seeded points; r up to 1.0)
+    n = 5000 if r < 1.0 else 1500
+    x = uniform(5000, n)
+    bi, bj, bd = oracle.brute_pairs(x, r, criterion=0)
+    for order in (0, 1):
+        li, lj, ld = oracle.leafbuild_traverse_bvh(x, r, 4, order=order)
+        assert np.array_equal(canon(li, lj, ld), canon(bi, bj, bd))
+        ai, aj, ad = oracle.build_traverse_bvh(x, r, 4, order=order)
+        assert np.array_equal(canon(ai, aj, ad), canon(bi, bj, bd))
+
+
+@pytest.mark.parametrize("apl", [2, 4, 5, 10, 20, 1000])
+def test_family_atomsperleaf(oracle, apl):
+    # test/BVHTraverse.jl:246-265 (apl = 1 is only valid on the TreeData path)
+    x = uniform(5001, 5000)
+    bi, bj, bd = oracle.brute_pairs(x, 0.1, criterion=0)
+    li, lj, ld = oracle.leafbuild_traverse_bvh(x, 0.1, apl)
+    assert np.array_equal(canon(li, lj, ld), canon(bi, bj, bd))
+    ai, aj, ad = oracle.build_traverse_bvh(x, 0.1, apl)
+    assert np.array_equal(canon(ai, aj, ad), canon(bi, bj, bd))
+
+
+def test_family_atomsperleaf_one_per_atom_path(oracle):
+    x = uniform(5002, 2000)
+    bi, bj, bd = oracle.brute_pairs(x, 0.1, criterion=0)
+    ai, aj, ad = oracle.build_traverse_bvh(x, 0.1, 1)
+    assert np.array_equal(canon(ai, aj, ad), canon(bi, bj, bd))
+    with pytest.raises(oracle.OracleError):
+        oracle.tree(x, 0.1, 1, boxes=oracle.REF_BOX_LEAF)
+
+
+@pytest.mark.parametrize("n", [10, 100, 1000, 2000, 3000, 20000])
+def test_family_positions(oracle, n):
+    # test/BVHTraverse.jl:268-287, atomsperleaf = 5, r = 0.1
+    x = uniform(n, n)
+    bi, bj, bd = oracle.brute_pairs(x, 0.1, criterion=0)
+    li, lj, ld = oracle.leafbuild_traverse_bvh(x, 0.1, 5)
+    assert np.array_equal(canon(li, lj, ld), canon(bi, bj, bd))
+
+
+def test_sqrt_criterion_disagreement_is_boundary_only(oracle):
+    # Leaf path uses d^2 < r^2, AllToAll / SIMD use sqrt(d^2) < r: any pair where
+    # they differ must sit within a few ulps of the cutoff.
+    x = uniform(77, 3000)
+    a0 = canon(*oracle.brute_pairs(x, 0.1, 0))
+    a1 = canon(*oracle.brute_pairs(x, 0.1, 1))
+    s0 = {tuple(r) for r in a0}
+    s1 = {tuple(r) for r in a1}
+    for row in s0 ^ s1:
+        d = np.array([row[2]], np.int32).view(np.float32)[0]
+        assert abs(d - np.float32(0.1)) <= 4 * np.spacing(np.float32(0.1))
+
+
+def test_golden_vectors(oracle):
+    for c in golden_cases():
+        x = np.array(c["position"], np.float32)
+        boxes = oracle.REF_BOX_LEAF if c["boxes"] == "leaf" else oracle.REF_BOX_ATOM
+        t = oracle.tree(x, c["r"], c["apl"], boxes=boxes)
+        nl = t["leaves"]
+        assert list(oracle.morton_reference(x)) == c["codes"], c["name"]
+        assert list(t["perm"] + 1) == c["perm"], c["name"]
+        assert list(t["index"]) == c["index"], c["name"]
+        assert list(t["code"]) == c["code_sorted"], c["name"]
+        for k, g in zip(t["keys"][: 2 * nl - 1], c["keys"]):
+            assert [float(v) for v in k["min"]] == g[0]
+            assert [float(v) for v in k["max"]] == g[1]
+            assert (int(k["left"]), int(k["skip"])) == (g[2], g[3]), c["name"]
+        if c["boxes"] == "leaf":
+            pi, pj, pd = oracle.leaf_traverse(t, c["r"], c["apl"])
+        else:
+            pi, pj, pd = oracle.atom_traverse(t, c["r"], c["apl"])
+        got = [[int(a), int(b), float(d)] for a, b, d in zip(pi, pj, pd)]
+        assert got == c["pairs"], c["name"]
+
+
+def test_morton_errors(oracle):
+    x = uniform(1, 8)
+    x[3, 1] = np.nan
+    with pytest.raises(oracle.OracleError):
+        oracle.morton_reference(x)
+    x = uniform(1, 8)
+    x[2, 0] = 3.0e6  # 3e6 * 1023 > 2^31: InexactError in round(Int32, ...)
+    with pytest.raises(oracle.OracleError):
+        oracle.morton_reference(x)
+    x[2, 0] = -2.0e6  # -2.046e9 >= -2^31: still representable
+    oracle.morton_reference(x)
+
+
+def test_spec_checks(oracle):
+    with pytest.raises(oracle.OracleError):
+        oracle.spec(10, 4)          # 4 does not divide 10
+    with pytest.raises(oracle.OracleError):
+        oracle.spec(4, 4)           # a single leaf
+    assert oracle.spec(12, 4) == (3, 2)
+
+
+def test_hash_order_free(oracle):
+    x = uniform(3, 500)
+    pi, pj, pd = oracle.leafbuild_traverse_bvh(x, 0.2, 4)
+    h = oracle.pair_hash(pi, pj, pd)
+    p = np.random.default_rng(0).permutation(len(pi))
+    assert oracle.pair_hash(pj[p], pi[p], pd[p]) == h
+    t = oracle.tree(x, 0.2, 4)
+    assert oracle.leaf_traverse_hash(t, 0.2, 4) == (len(pi), h)
+
+
+# ------------------------------------------------------------ physics oracle
+
+def _lj_box(n=216, side=7.0, seed=3):
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*[np.arange(6)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    x = (g + 0.5) * (side / 6) + rng.normal(0, 0.08, (n, 3))
+    return x
+
+
+def test_forces_are_minus_gradient(oracle):
+    x = _lj_box()
+    q = np.where(np.arange(len(x)) % 2 == 0, 1.0, -1.0)
+    p = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(7, 7, 7))
+    f, _, _ = oracle.forces(p, x, q)
+    h = 1e-6
+    for (i, d) in [(0, 0), (17, 1), (100, 2), (215, 0)]:
+        xp, xm = x.copy(), x.copy()
+        xp[i, d] += h
+        xm[i, d] -= h
+        up = oracle.forces(p, xp, q)[1]
+        um = oracle.forces(p, xm, q)[1]
+        assert abs(-(up - um) / (2 * h) - f[i, d]) < 1e-5 * max(1.0, abs(f[i, d]))
+
+
+def test_forces_newton_third_law_and_cells(oracle):
+    x = _lj_box()
+    p = oracle.md_params(cutoff=2.5, box_hi=(7, 7, 7))
+    f, u, npairs = oracle.forces(p, x)
+    assert np.abs(f.sum(0)).max() < 1e-9 * np.abs(f).max()
+    # brute force reference of the same sum
+    d = x[:, None, :] - x[None, :, :]
+    r2 = (d ** 2).sum(-1)
+    iu = np.triu_indices(len(x), 1)
+    m = r2[iu] < 2.5 ** 2
+    s6 = (1.0 / r2[iu][m]) ** 3
+    assert npairs == int(m.sum())
+    assert abs(u - np.sum(4 * (s6 * s6 - s6))) < 1e-9 * abs(u)
+
+
+def test_md_energy_conservation(oracle):
+    # Velocity Verlet is second order: the energy error over a fixed time
+    # shrinks 4x per halving of dt.  The cutoff covers every pair, so the
+    # truncated (unshifted) potential has no jumps.
+    x = _lj_box()
+    v = np.random.default_rng(1).normal(0, 0.5, x.shape)
+    errs = []
+    for dt in (1e-3, 5e-4):
+        p = oracle.md_params(cutoff=30.0, box_lo=(-50, -50, -50), box_hi=(50, 50, 50), dt=dt)
+        u0 = oracle.forces(p, x)[1]
+        e0 = u0 + 0.5 * (v ** 2).sum()
+        x1, v1, _ = oracle.md_run(p, x, v, steps=int(round(0.2 / dt)))
+        e1 = oracle.forces(p, x1)[1] + 0.5 * (v1 ** 2).sum()
+        errs.append(abs(e1 - e0) / abs(e0))
+    assert errs[0] < 5e-4
+    assert 3.5 < errs[0] / errs[1] < 4.5
+
+
+def test_md_walls_reflect(oracle):
+    x = np.array([[0.5, 0.5, 0.5], [5.0, 5.0, 5.0]])
+    v = np.array([[-100.0, 0.0, 0.0], [0.0, 0.0, 300.0]])
+    p = oracle.md_params(cutoff=2.5, box_lo=(0, 0, 0), box_hi=(6, 6, 6), dt=1e-2)
+    x1, v1, _ = oracle.md_run(p, x, v, steps=1)
+    assert x1[0, 0] == 0.0 and v1[0, 0] == 100.0
+    assert x1[1, 2] == 6.0 and v1[1, 2] == -300.0
+
+
+def test_cpu_baseline_matches_fp64_step(oracle):
+    # ref_md_run_bvh (the timed CPU baseline) equals ref_md_run while the list holds.
+    x = _lj_box()
+    v = np.random.default_rng(2).normal(0, 0.5, x.shape)
+    p = oracle.md_params(cutoff=2.5, box_lo=(-50, -50, -50), box_hi=(50, 50, 50))
+    xa, va, fa = oracle.md_run(p, x, v, steps=20)
+    xb, vb, fb, _ = oracle.md_run_bvh(p, x, v, steps=20, rebuild=10, skin=0.3, apl=4)
+    assert np.abs(xa - xb).max() < 1e-11
+    assert np.abs(va - vb).max() < 1e-9
