@@ -1,0 +1,343 @@
+"""Benchmark: LJ + Coulomb velocity-Verlet throughput (atom-steps/s) on GB300.
+
+Workload (the at-scale configuration): 262,144 atoms uniform in a cube of side
+68 (no two closer than 0.8 sigma), charges +/-1 (half each), sigma = eps = 1,
+Coulomb k = 1, cutoff 2.5, skin 0.3, dt = 1e-3, FP32 forces with FP64
+positions and velocities, neighbour list rebuilt every 10 steps.  One bench
+step = 100 MD steps (10 rebuild windows), so the default --steps 10 times the
+configuration's 1000 MD steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints ONE JSON line on rank 0.  Multi-GPU runs are independent replicas (the
+path has no exchange step): value = all ranks' atom-steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "naivedynamics.jl_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+N_ATOMS = 262144
+SIDE = 68.0
+MD_PER_STEP = 100
+REBUILD = 10
+SEED = 0x4E440002
+METRIC = "LJ+Coulomb atom-steps/s @262k (FP32 forces, FP64 x/v, rebuild every 10)"
+UNIT = "atom-steps/s"
+WORKLOAD = ("lj_coulomb_262144: N=262144 uniform cube side 68 (min separation 0.8), q=+/-1, "
+            "sigma=eps=1, k=1, r_c=2.5, skin=0.3, dt=1e-3, rebuild every 10, 100 MD steps per "
+            "bench step")
+
+
+def _md_params(nd, order=None):
+    return nd.md_params(sigma=1.0, epsilon=1.0, coulomb_k=1.0, cutoff=2.5, skin=0.3, dt=1e-3,
+                        box_lo=(0, 0, 0), box_hi=(SIDE, SIDE, SIDE), atomsperleaf=4,
+                        rebuild_every=REBUILD,
+                        order=nd.ND_ORDER_SPATIAL if order is None else order)
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for (_, _, r) in rows for k in range(4) if r[k] == "Active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def _ncu_traffic():
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(REPO, "profiles", "md_step_262k.json")) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_sample(steps=10):
+    """The reference path on the host cores: the oracle restatement of
+    leafbuild_traverse_bvh (reference Morton order) rebuilt every 10 steps at
+    r_c + skin, FP64 LJ+Coulomb forces over that list, KDK velocity Verlet."""
+    import naivedynamics as nd
+    from oracle import naiveref as R
+    x, v, q = nd.synth.lj_system(SEED, N_ATOMS, SIDE, 0.8, charges=True)
+    p = R.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(SIDE,) * 3, dt=1e-3)
+    t0 = time.perf_counter()
+    R.md_run_bvh(p, x, v, q, steps=steps, rebuild=REBUILD, skin=0.3, apl=4,
+                 order=R.REF_ORDER_REFERENCE)
+    dt = time.perf_counter() - t0
+    return {"value": N_ATOMS * steps / dt, "unit": UNIT, "cores": R.num_threads(),
+            "kind": "port",
+            "sample": f"{N_ATOMS} atoms x {steps} MD steps (initial leaf-BVH build + 1 rebuild, "
+                      f"reference Morton order, OpenMP over {R.num_threads()} threads), {dt:.2f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    import naivedynamics as nd  # noqa: F401  (synthetic inputs only)
+    samples = []
+    for k in range(args.warmup + args.steps):
+        s = cpu_baseline_sample(steps=10)
+        if k >= args.warmup:
+            samples.append(s)
+    total_as = sum(N_ATOMS * 10 for _ in samples)
+    total_t = sum(N_ATOMS * 10 / s["value"] for s in samples)
+    value = total_as / total_t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total_t / len(samples), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("100 MD steps", "10 MD steps"),
+                       "reference_path": "oracle port of leafbuild_traverse_bvh + FP64 forces "
+                                         "+ KDK (reference Julia not installable: no julia)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": samples[0]["cores"],
+                             "kind": "port", "sample": samples[0]["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    import naivedynamics as nd
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ctx = nd.Context(local)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    x, v, q = nd.synth.lj_system(SEED + rank, N_ATOMS, SIDE, 0.8, charges=True)
+    xd = torch.from_numpy(x).cuda()
+    vd = torch.from_numpy(v).cuda()
+    qd = torch.from_numpy(q).cuda()
+    params = _md_params(nd)
+    eng = nd.MDEngine(params, xd, vd, qd, device=True, ctx=ctx)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        eng.run(MD_PER_STEP)
+    eng.sync()
+
+    # ---- timed region: K bench steps, L2 flushed before each (outside the events)
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    launches0 = ctx.launch_count()
+    barrier()
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.synchronize()
+            with torch.cuda.stream(ext):
+                events[k][0].record(ext)
+                eng.run(MD_PER_STEP)
+                events[k][1].record(ext)
+        eng.sync()
+        barrier()
+    wall = time.perf_counter() - wall0
+    launches = ctx.launch_count() - launches0
+    t_ms = sum(s.elapsed_time(e) for (s, e) in events)
+    t_max = t_ms
+    if ws > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    diag = eng.diagnostics()
+    stats = eng.stats()
+
+    # ---- roofline of the dominant kernel: single k_md_step launches timed with
+    # events on the library's stream (mid-window eager steps: one kernel each)
+    eng.run(REBUILD - (stats["steps"] % REBUILD) if stats["steps"] % REBUILD else 0)
+    eng.run(1)  # opens a window: rebuild + first step
+    single = []
+    with torch.cuda.stream(ext):
+        for _ in range(REBUILD - 2):
+            s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s_.record(ext)
+            eng.run(1)
+            e_.record(ext)
+            single.append((s_, e_))
+    eng.sync()
+    k_ms = statistics.mean(s.elapsed_time(e) for (s, e) in single)
+    nbr = stats["list_pairs"] / N_ATOMS  # full-list neighbours per atom
+    # algorithmic bytes per atom of one fused step: x, v read+write (FP64, 96),
+    # own shadow record read (32) + next shadow write (32), force write (16),
+    # build-position read (16), list count (4), 4 B per listed neighbour
+    bytes_per_atom = 96 + 32 + 32 + 16 + 16 + 4 + 4 * nbr
+    traffic_alg = bytes_per_atom * N_ATOMS
+    peaks, peak_kind = _peaks()
+    achieved = traffic_alg / (k_ms * 1e-3) / 1e9
+    traffic = _ncu_traffic()
+
+    # ---- e2e: simulate!(sys, spec, clct) through the public API with pinned
+    # host buffers: H2D of x, v, q and D2H of x, v, f inside every step
+    xh = torch.from_numpy(x.copy()).pin_memory()
+    vh = torch.from_numpy(v.copy()).pin_memory()
+    qh = torch.from_numpy(q.copy()).pin_memory()
+    fh = torch.empty((N_ATOMS, 3), dtype=torch.float32).pin_memory()
+    import ctypes
+    from naivedynamics import _lib
+    L = _lib.lib()
+
+    def e2e_call():
+        st = L.nd_simulate(ctx.handle, ctypes.byref(params), N_ATOMS, xh.data_ptr(),
+                           vh.data_ptr(), fh.data_ptr(), qh.data_ptr(), None, MD_PER_STEP)
+        ctx.check(st, "nd_simulate")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_call()
+    barrier()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_call()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t)
+    if ws > 1:
+        tt = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+
+    total_atom_steps = ws * N_ATOMS * MD_PER_STEP * args.steps
+    value = total_atom_steps / (t_max * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 state",
+        "data": "synthetic (seeded splitmix64 generators)",
+        "config": {"workload": WORKLOAD, "n_atoms": N_ATOMS, "md_steps_per_step": MD_PER_STEP,
+                   "rebuild_every": REBUILD, "atom_order": "spatial Morton",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
+                   "l2": "512 MB buffer written before every timed step (outside the events)",
+                   "neighbours_per_atom": round(nbr, 2),
+                   "skin_violations": diag["skin_violations"],
+                   "wall_s_timed_region": round(wall, 4)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": traffic, "kernel": "k_md_step (fused force + KDK step)",
+                     "kernel_ms": k_ms, "algorithmic_bytes_per_launch": traffic_alg,
+                     "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+        "e2e": {"value": total_atom_steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(x.nbytes + v.nbytes + q.nbytes),
+                "d2h_bytes_per_step": int(x.nbytes + v.nbytes + fh.numel() * 4),
+                "api": "nd_simulate (simulate!) with pinned host buffers"},
+    }
+    clocks = clk.summary()
+    if clocks:
+        line["clocks"] = clocks
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(steps=10)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -233,6 +233,10 @@ nd_status nd_md_energy(nd_md* md, double* potential, double* kinetic);
 /* Steps taken, rebuilds done, pairs in the current list, list capacity. */
 nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* list_pairs,
                       int32_t* capacity);
+/* Atom-steps in which an atom had moved more than skin/2 since the last
+ * rebuild (the list may then miss pairs: raise skin or rebuild more often),
+ * and the largest per-atom neighbour count seen in any build. */
+nd_status nd_md_diagnostics(nd_md* md, int64_t* skin_violations, int32_t* max_neighbors);
 /* Number of kernel launches one nd_md_run(steps) enqueues (for diagnostics). */
 int64_t nd_md_launches_per_run(nd_md* md, int64_t steps);
 

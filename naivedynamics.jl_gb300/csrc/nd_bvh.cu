@@ -624,11 +624,21 @@ __device__ __forceinline__ void leaf_pairs_fixed(const float4 (&qa)[APL],
 }
 
 // leafneighbor_traverse (BVHTraverse.jl:1236-1323) for one query leaf q (1-based).
+// A rope walk visits every node at most once; a longer walk or a node index
+// outside [1, 2nL-1] can only come from a corrupted tree and is reported
+// instead of looping.
+#define ND_WALK_GUARD(t, nnodes, visits, err, who)                          \
+    if ((t) < 1 || (t) > (nnodes) || ++(visits) > (nnodes)) {               \
+        set_error((err), ND_ERR_INTERNAL, (who));                           \
+        break;                                                              \
+    }
+
 template <int APL, class Sink>
 __device__ __forceinline__ void leaf_query(int32_t q, const float4* __restrict__ keys,
                                            const float4* __restrict__ pos, int32_t apl, float r2,
-                                           Sink& s) {
+                                           int32_t nnodes, int32_t* err, Sink& s) {
     Node ql = load_node(keys, q);
+    int32_t visits = 0;
     int64_t A = (int64_t)(q - 1) * apl;
     if constexpr (APL > 0) {
         float4 qa[APL];
@@ -643,6 +653,7 @@ __device__ __forceinline__ void leaf_query(int32_t q, const float4* __restrict__
             }
         int32_t t = ql.skip;
         while (t != 0) {
+            ND_WALK_GUARD(t, nnodes, visits, err, q)
             Node nd_ = load_node(keys, t);
             if (overlap(ql, nd_)) {
                 if (nd_.left == 0) {
@@ -659,6 +670,7 @@ __device__ __forceinline__ void leaf_query(int32_t q, const float4* __restrict__
         leaf_pairs_generic(pos, A, A, apl, r2, true, s);
         int32_t t = ql.skip;
         while (t != 0) {
+            ND_WALK_GUARD(t, nnodes, visits, err, q)
             Node nd_ = load_node(keys, t);
             if (overlap(ql, nd_)) {
                 if (nd_.left == 0) {
@@ -678,10 +690,12 @@ __device__ __forceinline__ void leaf_query(int32_t q, const float4* __restrict__
 template <class Sink>
 __device__ __forceinline__ void atom_query(int32_t qi, const float4* __restrict__ keys,
                                            const float4* __restrict__ pos, int32_t apl, float r2,
-                                           Sink& s) {
+                                           int32_t nnodes, int32_t* err, Sink& s) {
     float4 p = __ldg(&pos[qi - 1]);
     int32_t t = (qi + apl - 1) / apl;
+    int32_t visits = 0;
     while (t != 0) {
+        ND_WALK_GUARD(t, nnodes, visits, err, qi)
         Node nd_ = load_node(keys, t);
         bool in = (nd_.mnx < p.x) & (p.x < nd_.mxx) & (nd_.mny < p.y) & (p.y < nd_.mxy) &
                   (nd_.mnz < p.z) & (p.z < nd_.mxz);
@@ -711,11 +725,11 @@ __device__ __forceinline__ void atom_query(int32_t qi, const float4* __restrict_
 template <int APL>
 __global__ void __launch_bounds__(128)
     k_leaf_count(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
-                 int32_t apl, float r2, int64_t* __restrict__ counts) {
+                 int32_t apl, float r2, int64_t* __restrict__ counts, int32_t* err) {
     int32_t q = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (q > nL) return;
     SinkCount s;
-    leaf_query<APL>(q, keys, pos, apl, r2, s);
+    leaf_query<APL>(q, keys, pos, apl, r2, 2 * nL - 1, err, s);
     counts[q - 1] = s.n;
 }
 
@@ -723,11 +737,11 @@ template <int APL>
 __global__ void __launch_bounds__(128)
     k_leaf_write(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
                  int32_t apl, float r2, const int64_t* __restrict__ offsets, int32_t* pi,
-                 int32_t* pj, float* pd) {
+                 int32_t* pj, float* pd, int32_t* err) {
     int32_t q = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (q > nL) return;
     SinkWrite s{pi, pj, pd, offsets[q - 1]};
-    leaf_query<APL>(q, keys, pos, apl, r2, s);
+    leaf_query<APL>(q, keys, pos, apl, r2, 2 * nL - 1, err, s);
 }
 
 // One-pass emission: pairs of one leaf-vs-leaf test are staged in registers
@@ -770,7 +784,7 @@ __device__ __forceinline__ void flush_stage(SinkStage& s, unsigned long long* cu
 __global__ void __launch_bounds__(128)
     k_leaf_unordered4(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
                       float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
-                      float* pd) {
+                      float* pd, int32_t* err) {
     int32_t q = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (q > nL) return;
     constexpr int APL = 4;
@@ -789,7 +803,10 @@ __global__ void __launch_bounds__(128)
         }
     flush_stage(s, cursor, cap, pi, pj, pd);
     int32_t t = ql.skip;
+    int32_t visits = 0;
+    const int32_t nnodes = 2 * nL - 1;
     while (t != 0) {
+        ND_WALK_GUARD(t, nnodes, visits, err, q)
         Node nd_ = load_node(keys, t);
         if (overlap(ql, nd_)) {
             if (nd_.left == 0) {
@@ -807,22 +824,22 @@ __global__ void __launch_bounds__(128)
 
 __global__ void __launch_bounds__(128)
     k_atom_count(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t n,
-                 int32_t apl, float r2, int64_t* __restrict__ counts) {
+                 int32_t apl, float r2, int64_t* __restrict__ counts, int32_t* err) {
     int32_t qi = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (qi > n) return;
     SinkCount s;
-    if (qi <= n - 1) atom_query(qi, keys, pos, apl, r2, s);
+    if (qi <= n - 1) atom_query(qi, keys, pos, apl, r2, 2 * (n / apl) - 1, err, s);
     counts[qi - 1] = s.n;
 }
 
 __global__ void __launch_bounds__(128)
     k_atom_write(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t n,
                  int32_t apl, float r2, const int64_t* __restrict__ offsets, int32_t* pi,
-                 int32_t* pj, float* pd) {
+                 int32_t* pj, float* pd, int32_t* err) {
     int32_t qi = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (qi > n - 1) return;
     SinkWrite s{pi, pj, pd, offsets[qi - 1]};
-    atom_query(qi, keys, pos, apl, r2, s);
+    atom_query(qi, keys, pos, apl, r2, 2 * (n / apl) - 1, err, s);
 }
 
 nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int32_t* pj,
@@ -834,7 +851,7 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
     unsigned long long* cursor = (unsigned long long*)c->misc.p;
     cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
     k_leaf_unordered4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
-        t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd);
+        t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd, c->d_err);
     c->launches++;
     if ((st = check_launch(c, "leaf pairs (unordered)"))) return st;
     unsigned long long tot = 0;
@@ -856,11 +873,11 @@ nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int64_t* 
     unsigned grid = (unsigned)cdiv(nq, 128);
     if (kind == 0) {
         if (t.apl == 4)
-            k_leaf_count<4><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, counts);
+            k_leaf_count<4><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, counts, c->d_err);
         else
-            k_leaf_count<0><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, counts);
+            k_leaf_count<0><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, counts, c->d_err);
     } else {
-        k_atom_count<<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.n, t.apl, r2, counts);
+        k_atom_count<<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.n, t.apl, r2, counts, c->d_err);
     }
     c->launches++;
     if ((st = check_launch(c, "pair count"))) return st;
@@ -883,13 +900,13 @@ nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int32_t* 
     if (kind == 0) {
         if (t.apl == 4)
             k_leaf_write<4><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, offsets,
-                                                        pi, pj, pd);
+                                                        pi, pj, pd, c->d_err);
         else
             k_leaf_write<0><<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.nL, t.apl, r2, offsets,
-                                                        pi, pj, pd);
+                                                        pi, pj, pd, c->d_err);
     } else {
         k_atom_write<<<grid, 128, 0, c->stream>>>(t.keys, t.pos4, t.n, t.apl, r2, offsets, pi, pj,
-                                                  pd);
+                                                  pd, c->d_err);
     }
     c->launches++;
     return check_launch(c, "pair write");

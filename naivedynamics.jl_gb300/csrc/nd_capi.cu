@@ -258,6 +258,8 @@ nd_status nd_ctx_destroy(nd_ctx* h) {
     if (!h) return ND_OK;
     Ctx* c = &h->c;
     cudaSetDevice(c->device);
+    if (c->sim_cache) nd::md_destroy(c->sim_cache);
+    c->sim_cache = nullptr;
     if (c->stream) cudaStreamSynchronize(c->stream);
     nd::DevBuf* bufs[] = {&c->xyz, &c->codes, &c->codes_alt, &c->perm, &c->perm_alt, &c->pos4,
                           &c->idx, &c->keys, &c->store, &c->hist, &c->counts, &c->offsets,
@@ -502,6 +504,11 @@ nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* lis
     return md_wrap(md, nd::md_stats(md->e, steps, rebuilds, list_pairs, capacity));
 }
 
+nd_status nd_md_diagnostics(nd_md* md, int64_t* skin_violations, int32_t* max_neighbors) {
+    if (!md) return ND_ERR_ARG;
+    return md_wrap(md, nd::md_diagnostics(md->e, skin_violations, max_neighbors));
+}
+
 int64_t nd_md_launches_per_run(nd_md* md, int64_t steps) {
     return md ? nd::md_launches_per_run(md->e, steps) : 0;
 }
@@ -512,13 +519,28 @@ nd_status nd_simulate(nd_ctx* h, const nd_md_params* p, int32_t n, double* x, do
     Ctx* c = &h->c;
     nd_status st = nd::set_device(c);
     if (st) return st;
-    nd::MDEngine* e = nullptr;
-    const bool capture = steps >= 2LL * std::max(p->rebuild_every, 1);
-    if ((st = nd::md_create(c, p, n, x, v, q, m, true, capture, &e))) return st;
+    // The context keeps the engine of its last call: a call with the same size
+    // and parameters re-uses its buffers and captured graphs.
+    nd::MDEngine* e = c->sim_cache;
+    bool fresh = !nd::md_compatible(e, p, n, q != nullptr, m != nullptr);
+    if (!fresh) {
+        st = nd::md_reset(e, x, v, q, m, true);
+        if (st == ND_ERR_OVERFLOW) fresh = true;
+        else if (st) { c->last_error = nd::md_last_error(e); return st; }
+    }
+    if (fresh) {
+        if (e) nd::md_destroy(e);
+        c->sim_cache = nullptr;
+        if ((st = nd::md_create(c, p, n, x, v, q, m, true, true, &e))) return st;
+        c->sim_cache = e;
+    }
     st = nd::md_run(e, steps);
     if (st == ND_OK) st = nd::md_get(e, x, v, f, true);
-    if (st) c->last_error = nd::md_last_error(e);
-    nd::md_destroy(e);
+    if (st) {
+        c->last_error = nd::md_last_error(e);
+        nd::md_destroy(e);
+        c->sim_cache = nullptr;
+    }
     return st;
 }
 

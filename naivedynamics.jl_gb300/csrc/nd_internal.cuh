@@ -12,6 +12,8 @@
 
 namespace nd {
 
+struct MDEngine;
+
 // ------------------------------------------------------------------ errors
 
 // Device error word layout: [0] first error status, [1] its info (an index),
@@ -102,6 +104,7 @@ struct Ctx {
     // scratch buffers of the neighbour-search pipeline, grown on demand
     DevBuf xyz, codes, codes_alt, perm, perm_alt, pos4, idx, keys, store, hist, counts, offsets,
         partial, pairs_i, pairs_j, pairs_d, misc, hash;
+    struct MDEngine* sim_cache = nullptr;  // engine re-used by nd_simulate
 };
 
 // Grow `b` to at least `bytes` (contents are not preserved).
@@ -155,6 +158,9 @@ nd_status md_create(Ctx* parent, const nd_md_params* p, int32_t n, const double*
                     const double* v, const double* q, const double* mass, bool host,
                     bool capture, MDEngine** out);
 nd_status md_destroy(MDEngine* m);
+nd_status md_reset(MDEngine* m, const double* x, const double* v, const double* q,
+                   const double* mass, bool host);
+bool md_compatible(MDEngine* m, const nd_md_params* p, int32_t n, bool has_q, bool has_m);
 nd_status md_run(MDEngine* m, int64_t steps);
 nd_status md_sync(MDEngine* m);
 nd_status md_get(MDEngine* m, double* x, double* v, float* f, bool host);
@@ -162,6 +168,7 @@ nd_status md_energy(MDEngine* m, double* pot, double* kin);
 nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list_pairs,
                    int32_t* capacity);
 int64_t md_launches_per_run(MDEngine* m, int64_t steps);
+nd_status md_diagnostics(MDEngine* m, int64_t* skin_violations, int32_t* max_neighbors);
 const char* md_last_error(MDEngine* m);
 nd_status forces_pairs(Ctx* c, const nd_md_params* p, int32_t n, const double* x,
                        const double* q, const int32_t* pi, const int32_t* pj, int64_t np,

@@ -8,8 +8,9 @@
 //   x[3][N], w[3][N]   FP64 positions and velocities, one array per component
 //                      (two sets, ping-ponged by the reorder at each rebuild)
 //   q[N], im[N]        FP64 charge and inverse mass (optional)
-//   hi[N], lo[N]       float4 shadow of x for the pair math: hi = fl32(x),
-//                      lo = fl32(x - hi), hi.w = charge (ping-ponged per step)
+//   sh[2N]             float4 shadow of x for the pair math, one 32-byte record
+//                      per atom: sh[2k] = (hi, q) with hi = fl32(x), sh[2k+1] =
+//                      (lo, 0) with lo = fl32(x - hi) (ping-ponged per step)
 //   nbr[cap][N]        full neighbour list, slot-major (coalesced per slot)
 //   f[N]               float4 forces of the last evaluation
 // One MD step is ONE kernel: each thread owns an atom, sums its pair forces
@@ -73,7 +74,7 @@ struct SetPtrs {
 // float shadows; pos32 keeps the Float32 positions used by the tree.
 __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict__ perm,
                              const float* __restrict__ xyz32, int32_t n, float4* __restrict__ pos32,
-                             float4* __restrict__ hi, float4* __restrict__ lo) {
+                             float4* __restrict__ sh) {
     int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int32_t o = perm[k];
@@ -91,8 +92,8 @@ __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict
     dst.orig[k] = src.orig[o];
     pos32[k] = make_float4(xyz32[3 * (int64_t)o], xyz32[3 * (int64_t)o + 1],
                            xyz32[3 * (int64_t)o + 2], __int_as_float(k));
-    hi[k] = make_float4(h[0], h[1], h[2], (float)qv);
-    lo[k] = make_float4(l[0], l[1], l[2], 0.0f);
+    sh[2 * (int64_t)k] = make_float4(h[0], h[1], h[2], (float)qv);
+    sh[2 * (int64_t)k + 1] = make_float4(l[0], l[1], l[2], 0.0f);
 }
 
 // Leaf boxes (p -/+ h) of already sorted Float32 positions.
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(128)
     int64_t guard = 0;
     const int64_t max_visits = 4LL * nL + 8;
     while (t != 0) {
-        if (++guard > max_visits) { set_error(err, ND_ERR_INTERNAL, i); break; }
+        if (++guard > max_visits || t < 1 || t > 2 * nL - 1) { set_error(err, ND_ERR_INTERNAL, i); break; }
         float4 a = __ldg(&keys[2 * (int64_t)(t - 1)]);
         float4 b = __ldg(&keys[2 * (int64_t)(t - 1) + 1]);
         int32_t left = __float_as_int(b.z), skip = __float_as_int(b.w);
@@ -167,16 +168,17 @@ struct StepArgs {
     int32_t n;
     const int32_t* __restrict__ nbr;
     const int32_t* __restrict__ ncount;
-    const float4* __restrict__ hi_in;
-    const float4* __restrict__ lo_in;
-    float4* __restrict__ hi_out;
-    float4* __restrict__ lo_out;
+    const float4* __restrict__ sh_in;  // interleaved (hi, lo) records
+    float4* __restrict__ sh_out;
     double* x[3];
     double* w[3];
     const double* __restrict__ im;
     float4* __restrict__ f_out;
     double* __restrict__ v_out[3];  // measure kernel: integer-step velocity
     double* __restrict__ acc;       // measure kernel: [0] potential, [1] kinetic
+    const float4* __restrict__ pos_build;  // Float32 positions at the last rebuild
+    unsigned long long* __restrict__ diag; // [0] atom-steps that moved > skin/2 since the build
+    float half_skin2;
     float rc2, sig2, eps24, eps4, kc;
     float hdt;                      // dt / 2
     double dt;
@@ -201,6 +203,28 @@ __device__ __forceinline__ void pair_lj_coul(float r2, float qq, const StepArgs&
     }
 }
 
+// Pair (i, j): displacement from the (hi, lo) records -- the hi difference of
+// two nearby floats is exact or correctly rounded relative to the result, so
+// r_ij keeps ~1e-7 relative accuracy even at box sides of 68 -- then the
+// cutoff test and the accumulation of F_i and (optionally) U_i.
+template <bool COUL, bool ENERGY>
+__device__ __forceinline__ void accum_pair(const float4& hi, const float4& lo, const float4& hj,
+                                          const float4& lj, const StepArgs& a, float& fx,
+                                          float& fy, float& fz, float& ue) {
+    float dx = (hi.x - hj.x) + (lo.x - lj.x);
+    float dy = (hi.y - hj.y) + (lo.y - lj.y);
+    float dz = (hi.z - hj.z) + (lo.z - lj.z);
+    float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < a.rc2) {
+        float fmag, u = 0.f;
+        pair_lj_coul<COUL, ENERGY>(r2, hi.w * hj.w, a, fmag, u);
+        fx += fmag * dx;
+        fy += fmag * dy;
+        fz += fmag * dz;
+        if (ENERGY) ue += u;
+    }
+}
+
 // One thread per atom.  MODE 0: step (force, pending half kick, kick, drift,
 // reflect, new shadow).  MODE 1: measure (force, integer-step velocity and
 // energies; state untouched).
@@ -210,27 +234,34 @@ __global__ void __launch_bounds__(128) k_md_step(StepArgs a) {
     const bool valid = i < a.n;
     if (MODE == 0 && !valid) return;
     if (!valid) i = a.n - 1;  // measure: idle lanes join the warp reduction with zeros
-    const float4 hi = __ldg(&a.hi_in[i]);
-    const float4 lo = __ldg(&a.lo_in[i]);
+    const float4 hi = __ldg(&a.sh_in[2 * (int64_t)i]);
+    const float4 lo = __ldg(&a.sh_in[2 * (int64_t)i + 1]);
     const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
     float fx = 0.f, fy = 0.f, fz = 0.f, ue = 0.f;
     const int32_t* __restrict__ nb = a.nbr + i;
-    for (int32_t s = 0; s < cnt; ++s) {
-        int32_t j = __ldg(nb + (int64_t)s * a.n);
-        float4 hj = __ldg(&a.hi_in[j]);
-        float4 lj = __ldg(&a.lo_in[j]);
-        float dx = (hi.x - hj.x) + (lo.x - lj.x);
-        float dy = (hi.y - hj.y) + (lo.y - lj.y);
-        float dz = (hi.z - hj.z) + (lo.z - lj.z);
-        float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < a.rc2) {
-            float fmag, u = 0.f;
-            pair_lj_coul<COUL, MODE == 1>(r2, hi.w * hj.w, a, fmag, u);
-            fx += fmag * dx;
-            fy += fmag * dy;
-            fz += fmag * dz;
-            if (MODE == 1) ue += u;
+    const int64_t stride = a.n;
+    // Neighbours in groups of four: the four index loads and eight record
+    // loads of a group are independent, so they are in flight together.
+    int32_t s = 0;
+    for (; s + 4 <= cnt; s += 4) {
+        int32_t j[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) j[k] = __ldg(nb + (int64_t)(s + k) * stride);
+        float4 hj[4], lj[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            hj[k] = __ldg(&a.sh_in[2 * (int64_t)j[k]]);
+            lj[k] = __ldg(&a.sh_in[2 * (int64_t)j[k] + 1]);
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            accum_pair<COUL, MODE == 1>(hi, lo, hj[k], lj[k], a, fx, fy, fz, ue);
+    }
+    for (; s < cnt; ++s) {
+        int32_t j = __ldg(nb + (int64_t)s * stride);
+        float4 hj = __ldg(&a.sh_in[2 * (int64_t)j]);
+        float4 lj = __ldg(&a.sh_in[2 * (int64_t)j + 1]);
+        accum_pair<COUL, MODE == 1>(hi, lo, hj, lj, a, fx, fy, fz, ue);
     }
     if (valid) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
     const double imv = MASS ? a.im[i] : 1.0;
@@ -271,8 +302,13 @@ __global__ void __launch_bounds__(128) k_md_step(StepArgs a) {
         a.w[d][i] = v;
         split_df(x, h[d], l[d]);
     }
-    a.hi_out[i] = make_float4(h[0], h[1], h[2], hi.w);
-    a.lo_out[i] = make_float4(l[0], l[1], l[2], 0.f);
+    a.sh_out[2 * (int64_t)i] = make_float4(h[0], h[1], h[2], hi.w);
+    a.sh_out[2 * (int64_t)i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+    // A list built at r_c + skin stays valid while no atom moved more than
+    // skin/2 since the build; count the atom-steps that broke that bound.
+    const float4 pb = __ldg(&a.pos_build[i]);
+    const float ex = h[0] - pb.x, ey = h[1] - pb.y, ez = h[2] - pb.z;
+    if (ex * ex + ey * ey + ez * ez > a.half_skin2) atomicAdd(a.diag, 1ull);
 }
 
 __global__ void k_md_unsort(const int32_t* __restrict__ orig, int32_t n, const double* x0,
@@ -336,9 +372,9 @@ struct MDEngine {
     int32_t in_window = 0;  // steps done in the current window
     bool rebuild_due = false;
     int64_t steps = 0, rebuilds = 0;
-    DevBuf set_buf[2], sh_buf[2], xyz32, pos32, keys, store, nbr, ncount, f, vtmp, acc, aos;
+    DevBuf set_buf[2], sh_buf[2], xyz32, pos32, keys, store, nbr, ncount, f, vtmp, acc, aos, diag;
     SetPtrs set[2];
-    float4 *hi[2], *lo[2];
+    float4* shadow[2];
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int64_t graph_launches = 0;  // kernels per captured window
 };
@@ -356,8 +392,7 @@ static nd_status md_alloc(MDEngine* m) {
         m->set[s].im = b + 7 * n;
         m->set[s].orig = (int32_t*)(b + 8 * n);
         if ((st = ensure(c, m->sh_buf[s], 2 * n * sizeof(float4)))) return st;
-        m->hi[s] = (float4*)m->sh_buf[s].p;
-        m->lo[s] = m->hi[s] + n;
+        m->shadow[s] = (float4*)m->sh_buf[s].p;
     }
     if ((st = ensure(c, m->xyz32, 3 * n * sizeof(float)))) return st;
     if ((st = ensure(c, m->pos32, n * sizeof(float4)))) return st;
@@ -367,6 +402,8 @@ static nd_status md_alloc(MDEngine* m) {
     if ((st = ensure(c, m->f, sizeof(float4) * n))) return st;
     if ((st = ensure(c, m->vtmp, 3 * sizeof(double) * n))) return st;
     if ((st = ensure(c, m->acc, 64))) return st;
+    if ((st = ensure(c, m->diag, 64))) return st;
+    if (cudaMemsetAsync(m->diag.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
     // rebuild pipeline scratch: codes + perm + sort ping-pong + histograms
     if ((st = ensure(c, c->codes, sizeof(int32_t) * n))) return st;
     if ((st = ensure(c, c->perm, sizeof(int32_t) * n))) return st;
@@ -383,10 +420,8 @@ static StepArgs md_step_args(MDEngine* m, int shadow_in) {
     a.n = m->n;
     a.nbr = (const int32_t*)m->nbr.p;
     a.ncount = (const int32_t*)m->ncount.p;
-    a.hi_in = m->hi[shadow_in];
-    a.lo_in = m->lo[shadow_in];
-    a.hi_out = m->hi[shadow_in ^ 1];
-    a.lo_out = m->lo[shadow_in ^ 1];
+    a.sh_in = m->shadow[shadow_in];
+    a.sh_out = m->shadow[shadow_in ^ 1];
     for (int d = 0; d < 3; ++d) {
         a.x[d] = m->set[m->cur].x[d];
         a.w[d] = m->set[m->cur].w[d];
@@ -397,6 +432,12 @@ static StepArgs md_step_args(MDEngine* m, int shadow_in) {
     a.im = m->set[m->cur].im;
     a.f_out = (float4*)m->f.p;
     a.acc = (double*)m->acc.p;
+    a.pos_build = (const float4*)m->pos32.p;
+    a.diag = (unsigned long long*)m->diag.p;
+    {
+        float hs = (float)(0.5 * p.skin);
+        a.half_skin2 = hs * hs;
+    }
     a.rc2 = (float)(p.cutoff * p.cutoff);
     a.sig2 = (float)(p.sigma * p.sigma);
     a.eps24 = (float)(24.0 * p.epsilon);
@@ -441,7 +482,7 @@ static nd_status md_rebuild(MDEngine* m) {
     if ((st = morton_codes(c, (const float*)m->xyz32.p, n, m->p.order, codes, perm))) return st;
     if ((st = radix_sort_pairs(c, (uint32_t*)codes, perm, n, 30))) return st;
     k_md_reorder<<<g, 256, 0, c->stream>>>(s, t, perm, (const float*)m->xyz32.p, n,
-                                           (float4*)m->pos32.p, m->hi[0], m->lo[0]);
+                                           (float4*)m->pos32.p, m->shadow[0]);
     c->launches++;
     float4* keys = (float4*)m->keys.p;
     const float rl = (float)(m->p.cutoff + m->p.skin);
@@ -532,6 +573,60 @@ static nd_status md_size_list(MDEngine* m) {
 
 nd_status md_destroy(MDEngine* m);
 
+// Copy x, v (N x 3), q, m (N) from host or device memory into state set 0 in
+// the caller's order and reset the step bookkeeping.
+static nd_status md_upload(MDEngine* m, const double* xd, const double* vd, const double* qd,
+                           const double* md_, bool host) {
+    Ctx* c = &m->sub;
+    const int32_t n = m->n;
+    const size_t bytes = 3 * sizeof(double) * (size_t)n;
+    nd_status st;
+    if ((st = ensure(c, m->aos, 2 * bytes + 2 * sizeof(double) * (size_t)n))) return st;
+    double* ax = (double*)m->aos.p;
+    double* av = ax + 3 * (size_t)n;
+    double* aq = av + 3 * (size_t)n;
+    double* am = aq + (size_t)n;
+    cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    cudaError_t e = cudaMemcpyAsync(ax, xd, bytes, kind, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(av, vd, bytes, kind, c->stream);
+    if (e == cudaSuccess && qd) e = cudaMemcpyAsync(aq, qd, sizeof(double) * n, kind, c->stream);
+    if (e == cudaSuccess && md_) e = cudaMemcpyAsync(am, md_, sizeof(double) * n, kind, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "md upload");
+    const unsigned g = (unsigned)cdiv(n, 256);
+    SetPtrs& s = m->set[0];
+    k_md_split_aos<<<g, 256, 0, c->stream>>>(ax, n, s.x[0], s.x[1], s.x[2]);
+    k_md_split_aos<<<g, 256, 0, c->stream>>>(av, n, s.w[0], s.w[1], s.w[2]);
+    k_md_init_scalars<<<g, 256, 0, c->stream>>>(qd ? aq : nullptr, md_ ? am : nullptr, n, s.q, s.im,
+                                                s.orig);
+    c->launches += 3;
+    if (cudaMemsetAsync(m->diag.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
+    m->cur = 0;
+    m->first = true;
+    m->steps = 0;
+    m->rebuilds = 0;
+    m->in_window = 0;
+    m->rebuild_due = false;
+    return check_launch(c, "md upload");
+}
+
+// Re-use an engine (buffers, captured graphs) for a new state of the same
+// size and parameters: upload, then the opening rebuild with the current list
+// capacity.  ND_ERR_OVERFLOW means the caller must create a new engine.
+nd_status md_reset(MDEngine* m, const double* x, const double* v, const double* q,
+                   const double* mass, bool host) {
+    if ((q != nullptr) != m->has_q || (mass != nullptr) != m->has_m) return ND_ERR_ARG;
+    nd_status st = md_upload(m, x, v, q, mass, host);
+    if (st) return st;
+    if ((st = md_rebuild(m))) return st;
+    m->rebuilds = 1;
+    return sync_and_check(&m->sub, "md reset");
+}
+
+bool md_compatible(MDEngine* m, const nd_md_params* p, int32_t n, bool has_q, bool has_m) {
+    return m && m->n == n && m->has_q == has_q && m->has_m == has_m &&
+           memcmp(&m->p, p, sizeof(nd_md_params)) == 0;
+}
+
 static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
                                   const double* xd, const double* vd, const double* qd,
                                   const double* md_, bool host, bool capture, MDEngine** out) {
@@ -554,26 +649,7 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     nd_status st = md_alloc(m);
     if (st) { parent->last_error = m->sub.last_error; md_destroy(m); return st; }
     Ctx* c = &m->sub;
-    const size_t bytes = 3 * sizeof(double) * (size_t)n;
-    // staging: x and v (AoS), q, m
-    if ((st = ensure(c, m->aos, 2 * bytes + 2 * sizeof(double) * (size_t)n))) { md_destroy(m); return st; }
-    double* ax = (double*)m->aos.p;
-    double* av = ax + 3 * (size_t)n;
-    double* aq = av + 3 * (size_t)n;
-    double* am = aq + (size_t)n;
-    cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-    cudaError_t e = cudaMemcpyAsync(ax, xd, bytes, kind, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(av, vd, bytes, kind, c->stream);
-    if (e == cudaSuccess && qd) e = cudaMemcpyAsync(aq, qd, sizeof(double) * n, kind, c->stream);
-    if (e == cudaSuccess && md_) e = cudaMemcpyAsync(am, md_, sizeof(double) * n, kind, c->stream);
-    if (e != cudaSuccess) { st = cuda_fail(c, e, "md upload"); parent->last_error = c->last_error; md_destroy(m); return st; }
-    const unsigned g = (unsigned)cdiv(n, 256);
-    SetPtrs& s = m->set[0];
-    k_md_split_aos<<<g, 256, 0, c->stream>>>(ax, n, s.x[0], s.x[1], s.x[2]);
-    k_md_split_aos<<<g, 256, 0, c->stream>>>(av, n, s.w[0], s.w[1], s.w[2]);
-    k_md_init_scalars<<<g, 256, 0, c->stream>>>(qd ? aq : nullptr, md_ ? am : nullptr, n, s.q, s.im,
-                                                s.orig);
-    c->launches += 3;
+    if ((st = md_upload(m, xd, vd, qd, md_, host))) { parent->last_error = c->last_error; md_destroy(m); return st; }
     m->cur = 0;
     m->first = true;
     if ((st = md_size_list(m))) { parent->last_error = c->last_error; md_destroy(m); return st; }
@@ -597,7 +673,7 @@ nd_status md_destroy(MDEngine* m) {
         if (m->graph[w]) cudaGraphExecDestroy(m->graph[w]);
     DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->sh_buf[0], &m->sh_buf[1], &m->xyz32,
                       &m->pos32, &m->keys, &m->store, &m->nbr, &m->ncount, &m->f, &m->vtmp,
-                      &m->acc, &m->aos, &m->sub.codes, &m->sub.codes_alt, &m->sub.perm,
+                      &m->acc, &m->aos, &m->diag, &m->sub.codes, &m->sub.codes_alt, &m->sub.perm,
                       &m->sub.perm_alt, &m->sub.hist, &m->sub.misc};
     if (m->sub.stream) cudaStreamSynchronize(m->sub.stream);
     for (DevBuf* b : bufs)
@@ -717,6 +793,20 @@ nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list
         for (int32_t v : h) s += v;
         *list_pairs = s;
     }
+    return ND_OK;
+}
+
+nd_status md_diagnostics(MDEngine* m, int64_t* skin_violations, int32_t* max_neighbors) {
+    Ctx* c = &m->sub;
+    unsigned long long v = 0;
+    int32_t h[kErrWords];
+    cudaError_t e = cudaMemcpyAsync(&v, m->diag.p, sizeof(v), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h, c->d_err, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "md diagnostics");
+    if (skin_violations) *skin_violations = (int64_t)v;
+    if (max_neighbors) *max_neighbors = h[2];
     return ND_OK;
 }
 

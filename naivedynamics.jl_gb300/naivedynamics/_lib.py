@@ -113,6 +113,7 @@ SIGNATURES = {
     "nd_md_stats": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                            ctypes.POINTER(_i32)]),
     "nd_md_launches_per_run": (_i64, [_vp, _i64]),
+    "nd_md_diagnostics": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i32)]),
     "nd_simulate": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _vp, _i64]),
     "nd_synth_uniform": (_i32, [_u64, _i32, _d, _d, _vp]),
     "nd_synth_uniform_mindist": (_i32, [_u64, _i32, _d, _d, _vp]),

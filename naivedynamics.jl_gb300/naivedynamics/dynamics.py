@@ -256,5 +256,11 @@ class MDEngine:
                                               ctypes.byref(p), ctypes.byref(cap)), "nd_md_stats")
         return dict(steps=s.value, rebuilds=r.value, list_pairs=p.value, capacity=cap.value)
 
+    def diagnostics(self):
+        v, mx = ctypes.c_int64(), ctypes.c_int32()
+        self.ctx.check(_lib.lib().nd_md_diagnostics(self.handle, ctypes.byref(v), ctypes.byref(mx)),
+                       "nd_md_diagnostics")
+        return dict(skin_violations=v.value, max_neighbors=mx.value)
+
     def launches_per_run(self, steps: int) -> int:
         return int(_lib.lib().nd_md_launches_per_run(self.handle, int(steps)))
