@@ -172,6 +172,27 @@ nd_status nd_leaf_pairs_dev(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* sp
 nd_status nd_atom_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, int32_t order,
                         int32_t* pi, int32_t* pj, float* pd, int64_t capacity, int64_t* count);
 
+/*
+ * The leaf pair-list pipeline of nd_leaf_pairs_dev (same kernels, same results,
+ * bit for bit) for callers that cannot allocate device memory: code running
+ * under a host runtime that owns the device memory budget through its own pool,
+ * or a time-critical loop in which cudaMalloc/cudaFree would stall the device.
+ * No counterpart in the reference (it allocates freely).  Takes no context:
+ * positions (xyz, N x 3 Float32) and outputs (pi, pj, pd) are device pointers
+ * on the current device; *count is a host pointer; work is enqueued on `stream`
+ * (a cudaStream_t, NULL = default stream) and the call synchronises it to read
+ * the pair count.  Scratch is one file-scope device array of ~5.3 MB reserved
+ * on every GPU that loads the library until the process exits; nothing is
+ * allocated.  Limits: atom_count <= 65536 and atomsperleaf >= 2, otherwise
+ * ND_ERR_ARG.  All calls share that array, so calls that overlap on the GPU
+ * (other streams or host threads) race: serialise them.  The first call on a
+ * device looks up the array's address (with that device current); make it
+ * before any stream capture.  Errors are returned as status codes only.
+ */
+nd_status nd_leaf_pairs_noalloc_dev(const float* xyz, const nd_bvh_spec* spec, int32_t order,
+                                    int32_t mode, int32_t* pi, int32_t* pj, float* pd,
+                                    int64_t capacity, int64_t* count, void* stream);
+
 /* Order-free 128-bit hash of canonical (min(i,j), max(i,j), bits(d)) triples of
  * a device pair list (for verifying lists too large to copy to the host). */
 nd_status nd_pair_hash_dev(nd_ctx* ctx, const int32_t* pi, const int32_t* pj, const float* pd,

@@ -36,6 +36,10 @@ nd_status check_launch(Ctx* c, const char* what) {
 nd_status ensure(Ctx* c, DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.p && b.bytes >= bytes) return ND_OK;
+    if (c->no_alloc) {
+        c->last_error = "scratch slice too small (no-allocation mode)";
+        return ND_ERR_NOMEM;
+    }
     if (b.p) {
         cudaFree(b.p);
         b.p = nullptr;
@@ -123,9 +127,9 @@ static nd_status tree_from_host(Ctx* c, const float* xyz, const nd_bvh_spec* s, 
                       boxes, nkeys, overwrite_root, t);
 }
 
-static nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode,
-                              int kind, const float* xyz, bool host, int32_t* pi, int32_t* pj,
-                              float* pd, int64_t capacity, int64_t* count) {
+nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode, int kind,
+                       const float* xyz, bool host, int32_t* pi, int32_t* pj, float* pd,
+                       int64_t capacity, int64_t* count) {
     nd_status st = spec_ok(s);
     if (st) return st;
     if (!xyz || !count || capacity < 0) return ND_ERR_ARG;

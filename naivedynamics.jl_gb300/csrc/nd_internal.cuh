@@ -105,6 +105,7 @@ struct Ctx {
     DevBuf xyz, codes, codes_alt, perm, perm_alt, pos4, idx, keys, store, hist, counts, offsets,
         partial, pairs_i, pairs_j, pairs_d, misc, hash;
     struct MDEngine* sim_cache = nullptr;  // engine re-used by nd_simulate
+    bool no_alloc = false;                 // buffers are fixed slices: never grow them
 };
 
 // Grow `b` to at least `bytes` (contents are not preserved).
@@ -139,7 +140,11 @@ nd_status build_tree(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t a
 nd_status scan_exclusive(Ctx* c, const int64_t* in, int64_t* out, int64_t n, int64_t* total_dev);
 
 // Pair emission over a built tree (kind: 0 = leaf path, 1 = per-atom path) is
-// declared with the MD engine below.
+// declared with the MD engine below.  pairs_common runs the whole pair-list
+// pipeline on the context's buffers (host or device positions and outputs).
+nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode, int kind,
+                       const float* xyz, bool host, int32_t* pi, int32_t* pj, float* pd,
+                       int64_t capacity, int64_t* count);
 nd_status pair_hash(Ctx* c, const int32_t* pi, const int32_t* pj, const float* pd, int64_t np,
                     uint64_t out[2]);
 

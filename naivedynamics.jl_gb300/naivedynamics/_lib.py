@@ -98,6 +98,8 @@ SIGNATURES = {
     "nd_atom_pairs": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _i32, _vp, _vp, _vp, _i64,
                              ctypes.POINTER(_i64)]),
     "nd_pair_hash_dev": (_i32, [_vp, _vp, _vp, _vp, _i64, ctypes.POINTER(_u64)]),
+    "nd_leaf_pairs_noalloc_dev": (_i32, [_vp, ctypes.POINTER(BVHSpec), _i32, _i32, _vp, _vp, _vp,
+                                         _i64, ctypes.POINTER(_i64), _vp]),
     "nd_forces_pairs": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _i64,
                                _vp, ctypes.POINTER(_d)]),
     "nd_forces": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp,
