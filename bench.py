@@ -246,9 +246,10 @@ def run_gb300(args):
     k_ms = statistics.mean(s.elapsed_time(e) for (s, e) in single)
     nbr = stats["list_pairs"] / N_ATOMS  # full-list neighbours per atom
     # algorithmic bytes per atom of one fused step: x, v read+write (FP64, 96),
-    # own shadow record read (32) + next shadow write (32), force write (16),
-    # build-position read (16), list count (4), 4 B per listed neighbour
-    bytes_per_atom = 96 + 32 + 32 + 16 + 16 + 4 + 4 * nbr
+    # own fixed-point record read (16) + next record write (16), force write
+    # (16), build-position read (16), list count (4), 2 B per listed neighbour
+    # (uint16 index into the block's staged union)
+    bytes_per_atom = 96 + 16 + 16 + 16 + 16 + 4 + 2 * nbr
     traffic_alg = bytes_per_atom * N_ATOMS
     peaks, peak_kind = _peaks()
     achieved = traffic_alg / (k_ms * 1e-3) / 1e9

@@ -47,7 +47,7 @@ typedef int32_t nd_status;
 
 /* Atom ordering before the tree build. */
 #define ND_ORDER_REFERENCE 0  /* mortoncodes! bit-select code, bit-exact with the reference */
-#define ND_ORDER_SPATIAL   1  /* interleaved 10-bit/axis Morton code over the bounding box  */
+#define ND_ORDER_SPATIAL   1  /* 3-D Hilbert index, 10 bits/axis over the bounding box      */
 
 /* Leaf boxes. */
 #define ND_BOX_LEAF 0  /* leafcluster_primitives: p -/+ r/2 (BVHTraverse.jl:376-410) */

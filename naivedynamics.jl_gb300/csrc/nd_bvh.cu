@@ -79,7 +79,7 @@ __global__ void k_bbox_init(uint32_t* bbox) {
     if (threadIdx.x < 6) bbox[threadIdx.x] = threadIdx.x < 3 ? 0xffffffffu : 0u;
 }
 
-// Interleaved Morton code over the bounding box, 1024 bins per axis.
+// Spatial code: 3-D Hilbert index over the bounding box, 1024 bins per axis.
 __global__ void k_morton_spatial(const float* __restrict__ xyz, int32_t n,
                                  const uint32_t* __restrict__ bbox, int32_t* __restrict__ codes,
                                  int32_t* __restrict__ iota) {
@@ -95,7 +95,7 @@ __global__ void k_morton_spatial(const float* __restrict__ xyz, int32_t n,
         int32_t qi = (t < 0.0f) ? 0 : (t > 1023.0f ? 1023 : (int32_t)t);
         q[d] = (uint32_t)qi;
     }
-    codes[i] = (int32_t)(spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2));
+    codes[i] = (int32_t)hilbert3_10(q[0], q[1], q[2]);
     if (iota) iota[i] = i;
 }
 

@@ -65,6 +65,39 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
     return v;
 }
 
+// 3-D Hilbert index of a cell of a 1024^3 grid (10 bits per axis, 30-bit
+// result), by J. Skilling's transpose method ("Programming the Hilbert curve",
+// AIP Conf. Proc. 707, 2004): undo the excess work per bit plane, Gray-encode,
+// then interleave the transposed bits, x first.  Consecutive indices are
+// face-adjacent cells, so runs of consecutive atoms stay spatially compact.
+__host__ __device__ inline uint32_t hilbert3_10(uint32_t x, uint32_t y, uint32_t z) {
+    uint32_t X[3] = {x & 1023u, y & 1023u, z & 1023u};
+    for (uint32_t Q = 1u << 9; Q > 1u; Q >>= 1) {
+        const uint32_t P = Q - 1u;
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = 1u << 9; Q > 1u; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1u;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    uint32_t h = 0;
+    for (int q = 9; q >= 0; --q)
+        for (int i = 0; i < 3; ++i) h = (h << 1) | ((X[i] >> q) & 1u);
+    return h;
+}
+
 __host__ __device__ inline uint64_t mix64(uint64_t z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;

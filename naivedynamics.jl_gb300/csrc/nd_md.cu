@@ -7,16 +7,20 @@
 // Layout in HBM (atoms are kept in tree order and re-sorted at every rebuild):
 //   x[3][N], w[3][N]   FP64 positions and velocities, one array per component
 //                      (two sets, ping-ponged by the reorder at each rebuild)
-//   q[N], im[N]        FP64 charge and inverse mass (optional)
-//   sh[2N]             float4 shadow of x for the pair math, one 32-byte record
-//                      per atom: sh[2k] = (hi, q) with hi = fl32(x), sh[2k+1] =
-//                      (lo, 0) with lo = fl32(x - hi) (ping-ponged per step)
-//   nbr[cap][N]        full neighbour list, slot-major (coalesced per slot)
-//   f[N]               float4 forces of the last evaluation
-// One MD step is ONE kernel: each thread owns an atom, sums its pair forces
-// over its list (no atomics, deterministic), completes the pending half kick,
-// kicks, drifts, reflects and writes the next shadow.  Velocities are stored
-// at half steps between kernels (w = v_{n-1/2} after reflection).
+//   q[N], im[N]        FP64 charge and inverse mass
+//   rec[2][N]          int4 pair-math record per atom: fixed-point position
+//                      (int32 x, y, z in units of 1/S from the frame origin)
+//                      and the charge's float bits (ping-ponged per step)
+//   pos32[N]           float4 Float32 positions at the last rebuild (tree input)
+//   ulist[B][ucap]     per block of 256 atoms: the sorted leaves that hold any
+//                      neighbour of the block (the block's union), ucount[B]
+//   llist[B][lcap][256] uint16 per-atom neighbour lists as indices into the
+//                      block's union (slot-major inside the block), ncount[N]
+// One MD step is ONE kernel: a block stages its union's records in shared
+// memory, each thread sums its atom's pair forces over its own exact list (no
+// atomics, deterministic), completes the pending half kick, kicks, drifts,
+// reflects and writes the next record.  Velocities are stored at half steps
+// between kernels (w = v_{n-1/2} after reflection).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -26,9 +30,25 @@
 
 namespace nd {
 
-struct MDEngine;
+constexpr int kBlock = 256;          // atoms per block in the list and step kernels
+constexpr int kFrontierCap = 4096;   // BFS frontier entries per buffer
+constexpr int kSizingUcap = 8192;    // union capacity of the sizing build
 
-// ------------------------------------------------------------- kernels
+// Fixed-point frame of the pair records: x_fp = rint((x - origin) * scale).
+struct Frame {
+    double o[3];
+    double s;
+};
+
+struct SetPtrs {
+    double* x[3];
+    double* w[3];
+    double* q;
+    double* im;
+    int32_t* orig;
+};
+
+// ------------------------------------------------------------- small kernels
 
 __global__ void k_md_split_aos(const double* __restrict__ aos, int32_t n, double* x0, double* x1,
                                double* x2) {
@@ -57,34 +77,31 @@ __global__ void k_md_pos32(const double* __restrict__ x0, const double* __restri
     xyz[3 * (int64_t)i + 2] = (float)x2[i];
 }
 
-__device__ __forceinline__ void split_df(double x, float& hi, float& lo) {
-    hi = __double2float_rn(x);
-    lo = __double2float_rn(x - (double)hi);
+__device__ __forceinline__ int32_t to_fixed(double x, double o, double s, int32_t* err,
+                                            int32_t who) {
+    double t = (x - o) * s;
+    if (!(t > -2147483000.0 && t < 2147483000.0)) {
+        set_error(err, isfinite(x) ? ND_ERR_RANGE : ND_ERR_NONFINITE, who);
+        t = 0.0;
+    }
+    return __double2int_rn(t);
 }
 
-struct SetPtrs {
-    double* x[3];
-    double* w[3];
-    double* q;
-    double* im;
-    int32_t* orig;
-};
-
-// Gather every per-atom array into the new (sorted) order and refresh the
-// float shadows; pos32 keeps the Float32 positions used by the tree.
+// Gather every per-atom array into the new (sorted) order; write the pair
+// records and the Float32 positions of the tree.
 __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict__ perm,
-                             const float* __restrict__ xyz32, int32_t n, float4* __restrict__ pos32,
-                             float4* __restrict__ sh) {
+                             const float* __restrict__ xyz32, int32_t n, Frame fr,
+                             float4* __restrict__ pos32, int4* __restrict__ rec, int32_t* err) {
     int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int32_t o = perm[k];
-    float h[3], l[3];
+    int32_t f[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double xv = src.x[d][o];
         dst.x[d][k] = xv;
         dst.w[d][k] = src.w[d][o];
-        split_df(xv, h[d], l[d]);
+        f[d] = to_fixed(xv, fr.o[d], fr.s, err, k);
     }
     double qv = src.q[o];
     dst.q[k] = qv;
@@ -92,8 +109,7 @@ __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict
     dst.orig[k] = src.orig[o];
     pos32[k] = make_float4(xyz32[3 * (int64_t)o], xyz32[3 * (int64_t)o + 1],
                            xyz32[3 * (int64_t)o + 2], __int_as_float(k));
-    sh[2 * (int64_t)k] = make_float4(h[0], h[1], h[2], (float)qv);
-    sh[2 * (int64_t)k + 1] = make_float4(l[0], l[1], l[2], 0.0f);
+    rec[k] = make_int4(f[0], f[1], f[2], __float_as_int((float)qv));
 }
 
 // Leaf boxes (p -/+ h) of already sorted Float32 positions.
@@ -115,109 +131,223 @@ __global__ void k_md_leaf_boxes(const float4* __restrict__ pos, int32_t nL, int3
     keys[2 * (int64_t)leaf + 1] = make_float4(mx[1], mx[2], __int_as_float(0), __int_as_float(0));
 }
 
-// Full neighbour list: every atom walks the tree from the root with its own
-// box (p -/+ h_q, h_q slightly above r_list/2 so the box test never drops a
-// pair) and keeps the j != i with d^2 < r_list^2 (Float32, reference formula).
-__global__ void __launch_bounds__(128)
-    k_md_neighbors(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t n,
-                   int32_t nL, int32_t apl, float hq, float rl2, int32_t cap,
-                   int32_t* __restrict__ nbr, int32_t* __restrict__ ncount, int32_t* err) {
-    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 p = __ldg(&pos[i]);
-    float qmnx = __fsub_rn(p.x, hq), qmny = __fsub_rn(p.y, hq), qmnz = __fsub_rn(p.z, hq);
-    float qmxx = __fadd_rn(p.x, hq), qmxy = __fadd_rn(p.y, hq), qmxz = __fadd_rn(p.z, hq);
-    int32_t cnt = 0;
-    int32_t t = nL + 1;
-    int64_t guard = 0;
-    const int64_t max_visits = 4LL * nL + 8;
-    while (t != 0) {
-        if (++guard > max_visits || t < 1 || t > 2 * nL - 1) { set_error(err, ND_ERR_INTERNAL, i); break; }
-        float4 a = __ldg(&keys[2 * (int64_t)(t - 1)]);
-        float4 b = __ldg(&keys[2 * (int64_t)(t - 1) + 1]);
-        int32_t left = __float_as_int(b.z), skip = __float_as_int(b.w);
-        bool ov = (qmnx < a.w) & (qmxx > a.x) & (qmny < b.x) & (qmxy > a.y) & (qmnz < b.y) &
-                  (qmxz > a.z);
-        if (ov) {
-            if (left == 0) {
-                int64_t base = (int64_t)(t - 1) * apl;
-                for (int32_t e = 0; e < apl; ++e) {
-                    int32_t j = (int32_t)(base + e);
-                    if (j == i) continue;
-                    float4 q = __ldg(&pos[j]);
-                    float d2 = dist2_ref(p.x, p.y, p.z, q.x, q.y, q.z);
-                    if (d2 < rl2) {
-                        if (cnt < cap) nbr[(int64_t)cnt * n + i] = j;
-                        ++cnt;
-                    }
-                }
-                t = skip;
-            } else {
-                t = left;
-            }
-        } else {
-            t = skip;
-        }
-    }
-    ncount[i] = min(cnt, cap);
-    if (cnt > cap) set_error(err, ND_ERR_OVERFLOW, i);
-    atomicMax(err + 2, cnt);
+// ------------------------------------------------ block union (tree BFS)
+
+__device__ __forceinline__ bool box_overlap(float qmnx, float qmny, float qmnz, float qmxx,
+                                            float qmxy, float qmxz, const float4& a,
+                                            const float4& b) {
+    // aabb_overlap_test (BVHTraverse.jl:1094-1098) against a node stored as
+    // (min.x, min.y, min.z, max.x), (max.y, max.z, left, skip)
+    return (qmnx < a.w) & (qmxx > a.x) & (qmny < b.x) & (qmxy > a.y) & (qmnz < b.y) &
+           (qmxz > a.z);
 }
 
+// One block per 256 atoms: the boxes of its eight warps (their atoms -/+ hq)
+// are tested against the tree breadth-first -- all 256 threads expand the
+// current level together, a node's children being (left, skip of left) in the
+// rope layout -- and every leaf overlapping any of them joins the union.  The union is sorted (bitonic)
+// so list order, and hence force summation order, is deterministic.
+// Shared memory: two frontier buffers of kFrontierCap and the union (upow2).
+__global__ void __launch_bounds__(kBlock)
+    k_md_block_union(const float4* __restrict__ keys, const float4* __restrict__ pos,
+                     int32_t n, int32_t nL, float hq, int32_t ucap, int32_t upow2,
+                     int32_t* __restrict__ ulist, int32_t* __restrict__ ucount, int32_t* err,
+                     int32_t* diag, int32_t sizing) {
+    extern __shared__ int32_t smem[];
+    int32_t* fr[2] = {smem, smem + kFrontierCap};
+    int32_t* su = smem + 2 * kFrontierCap;
+    __shared__ int32_t s_cnt[2];
+    __shared__ int32_t s_nu;
+    __shared__ float s_wb[kBlock / 32][6];  // per-warp query boxes (min xyz, max xyz)
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t i = (int64_t)blockIdx.x * kBlock + tid;
+    float mn[3], mx[3];
+    {
+        float4 p = pos[i < n ? i : (int64_t)blockIdx.x * kBlock];
+        mn[0] = mx[0] = p.x; mn[1] = mx[1] = p.y; mn[2] = mx[2] = p.z;
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        for (int s = 16; s > 0; s >>= 1) {
+            mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], s));
+            mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], s));
+        }
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) { s_wb[warp][d] = mn[d] - hq; s_wb[warp][3 + d] = mx[d] + hq; }
+    if (tid == 0) { s_cnt[0] = 1; s_cnt[1] = 0; s_nu = 0; fr[0][0] = (nL + 1) << 1; }
+    __syncthreads();
+    int cur = 0;
+    for (int level = 0; level < 256; ++level) {
+        const int32_t nf = min(s_cnt[cur], kFrontierCap);
+        if (nf == 0) break;
+        for (int32_t k = tid; k < nf; k += kBlock) {
+            const int32_t e = fr[cur][k];
+            const int32_t t = e >> 1;
+            if (t < 1 || t > 2 * nL - 1) { set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x); continue; }
+            const float4 a = __ldg(&keys[2 * (int64_t)(t - 1)]);
+            const float4 b = __ldg(&keys[2 * (int64_t)(t - 1) + 1]);
+            const int32_t left = __float_as_int(b.z), skip = __float_as_int(b.w);
+            if (e & 1) {  // a left child: its skip rope is its right sibling
+                int32_t slot = atomicAdd(&s_cnt[cur ^ 1], 1);
+                if (slot < kFrontierCap) fr[cur ^ 1][slot] = skip << 1;
+            }
+            bool hit = false;
+            for (int w = 0; w < kBlock / 32 && !hit; ++w)
+                hit = box_overlap(s_wb[w][0], s_wb[w][1], s_wb[w][2], s_wb[w][3], s_wb[w][4],
+                                  s_wb[w][5], a, b);
+            if (hit) {
+                if (left == 0) {
+                    int32_t slot = atomicAdd(&s_nu, 1);
+                    if (slot < upow2) su[slot] = t - 1;
+                } else {
+                    int32_t slot = atomicAdd(&s_cnt[cur ^ 1], 1);
+                    if (slot < kFrontierCap) fr[cur ^ 1][slot] = (left << 1) | 1;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (s_cnt[cur ^ 1] > kFrontierCap) set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x);
+            s_cnt[cur] = 0;
+        }
+        cur ^= 1;
+        __syncthreads();
+    }
+    const int32_t nu = s_nu;
+    if (tid == 0) atomicMax(&diag[0], nu);
+    if (nu > ucap) {
+        if (tid == 0 && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)blockIdx.x);
+        if (tid == 0) ucount[blockIdx.x] = 0;
+        return;
+    }
+    // bitonic sort of the union (padded to a power of two)
+    int32_t p2 = 1;
+    while (p2 < nu) p2 <<= 1;
+    for (int32_t k = nu + tid; k < p2; k += kBlock) su[k] = INT32_MAX;
+    __syncthreads();
+    for (int32_t size = 2; size <= p2; size <<= 1) {
+        for (int32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int32_t k = tid; k < p2 / 2; k += kBlock) {
+                int32_t lo = 2 * k - (k & (stride - 1));
+                int32_t hi = lo + stride;
+                bool up = ((lo & size) == 0);
+                int32_t a = su[lo], b = su[hi];
+                if ((a > b) == up) { su[lo] = b; su[hi] = a; }
+            }
+            __syncthreads();
+        }
+    }
+    int32_t* dst = ulist + (int64_t)blockIdx.x * ucap;
+    for (int32_t k = tid; k < nu; k += kBlock) dst[k] = su[k];
+    if (tid == 0) ucount[blockIdx.x] = nu;
+}
+
+// Exact per-atom lists inside the block's union: every thread scans the union
+// with block-uniform loads (one address per warp request), tests its own box
+// (p -/+ hq) against each leaf box and the leaf's atoms with the reference
+// distance (Float32, d^2 < r_list^2), and stores union indices as uint16.
+__global__ void __launch_bounds__(kBlock)
+    k_md_block_lists(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t n,
+                     int32_t apl, float hq, float rl2, int32_t ucap,
+                     const int32_t* __restrict__ ulist, const int32_t* __restrict__ ucount,
+                     int32_t lcap, uint16_t* __restrict__ llist, int32_t* __restrict__ ncount,
+                     int32_t* err, int32_t* diag, int32_t sizing) {
+    const int tid = threadIdx.x;
+    const int64_t i = (int64_t)blockIdx.x * kBlock + tid;
+    const bool valid = i < n;
+    const float4 p = __ldg(&pos[valid ? i : (int64_t)blockIdx.x * kBlock]);
+    const float qmnx = __fsub_rn(p.x, hq), qmny = __fsub_rn(p.y, hq), qmnz = __fsub_rn(p.z, hq);
+    const float qmxx = __fadd_rn(p.x, hq), qmxy = __fadd_rn(p.y, hq), qmxz = __fadd_rn(p.z, hq);
+    const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
+    const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
+    uint16_t* __restrict__ L = llist + (int64_t)blockIdx.x * lcap * kBlock + tid;
+    int32_t cnt = 0;
+    for (int32_t u = 0; u < nu; ++u) {
+        const int32_t leaf = __ldg(&U[u]);
+        const float4 a = __ldg(&keys[2 * (int64_t)leaf]);
+        const float4 b = __ldg(&keys[2 * (int64_t)leaf + 1]);
+        if (valid && box_overlap(qmnx, qmny, qmnz, qmxx, qmxy, qmxz, a, b)) {
+            for (int32_t e = 0; e < apl; ++e) {
+                const int64_t j = (int64_t)leaf * apl + e;
+                if (j == i) continue;
+                const float4 q = __ldg(&pos[j]);
+                if (dist2_ref(p.x, p.y, p.z, q.x, q.y, q.z) < rl2) {
+                    if (cnt < lcap) L[(int64_t)cnt * kBlock] = (uint16_t)(u * apl + e);
+                    ++cnt;
+                }
+            }
+        }
+    }
+    if (!valid) return;
+    ncount[i] = min(cnt, lcap);
+    if (cnt > lcap && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)i);
+    atomicMax(&diag[1], cnt);
+}
+
+// ------------------------------------------------------------- step kernel
+
 struct StepArgs {
-    int32_t n;
-    const int32_t* __restrict__ nbr;
+    int32_t n, apl, ucap, lcap;
+    const int32_t* __restrict__ ulist;
+    const int32_t* __restrict__ ucount;
+    const uint16_t* __restrict__ llist;
     const int32_t* __restrict__ ncount;
-    const float4* __restrict__ sh_in;  // interleaved (hi, lo) records
-    float4* __restrict__ sh_out;
+    const int4* __restrict__ rec_in;
+    int4* __restrict__ rec_out;
     double* x[3];
     double* w[3];
     const double* __restrict__ im;
     float4* __restrict__ f_out;
-    double* __restrict__ v_out[3];  // measure kernel: integer-step velocity
-    double* __restrict__ acc;       // measure kernel: [0] potential, [1] kinetic
-    const float4* __restrict__ pos_build;  // Float32 positions at the last rebuild
-    unsigned long long* __restrict__ diag; // [0] atom-steps that moved > skin/2 since the build
+    double* __restrict__ v_out[3];  // measure mode: integer-step velocity
+    double* __restrict__ acc;       // measure mode: [0] potential, [1] kinetic
+    const float4* __restrict__ pos_build;   // Float32 positions at the last rebuild
+    unsigned long long* __restrict__ diag;  // [0] atom-steps moved > skin/2 since the build
+    int32_t* err;
     float half_skin2;
-    float rc2, sig2, eps24, eps4, kc;
-    float hdt;                      // dt / 2
+    // pair constants in fixed-point units (S = frame scale)
+    float rc2u;    // (r_c S)^2
+    float sig2u;   // (sigma S)^2
+    float eps24u;  // 24 eps S
+    float eps4;    // 4 eps
+    float kcu;     // k S^2   (Coulomb force)
+    float kceu;    // k S     (Coulomb energy)
+    float hdt;     // dt / 2
     double dt;
     double lo[3], hi[3];
+    Frame fr;
 };
 
-// LJ + Coulomb pair force magnitude over r (F_ij = fmag * r_ij) and energy.
+// Pair (i, j) from fixed-point records: the integer difference is exact, its
+// conversion to float rounds once, so r_ij keeps full single precision at any
+// box size inside the frame.  Constants are pre-scaled, so the force comes out
+// in physical units per fixed-point unit of displacement.
 template <bool COUL, bool ENERGY>
-__device__ __forceinline__ void pair_lj_coul(float r2, float qq, const StepArgs& a, float& fmag,
-                                             float& u) {
-    float inv_r2 = __frcp_rn(r2);
-    float s2 = a.sig2 * inv_r2;
-    float s6 = s2 * s2 * s2;
-    fmag = a.eps24 * inv_r2 * s6 * (2.0f * s6 - 1.0f);
-    if (ENERGY) u = a.eps4 * s6 * (s6 - 1.0f);
-    if (COUL) {
-        float inv_r = rsqrtf(r2);
-        inv_r = inv_r * (1.5f - 0.5f * r2 * inv_r * inv_r);  // one Newton step
-        float e = a.kc * qq * inv_r;
-        fmag += e * inv_r2;
-        if (ENERGY) u += e;
-    }
-}
-
-// Pair (i, j): displacement from the (hi, lo) records -- the hi difference of
-// two nearby floats is exact or correctly rounded relative to the result, so
-// r_ij keeps ~1e-7 relative accuracy even at box sides of 68 -- then the
-// cutoff test and the accumulation of F_i and (optionally) U_i.
-template <bool COUL, bool ENERGY>
-__device__ __forceinline__ void accum_pair(const float4& hi, const float4& lo, const float4& hj,
-                                          const float4& lj, const StepArgs& a, float& fx,
-                                          float& fy, float& fz, float& ue) {
-    float dx = (hi.x - hj.x) + (lo.x - lj.x);
-    float dy = (hi.y - hj.y) + (lo.y - lj.y);
-    float dz = (hi.z - hj.z) + (lo.z - lj.z);
-    float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < a.rc2) {
-        float fmag, u = 0.f;
-        pair_lj_coul<COUL, ENERGY>(r2, hi.w * hj.w, a, fmag, u);
+__device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const StepArgs& a,
+                                          float& fx, float& fy, float& fz, float& ue) {
+    const float dx = (float)(ri.x - rj.x);
+    const float dy = (float)(ri.y - rj.y);
+    const float dz = (float)(ri.z - rj.z);
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < a.rc2u) {
+        float inv_r2, inv_r = 0.f;
+        if (COUL) {
+            inv_r = rsqrtf(r2);
+            inv_r = inv_r * (1.5f - 0.5f * r2 * inv_r * inv_r);  // one Newton step
+            inv_r2 = inv_r * inv_r;
+        } else {
+            inv_r2 = __fdividef(1.0f, r2);
+            inv_r2 = inv_r2 * (2.0f - r2 * inv_r2);  // one Newton step
+        }
+        const float s2 = a.sig2u * inv_r2;
+        const float s6 = s2 * s2 * s2;
+        float fmag = a.eps24u * inv_r2 * s6 * (2.0f * s6 - 1.0f);
+        float u = 0.f;
+        if (ENERGY) u = a.eps4 * s6 * (s6 - 1.0f);
+        if (COUL) {
+            const float qq = __int_as_float(ri.w) * __int_as_float(rj.w);
+            fmag += a.kcu * qq * inv_r * inv_r2;
+            if (ENERGY) u += a.kceu * qq * inv_r;
+        }
         fx += fmag * dx;
         fy += fmag * dy;
         fz += fmag * dz;
@@ -225,48 +355,46 @@ __device__ __forceinline__ void accum_pair(const float4& hi, const float4& lo, c
     }
 }
 
-// One thread per atom.  MODE 0: step (force, pending half kick, kick, drift,
-// reflect, new shadow).  MODE 1: measure (force, integer-step velocity and
-// energies; state untouched).
+// One block per 256 atoms.  MODE 0: step (force, pending half kick, kick,
+// drift, reflect, next record).  MODE 1: measure (force, integer-step velocity
+// and energies; state untouched).
 template <bool COUL, bool MASS, bool FIRST, int MODE>
-__global__ void __launch_bounds__(128) k_md_step(StepArgs a) {
-    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
+    extern __shared__ int4 srec[];
+    const int tid = threadIdx.x;
+    int64_t i = (int64_t)blockIdx.x * kBlock + tid;
     const bool valid = i < a.n;
+    // stage the block's union: record of atom (leaf * apl + e) at u * apl + e
+    {
+        const int32_t nu = min(__ldg(&a.ucount[blockIdx.x]), a.ucap);
+        const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
+        const int32_t m = nu * a.apl;
+        for (int32_t k = tid; k < m; k += kBlock) {
+            const int32_t u = k / a.apl, e = k - u * a.apl;
+            srec[k] = __ldg(&a.rec_in[(int64_t)__ldg(&U[u]) * a.apl + e]);
+        }
+    }
+    __syncthreads();
     if (MODE == 0 && !valid) return;
     if (!valid) i = a.n - 1;  // measure: idle lanes join the warp reduction with zeros
-    const float4 hi = __ldg(&a.sh_in[2 * (int64_t)i]);
-    const float4 lo = __ldg(&a.sh_in[2 * (int64_t)i + 1]);
+    const int4 ri = __ldg(&a.rec_in[i]);
     const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
+    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
     float fx = 0.f, fy = 0.f, fz = 0.f, ue = 0.f;
-    const int32_t* __restrict__ nb = a.nbr + i;
-    const int64_t stride = a.n;
-    // Neighbours in groups of four: the four index loads and eight record
-    // loads of a group are independent, so they are in flight together.
     int32_t s = 0;
     for (; s + 4 <= cnt; s += 4) {
-        int32_t j[4];
+        int4 rj[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) j[k] = __ldg(nb + (int64_t)(s + k) * stride);
-        float4 hj[4], lj[4];
+        for (int k = 0; k < 4; ++k) rj[k] = srec[L[(int64_t)(s + k) * kBlock]];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            hj[k] = __ldg(&a.sh_in[2 * (int64_t)j[k]]);
-            lj[k] = __ldg(&a.sh_in[2 * (int64_t)j[k] + 1]);
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            accum_pair<COUL, MODE == 1>(hi, lo, hj[k], lj[k], a, fx, fy, fz, ue);
+        for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], a, fx, fy, fz, ue);
     }
-    for (; s < cnt; ++s) {
-        int32_t j = __ldg(nb + (int64_t)s * stride);
-        float4 hj = __ldg(&a.sh_in[2 * (int64_t)j]);
-        float4 lj = __ldg(&a.sh_in[2 * (int64_t)j + 1]);
-        accum_pair<COUL, MODE == 1>(hi, lo, hj, lj, a, fx, fy, fz, ue);
-    }
+    for (; s < cnt; ++s)
+        accum_pair<COUL, MODE == 1>(ri, srec[L[(int64_t)s * kBlock]], a, fx, fy, fz, ue);
     if (valid) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
     const double imv = MASS ? a.im[i] : 1.0;
     const float fv[3] = {fx, fy, fz};
-    if (MODE == 1) {
+    if constexpr (MODE == 1) {
         double ke = 0.0;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -278,18 +406,18 @@ __global__ void __launch_bounds__(128) k_md_step(StepArgs a) {
         double mass = MASS ? 1.0 / imv : 1.0;
         double pe = valid ? 0.5 * (double)ue : 0.0;
         ke = valid ? ke * 0.5 * mass : 0.0;
-        // warp reduction then one FP64 atomic per warp (all 32 lanes present)
-        for (int s = 16; s > 0; s >>= 1) {
-            pe += __shfl_xor_sync(0xffffffffu, pe, s);
-            ke += __shfl_xor_sync(0xffffffffu, ke, s);
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            pe += __shfl_xor_sync(0xffffffffu, pe, sh);
+            ke += __shfl_xor_sync(0xffffffffu, ke, sh);
         }
-        if ((threadIdx.x & 31) == 0) {
+        if ((tid & 31) == 0) {
             atomicAdd(&a.acc[0], pe);
             atomicAdd(&a.acc[1], ke);
         }
         return;
     }
-    float h[3], l[3];
+    int32_t fx3[3];
+    float xf[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double kick = (double)(a.hdt * fv[d]) * imv;
@@ -300,14 +428,14 @@ __global__ void __launch_bounds__(128) k_md_step(StepArgs a) {
         if (a.hi[d] < x) { v = -v; x = a.hi[d]; }
         a.x[d][i] = x;
         a.w[d][i] = v;
-        split_df(x, h[d], l[d]);
+        fx3[d] = to_fixed(x, a.fr.o[d], a.fr.s, a.err, (int32_t)i);
+        xf[d] = (float)x;
     }
-    a.sh_out[2 * (int64_t)i] = make_float4(h[0], h[1], h[2], hi.w);
-    a.sh_out[2 * (int64_t)i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+    a.rec_out[i] = make_int4(fx3[0], fx3[1], fx3[2], ri.w);
     // A list built at r_c + skin stays valid while no atom moved more than
     // skin/2 since the build; count the atom-steps that broke that bound.
     const float4 pb = __ldg(&a.pos_build[i]);
-    const float ex = h[0] - pb.x, ey = h[1] - pb.y, ez = h[2] - pb.z;
+    const float ex = xf[0] - pb.x, ey = xf[1] - pb.y, ez = xf[2] - pb.z;
     if (ex * ex + ey * ey + ez * ez > a.half_skin2) atomicAdd(a.diag, 1ull);
 }
 
@@ -323,7 +451,13 @@ __global__ void k_md_unsort(const int32_t* __restrict__ orig, int32_t n, const d
     if (fo) { float4 g = f[k]; fo[3 * o] = g.x; fo[3 * o + 1] = g.y; fo[3 * o + 2] = g.z; }
 }
 
-// Reference call shape: forces over an explicit (1-based) pair list.
+// Reference call shape: forces over an explicit (1-based) pair list, physical
+// units; displacement from hi/lo float splits of the FP64 positions.
+__device__ __forceinline__ void split_df(double x, float& hi, float& lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+}
+
 __global__ void k_pair_forces(const double* __restrict__ x, const double* __restrict__ q,
                               const int32_t* __restrict__ pi, const int32_t* __restrict__ pj,
                               int64_t np, int32_t n, float rc2, float sig2, float eps24,
@@ -334,20 +468,28 @@ __global__ void k_pair_forces(const double* __restrict__ x, const double* __rest
          k += (int64_t)gridDim.x * blockDim.x) {
         int32_t i = pi[k] - 1, j = pj[k] - 1;
         if (i < 0 || j < 0 || i >= n || j >= n) { set_error(err, ND_ERR_ARG, (int32_t)k); continue; }
-        float hx, lx, hy, ly, hz, lz, gx, mx, gy, my, gz, mz;
-        split_df(x[3 * (int64_t)i], hx, lx); split_df(x[3 * (int64_t)i + 1], hy, ly);
-        split_df(x[3 * (int64_t)i + 2], hz, lz);
-        split_df(x[3 * (int64_t)j], gx, mx); split_df(x[3 * (int64_t)j + 1], gy, my);
-        split_df(x[3 * (int64_t)j + 2], gz, mz);
-        float dx = (hx - gx) + (lx - mx), dy = (hy - gy) + (ly - my), dz = (hz - gz) + (lz - mz);
+        float h[6], l[6];
+        for (int d = 0; d < 3; ++d) {
+            split_df(x[3 * (int64_t)i + d], h[d], l[d]);
+            split_df(x[3 * (int64_t)j + d], h[3 + d], l[3 + d]);
+        }
+        float dx = (h[0] - h[3]) + (l[0] - l[3]);
+        float dy = (h[1] - h[4]) + (l[1] - l[4]);
+        float dz = (h[2] - h[5]) + (l[2] - l[5]);
         float r2 = dx * dx + dy * dy + dz * dz;
         if (!(r2 < rc2)) continue;
-        StepArgs a;
-        a.sig2 = sig2; a.eps24 = eps24; a.eps4 = eps4; a.kc = kc;
-        float fmag, u = 0.f;
-        float qq = q ? (float)q[i] * (float)q[j] : 0.f;
-        if (q) pair_lj_coul<true, true>(r2, qq, a, fmag, u);
-        else pair_lj_coul<false, true>(r2, qq, a, fmag, u);
+        float inv_r2 = 1.0f / r2;
+        float s2 = sig2 * inv_r2;
+        float s6 = s2 * s2 * s2;
+        float fmag = eps24 * inv_r2 * s6 * (2.0f * s6 - 1.0f);
+        float u = eps4 * s6 * (s6 - 1.0f);
+        if (q) {
+            float inv_r = rsqrtf(r2);
+            inv_r = inv_r * (1.5f - 0.5f * r2 * inv_r * inv_r);
+            float e = kc * (float)q[i] * (float)q[j] * inv_r;
+            fmag += e * inv_r2;
+            u += e;
+        }
         ue += (double)u;
         atomicAdd(&f[3 * (int64_t)i], fmag * dx); atomicAdd(&f[3 * (int64_t)i + 1], fmag * dy);
         atomicAdd(&f[3 * (int64_t)i + 2], fmag * dz);
@@ -364,19 +506,22 @@ struct MDEngine {
     Ctx* parent = nullptr;
     Ctx sub;  // private scratch for the rebuild pipeline (stable pointers for graphs)
     nd_md_params p{};
-    int32_t n = 0, nL = 0, apl = 4, cap = 0;
+    int32_t n = 0, nL = 0, apl = 4, nblocks = 0;
+    int32_t lcap = 0, ucap = 0, upow2 = 0;
     bool has_q = false, has_m = false;
     bool first = true;
-    int cur = 0;        // current state set
-    int sh = 0;         // current shadow buffer
+    int cur = 0;            // current state set
+    int rc = 0;             // current record buffer
     int32_t in_window = 0;  // steps done in the current window
     bool rebuild_due = false;
     int64_t steps = 0, rebuilds = 0;
-    DevBuf set_buf[2], sh_buf[2], xyz32, pos32, keys, store, nbr, ncount, f, vtmp, acc, aos, diag;
+    Frame fr{};
+    DevBuf set_buf[2], rec_buf[2], xyz32, pos32, keys, store, ulist, ucount, llist, ncount, f,
+        vtmp, acc, aos, diag;
     SetPtrs set[2];
-    float4* shadow[2];
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int64_t graph_launches = 0;  // kernels per captured window
+    size_t step_smem = 0, union_smem = 0;
 };
 
 static nd_status md_alloc(MDEngine* m) {
@@ -391,13 +536,13 @@ static nd_status md_alloc(MDEngine* m) {
         m->set[s].q = b + 6 * n;
         m->set[s].im = b + 7 * n;
         m->set[s].orig = (int32_t*)(b + 8 * n);
-        if ((st = ensure(c, m->sh_buf[s], 2 * n * sizeof(float4)))) return st;
-        m->shadow[s] = (float4*)m->sh_buf[s].p;
+        if ((st = ensure(c, m->rec_buf[s], n * sizeof(int4)))) return st;
     }
     if ((st = ensure(c, m->xyz32, 3 * n * sizeof(float)))) return st;
     if ((st = ensure(c, m->pos32, n * sizeof(float4)))) return st;
     if ((st = ensure(c, m->keys, 32 * (size_t)(2 * m->nL)))) return st;
     if ((st = ensure(c, m->store, sizeof(int32_t) * (size_t)m->nL))) return st;
+    if ((st = ensure(c, m->ucount, sizeof(int32_t) * (size_t)m->nblocks))) return st;
     if ((st = ensure(c, m->ncount, sizeof(int32_t) * n))) return st;
     if ((st = ensure(c, m->f, sizeof(float4) * n))) return st;
     if ((st = ensure(c, m->vtmp, 3 * sizeof(double) * n))) return st;
@@ -414,14 +559,69 @@ static nd_status md_alloc(MDEngine* m) {
     return ND_OK;
 }
 
-static StepArgs md_step_args(MDEngine* m, int shadow_in) {
+static cudaError_t raise_smem_limit(const void* fn, int maxsm) {
+    cudaFuncAttributes fa{};
+    cudaError_t e = cudaFuncGetAttributes(&fa, fn);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                maxsm - (int)fa.sharedSizeBytes);
+}
+
+// Union and list buffers for capacities (ucap, lcap), and the shared-memory
+// opt-ins of the kernels that stage them.
+static nd_status md_alloc_lists(MDEngine* m, int32_t ucap, int32_t lcap) {
+    Ctx* c = &m->sub;
+    nd_status st;
+    m->ucap = ucap;
+    m->lcap = lcap;
+    int32_t p2 = 1;
+    while (p2 < ucap) p2 <<= 1;
+    m->upow2 = p2;
+    if ((st = ensure(c, m->ulist, sizeof(int32_t) * (size_t)ucap * m->nblocks))) return st;
+    if (lcap > 0 &&
+        (st = ensure(c, m->llist, sizeof(uint16_t) * (size_t)lcap * kBlock * m->nblocks)))
+        return st;
+    m->union_smem = sizeof(int32_t) * (2 * (size_t)kFrontierCap + p2);
+    m->step_smem = sizeof(int4) * (size_t)ucap * m->apl;
+    int maxsm = 0;
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    if ((int)m->union_smem + 1024 > maxsm || (lcap > 0 && (int)m->step_smem + 1024 > maxsm)) {
+        c->last_error = "neighbour union too large for shared memory";
+        return ND_ERR_OVERFLOW;
+    }
+    // The dynamic shared-memory limit is a per-function, process-wide
+    // attribute; every engine launches with its own size, so the limit is
+    // raised once to the device maximum (less the function's static shared
+    // memory) rather than set per engine.
+    cudaError_t e = raise_smem_limit((const void*)k_md_block_union, maxsm);
+#define ND_SMEM(C, M, F, MODE) \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE>, maxsm);
+    ND_SMEM(true, true, true, 0) ND_SMEM(true, true, false, 0) ND_SMEM(true, false, true, 0)
+    ND_SMEM(true, false, false, 0) ND_SMEM(false, true, true, 0)
+    ND_SMEM(false, true, false, 0) ND_SMEM(false, false, true, 0)
+    ND_SMEM(false, false, false, 0) ND_SMEM(true, true, true, 1)
+    ND_SMEM(true, true, false, 1) ND_SMEM(true, false, true, 1)
+    ND_SMEM(true, false, false, 1) ND_SMEM(false, true, true, 1)
+    ND_SMEM(false, true, false, 1) ND_SMEM(false, false, true, 1)
+    ND_SMEM(false, false, false, 1)
+#undef ND_SMEM
+    if (e != cudaSuccess) return cuda_fail(c, e, "shared memory opt-in");
+    return ND_OK;
+}
+
+static StepArgs md_step_args(MDEngine* m, int rec_in) {
     StepArgs a{};
     const nd_md_params& p = m->p;
     a.n = m->n;
-    a.nbr = (const int32_t*)m->nbr.p;
+    a.apl = m->apl;
+    a.ucap = m->ucap;
+    a.lcap = m->lcap;
+    a.ulist = (const int32_t*)m->ulist.p;
+    a.ucount = (const int32_t*)m->ucount.p;
+    a.llist = (const uint16_t*)m->llist.p;
     a.ncount = (const int32_t*)m->ncount.p;
-    a.sh_in = m->shadow[shadow_in];
-    a.sh_out = m->shadow[shadow_in ^ 1];
+    a.rec_in = (const int4*)m->rec_buf[rec_in].p;
+    a.rec_out = (int4*)m->rec_buf[rec_in ^ 1].p;
     for (int d = 0; d < 3; ++d) {
         a.x[d] = m->set[m->cur].x[d];
         a.w[d] = m->set[m->cur].w[d];
@@ -434,27 +634,30 @@ static StepArgs md_step_args(MDEngine* m, int shadow_in) {
     a.acc = (double*)m->acc.p;
     a.pos_build = (const float4*)m->pos32.p;
     a.diag = (unsigned long long*)m->diag.p;
-    {
-        float hs = (float)(0.5 * p.skin);
-        a.half_skin2 = hs * hs;
-    }
-    a.rc2 = (float)(p.cutoff * p.cutoff);
-    a.sig2 = (float)(p.sigma * p.sigma);
-    a.eps24 = (float)(24.0 * p.epsilon);
+    a.err = m->sub.d_err;
+    const float hs = (float)(0.5 * p.skin);
+    a.half_skin2 = hs * hs;
+    const double S = m->fr.s;
+    a.rc2u = (float)(p.cutoff * p.cutoff * S * S);
+    a.sig2u = (float)(p.sigma * p.sigma * S * S);
+    a.eps24u = (float)(24.0 * p.epsilon * S);
     a.eps4 = (float)(4.0 * p.epsilon);
-    a.kc = (float)p.coulomb_k;
+    a.kcu = (float)(p.coulomb_k * S * S);
+    a.kceu = (float)(p.coulomb_k * S);
     a.hdt = (float)(0.5 * p.dt);
     a.dt = p.dt;
+    a.fr = m->fr;
     return a;
 }
 
 template <int MODE>
 static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
     Ctx* c = &m->sub;
-    const unsigned grid = (unsigned)cdiv(m->n, 128);
+    const unsigned grid = (unsigned)m->nblocks;
+    const size_t sm = m->step_smem;
     const bool coul = m->has_q && m->p.coulomb_k != 0.0;
     const bool mass = m->has_m;
-#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE><<<grid, 128, 0, c->stream>>>(a)
+#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE><<<grid, kBlock, sm, c->stream>>>(a)
     if (coul) {
         if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
         else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
@@ -467,8 +670,8 @@ static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
 }
 
 // Rebuild: Float32 positions -> codes -> sort -> reorder state -> leaf boxes ->
-// build -> full neighbour list.  Switches the current state set.
-static nd_status md_rebuild(MDEngine* m) {
+// build -> block unions -> per-atom lists.  Switches the current state set.
+static nd_status md_rebuild(MDEngine* m, bool sizing = false) {
     Ctx* c = &m->sub;
     const int32_t n = m->n;
     const unsigned g = (unsigned)cdiv(n, 256);
@@ -481,8 +684,8 @@ static nd_status md_rebuild(MDEngine* m) {
     nd_status st;
     if ((st = morton_codes(c, (const float*)m->xyz32.p, n, m->p.order, codes, perm))) return st;
     if ((st = radix_sort_pairs(c, (uint32_t*)codes, perm, n, 30))) return st;
-    k_md_reorder<<<g, 256, 0, c->stream>>>(s, t, perm, (const float*)m->xyz32.p, n,
-                                           (float4*)m->pos32.p, m->shadow[0]);
+    k_md_reorder<<<g, 256, 0, c->stream>>>(s, t, perm, (const float*)m->xyz32.p, n, m->fr,
+                                           (float4*)m->pos32.p, (int4*)m->rec_buf[0].p, c->d_err);
     c->launches++;
     float4* keys = (float4*)m->keys.p;
     const float rl = (float)(m->p.cutoff + m->p.skin);
@@ -490,30 +693,37 @@ static nd_status md_rebuild(MDEngine* m) {
         (const float4*)m->pos32.p, m->nL, m->apl, rl / 2.0f, keys);
     c->launches++;
     if ((st = build_internal_nodes(c, keys, (int32_t*)m->store.p, codes, m->nL, m->apl))) return st;
+    // query boxes slightly above r_list/2 so the box tests never drop a pair;
+    // the distance test alone decides membership
     const float hq = (rl / 2.0f) * 1.0001f + 1e-6f;
-    k_md_neighbors<<<(unsigned)cdiv(n, 128), 128, 0, c->stream>>>(
-        keys, (const float4*)m->pos32.p, n, m->nL, m->apl, hq, rl * rl, m->cap,
-        (int32_t*)m->nbr.p, (int32_t*)m->ncount.p, c->d_err);
-    c->launches++;
+    k_md_block_union<<<(unsigned)m->nblocks, kBlock, m->union_smem, c->stream>>>(
+        keys, (const float4*)m->pos32.p, n, m->nL, hq, m->ucap, m->upow2, (int32_t*)m->ulist.p,
+        (int32_t*)m->ucount.p, c->d_err, (int32_t*)m->diag.p + 2, sizing ? 1 : 0);
+    k_md_block_lists<<<(unsigned)m->nblocks, kBlock, 0, c->stream>>>(
+        keys, (const float4*)m->pos32.p, n, m->apl, hq, rl * rl, m->ucap,
+        (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p, m->lcap,
+        (uint16_t*)m->llist.p, (int32_t*)m->ncount.p, c->d_err, (int32_t*)m->diag.p + 2,
+        sizing ? 1 : 0);
+    c->launches += 2;
     m->cur ^= 1;
-    m->sh = 0;
+    m->rc = 0;
     return check_launch(c, "md rebuild");
 }
 
 // Enqueue `k` steps inside the current window (no rebuild).
 static void md_steps(MDEngine* m, int32_t k) {
     for (int32_t s = 0; s < k; ++s) {
-        StepArgs a = md_step_args(m, m->sh);
+        StepArgs a = md_step_args(m, m->rc);
         launch_step<0>(m, a, m->first);
         m->first = false;
-        m->sh ^= 1;
+        m->rc ^= 1;
     }
 }
 
 static nd_status md_capture_window(MDEngine* m, int which) {
     // Captures rebuild + R steps starting from state set `which`.
     Ctx* c = &m->sub;
-    int save_cur = m->cur, save_sh = m->sh;
+    int save_cur = m->cur, save_rc = m->rc;
     bool save_first = m->first;
     int64_t save_launch = c->launches;
     m->cur = which;
@@ -532,39 +742,37 @@ static nd_status md_capture_window(MDEngine* m, int which) {
     m->graph_launches = c->launches - save_launch;
     c->launches = save_launch;
     m->cur = save_cur;
-    m->sh = save_sh;
+    m->rc = save_rc;
     m->first = save_first;
     return ND_OK;
 }
 
-static nd_status md_size_list(MDEngine* m) {
-    // First build with capacity 0: counts only, then size the list.
+// First build: a sizing pass (lists counted, not stored; union capacity
+// generous) measures the largest union and list, then the capacities are set
+// with head-room and the real build runs.
+static nd_status md_size_lists(MDEngine* m) {
     Ctx* c = &m->sub;
-    int save_cur = m->cur;
-    nd_status st = md_rebuild(m);
-    if (st) return st;
-    int32_t h[kErrWords];
-    cudaError_t e = cudaMemcpyAsync(h, c->d_err, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "size list");
-    e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "size list");
-    if (h[0] != 0 && h[0] != ND_ERR_OVERFLOW) {
-        c->last_error = "device error during the first neighbour-list build";
-        cudaMemsetAsync(c->d_err, 0, sizeof(int32_t) * kErrWords, c->stream);
-        return h[0];
+    nd_status st;
+    if ((st = md_alloc_lists(m, kSizingUcap, 0))) return st;
+    cudaMemsetAsync((int32_t*)m->diag.p + 2, 0, 2 * sizeof(int32_t), c->stream);
+    if ((st = md_rebuild(m, true))) return st;
+    int32_t h[2];
+    cudaError_t e = cudaMemcpyAsync(h, (int32_t*)m->diag.p + 2, sizeof(h),
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "size lists");
+    if ((st = sync_and_check(c, "md sizing build"))) return st;
+    const int32_t max_u = h[0], max_n = h[1];
+    if (max_u > kSizingUcap) {
+        c->last_error = "neighbour union of a block exceeds the supported size";
+        return ND_ERR_OVERFLOW;
     }
-    cudaMemsetAsync(c->d_err, 0, sizeof(int32_t) * kErrWords, c->stream);
-    int32_t maxc = h[2];
-    int32_t cap = m->p.max_neighbors > 0 ? m->p.max_neighbors
-                                         : (int32_t)std::ceil(maxc * 1.35) + 16;
-    cap = (cap + 3) & ~3;
-    m->cap = cap;
-    if ((st = ensure(c, m->nbr, sizeof(int32_t) * (size_t)cap * (size_t)m->n))) return st;
-    // The sizing build reordered the state; undo nothing (the order is free),
-    // just rebuild for real with the list allocated.
-    (void)save_cur;
-    st = md_rebuild(m);
-    if (st) return st;
+    int32_t lcap = m->p.max_neighbors > 0 ? m->p.max_neighbors
+                                          : (int32_t)std::ceil(max_n * 1.35) + 16;
+    lcap = (lcap + 7) & ~7;
+    int32_t ucap = ((int32_t)std::ceil(max_u * 1.25) + 32 + 31) & ~31;
+    if ((int64_t)ucap * m->apl > 65536) ucap = 65536 / m->apl;
+    if ((st = md_alloc_lists(m, ucap, lcap))) return st;
+    if ((st = md_rebuild(m))) return st;
     m->in_window = 0;
     m->rebuild_due = false;
     m->rebuilds = 1;
@@ -611,7 +819,7 @@ static nd_status md_upload(MDEngine* m, const double* xd, const double* vd, cons
 
 // Re-use an engine (buffers, captured graphs) for a new state of the same
 // size and parameters: upload, then the opening rebuild with the current list
-// capacity.  ND_ERR_OVERFLOW means the caller must create a new engine.
+// capacities.  ND_ERR_OVERFLOW means the caller must create a new engine.
 nd_status md_reset(MDEngine* m, const double* x, const double* v, const double* q,
                    const double* mass, bool host) {
     if ((q != nullptr) != m->has_q || (mass != nullptr) != m->has_m) return ND_ERR_ARG;
@@ -625,6 +833,20 @@ nd_status md_reset(MDEngine* m, const double* x, const double* v, const double* 
 bool md_compatible(MDEngine* m, const nd_md_params* p, int32_t n, bool has_q, bool has_m) {
     return m && m->n == n && m->has_q == has_q && m->has_m == has_m &&
            memcmp(&m->p, p, sizeof(nd_md_params)) == 0;
+}
+
+// Fixed-point frame from the walls: a margin of 1/16 of the largest extent on
+// every side, scale = the largest power of two that keeps the frame in int32.
+static nd_status md_frame(MDEngine* m) {
+    double ext = 0.0;
+    for (int d = 0; d < 3; ++d) ext = std::max(ext, m->p.box_hi[d] - m->p.box_lo[d]);
+    if (!(ext > 0.0) || !std::isfinite(ext)) return ND_ERR_ARG;
+    const double margin = ext / 16.0;
+    for (int d = 0; d < 3; ++d) m->fr.o[d] = m->p.box_lo[d] - margin;
+    const double range = ext + 2.0 * margin;
+    int k = (int)std::floor(std::log2(2147480000.0 / range));
+    m->fr.s = std::ldexp(1.0, k);
+    return ND_OK;
 }
 
 static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
@@ -644,15 +866,17 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     m->n = n;
     m->apl = p->atomsperleaf;
     m->nL = n / m->apl;
+    m->nblocks = (int32_t)cdiv(n, kBlock);
     m->has_q = qd != nullptr;
     m->has_m = md_ != nullptr;
-    nd_status st = md_alloc(m);
+    nd_status st = md_frame(m);
+    if (st == ND_OK) st = md_alloc(m);
     if (st) { parent->last_error = m->sub.last_error; md_destroy(m); return st; }
     Ctx* c = &m->sub;
     if ((st = md_upload(m, xd, vd, qd, md_, host))) { parent->last_error = c->last_error; md_destroy(m); return st; }
     m->cur = 0;
     m->first = true;
-    if ((st = md_size_list(m))) { parent->last_error = c->last_error; md_destroy(m); return st; }
+    if ((st = md_size_lists(m))) { parent->last_error = c->last_error; md_destroy(m); return st; }
     for (int w = 0; capture && w < 2; ++w)
         if ((st = md_capture_window(m, w))) { parent->last_error = c->last_error; md_destroy(m); return st; }
     parent->launches += c->launches;
@@ -671,10 +895,11 @@ nd_status md_destroy(MDEngine* m) {
     if (!m) return ND_OK;
     for (int w = 0; w < 2; ++w)
         if (m->graph[w]) cudaGraphExecDestroy(m->graph[w]);
-    DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->sh_buf[0], &m->sh_buf[1], &m->xyz32,
-                      &m->pos32, &m->keys, &m->store, &m->nbr, &m->ncount, &m->f, &m->vtmp,
-                      &m->acc, &m->aos, &m->diag, &m->sub.codes, &m->sub.codes_alt, &m->sub.perm,
-                      &m->sub.perm_alt, &m->sub.hist, &m->sub.misc};
+    DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->rec_buf[0], &m->rec_buf[1], &m->xyz32,
+                      &m->pos32, &m->keys, &m->store, &m->ulist, &m->ucount, &m->llist,
+                      &m->ncount, &m->f, &m->vtmp, &m->acc, &m->aos, &m->diag, &m->sub.codes,
+                      &m->sub.codes_alt, &m->sub.perm, &m->sub.perm_alt, &m->sub.hist,
+                      &m->sub.misc};
     if (m->sub.stream) cudaStreamSynchronize(m->sub.stream);
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
@@ -695,7 +920,7 @@ nd_status md_run(MDEngine* m, int64_t steps) {
                 if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
                 c->launches += m->graph_launches;
                 m->cur ^= 1;
-                m->sh = R & 1;
+                m->rc = R & 1;
                 m->rebuilds++;
                 m->steps += R;
                 steps -= R;
@@ -721,7 +946,7 @@ nd_status md_run(MDEngine* m, int64_t steps) {
 nd_status md_measure(MDEngine* m) {
     Ctx* c = &m->sub;
     cudaMemsetAsync(m->acc.p, 0, 2 * sizeof(double), c->stream);
-    StepArgs a = md_step_args(m, m->sh);
+    StepArgs a = md_step_args(m, m->rc);
     launch_step<1>(m, a, m->first);
     return check_launch(c, "md measure");
 }
@@ -780,7 +1005,7 @@ nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list
                    int32_t* capacity) {
     if (steps) *steps = m->steps;
     if (rebuilds) *rebuilds = m->rebuilds;
-    if (capacity) *capacity = m->cap;
+    if (capacity) *capacity = m->lcap;
     if (list_pairs) {
         // sum of ncount (full list: each pair twice)
         std::vector<int32_t> h(m->n);
@@ -798,15 +1023,13 @@ nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list
 
 nd_status md_diagnostics(MDEngine* m, int64_t* skin_violations, int32_t* max_neighbors) {
     Ctx* c = &m->sub;
-    unsigned long long v = 0;
-    int32_t h[kErrWords];
-    cudaError_t e = cudaMemcpyAsync(&v, m->diag.p, sizeof(v), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(h, c->d_err, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    unsigned long long d[2] = {0, 0};
+    cudaError_t e = cudaMemcpyAsync(d, m->diag.p, sizeof(d), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "md diagnostics");
-    if (skin_violations) *skin_violations = (int64_t)v;
-    if (max_neighbors) *max_neighbors = h[2];
+    if (skin_violations) *skin_violations = (int64_t)d[0];
+    // diag int32 words 2 and 3 hold the largest union and list seen
+    if (max_neighbors) *max_neighbors = (int32_t)(d[1] >> 32);
     return ND_OK;
 }
 

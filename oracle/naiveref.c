@@ -89,19 +89,40 @@ int ref_morton_reference(const float* xyz, int64_t n, int32_t* codes) {
     return REF_OK;
 }
 
-static inline uint32_t spread10(uint32_t v) {
-    v &= 0x3ffu;
-    v = (v | (v << 16)) & 0x030000FFu;
-    v = (v | (v << 8)) & 0x0300F00Fu;
-    v = (v | (v << 4)) & 0x030C30C3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
+/* 3-D Hilbert index of a cell of a 1024^3 grid: J. Skilling's transpose
+ * method ("Programming the Hilbert curve", AIP Conf. Proc. 707, 2004), x
+ * first in the interleave.  Consecutive indices are face-adjacent cells. */
+static uint32_t hilbert3_10(uint32_t x, uint32_t y, uint32_t z) {
+    uint32_t X[3] = {x & 1023u, y & 1023u, z & 1023u};
+    for (uint32_t Q = 1u << 9; Q > 1u; Q >>= 1) {
+        uint32_t P = Q - 1u;
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = 1u << 9; Q > 1u; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1u;
+    for (int i = 0; i < 3; ++i) X[i] ^= t;
+    uint32_t h = 0;
+    for (int q = 9; q >= 0; --q)
+        for (int i = 0; i < 3; ++i) h = (h << 1) | ((X[i] >> q) & 1u);
+    return h;
 }
 
+uint32_t ref_hilbert3(uint32_t x, uint32_t y, uint32_t z) { return hilbert3_10(x, y, z); }
+
 int ref_morton_spatial(const float* xyz, int64_t n, int32_t* codes) {
-    /* Interleaved Morton code (x in bit 0, y bit 1, z bit 2 of each triple)
-     * over the Float32 bounding box, 1024 bins per axis:
-     *   s = 1024 / (hi - lo); q = clamp(floor((p - lo) * s), 0, 1023). */
+    /* Spatial code: 3-D Hilbert index over the Float32 bounding box, 1024 bins
+     * per axis: s = 1024 / (hi - lo); q = clamp(floor((p - lo) * s), 0, 1023). */
     float lo[3], hi[3], s[3];
     for (int d = 0; d < 3; ++d) { lo[d] = INFINITY; hi[d] = -INFINITY; }
     for (int64_t a = 0; a < n; ++a)
@@ -123,7 +144,7 @@ int ref_morton_spatial(const float* xyz, int64_t n, int32_t* codes) {
             int32_t qi = (t < 0.0f) ? 0 : (t > 1023.0f ? 1023 : (int32_t)t);
             q[d] = (uint32_t)qi;
         }
-        codes[a] = (int32_t)(spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2));
+        codes[a] = (int32_t)hilbert3_10(q[0], q[1], q[2]);
     }
     return REF_OK;
 }

@@ -40,7 +40,7 @@ typedef struct {
 
 /* Ordering of atoms before the tree build. */
 #define REF_ORDER_REFERENCE 0 /* mortoncodes! bit-select code (BVHTraverse.jl:237-288) */
-#define REF_ORDER_SPATIAL   1 /* 10-bit-per-axis interleaved Morton code over the bounding box */
+#define REF_ORDER_SPATIAL   1 /* 3-D Hilbert index, 10 bits per axis over the bounding box */
 
 /* Leaf bounding boxes. */
 #define REF_BOX_LEAF 0 /* leafcluster_primitives: p -/+ r/2, key array N-1 (BVHTraverse.jl:376-410) */
@@ -52,8 +52,9 @@ int ref_spec(int64_t atom_count, int64_t atomsperleaf, int32_t* leaves, int32_t*
 /* mortoncodes! for K = Int32 (BVHTraverse.jl:237-288) with binwidth = Float32(1/1023) (:184). */
 int ref_morton_reference(const float* xyz, int64_t n, int32_t* codes);
 
-/* Spatial (true interleaved) Morton code: 10 bits per axis over [lo, hi]. */
+/* Spatial code: 3-D Hilbert index, 10 bits per axis over the bounding box. */
 int ref_morton_spatial(const float* xyz, int64_t n, int32_t* codes);
+uint32_t ref_hilbert3(uint32_t x, uint32_t y, uint32_t z);
 
 /* Stable ascending sortperm (BVHTraverse.jl:570); perm is 0-based. */
 int ref_sortperm(const int32_t* codes, int64_t n, int32_t* perm);

@@ -68,6 +68,8 @@ def lib():
             L.ref_morton_reference.restype = ctypes.c_int
             L.ref_morton_spatial.argtypes = [f32p, ctypes.c_int64, i32p]
             L.ref_morton_spatial.restype = ctypes.c_int
+            L.ref_hilbert3.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
+            L.ref_hilbert3.restype = ctypes.c_uint32
             L.ref_sortperm.argtypes = [i32p, ctypes.c_int64, i32p]
             L.ref_sortperm.restype = ctypes.c_int
             L.ref_delta.argtypes = [ctypes.c_int32, i32p, ctypes.c_int32, ctypes.c_int32]
@@ -135,6 +137,11 @@ def morton_spatial(xyz):
     out = np.empty(a.shape[0], np.int32)
     _check(lib().ref_morton_spatial(_p(a, ctypes.c_float), a.shape[0], _p(out, ctypes.c_int32)))
     return out
+
+
+def hilbert3(x, y, z):
+    """3-D Hilbert index of grid cell (x, y, z), each in [0, 1024)."""
+    return int(lib().ref_hilbert3(x, y, z))
 
 
 def sortperm(codes):

@@ -157,6 +157,23 @@ def test_morton_errors(oracle):
     oracle.morton_reference(x)
 
 
+def test_hilbert_curve_is_continuous(oracle):
+    # On the coarse 8^3 grid (cells at multiples of 128 of the 1024 grid) the
+    # top 9 index bits order the cells along a Hilbert curve: consecutive cells
+    # are face neighbours and every cell appears once.
+    cells = [(a << 7, b << 7, c << 7) for a in range(8) for b in range(8) for c in range(8)]
+    idx = [oracle.hilbert3(*p) >> 21 for p in cells]
+    assert sorted(idx) == list(range(512))
+    order = [p for _, p in sorted(zip(idx, cells))]
+    for p, q in zip(order, order[1:]):
+        assert sum(abs(a - b) for a, b in zip(p, q)) == 128
+    # and at full resolution along a random walk of neighbouring cells the
+    # indices are distinct
+    rng = np.random.default_rng(5)
+    pts = {tuple(rng.integers(0, 1024, 3)) for _ in range(2000)}
+    assert len({oracle.hilbert3(*p) for p in pts}) == len(pts)
+
+
 def test_spec_checks(oracle):
     with pytest.raises(oracle.OracleError):
         oracle.spec(10, 4)          # 4 does not divide 10
