@@ -294,7 +294,7 @@ def run_gb300(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 state",
         "data": "synthetic (seeded splitmix64 generators)",
         "config": {"workload": WORKLOAD, "n_atoms": N_ATOMS, "md_steps_per_step": MD_PER_STEP,
-                   "rebuild_every": REBUILD, "atom_order": "spatial Morton",
+                   "rebuild_every": REBUILD, "atom_order": "3-D Hilbert, re-sorted every 5th rebuild, refit between",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "512 MB buffer written before every timed step (outside the events)",
                    "neighbours_per_atom": round(nbr, 2),

@@ -89,7 +89,7 @@ typedef struct {
     double dt;             /* stepwidth */
     double box_lo[3];      /* reflecting walls (boundary_reflect!, Simulator.jl:81-111) */
     double box_hi[3];
-    int32_t atomsperleaf;  /* leaf size of the tree used for the neighbour list */
+    int32_t atomsperleaf;  /* leaf size of the tree used for the neighbour list (divides 32) */
     int32_t rebuild_every; /* steps between neighbour-list rebuilds */
     int32_t order;         /* ND_ORDER_* used for the rebuilds */
     int32_t max_neighbors; /* per-atom list capacity, 0 = sized from the first build */

@@ -66,12 +66,18 @@ __global__ void k_bbox(const float* __restrict__ xyz, int32_t n, uint32_t* bbox,
             mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], s));
         }
     }
-    if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            atomicMin(&bbox[d], mn[d]);
-            atomicMax(&bbox[3 + d], mx[d]);
-        }
+    // block reduction first: one atomic per block and component
+    __shared__ uint32_t s_b[32][6];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) { s_b[warp][d] = mn[d]; s_b[warp][3 + d] = mx[d]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        uint32_t v = s_b[0][k];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = k < 3 ? min(v, s_b[w][k]) : max(v, s_b[w][k]);
+        if (k < 3) atomicMin(&bbox[k], v);
+        else atomicMax(&bbox[k], v);
     }
 }
 

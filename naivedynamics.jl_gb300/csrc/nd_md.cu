@@ -31,7 +31,7 @@
 namespace nd {
 
 constexpr int kBlock = 256;          // atoms per block in the list and step kernels
-constexpr int kFrontierCap = 4096;   // BFS frontier entries per buffer
+constexpr int kSizingFcap = 8192;    // BFS frontier entries per buffer in the sizing build
 constexpr int kSizingUcap = 8192;    // union capacity of the sizing build
 
 // Fixed-point frame of the pair records: x_fp = rint((x - origin) * scale).
@@ -79,7 +79,7 @@ __global__ void k_md_pos32(const double* __restrict__ x0, const double* __restri
 
 __device__ __forceinline__ int32_t to_fixed(double x, double o, double s, int32_t* err,
                                             int32_t who) {
-    double t = (x - o) * s;
+    double t = fma(x, s, -(o * s));
     if (!(t > -2147483000.0 && t < 2147483000.0)) {
         set_error(err, isfinite(x) ? ND_ERR_RANGE : ND_ERR_NONFINITE, who);
         t = 0.0;
@@ -91,7 +91,8 @@ __device__ __forceinline__ int32_t to_fixed(double x, double o, double s, int32_
 // records and the Float32 positions of the tree.
 __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict__ perm,
                              const float* __restrict__ xyz32, int32_t n, Frame fr,
-                             float4* __restrict__ pos32, int4* __restrict__ rec, int32_t* err) {
+                             float4* __restrict__ pos32, int4* __restrict__ rec,
+                             int4* __restrict__ recb, int32_t* err) {
     int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int32_t o = perm[k];
@@ -110,6 +111,7 @@ __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict
     pos32[k] = make_float4(xyz32[3 * (int64_t)o], xyz32[3 * (int64_t)o + 1],
                            xyz32[3 * (int64_t)o + 2], __int_as_float(k));
     rec[k] = make_int4(f[0], f[1], f[2], __float_as_int((float)qv));
+    recb[k] = rec[k];
 }
 
 // Leaf boxes (p -/+ h) of already sorted Float32 positions.
@@ -147,15 +149,16 @@ __device__ __forceinline__ bool box_overlap(float qmnx, float qmny, float qmnz, 
 // current level together, a node's children being (left, skip of left) in the
 // rope layout -- and every leaf overlapping any of them joins the union.  The union is sorted (bitonic)
 // so list order, and hence force summation order, is deterministic.
-// Shared memory: two frontier buffers of kFrontierCap and the union (upow2).
+// Shared memory: two frontier buffers of fcap entries and the union (upow2).
 __global__ void __launch_bounds__(kBlock)
     k_md_block_union(const float4* __restrict__ keys, const float4* __restrict__ pos,
-                     int32_t n, int32_t nL, float hq, int32_t ucap, int32_t upow2,
-                     int32_t* __restrict__ ulist, int32_t* __restrict__ ucount, int32_t* err,
-                     int32_t* diag, int32_t sizing) {
+                     int32_t n, int32_t nL, int32_t apl, float hq, int32_t fcap, int32_t ucap,
+                     int32_t upow2, int32_t* __restrict__ ulist, int32_t* __restrict__ ucount,
+                     uint16_t* __restrict__ llist_leaf, int32_t* __restrict__ lcount_leaf,
+                     int32_t lcap_leaf, int32_t* err, int32_t* diag, int32_t sizing) {
     extern __shared__ int32_t smem[];
-    int32_t* fr[2] = {smem, smem + kFrontierCap};
-    int32_t* su = smem + 2 * kFrontierCap;
+    int32_t* fr[2] = {smem, smem + fcap};
+    int32_t* su = smem + 2 * fcap;
     __shared__ int32_t s_cnt[2];
     __shared__ int32_t s_nu;
     __shared__ float s_wb[kBlock / 32][6];  // per-warp query boxes (min xyz, max xyz)
@@ -178,7 +181,7 @@ __global__ void __launch_bounds__(kBlock)
     __syncthreads();
     int cur = 0;
     for (int level = 0; level < 256; ++level) {
-        const int32_t nf = min(s_cnt[cur], kFrontierCap);
+        const int32_t nf = min(s_cnt[cur], fcap);
         if (nf == 0) break;
         for (int32_t k = tid; k < nf; k += kBlock) {
             const int32_t e = fr[cur][k];
@@ -189,7 +192,7 @@ __global__ void __launch_bounds__(kBlock)
             const int32_t left = __float_as_int(b.z), skip = __float_as_int(b.w);
             if (e & 1) {  // a left child: its skip rope is its right sibling
                 int32_t slot = atomicAdd(&s_cnt[cur ^ 1], 1);
-                if (slot < kFrontierCap) fr[cur ^ 1][slot] = skip << 1;
+                if (slot < fcap) fr[cur ^ 1][slot] = skip << 1;
             }
             bool hit = false;
             for (int w = 0; w < kBlock / 32 && !hit; ++w)
@@ -201,23 +204,28 @@ __global__ void __launch_bounds__(kBlock)
                     if (slot < upow2) su[slot] = t - 1;
                 } else {
                     int32_t slot = atomicAdd(&s_cnt[cur ^ 1], 1);
-                    if (slot < kFrontierCap) fr[cur ^ 1][slot] = (left << 1) | 1;
+                    if (slot < fcap) fr[cur ^ 1][slot] = (left << 1) | 1;
                 }
             }
         }
         __syncthreads();
         if (tid == 0) {
-            if (s_cnt[cur ^ 1] > kFrontierCap) set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x);
+            atomicMax(&diag[4], s_cnt[cur ^ 1]);
+            if (s_cnt[cur ^ 1] > fcap && !sizing) set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x);
             s_cnt[cur] = 0;
         }
         cur ^= 1;
         __syncthreads();
     }
     const int32_t nu = s_nu;
-    if (tid == 0) atomicMax(&diag[0], nu);
+    if (tid == 0) { atomicMax(&diag[0], nu); atomicAdd(&diag[3], nu); }
     if (nu > ucap) {
         if (tid == 0 && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)blockIdx.x);
         if (tid == 0) ucount[blockIdx.x] = 0;
+        for (int32_t k = tid; k < kBlock / apl; k += kBlock) {
+            const int64_t leaf = (int64_t)blockIdx.x * (kBlock / apl) + k;
+            if (leaf < nL) lcount_leaf[leaf] = 0;
+        }
         return;
     }
     // bitonic sort of the union (padded to a power of two)
@@ -240,41 +248,119 @@ __global__ void __launch_bounds__(kBlock)
     int32_t* dst = ulist + (int64_t)blockIdx.x * ucap;
     for (int32_t k = tid; k < nu; k += kBlock) dst[k] = su[k];
     if (tid == 0) ucount[blockIdx.x] = nu;
+    // Per-leaf candidate lists: for each of its leaves a warp keeps the union
+    // positions whose leaf box overlaps that leaf's box (the leaf-leaf test of
+    // leafneighbor_traverse, BVHTraverse.jl:1282), ballot-compacted in union
+    // order.  A lane loads one union box per chunk and tests it against up to
+    // eight own leaves.  The own boxes are widened by a few ulps so no pair is
+    // lost to rounding; the atom distance test decides.
+    __shared__ float s_own[kBlock / 32][8][6];
+    const unsigned below = (1u << lane) - 1u;
+    const int32_t leaves_per_warp = 32 / apl;
+    const int64_t first_own = ((int64_t)blockIdx.x * kBlock + warp * 32) / apl;
+    for (int32_t k0 = 0; k0 < leaves_per_warp; k0 += 8) {
+        const int32_t nown = min(8, leaves_per_warp - k0);
+        if (lane < nown) {
+            const int64_t own = first_own + k0 + lane;
+            float4 oa = make_float4(1.f, 1.f, 1.f, -1.f), ob = make_float4(-1.f, -1.f, 0.f, 0.f);
+            if (own < nL) { oa = __ldg(&keys[2 * own]); ob = __ldg(&keys[2 * own + 1]); }
+            s_own[warp][lane][0] = oa.x - 1e-5f * fabsf(oa.x) - 1e-6f;
+            s_own[warp][lane][1] = oa.y - 1e-5f * fabsf(oa.y) - 1e-6f;
+            s_own[warp][lane][2] = oa.z - 1e-5f * fabsf(oa.z) - 1e-6f;
+            s_own[warp][lane][3] = oa.w + 1e-5f * fabsf(oa.w) + 1e-6f;
+            s_own[warp][lane][4] = ob.x + 1e-5f * fabsf(ob.x) + 1e-6f;
+            s_own[warp][lane][5] = ob.y + 1e-5f * fabsf(ob.y) + 1e-6f;
+        }
+        __syncwarp();
+        int32_t lc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int32_t base = 0; base < nu; base += 32) {
+            const int32_t u = base + lane;
+            float4 a = make_float4(1.f, 1.f, 1.f, -1.f), b = make_float4(-1.f, -1.f, 0.f, 0.f);
+            if (u < nu) {
+                const int32_t leaf = su[u];
+                a = __ldg(&keys[2 * (int64_t)leaf]);
+                b = __ldg(&keys[2 * (int64_t)leaf + 1]);
+            }
+#pragma unroll
+            for (int kl = 0; kl < 8; ++kl) {
+                if (kl >= nown) break;
+                const float* o = s_own[warp][kl];
+                const bool hit = (u < nu) && box_overlap(o[0], o[1], o[2], o[3], o[4], o[5], a, b);
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) {
+                    const int32_t pos = lc[kl] + __popc(m & below);
+                    if (pos < lcap_leaf) llist_leaf[(first_own + k0 + kl) * lcap_leaf + pos] = (uint16_t)u;
+                }
+                lc[kl] += __popc(m);
+            }
+        }
+        if (lane < nown) {
+            int32_t mine = 0;
+#pragma unroll
+            for (int kl = 0; kl < 8; ++kl)
+                if (kl == lane) mine = lc[kl];
+            const int64_t own = first_own + k0 + lane;
+            if (own < nL) {
+                lcount_leaf[own] = min(mine, lcap_leaf);
+                atomicMax(&diag[2], mine);
+                if (mine > lcap_leaf && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)own);
+            }
+        }
+        __syncwarp();
+    }
 }
 
-// Exact per-atom lists inside the block's union: every thread scans the union
-// with block-uniform loads (one address per warp request), tests its own box
-// (p -/+ hq) against each leaf box and the leaf's atoms with the reference
-// distance (Float32, d^2 < r_list^2), and stores union indices as uint16.
+// Exact per-atom lists inside the block's union: the union's Float32
+// positions are staged in shared memory (up to smpos entries; the rest are read
+// from L2), then the APL lanes of a leaf walk that leaf's candidate list
+// together, each testing its own atom against the candidate leaf's atoms with
+// the reference distance (Float32, d^2 < r_list^2) and storing union indices
+// as uint16.  pos.w holds the atom's sorted index (excludes the atom itself).
+template <int APL>
 __global__ void __launch_bounds__(kBlock)
-    k_md_block_lists(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t n,
-                     int32_t apl, float hq, float rl2, int32_t ucap,
-                     const int32_t* __restrict__ ulist, const int32_t* __restrict__ ucount,
-                     int32_t lcap, uint16_t* __restrict__ llist, int32_t* __restrict__ ncount,
-                     int32_t* err, int32_t* diag, int32_t sizing) {
+    k_md_block_lists(const float4* __restrict__ pos, int32_t n, float rl2, int32_t ucap,
+                     int32_t smpos, const int32_t* __restrict__ ulist,
+                     const int32_t* __restrict__ ucount, const uint16_t* __restrict__ llist_leaf,
+                     const int32_t* __restrict__ lcount_leaf, int32_t lcap_leaf, int32_t lcap,
+                     uint16_t* __restrict__ llist, int32_t* __restrict__ ncount, int32_t* err,
+                     int32_t* diag, int32_t sizing) {
+    extern __shared__ float4 spos[];
     const int tid = threadIdx.x;
+    const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
+    {
+        const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
+        const int32_t m = min(nu * APL, smpos);
+        for (int32_t k = tid; k < m; k += kBlock)
+            spos[k] = __ldg(&pos[(int64_t)__ldg(&U[k / APL]) * APL + (k % APL)]);
+    }
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * kBlock + tid;
     const bool valid = i < n;
+    const int64_t own = (valid ? i : (int64_t)blockIdx.x * kBlock) / APL;
     const float4 p = __ldg(&pos[valid ? i : (int64_t)blockIdx.x * kBlock]);
-    const float qmnx = __fsub_rn(p.x, hq), qmny = __fsub_rn(p.y, hq), qmnz = __fsub_rn(p.z, hq);
-    const float qmxx = __fadd_rn(p.x, hq), qmxy = __fadd_rn(p.y, hq), qmxz = __fadd_rn(p.z, hq);
-    const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
-    const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
+    const int32_t nc = valid ? min(__ldg(&lcount_leaf[own]), lcap_leaf) : 0;
+    const uint16_t* __restrict__ C = llist_leaf + own * lcap_leaf;
     uint16_t* __restrict__ L = llist + (int64_t)blockIdx.x * lcap * kBlock + tid;
+    const int32_t self = (int32_t)i;
     int32_t cnt = 0;
-    for (int32_t u = 0; u < nu; ++u) {
-        const int32_t leaf = __ldg(&U[u]);
-        const float4 a = __ldg(&keys[2 * (int64_t)leaf]);
-        const float4 b = __ldg(&keys[2 * (int64_t)leaf + 1]);
-        if (valid && box_overlap(qmnx, qmny, qmnz, qmxx, qmxy, qmxz, a, b)) {
-            for (int32_t e = 0; e < apl; ++e) {
-                const int64_t j = (int64_t)leaf * apl + e;
-                if (j == i) continue;
-                const float4 q = __ldg(&pos[j]);
-                if (dist2_ref(p.x, p.y, p.z, q.x, q.y, q.z) < rl2) {
-                    if (cnt < lcap) L[(int64_t)cnt * kBlock] = (uint16_t)(u * apl + e);
-                    ++cnt;
-                }
+    for (int32_t k = 0; k < nc; ++k) {
+        const int32_t u = __ldg(&C[k]);
+        float4 q[APL];
+        if ((u + 1) * APL <= smpos) {
+#pragma unroll
+            for (int e = 0; e < APL; ++e) q[e] = spos[u * APL + e];
+        } else {
+            const int64_t base = (int64_t)__ldg(&U[u]) * APL;
+#pragma unroll
+            for (int e = 0; e < APL; ++e) q[e] = __ldg(&pos[base + e]);
+        }
+#pragma unroll
+        for (int e = 0; e < APL; ++e) {
+            const bool hit = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z) < rl2 &&
+                             __float_as_int(q[e].w) != self;
+            if (hit) {
+                if (cnt < lcap) L[(int64_t)cnt * kBlock] = (uint16_t)(u * APL + e);
+                ++cnt;
             }
         }
     }
@@ -284,10 +370,32 @@ __global__ void __launch_bounds__(kBlock)
     atomicMax(&diag[1], cnt);
 }
 
+// Refit: positions changed, order and tree topology kept.  Float32 positions
+// and pair records (and the build records of the skin check) from the FP64
+// state in its current order.
+__global__ void k_md_refit_pos(SetPtrs st, int32_t n, Frame fr, float4* __restrict__ pos32,
+                               int4* __restrict__ rec, int4* __restrict__ recb, int32_t* err) {
+    int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int32_t f[3];
+    float xf[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double xv = st.x[d][k];
+        xf[d] = (float)xv;
+        f[d] = to_fixed(xv, fr.o[d], fr.s, err, k);
+    }
+    pos32[k] = make_float4(xf[0], xf[1], xf[2], __int_as_float(k));
+    int4 r = make_int4(f[0], f[1], f[2], __float_as_int((float)st.q[k]));
+    rec[k] = r;
+    recb[k] = r;
+}
+
 // ------------------------------------------------------------- step kernel
 
 struct StepArgs {
     int32_t n, apl, ucap, lcap;
+    int32_t smrec;  // union records staged in shared memory (the rest read from global)
     const int32_t* __restrict__ ulist;
     const int32_t* __restrict__ ucount;
     const uint16_t* __restrict__ llist;
@@ -300,10 +408,12 @@ struct StepArgs {
     float4* __restrict__ f_out;
     double* __restrict__ v_out[3];  // measure mode: integer-step velocity
     double* __restrict__ acc;       // measure mode: [0] potential, [1] kinetic
-    const float4* __restrict__ pos_build;   // Float32 positions at the last rebuild
+    const int4* __restrict__ rec_build;     // records at the last rebuild
     unsigned long long* __restrict__ diag;  // [0] atom-steps moved > skin/2 since the build
     int32_t* err;
-    float half_skin2;
+    float half_skin2u;  // (skin/2)^2 in fixed-point units
+    double os[3];       // origin * scale (fixed-point offset)
+    int32_t lo_fp[3], hi_fp[3];  // walls in fixed point (filter for the exact FP64 test)
     // pair constants in fixed-point units (S = frame scale)
     float rc2u;    // (r_c S)^2
     float sig2u;   // (sigma S)^2
@@ -364,11 +474,12 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
     const int tid = threadIdx.x;
     int64_t i = (int64_t)blockIdx.x * kBlock + tid;
     const bool valid = i < a.n;
-    // stage the block's union: record of atom (leaf * apl + e) at u * apl + e
+    const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
+    // stage the block's union: record of atom (leaf * apl + e) at u * apl + e,
+    // up to the shared-memory capacity; larger unions read the rest from L2
     {
         const int32_t nu = min(__ldg(&a.ucount[blockIdx.x]), a.ucap);
-        const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
-        const int32_t m = nu * a.apl;
+        const int32_t m = min(nu * a.apl, a.smrec);
         for (int32_t k = tid; k < m; k += kBlock) {
             const int32_t u = k / a.apl, e = k - u * a.apl;
             srec[k] = __ldg(&a.rec_in[(int64_t)__ldg(&U[u]) * a.apl + e]);
@@ -380,17 +491,32 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
     const int4 ri = __ldg(&a.rec_in[i]);
     const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
+    auto fetch = [&](int32_t li) -> int4 {
+        if (li < a.smrec) return srec[li];
+        const int32_t u = li / a.apl, e = li - u * a.apl;
+        return __ldg(&a.rec_in[(int64_t)__ldg(&U[u]) * a.apl + e]);
+    };
     float fx = 0.f, fy = 0.f, fz = 0.f, ue = 0.f;
+    // groups of four neighbours; the next group's indices are loaded while the
+    // current group is computed
     int32_t s = 0;
+    int32_t li[4];
+    if (cnt >= 4) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)k * kBlock];
+    }
     for (; s + 4 <= cnt; s += 4) {
         int4 rj[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) rj[k] = srec[L[(int64_t)(s + k) * kBlock]];
+        for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
+        if (s + 8 <= cnt) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)(s + 4 + k) * kBlock];
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], a, fx, fy, fz, ue);
     }
-    for (; s < cnt; ++s)
-        accum_pair<COUL, MODE == 1>(ri, srec[L[(int64_t)s * kBlock]], a, fx, fy, fz, ue);
+    for (; s < cnt; ++s) accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), a, fx, fy, fz, ue);
     if (valid) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
     const double imv = MASS ? a.im[i] : 1.0;
     const float fv[3] = {fx, fy, fz};
@@ -415,28 +541,36 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
             atomicAdd(&a.acc[1], ke);
         }
         return;
-    }
-    int32_t fx3[3];
-    float xf[3];
+    } else {
+        // v_{n+1/2} = v_{n-1/2} + dt F/m (the pending half kick and this step's
+        // half kick in one add), x += dt v, walls, next record.
+        const float kdt = FIRST ? a.hdt : 2.0f * a.hdt;
+        int32_t xi[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        double kick = (double)(a.hdt * fv[d]) * imv;
-        double v = FIRST ? a.w[d][i] : a.w[d][i] + kick;  // completes v_n
-        v = v + kick;                                      // v_{n+1/2}
-        double x = fma(a.dt, v, a.x[d][i]);                // x_{n+1}
-        if (a.lo[d] > x) { v = -v; x = a.lo[d]; }          // boundary_reflect!
-        if (a.hi[d] < x) { v = -v; x = a.hi[d]; }
-        a.x[d][i] = x;
-        a.w[d][i] = v;
-        fx3[d] = to_fixed(x, a.fr.o[d], a.fr.s, a.err, (int32_t)i);
-        xf[d] = (float)x;
+        for (int d = 0; d < 3; ++d) {
+            double v = a.w[d][i] + (double)(kdt * fv[d]) * imv;
+            double x = fma(a.dt, v, a.x[d][i]);
+            int32_t q = __double2int_rn(fma(x, a.fr.s, -a.os[d]));
+            // integer pre-check; the exact FP64 test of boundary_reflect! runs
+            // only for atoms within a grid step of a wall
+            if (q <= a.lo_fp[d] + 1 || q >= a.hi_fp[d] - 1) {
+                if (a.lo[d] > x) { v = -v; x = a.lo[d]; }
+                if (a.hi[d] < x) { v = -v; x = a.hi[d]; }
+                q = __double2int_rn(fma(x, a.fr.s, -a.os[d]));
+                if (!(x == x)) set_error(a.err, ND_ERR_NONFINITE, (int32_t)i);
+            }
+            a.x[d][i] = x;
+            a.w[d][i] = v;
+            xi[d] = q;
+        }
+        a.rec_out[i] = make_int4(xi[0], xi[1], xi[2], ri.w);
+        // A list built at r_c + skin stays valid while no atom moved more than
+        // skin/2 since the build; count the atom-steps that broke that bound.
+        const int4 rb = __ldg(&a.rec_build[i]);
+        const float ex = (float)(xi[0] - rb.x), ey = (float)(xi[1] - rb.y),
+                    ez = (float)(xi[2] - rb.z);
+        if (ex * ex + ey * ey + ez * ez > a.half_skin2u) atomicAdd(a.diag, 1ull);
     }
-    a.rec_out[i] = make_int4(fx3[0], fx3[1], fx3[2], ri.w);
-    // A list built at r_c + skin stays valid while no atom moved more than
-    // skin/2 since the build; count the atom-steps that broke that bound.
-    const float4 pb = __ldg(&a.pos_build[i]);
-    const float ex = xf[0] - pb.x, ey = xf[1] - pb.y, ez = xf[2] - pb.z;
-    if (ex * ex + ey * ey + ez * ez > a.half_skin2) atomicAdd(a.diag, 1ull);
 }
 
 __global__ void k_md_unsort(const int32_t* __restrict__ orig, int32_t n, const double* x0,
@@ -507,7 +641,7 @@ struct MDEngine {
     Ctx sub;  // private scratch for the rebuild pipeline (stable pointers for graphs)
     nd_md_params p{};
     int32_t n = 0, nL = 0, apl = 4, nblocks = 0;
-    int32_t lcap = 0, ucap = 0, upow2 = 0;
+    int32_t lcap = 0, ucap = 0, upow2 = 0, fcap = 0, lcap_leaf = 0, ucap_sm = 0;
     bool has_q = false, has_m = false;
     bool first = true;
     int cur = 0;            // current state set
@@ -516,12 +650,13 @@ struct MDEngine {
     bool rebuild_due = false;
     int64_t steps = 0, rebuilds = 0;
     Frame fr{};
-    DevBuf set_buf[2], rec_buf[2], xyz32, pos32, keys, store, ulist, ucount, llist, ncount, f,
-        vtmp, acc, aos, diag;
+    DevBuf set_buf[2], rec_buf[2], recb, xyz32, pos32, keys, store, ulist, ucount, llist_leaf,
+        lcount_leaf, llist, ncount, f, vtmp, acc, aos, diag;
     SetPtrs set[2];
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int64_t graph_launches = 0;  // kernels per captured window
-    size_t step_smem = 0, union_smem = 0;
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [refit][set]
+    int32_t resort_every = 5;  // re-sort (new order + topology) every k-th rebuild, refit between
+    int64_t graph_launches[2] = {0, 0};  // kernels per captured window [refit]
+    size_t step_smem = 0, union_smem = 0, lists_smem = 0;
 };
 
 static nd_status md_alloc(MDEngine* m) {
@@ -538,6 +673,8 @@ static nd_status md_alloc(MDEngine* m) {
         m->set[s].orig = (int32_t*)(b + 8 * n);
         if ((st = ensure(c, m->rec_buf[s], n * sizeof(int4)))) return st;
     }
+    if ((st = ensure(c, m->recb, n * sizeof(int4)))) return st;
+    if ((st = ensure(c, m->lcount_leaf, sizeof(int32_t) * (size_t)m->nL))) return st;
     if ((st = ensure(c, m->xyz32, 3 * n * sizeof(float)))) return st;
     if ((st = ensure(c, m->pos32, n * sizeof(float4)))) return st;
     if ((st = ensure(c, m->keys, 32 * (size_t)(2 * m->nL)))) return st;
@@ -569,11 +706,15 @@ static cudaError_t raise_smem_limit(const void* fn, int maxsm) {
 
 // Union and list buffers for capacities (ucap, lcap), and the shared-memory
 // opt-ins of the kernels that stage them.
-static nd_status md_alloc_lists(MDEngine* m, int32_t ucap, int32_t lcap) {
+static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t lcap_leaf,
+                                int32_t lcap, int32_t ucap_sm) {
     Ctx* c = &m->sub;
     nd_status st;
+    m->fcap = fcap;
     m->ucap = ucap;
     m->lcap = lcap;
+    m->lcap_leaf = lcap_leaf;
+    m->ucap_sm = std::min(ucap_sm, ucap);
     int32_t p2 = 1;
     while (p2 < ucap) p2 <<= 1;
     m->upow2 = p2;
@@ -581,8 +722,12 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t ucap, int32_t lcap) {
     if (lcap > 0 &&
         (st = ensure(c, m->llist, sizeof(uint16_t) * (size_t)lcap * kBlock * m->nblocks)))
         return st;
-    m->union_smem = sizeof(int32_t) * (2 * (size_t)kFrontierCap + p2);
-    m->step_smem = sizeof(int4) * (size_t)ucap * m->apl;
+    if (lcap_leaf > 0 &&
+        (st = ensure(c, m->llist_leaf, sizeof(uint16_t) * (size_t)lcap_leaf * m->nL)))
+        return st;
+    m->union_smem = sizeof(int32_t) * (2 * (size_t)fcap + p2);
+    m->step_smem = sizeof(int4) * (size_t)m->ucap_sm * m->apl;
+    m->lists_smem = sizeof(float4) * (size_t)m->ucap_sm * m->apl;
     int maxsm = 0;
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
     if ((int)m->union_smem + 1024 > maxsm || (lcap > 0 && (int)m->step_smem + 1024 > maxsm)) {
@@ -594,6 +739,12 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t ucap, int32_t lcap) {
     // raised once to the device maximum (less the function's static shared
     // memory) rather than set per engine.
     cudaError_t e = raise_smem_limit((const void*)k_md_block_union, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<1>, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<2>, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<4>, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<8>, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<16>, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<32>, maxsm);
 #define ND_SMEM(C, M, F, MODE) \
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE>, maxsm);
     ND_SMEM(true, true, true, 0) ND_SMEM(true, true, false, 0) ND_SMEM(true, false, true, 0)
@@ -616,6 +767,7 @@ static StepArgs md_step_args(MDEngine* m, int rec_in) {
     a.apl = m->apl;
     a.ucap = m->ucap;
     a.lcap = m->lcap;
+    a.smrec = m->ucap_sm * m->apl;
     a.ulist = (const int32_t*)m->ulist.p;
     a.ucount = (const int32_t*)m->ucount.p;
     a.llist = (const uint16_t*)m->llist.p;
@@ -632,12 +784,17 @@ static StepArgs md_step_args(MDEngine* m, int rec_in) {
     a.im = m->set[m->cur].im;
     a.f_out = (float4*)m->f.p;
     a.acc = (double*)m->acc.p;
-    a.pos_build = (const float4*)m->pos32.p;
+    a.rec_build = (const int4*)m->recb.p;
     a.diag = (unsigned long long*)m->diag.p;
     a.err = m->sub.d_err;
-    const float hs = (float)(0.5 * p.skin);
-    a.half_skin2 = hs * hs;
     const double S = m->fr.s;
+    const float hs = (float)(0.5 * p.skin * S);
+    a.half_skin2u = hs * hs;
+    for (int d = 0; d < 3; ++d) {
+        a.os[d] = m->fr.o[d] * S;
+        a.lo_fp[d] = (int32_t)std::floor((p.box_lo[d] - m->fr.o[d]) * S);
+        a.hi_fp[d] = (int32_t)std::ceil((p.box_hi[d] - m->fr.o[d]) * S);
+    }
     a.rc2u = (float)(p.cutoff * p.cutoff * S * S);
     a.sig2u = (float)(p.sigma * p.sigma * S * S);
     a.eps24u = (float)(24.0 * p.epsilon * S);
@@ -670,23 +827,33 @@ static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
 }
 
 // Rebuild: Float32 positions -> codes -> sort -> reorder state -> leaf boxes ->
-// build -> block unions -> per-atom lists.  Switches the current state set.
-static nd_status md_rebuild(MDEngine* m, bool sizing = false) {
+// build -> block unions -> per-atom lists; switches the current state set.
+// A refit keeps the order and the sorted codes (so the build reproduces the
+// topology) and only refreshes positions, boxes, unions and lists.
+static nd_status md_rebuild(MDEngine* m, bool sizing = false, bool refit = false) {
     Ctx* c = &m->sub;
     const int32_t n = m->n;
     const unsigned g = (unsigned)cdiv(n, 256);
-    SetPtrs& s = m->set[m->cur];
-    SetPtrs& t = m->set[m->cur ^ 1];
-    k_md_pos32<<<g, 256, 0, c->stream>>>(s.x[0], s.x[1], s.x[2], n, (float*)m->xyz32.p);
-    c->launches++;
     int32_t* codes = (int32_t*)c->codes.p;
     int32_t* perm = (int32_t*)c->perm.p;
     nd_status st;
-    if ((st = morton_codes(c, (const float*)m->xyz32.p, n, m->p.order, codes, perm))) return st;
-    if ((st = radix_sort_pairs(c, (uint32_t*)codes, perm, n, 30))) return st;
-    k_md_reorder<<<g, 256, 0, c->stream>>>(s, t, perm, (const float*)m->xyz32.p, n, m->fr,
-                                           (float4*)m->pos32.p, (int4*)m->rec_buf[0].p, c->d_err);
-    c->launches++;
+    if (refit) {
+        k_md_refit_pos<<<g, 256, 0, c->stream>>>(m->set[m->cur], n, m->fr, (float4*)m->pos32.p,
+                                                  (int4*)m->rec_buf[0].p, (int4*)m->recb.p,
+                                                  c->d_err);
+        c->launches++;
+    } else {
+        SetPtrs& s = m->set[m->cur];
+        SetPtrs& t = m->set[m->cur ^ 1];
+        k_md_pos32<<<g, 256, 0, c->stream>>>(s.x[0], s.x[1], s.x[2], n, (float*)m->xyz32.p);
+        c->launches++;
+        if ((st = morton_codes(c, (const float*)m->xyz32.p, n, m->p.order, codes, perm))) return st;
+        if ((st = radix_sort_pairs(c, (uint32_t*)codes, perm, n, 30))) return st;
+        k_md_reorder<<<g, 256, 0, c->stream>>>(s, t, perm, (const float*)m->xyz32.p, n, m->fr,
+                                               (float4*)m->pos32.p, (int4*)m->rec_buf[0].p,
+                                               (int4*)m->recb.p, c->d_err);
+        c->launches++;
+    }
     float4* keys = (float4*)m->keys.p;
     const float rl = (float)(m->p.cutoff + m->p.skin);
     k_md_leaf_boxes<<<(unsigned)cdiv(m->nL, 128), 128, 0, c->stream>>>(
@@ -697,15 +864,28 @@ static nd_status md_rebuild(MDEngine* m, bool sizing = false) {
     // the distance test alone decides membership
     const float hq = (rl / 2.0f) * 1.0001f + 1e-6f;
     k_md_block_union<<<(unsigned)m->nblocks, kBlock, m->union_smem, c->stream>>>(
-        keys, (const float4*)m->pos32.p, n, m->nL, hq, m->ucap, m->upow2, (int32_t*)m->ulist.p,
-        (int32_t*)m->ucount.p, c->d_err, (int32_t*)m->diag.p + 2, sizing ? 1 : 0);
-    k_md_block_lists<<<(unsigned)m->nblocks, kBlock, 0, c->stream>>>(
-        keys, (const float4*)m->pos32.p, n, m->apl, hq, rl * rl, m->ucap,
-        (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p, m->lcap,
-        (uint16_t*)m->llist.p, (int32_t*)m->ncount.p, c->d_err, (int32_t*)m->diag.p + 2,
+        keys, (const float4*)m->pos32.p, n, m->nL, m->apl, hq, m->fcap, m->ucap, m->upow2,
+        (int32_t*)m->ulist.p, (int32_t*)m->ucount.p, (uint16_t*)m->llist_leaf.p,
+        (int32_t*)m->lcount_leaf.p, m->lcap_leaf, c->d_err, (int32_t*)m->diag.p + 2,
         sizing ? 1 : 0);
+#define ND_LISTS(A)                                                                             \
+    k_md_block_lists<A><<<(unsigned)m->nblocks, kBlock, m->lists_smem, c->stream>>>(            \
+        (const float4*)m->pos32.p, n, rl * rl, m->ucap, m->ucap_sm * m->apl,                    \
+        (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p,                                \
+        (const uint16_t*)m->llist_leaf.p, (const int32_t*)m->lcount_leaf.p, m->lcap_leaf,       \
+        m->lcap, (uint16_t*)m->llist.p, (int32_t*)m->ncount.p, c->d_err,                        \
+        (int32_t*)m->diag.p + 2, sizing ? 1 : 0)
+    switch (m->apl) {
+        case 1: ND_LISTS(1); break;
+        case 2: ND_LISTS(2); break;
+        case 4: ND_LISTS(4); break;
+        case 8: ND_LISTS(8); break;
+        case 16: ND_LISTS(16); break;
+        default: ND_LISTS(32); break;
+    }
+#undef ND_LISTS
     c->launches += 2;
-    m->cur ^= 1;
+    if (!refit) m->cur ^= 1;
     m->rc = 0;
     return check_launch(c, "md rebuild");
 }
@@ -720,8 +900,8 @@ static void md_steps(MDEngine* m, int32_t k) {
     }
 }
 
-static nd_status md_capture_window(MDEngine* m, int which) {
-    // Captures rebuild + R steps starting from state set `which`.
+static nd_status md_capture_window(MDEngine* m, int which, int refit) {
+    // Captures (re-sort or refit) rebuild + R steps starting from state set `which`.
     Ctx* c = &m->sub;
     int save_cur = m->cur, save_rc = m->rc;
     bool save_first = m->first;
@@ -731,15 +911,15 @@ static nd_status md_capture_window(MDEngine* m, int which) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
-    nd_status st = md_rebuild(m);
+    nd_status st = md_rebuild(m, false, refit != 0);
     if (st == ND_OK) md_steps(m, m->p.rebuild_every);
     e = cudaStreamEndCapture(c->stream, &g);
     if (st) { if (g) cudaGraphDestroy(g); return st; }
     if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
-    e = cudaGraphInstantiate(&m->graph[which], g, 0);
+    e = cudaGraphInstantiate(&m->graph[refit][which], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
-    m->graph_launches = c->launches - save_launch;
+    m->graph_launches[refit] = c->launches - save_launch;
     c->launches = save_launch;
     m->cur = save_cur;
     m->rc = save_rc;
@@ -747,31 +927,50 @@ static nd_status md_capture_window(MDEngine* m, int which) {
     return ND_OK;
 }
 
-// First build: a sizing pass (lists counted, not stored; union capacity
-// generous) measures the largest union and list, then the capacities are set
-// with head-room and the real build runs.
+// Sizing build pass: diag int32 words 2..6 collect the largest union, the
+// largest per-atom list, the largest per-leaf candidate list, the sum of
+// union sizes and the largest BFS frontier.
+static nd_status md_sizing_pass(MDEngine* m, int32_t h[5]) {
+    Ctx* c = &m->sub;
+    cudaMemsetAsync((int32_t*)m->diag.p + 2, 0, 5 * sizeof(int32_t), c->stream);
+    nd_status st = md_rebuild(m, true);
+    if (st) return st;
+    cudaError_t e = cudaMemcpyAsync(h, (int32_t*)m->diag.p + 2, 5 * sizeof(int32_t),
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "size lists");
+    return sync_and_check(c, "md sizing build");
+}
+
+static int32_t round_up(double v, int32_t q) { return (((int32_t)std::ceil(v)) + q - 1) / q * q; }
+
+// First builds: (1) generous union and frontier, lists not stored -> union,
+// frontier and per-leaf capacities; (2) per-leaf lists stored, per-atom lists
+// counted -> list capacity; (3) the real build.  Capacities carry head-room
+// for the drift until later rebuilds.
 static nd_status md_size_lists(MDEngine* m) {
     Ctx* c = &m->sub;
     nd_status st;
-    if ((st = md_alloc_lists(m, kSizingUcap, 0))) return st;
-    cudaMemsetAsync((int32_t*)m->diag.p + 2, 0, 2 * sizeof(int32_t), c->stream);
-    if ((st = md_rebuild(m, true))) return st;
-    int32_t h[2];
-    cudaError_t e = cudaMemcpyAsync(h, (int32_t*)m->diag.p + 2, sizeof(h),
-                                    cudaMemcpyDeviceToHost, c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "size lists");
-    if ((st = sync_and_check(c, "md sizing build"))) return st;
-    const int32_t max_u = h[0], max_n = h[1];
-    if (max_u > kSizingUcap) {
+    int32_t h[5];
+    if ((st = md_alloc_lists(m, kSizingFcap, kSizingUcap, 0, 0, 0))) return st;
+    if ((st = md_sizing_pass(m, h))) return st;
+    const int32_t max_u = h[0], max_c = h[2], max_f = h[4];
+    const double mean_u = (double)h[3] / m->nblocks;
+    if (max_u > kSizingUcap || max_f > kSizingFcap) {
         c->last_error = "neighbour union of a block exceeds the supported size";
         return ND_ERR_OVERFLOW;
     }
-    int32_t lcap = m->p.max_neighbors > 0 ? m->p.max_neighbors
-                                          : (int32_t)std::ceil(max_n * 1.35) + 16;
-    lcap = (lcap + 7) & ~7;
-    int32_t ucap = ((int32_t)std::ceil(max_u * 1.25) + 32 + 31) & ~31;
+    int32_t ucap = round_up(max_u * 1.25 + 32, 32);
     if ((int64_t)ucap * m->apl > 65536) ucap = 65536 / m->apl;
-    if ((st = md_alloc_lists(m, ucap, lcap))) return st;
+    const int32_t fcap = round_up(max_f * 1.3 + 64, 32);
+    const int32_t lcap_leaf = std::min(ucap, round_up(max_c * 1.3 + 16, 8));
+    // Shared-memory staging sized near the mean union (head-room for drift);
+    // a block whose union is larger reads its remaining records from L2.
+    const int32_t ucap_sm = round_up(mean_u * 1.2 + 16, 16);
+    if ((st = md_alloc_lists(m, fcap, ucap, lcap_leaf, 0, ucap_sm))) return st;
+    if ((st = md_sizing_pass(m, h))) return st;
+    const int32_t max_n = h[1];
+    int32_t lcap = m->p.max_neighbors > 0 ? m->p.max_neighbors : round_up(max_n * 1.35 + 16, 8);
+    if ((st = md_alloc_lists(m, fcap, ucap, lcap_leaf, lcap, ucap_sm))) return st;
     if ((st = md_rebuild(m))) return st;
     m->in_window = 0;
     m->rebuild_due = false;
@@ -854,6 +1053,7 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
                                   const double* md_, bool host, bool capture, MDEngine** out) {
     if (!parent || !p || !out || !xd || !vd || n <= 0) return ND_ERR_ARG;
     if (p->atomsperleaf <= 0 || n % p->atomsperleaf || n / p->atomsperleaf < 2) return ND_ERR_SPEC;
+    if (32 % p->atomsperleaf != 0) return ND_ERR_SPEC;  // a warp holds whole leaves
     if (p->rebuild_every <= 0 || !(p->cutoff > 0) || !(p->skin >= 0) || !(p->dt > 0))
         return ND_ERR_ARG;
     MDEngine* m = new MDEngine();
@@ -877,8 +1077,8 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     m->cur = 0;
     m->first = true;
     if ((st = md_size_lists(m))) { parent->last_error = c->last_error; md_destroy(m); return st; }
-    for (int w = 0; capture && w < 2; ++w)
-        if ((st = md_capture_window(m, w))) { parent->last_error = c->last_error; md_destroy(m); return st; }
+    for (int w = 0; capture && w < 4; ++w)
+        if ((st = md_capture_window(m, w & 1, w >> 1))) { parent->last_error = c->last_error; md_destroy(m); return st; }
     parent->launches += c->launches;
     c->launches = 0;
     *out = m;
@@ -893,10 +1093,12 @@ nd_status md_create(Ctx* parent, const nd_md_params* p, int32_t n, const double*
 
 nd_status md_destroy(MDEngine* m) {
     if (!m) return ND_OK;
-    for (int w = 0; w < 2; ++w)
-        if (m->graph[w]) cudaGraphExecDestroy(m->graph[w]);
-    DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->rec_buf[0], &m->rec_buf[1], &m->xyz32,
-                      &m->pos32, &m->keys, &m->store, &m->ulist, &m->ucount, &m->llist,
+    for (int r = 0; r < 2; ++r)
+        for (int w = 0; w < 2; ++w)
+            if (m->graph[r][w]) cudaGraphExecDestroy(m->graph[r][w]);
+    DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->rec_buf[0], &m->rec_buf[1], &m->recb,
+                      &m->xyz32, &m->pos32, &m->keys, &m->store, &m->ulist, &m->ucount,
+                      &m->llist_leaf, &m->lcount_leaf, &m->llist,
                       &m->ncount, &m->f, &m->vtmp, &m->acc, &m->aos, &m->diag, &m->sub.codes,
                       &m->sub.codes_alt, &m->sub.perm, &m->sub.perm_alt, &m->sub.hist,
                       &m->sub.misc};
@@ -915,18 +1117,20 @@ nd_status md_run(MDEngine* m, int64_t steps) {
     nd_status st;
     while (steps > 0) {
         if (m->rebuild_due) {
-            if (steps >= R && !m->first && m->graph[m->cur]) {
-                cudaError_t e = cudaGraphLaunch(m->graph[m->cur], c->stream);
+            // every resort_every-th rebuild re-sorts; the others refit
+            const int refit = (m->rebuilds % m->resort_every) != 0 ? 1 : 0;
+            if (steps >= R && !m->first && m->graph[refit][m->cur]) {
+                cudaError_t e = cudaGraphLaunch(m->graph[refit][m->cur], c->stream);
                 if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
-                c->launches += m->graph_launches;
-                m->cur ^= 1;
+                c->launches += m->graph_launches[refit];
+                if (!refit) m->cur ^= 1;
                 m->rc = R & 1;
                 m->rebuilds++;
                 m->steps += R;
                 steps -= R;
                 continue;
             }
-            if ((st = md_rebuild(m))) return st;
+            if ((st = md_rebuild(m, false, refit != 0))) return st;
             m->rebuilds++;
             m->rebuild_due = false;
             m->in_window = 0;
@@ -1035,7 +1239,8 @@ nd_status md_diagnostics(MDEngine* m, int64_t* skin_violations, int32_t* max_nei
 
 int64_t md_launches_per_run(MDEngine* m, int64_t steps) {
     const int64_t R = m->p.rebuild_every;
-    return (steps / R) * m->graph_launches + (steps % R) * 1;
+    const int64_t w = steps / R, full = (w + m->resort_every - 1) / m->resort_every;
+    return full * m->graph_launches[0] + (w - full) * m->graph_launches[1] + (steps % R);
 }
 
 nd_status md_sync(MDEngine* m) { return sync_and_check(&m->sub, "md sync"); }
