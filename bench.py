@@ -37,8 +37,8 @@ SEED = 0x4E440002
 METRIC = "LJ+Coulomb atom-steps/s @262k (FP32 forces, FP64 x/v, rebuild every 10)"
 UNIT = "atom-steps/s"
 WORKLOAD = ("lj_coulomb_262144: N=262144 uniform cube side 68 (min separation 0.8), q=+/-1, "
-            "sigma=eps=1, k=1, r_c=2.5, skin=0.3, dt=1e-3, rebuild every 10, 100 MD steps per "
-            "bench step")
+            "sigma=eps=1, k=1, r_c=2.5, skin >= 0.3 (autotuned), dt=1e-3, rebuild every 10, "
+            "100 MD steps per bench step")
 
 
 def _md_params(nd, order=None):
@@ -172,6 +172,86 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+ENSEMBLE_STEPS = 200
+
+
+def batched_leg(nd, ctx, ext, flush):
+    """Batched ensemble (512 LJ systems, sizes log-uniform in [256, 16384],
+    density U[0.6, 0.9], sigma U[0.9, 1.1], eps U[0.8, 1.2], r_c 2.5, dt 1e-3,
+    rebuild every 10, 200 steps) through one autotuned engine, against the same
+    systems run one by one through the plain engine.  Both timed with CUDA
+    events on the library's stream, inputs resident, L2 flushed before each."""
+    import numpy as np
+    import torch
+
+    e = nd.synth.ensemble(nd.synth.SEED_ENSEMBLE)
+    table = nd.systems_table(e["n_atoms"], e["sigma"], e["epsilon"], e["box_lo"], e["box_hi"])
+    base = nd.md_params(cutoff=2.5, skin=0.3, dt=1e-3, atomsperleaf=4, rebuild_every=REBUILD)
+    t0 = time.perf_counter()
+    tuned, _ = nd.autotune(base, e["x"], e["v"], systems=table, trial_steps=50, ctx=ctx)
+    tune_s = time.perf_counter() - t0
+    n_tot = int(e["n_atoms"].sum())
+    off = np.concatenate([[0], np.cumsum(e["n_atoms"])])
+
+    def timed(run):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            a.record(ext)
+            run()
+            b.record(ext)
+        ctx.synchronize()
+        return a.elapsed_time(b) * 1e-3
+
+    bat = nd.Ensemble(tuned, table, e["x"], e["v"], ctx=ctx)
+    _, _, f_bat = bat.get()
+    bat.run(REBUILD)  # the opening window (its own captured graph)
+    bat.sync()
+    l0 = ctx.launch_count()
+    d0 = bat.diagnostics()
+    t_bat = timed(lambda: bat.run(ENSEMBLE_STEPS))
+    bat_diag = bat.diagnostics()
+    bat_launches = ctx.launch_count() - l0 + bat_diag["body_kernels"] - d0["body_kernels"]
+    bat.close()
+
+    plain = []
+    f_err = 0.0
+    for k in range(len(e["n_atoms"])):
+        sl = slice(int(off[k]), int(off[k + 1]))
+        side = float(e["box_hi"][k][0])
+        p = nd.md_params(sigma=float(e["sigma"][k]), epsilon=float(e["epsilon"][k]), cutoff=2.5,
+                         skin=tuned.skin, dt=1e-3, box_lo=(0, 0, 0), box_hi=(side, side, side),
+                         atomsperleaf=tuned.atomsperleaf, rebuild_every=REBUILD,
+                         resort_every=tuned.resort_every, stage_policy=tuned.stage_policy)
+        eng = nd.MDEngine(p, e["x"][sl], e["v"][sl], ctx=ctx)
+        _, _, fp = eng.get()
+        f_err = max(f_err, float(np.linalg.norm(f_bat[sl] - fp) / np.linalg.norm(fp)))
+        eng.run(REBUILD)
+        plain.append(eng)
+    ctx.synchronize()
+    t_plain = timed(lambda: [eng.run(ENSEMBLE_STEPS) for eng in plain])
+    for eng in plain:
+        eng.close()
+    v_bat = n_tot * ENSEMBLE_STEPS / t_bat
+    v_plain = n_tot * ENSEMBLE_STEPS / t_plain
+    return {"metric": "ensemble atom-steps/s, batched vs plain", "unit": UNIT,
+            "workload": (f"ensemble_512: {len(e['n_atoms'])} LJ systems, {n_tot} atoms "
+                         f"(N_s {int(e['n_atoms'].min())}..{int(e['n_atoms'].max())}), "
+                         "rho U[0.6,0.9], sigma U[0.9,1.1], eps U[0.8,1.2], r_c 2.5, "
+                         f"skin {tuned.skin:.1f} (autotuned), "
+                         f"dt 1e-3, rebuild every 10, {ENSEMBLE_STEPS} steps"),
+            "value": v_bat, "plain_value": v_plain, "batched_over_plain": v_bat / v_plain,
+            "batched_s": t_bat, "plain_s": t_plain, "batched_gpu_launches": bat_launches,
+            "force_rel_l2_batched_vs_plain_max": f_err,
+            "skin_violations": bat_diag["skin_violations"],
+            "early_refits": bat_diag["early_refits"],
+            "tuned": {"skin": tuned.skin, "atomsperleaf": tuned.atomsperleaf,
+                      "resort_every": tuned.resort_every,
+                      "stage_policy": tuned.stage_policy, "autotune_s": round(tune_s, 2)},
+            "plain_path": "512 nd_md engines run one after another on one stream (graphs)"}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -189,7 +269,11 @@ def run_gb300(args):
     xd = torch.from_numpy(x).cuda()
     vd = torch.from_numpy(v).cuda()
     qd = torch.from_numpy(q).cuda()
-    params = _md_params(nd)
+    # engine settings (skin, leaf width, re-sort interval, staging) from the
+    # library's autotuner on this state, outside the timed region
+    t0 = time.perf_counter()
+    params, _ = nd.autotune(_md_params(nd), x, v, q, trial_steps=50, ctx=ctx)
+    tune_s = time.perf_counter() - t0
     eng = nd.MDEngine(params, xd, vd, qd, device=True, ctx=ctx)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -207,6 +291,7 @@ def run_gb300(args):
     events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
     launches0 = ctx.launch_count()
+    diag0 = eng.diagnostics()
     barrier()
     wall0 = time.perf_counter()
     with ClockSampler(local) as clk:
@@ -220,30 +305,22 @@ def run_gb300(args):
         eng.sync()
         barrier()
     wall = time.perf_counter() - wall0
-    launches = ctx.launch_count() - launches0
+    diag = eng.diagnostics()
+    early = diag["early_refits"] - diag0["early_refits"]
+    # kernel nodes of the launched graphs plus the kernels of the conditional
+    # rebuild bodies that ran
+    launches = (ctx.launch_count() - launches0 + diag["body_kernels"] - diag0["body_kernels"])
     t_ms = sum(s.elapsed_time(e) for (s, e) in events)
     t_max = t_ms
     if ws > 1:
         tt = torch.tensor([t_ms], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_max = float(tt.item())
-    diag = eng.diagnostics()
     stats = eng.stats()
 
-    # ---- roofline of the dominant kernel: single k_md_step launches timed with
-    # events on the library's stream (mid-window eager steps: one kernel each)
-    eng.run(REBUILD - (stats["steps"] % REBUILD) if stats["steps"] % REBUILD else 0)
-    eng.run(1)  # opens a window: rebuild + first step
-    single = []
-    with torch.cuda.stream(ext):
-        for _ in range(REBUILD - 2):
-            s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s_.record(ext)
-            eng.run(1)
-            e_.record(ext)
-            single.append((s_, e_))
-    eng.sync()
-    k_ms = statistics.mean(s.elapsed_time(e) for (s, e) in single)
+    # ---- roofline of the dominant kernel: k_md_step launches each bracketed
+    # by a pair of CUDA events on the library's stream (nd_md_step_times)
+    k_ms = float(statistics.mean(eng.step_times(2 * REBUILD)))
     nbr = stats["list_pairs"] / N_ATOMS  # full-list neighbours per atom
     # algorithmic bytes per atom of one fused step: x, v read+write (FP64, 96),
     # own fixed-point record read (16) + next record write (16), force write
@@ -294,11 +371,19 @@ def run_gb300(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 state",
         "data": "synthetic (seeded splitmix64 generators)",
         "config": {"workload": WORKLOAD, "n_atoms": N_ATOMS, "md_steps_per_step": MD_PER_STEP,
-                   "rebuild_every": REBUILD, "atom_order": "3-D Hilbert, re-sorted every 5th rebuild, refit between",
+                   "rebuild_every": REBUILD,
+                   "atom_order": f"3-D Hilbert, re-sorted every {params.resort_every}th rebuild, "
+                                 "refit between",
+                   "tuned": {"skin": params.skin, "atomsperleaf": params.atomsperleaf,
+                             "resort_every": params.resort_every,
+                             "stage_policy": params.stage_policy, "autotune_s": round(tune_s, 2)},
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "512 MB buffer written before every timed step (outside the events)",
                    "neighbours_per_atom": round(nbr, 2),
                    "skin_violations": diag["skin_violations"],
+                   "early_refits_timed": early,
+                   "resorts_timed": diag["resorts"] - diag0["resorts"],
+                   "refits_timed": diag["refits"] - diag0["refits"],
                    "wall_s_timed_region": round(wall, 4)},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -314,11 +399,13 @@ def run_gb300(args):
     clocks = clk.summary()
     if clocks:
         line["clocks"] = clocks
+    eng.close()
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_leg(nd, ctx, ext, flush)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(steps=10)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -331,6 +418,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-ensemble measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -93,7 +93,22 @@ typedef struct {
     int32_t rebuild_every; /* steps between neighbour-list rebuilds */
     int32_t order;         /* ND_ORDER_* used for the rebuilds */
     int32_t max_neighbors; /* per-atom list capacity, 0 = sized from the first build */
+    int32_t resort_every;  /* every k-th rebuild re-sorts the atoms, the others refit the
+                              kept tree; 0 = 1 (always re-sort) */
+    int32_t stage_policy;  /* shared-memory staging of a block's neighbour records:
+                              0 = sized near the mean union, 1 = the largest union */
 } nd_md_params;
+
+/* One system of a batched ensemble: its atom count (a multiple of atomsperleaf),
+ * Lennard-Jones parameters and reflecting walls.  Systems never interact. */
+typedef struct {
+    int32_t n_atoms;
+    int32_t reserved;
+    double sigma;
+    double epsilon;
+    double box_lo[3];
+    double box_hi[3];
+} nd_system;
 
 /* ----------------------------------------------------------------- context */
 
@@ -254,12 +269,71 @@ nd_status nd_md_energy(nd_md* md, double* potential, double* kinetic);
 /* Steps taken, rebuilds done, pairs in the current list, list capacity. */
 nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* list_pairs,
                       int32_t* capacity);
-/* Atom-steps in which an atom had moved more than skin/2 since the last
- * rebuild (the list may then miss pairs: raise skin or rebuild more often),
- * and the largest per-atom neighbour count seen in any build. */
-nd_status nd_md_diagnostics(nd_md* md, int64_t* skin_violations, int32_t* max_neighbors);
+/* Engine diagnostics (nd_md_diagnostics). */
+typedef struct {
+    int64_t skin_violations; /* atom-steps in which an atom had moved more than skin/2
+                                since its list was built: the list may then miss pairs */
+    int32_t max_neighbors;   /* largest per-atom neighbour count of any build */
+    int32_t reserved;
+    int64_t resorts;         /* window rebuilds that re-sorted the atoms */
+    int64_t refits;          /* window rebuilds that refitted the kept tree */
+    int64_t early_refits;    /* refits inside a window: after a step that left some atom
+                                able to pass skin/2 in the next step */
+    int64_t resort_kernels;  /* kernels of one re-sort rebuild */
+    int64_t refit_kernels;   /* kernels of one refit */
+    int64_t body_kernels;    /* kernels run so far inside captured conditional nodes
+                                (not in nd_ctx_launch_count) */
+} nd_md_diag;
+
+/* Rebuilds are decided on the device: a window re-sorts every resort_every-th
+ * time or when a list has passed 90% of its capacity since the last re-sort,
+ * and refits otherwise; a step after which some atom could pass skin/2 from
+ * its list-build position in the next step (its displacement plus twice its
+ * last move reaches 95% of skin/2) is followed by an early refit. */
+nd_status nd_md_diagnostics(nd_md* md, nd_md_diag* out);
+/* Advance `steps` steps without captured graphs, timing each step kernel with
+ * its own pair of CUDA events on the context stream: ms[k] (host array of
+ * `steps`) receives the k-th step kernel's duration.  Synchronises. */
+nd_status nd_md_step_times(nd_md* md, int32_t steps, float* ms);
 /* Number of kernel launches one nd_md_run(steps) enqueues (for diagnostics). */
 int64_t nd_md_launches_per_run(nd_md* md, int64_t steps);
+
+/*
+ * Batched ensemble: `nsys` independent systems advanced together by one engine
+ * (each step is one launch over all systems' atoms; rebuild windows are
+ * captured CUDA graphs).  x, v: (sum n_atoms) x 3 FP64, systems concatenated
+ * in order; q, m may be NULL.  p supplies the shared settings (cutoff, skin,
+ * dt, coulomb_k, atomsperleaf, rebuild_every, resort_every, stage_policy);
+ * its sigma, epsilon and walls are ignored in favour of each system's.  The
+ * result is an nd_md: nd_md_run / get / sync / diagnostics apply unchanged and
+ * nd_md_energy returns the ensemble totals.  No counterpart in the reference
+ * (it runs one system per simulate! call).
+ */
+nd_status nd_batch_create(nd_ctx* ctx, const nd_md_params* p, int32_t nsys, const nd_system* sys,
+                          const double* x, const double* v, const double* q, const double* m,
+                          nd_md** out);
+/* Same, from device arrays. */
+nd_status nd_batch_create_dev(nd_ctx* ctx, const nd_md_params* p, int32_t nsys,
+                              const nd_system* sys, const double* x, const double* v,
+                              const double* q, const double* m, nd_md** out);
+/* Per-system potential and kinetic energies (arrays of nsys; either may be NULL). */
+nd_status nd_batch_energies(nd_md* md, double* potential, double* kinetic);
+
+/*
+ * Autotuner: times short runs of candidate engine settings on copies of the
+ * given state (host arrays; the state is not advanced) and writes the fastest
+ * into *best (skin -- p->skin, +0.1 or +0.2 --, atomsperleaf -- the
+ * leaf/traversal width --, resort_every and stage_policy; every other field
+ * copied from *p), tuning one setting at a time.  nsys == 0 tunes a plain
+ * engine (sys ignored).  Candidates change only the summation order of the
+ * forces, not which pairs interact.  trial_steps: timed steps per candidate
+ * (rounded up to whole rebuild windows).  seconds_per_step (may be NULL)
+ * receives the winner's time per MD step.
+ */
+nd_status nd_md_autotune(nd_ctx* ctx, const nd_md_params* p, int32_t n, int32_t nsys,
+                         const nd_system* sys, const double* x, const double* v, const double* q,
+                         const double* m, int32_t trial_steps, nd_md_params* best,
+                         double* seconds_per_step);
 
 /*
  * simulate!(sys, spec, clct) (Simulator.jl:154-256) with host arrays in and out:

@@ -85,6 +85,13 @@ __global__ void k_bbox_init(uint32_t* bbox) {
     if (threadIdx.x < 6) bbox[threadIdx.x] = threadIdx.x < 3 ? 0xffffffffu : 0u;
 }
 
+// A given frame in place of the bounding box.
+__global__ void k_bbox_set(uint32_t* bbox, float x0, float y0, float z0, float x1, float y1,
+                           float z1) {
+    const float v[6] = {x0, y0, z0, x1, y1, z1};
+    if (threadIdx.x < 6) bbox[threadIdx.x] = f2o(v[threadIdx.x]);
+}
+
 // Spatial code: 3-D Hilbert index over the bounding box, 1024 bins per axis.
 __global__ void k_morton_spatial(const float* __restrict__ xyz, int32_t n,
                                  const uint32_t* __restrict__ bbox, int32_t* __restrict__ codes,
@@ -106,17 +113,23 @@ __global__ void k_morton_spatial(const float* __restrict__ xyz, int32_t n,
 }
 
 nd_status morton_codes(Ctx* c, const float* xyz, int32_t n, int32_t order, int32_t* codes,
-                       int32_t* iota) {
+                       int32_t* iota, const float* frame) {
     if (n <= 0) return ND_OK;
     const int T = 256;
     if (order == ND_ORDER_SPATIAL) {
         nd_status st = ensure(c, c->misc, 64);
         if (st) return st;
-        k_bbox_init<<<1, 32, 0, c->stream>>>((uint32_t*)c->misc.p);
-        c->launches++;
-        int blocks = (int)std::min<int64_t>(cdiv(n, T), 152 * 8);
-        k_bbox<<<blocks, T, 0, c->stream>>>(xyz, n, (uint32_t*)c->misc.p, c->d_err);
-        c->launches++;
+        if (frame) {
+            k_bbox_set<<<1, 32, 0, c->stream>>>((uint32_t*)c->misc.p, frame[0], frame[1], frame[2],
+                                                frame[3], frame[4], frame[5]);
+            c->launches++;
+        } else {
+            k_bbox_init<<<1, 32, 0, c->stream>>>((uint32_t*)c->misc.p);
+            c->launches++;
+            int blocks = (int)std::min<int64_t>(cdiv(n, T), 152 * 8);
+            k_bbox<<<blocks, T, 0, c->stream>>>(xyz, n, (uint32_t*)c->misc.p, c->d_err);
+            c->launches++;
+        }
         k_morton_spatial<<<(int)cdiv(n, T), T, 0, c->stream>>>(xyz, n, (const uint32_t*)c->misc.p,
                                                               codes, iota);
         c->launches++;

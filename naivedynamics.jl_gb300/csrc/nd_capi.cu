@@ -6,18 +6,34 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <set>
 #include <vector>
 
 #include "nd_internal.cuh"
 
+struct nd_md;
+
+// A context tracks its live engines: destroying the context releases their
+// device state first and leaves the handles orphaned (every call on them then
+// returns ND_ERR_ARG and nd_md_destroy only frees the handle), so the two may
+// be destroyed in either order.
 struct nd_ctx {
     nd::Ctx c;
+    std::set<nd_md*> engines;
 };
 
 struct nd_md {
     nd_ctx* ctx;
     nd::MDEngine* e;
 };
+
+static nd_md* md_register(nd_ctx* h, nd::MDEngine* e) {
+    nd_md* md = new nd_md{h, e};
+    h->engines.insert(md);
+    return md;
+}
+
+static bool md_live(const nd_md* md) { return md && md->ctx && md->e; }
 
 namespace nd {
 
@@ -262,6 +278,12 @@ nd_status nd_ctx_destroy(nd_ctx* h) {
     if (!h) return ND_OK;
     Ctx* c = &h->c;
     cudaSetDevice(c->device);
+    for (nd_md* md : h->engines) {
+        nd::md_destroy(md->e);
+        md->e = nullptr;
+        md->ctx = nullptr;
+    }
+    h->engines.clear();
     if (c->sim_cache) nd::md_destroy(c->sim_cache);
     c->sim_cache = nullptr;
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -445,7 +467,7 @@ nd_status nd_md_create(nd_ctx* h, const nd_md_params* p, int32_t n, const double
     if (st) return st;
     nd::MDEngine* e = nullptr;
     if ((st = nd::md_create(&h->c, p, n, x, v, q, m, true, true, &e))) return st;
-    *out = new nd_md{h, e};
+    *out = md_register(h, e);
     return ND_OK;
 }
 
@@ -456,14 +478,60 @@ nd_status nd_md_create_dev(nd_ctx* h, const nd_md_params* p, int32_t n, const do
     if (st) return st;
     nd::MDEngine* e = nullptr;
     if ((st = nd::md_create(&h->c, p, n, x, v, q, m, false, true, &e))) return st;
-    *out = new nd_md{h, e};
+    *out = md_register(h, e);
     return ND_OK;
+}
+
+nd_status nd_batch_create(nd_ctx* h, const nd_md_params* p, int32_t nsys, const nd_system* sys,
+                          const double* x, const double* v, const double* q, const double* m,
+                          nd_md** out) {
+    if (!h || !out) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    nd::MDEngine* e = nullptr;
+    if ((st = nd::md_create_batch(&h->c, p, nsys, sys, x, v, q, m, true, &e))) return st;
+    *out = md_register(h, e);
+    return ND_OK;
+}
+
+nd_status nd_batch_create_dev(nd_ctx* h, const nd_md_params* p, int32_t nsys,
+                              const nd_system* sys, const double* x, const double* v,
+                              const double* q, const double* m, nd_md** out) {
+    if (!h || !out) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    nd::MDEngine* e = nullptr;
+    if ((st = nd::md_create_batch(&h->c, p, nsys, sys, x, v, q, m, false, &e))) return st;
+    *out = md_register(h, e);
+    return ND_OK;
+}
+
+nd_status nd_batch_energies(nd_md* md, double* potential, double* kinetic) {
+    if (!md_live(md)) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    nd_status st = nd::md_energies(md->e, potential, kinetic);
+    if (st) md->ctx->c.last_error = nd::md_last_error(md->e);
+    return st;
+}
+
+nd_status nd_md_autotune(nd_ctx* h, const nd_md_params* p, int32_t n, int32_t nsys,
+                         const nd_system* sys, const double* x, const double* v, const double* q,
+                         const double* m, int32_t trial_steps, nd_md_params* best,
+                         double* seconds_per_step) {
+    if (!h) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    return nd::md_autotune(&h->c, p, n, nsys, sys, x, v, q, m, trial_steps, best,
+                           seconds_per_step);
 }
 
 nd_status nd_md_destroy(nd_md* md) {
     if (!md) return ND_OK;
-    nd::set_device(&md->ctx->c);
-    nd::md_destroy(md->e);
+    if (md_live(md)) {
+        nd::set_device(&md->ctx->c);
+        md->ctx->engines.erase(md);
+        nd::md_destroy(md->e);
+    }
     delete md;
     return ND_OK;
 }
@@ -474,47 +542,53 @@ static nd_status md_wrap(nd_md* md, nd_status st) {
 }
 
 nd_status nd_md_run(nd_md* md, int64_t steps) {
-    if (!md || steps < 0) return ND_ERR_ARG;
+    if (!md_live(md) || steps < 0) return ND_ERR_ARG;
     nd::set_device(&md->ctx->c);
     return md_wrap(md, nd::md_run(md->e, steps));
 }
 
 nd_status nd_md_sync(nd_md* md) {
-    if (!md) return ND_ERR_ARG;
+    if (!md_live(md)) return ND_ERR_ARG;
     return md_wrap(md, nd::md_sync(md->e));
 }
 
 nd_status nd_md_get(nd_md* md, double* x, double* v, float* f) {
-    if (!md) return ND_ERR_ARG;
+    if (!md_live(md)) return ND_ERR_ARG;
     nd::set_device(&md->ctx->c);
     return md_wrap(md, nd::md_get(md->e, x, v, f, true));
 }
 
 nd_status nd_md_get_dev(nd_md* md, double* x, double* v, float* f) {
-    if (!md) return ND_ERR_ARG;
+    if (!md_live(md)) return ND_ERR_ARG;
     nd::set_device(&md->ctx->c);
     return md_wrap(md, nd::md_get(md->e, x, v, f, false));
 }
 
 nd_status nd_md_energy(nd_md* md, double* potential, double* kinetic) {
-    if (!md) return ND_ERR_ARG;
+    if (!md_live(md)) return ND_ERR_ARG;
     nd::set_device(&md->ctx->c);
     return md_wrap(md, nd::md_energy(md->e, potential, kinetic));
 }
 
 nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* list_pairs,
                       int32_t* capacity) {
-    if (!md) return ND_ERR_ARG;
+    if (!md_live(md)) return ND_ERR_ARG;
     return md_wrap(md, nd::md_stats(md->e, steps, rebuilds, list_pairs, capacity));
 }
 
-nd_status nd_md_diagnostics(nd_md* md, int64_t* skin_violations, int32_t* max_neighbors) {
-    if (!md) return ND_ERR_ARG;
-    return md_wrap(md, nd::md_diagnostics(md->e, skin_violations, max_neighbors));
+nd_status nd_md_diagnostics(nd_md* md, nd_md_diag* out) {
+    if (!md_live(md) || !out) return ND_ERR_ARG;
+    return md_wrap(md, nd::md_diagnostics(md->e, out));
+}
+
+nd_status nd_md_step_times(nd_md* md, int32_t steps, float* ms) {
+    if (!md_live(md)) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_step_times(md->e, steps, ms));
 }
 
 int64_t nd_md_launches_per_run(nd_md* md, int64_t steps) {
-    return md ? nd::md_launches_per_run(md->e, steps) : 0;
+    return md_live(md) ? nd::md_launches_per_run(md->e, steps) : 0;
 }
 
 nd_status nd_simulate(nd_ctx* h, const nd_md_params* p, int32_t n, double* x, double* v,

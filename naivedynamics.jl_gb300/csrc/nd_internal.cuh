@@ -161,8 +161,10 @@ struct TreeBuffers {
 };
 
 // Morton codes of n float3 positions (device, AoS) into codes + iota values.
+// frame (ND_ORDER_SPATIAL only, may be NULL): host min[3], max[3] of the
+// Hilbert grid instead of the positions' bounding box.
 nd_status morton_codes(Ctx* c, const float* xyz, int32_t n, int32_t order, int32_t* codes,
-                       int32_t* iota);
+                       int32_t* iota, const float* frame = nullptr);
 // Stable LSD radix sort of (codes, vals) on `bits` low bits; results in codes/vals.
 nd_status radix_sort_pairs(Ctx* c, uint32_t* keys, int32_t* vals, int32_t n, int bits);
 // Full tree pipeline: codes -> sort -> gather -> leaf boxes -> Apetrei build.
@@ -196,6 +198,14 @@ nd_status md_create(Ctx* parent, const nd_md_params* p, int32_t n, const double*
                     const double* v, const double* q, const double* mass, bool host,
                     bool capture, MDEngine** out);
 nd_status md_destroy(MDEngine* m);
+nd_status md_create_batch(Ctx* parent, const nd_md_params* p, int32_t nsys, const nd_system* sys,
+                          const double* x, const double* v, const double* q, const double* mass,
+                          bool host, MDEngine** out);
+nd_status md_energies(MDEngine* m, double* pot, double* kin);
+nd_status md_step_times(MDEngine* m, int32_t steps, float* ms);
+nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsys,
+                      const nd_system* sys, const double* x, const double* v, const double* q,
+                      const double* mass, int32_t trial_steps, nd_md_params* best, double* sps);
 nd_status md_reset(MDEngine* m, const double* x, const double* v, const double* q,
                    const double* mass, bool host);
 bool md_compatible(MDEngine* m, const nd_md_params* p, int32_t n, bool has_q, bool has_m);
@@ -206,7 +216,7 @@ nd_status md_energy(MDEngine* m, double* pot, double* kin);
 nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list_pairs,
                    int32_t* capacity);
 int64_t md_launches_per_run(MDEngine* m, int64_t steps);
-nd_status md_diagnostics(MDEngine* m, int64_t* skin_violations, int32_t* max_neighbors);
+nd_status md_diagnostics(MDEngine* m, nd_md_diag* out);
 const char* md_last_error(MDEngine* m);
 nd_status forces_pairs(Ctx* c, const nd_md_params* p, int32_t n, const double* x,
                        const double* q, const int32_t* pi, const int32_t* pj, int64_t np,

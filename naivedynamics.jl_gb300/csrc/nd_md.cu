@@ -46,6 +46,22 @@ struct SetPtrs {
     double* q;
     double* im;
     int32_t* orig;
+    int32_t* sid;  // batched ensembles: system of each atom (nullptr for one system)
+};
+
+// Per-system constants of a batched ensemble.  Each system keeps its own
+// fixed-point frame (origin o, scale s) and is placed in its own slot of the
+// tree frame (Float32 positions = x + off), slots far enough apart that no
+// neighbour-list pair crosses systems.  Pair constants are in the system's
+// fixed-point units.
+struct SysRow {
+    double o[3];                 // fixed-point frame origin
+    double os[3];                // o * s
+    double off[3];               // tree-frame offset
+    double lo[3], hi[3];         // walls
+    double s;                    // fixed-point scale
+    int32_t lo_fp[3], hi_fp[3];  // walls in fixed point
+    float sig2u, eps24u, eps4, rc2u, kcu, kceu, hs2u, hsu;
 };
 
 // ------------------------------------------------------------- small kernels
@@ -60,21 +76,31 @@ __global__ void k_md_split_aos(const double* __restrict__ aos, int32_t n, double
 }
 
 __global__ void k_md_init_scalars(const double* __restrict__ q_in, const double* __restrict__ m_in,
-                                  int32_t n, double* q, double* im, int32_t* orig) {
+                                  const int32_t* __restrict__ sid_in, int32_t n, double* q,
+                                  double* im, int32_t* orig, int32_t* sid) {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     q[i] = q_in ? q_in[i] : 0.0;
     im[i] = m_in ? 1.0 / m_in[i] : 1.0;
     orig[i] = i;
+    if (sid) sid[i] = sid_in[i];
 }
 
 __global__ void k_md_pos32(const double* __restrict__ x0, const double* __restrict__ x1,
-                           const double* __restrict__ x2, int32_t n, float* __restrict__ xyz) {
+                           const double* __restrict__ x2, const int32_t* __restrict__ sid,
+                           const SysRow* __restrict__ sys, int32_t n, float* __restrict__ xyz,
+                           unsigned* counter) {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (counter && i == 0) atomicAdd(counter, 1u);
     if (i >= n) return;
-    xyz[3 * (int64_t)i] = (float)x0[i];
-    xyz[3 * (int64_t)i + 1] = (float)x1[i];
-    xyz[3 * (int64_t)i + 2] = (float)x2[i];
+    double o0 = 0.0, o1 = 0.0, o2 = 0.0;
+    if (sid) {
+        const SysRow* r = sys + sid[i];
+        o0 = r->off[0]; o1 = r->off[1]; o2 = r->off[2];
+    }
+    xyz[3 * (int64_t)i] = (float)(x0[i] + o0);
+    xyz[3 * (int64_t)i + 1] = (float)(x1[i] + o1);
+    xyz[3 * (int64_t)i + 2] = (float)(x2[i] + o2);
 }
 
 __device__ __forceinline__ int32_t to_fixed(double x, double o, double s, int32_t* err,
@@ -91,18 +117,24 @@ __device__ __forceinline__ int32_t to_fixed(double x, double o, double s, int32_
 // records and the Float32 positions of the tree.
 __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict__ perm,
                              const float* __restrict__ xyz32, int32_t n, Frame fr,
-                             float4* __restrict__ pos32, int4* __restrict__ rec,
-                             int4* __restrict__ recb, int32_t* err) {
+                             const SysRow* __restrict__ sys, float4* __restrict__ pos32,
+                             int4* __restrict__ rec, int4* __restrict__ recb, int32_t* err) {
     int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int32_t o = perm[k];
+    const SysRow* r = nullptr;
+    if (src.sid) {
+        const int32_t sv = src.sid[o];
+        dst.sid[k] = sv;
+        r = sys + sv;
+    }
     int32_t f[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double xv = src.x[d][o];
         dst.x[d][k] = xv;
         dst.w[d][k] = src.w[d][o];
-        f[d] = to_fixed(xv, fr.o[d], fr.s, err, k);
+        f[d] = to_fixed(xv, r ? r->o[d] : fr.o[d], r ? r->s : fr.s, err, k);
     }
     double qv = src.q[o];
     dst.q[k] = qv;
@@ -112,6 +144,37 @@ __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict
                            xyz32[3 * (int64_t)o + 2], __int_as_float(k));
     rec[k] = make_int4(f[0], f[1], f[2], __float_as_int((float)qv));
     recb[k] = rec[k];
+}
+
+// Copy a state set (after the gather into the scratch set, so the live set
+// keeps its addresses and captured graphs stay valid).
+__global__ void k_md_copy_set(SetPtrs src, SetPtrs dst, int32_t n) {
+    int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        dst.x[d][k] = src.x[d][k];
+        dst.w[d][k] = src.w[d][k];
+    }
+    dst.q[k] = src.q[k];
+    dst.im[k] = src.im[k];
+    dst.orig[k] = src.orig[k];
+    if (src.sid) dst.sid[k] = src.sid[k];
+}
+
+// Start of a rebuild window: re-sort on the schedule (every resort_every-th
+// window) or when some list has passed 90% of its capacity since the last
+// re-sort (the kept tree has loosened); refit otherwise.  ctl[3] counts
+// windows, ctl[4] holds the capacity-pressure flag, ctl[5] the decision.
+__global__ void k_md_window_begin(unsigned* ctl, int32_t resort_every,
+                                  cudaGraphConditionalHandle h, int32_t use_cond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const unsigned w = ctl[3];
+    const unsigned need = (w % (unsigned)resort_every == 0u || ctl[4] != 0u) ? 1u : 0u;
+    ctl[3] = w + 1u;
+    if (need) ctl[4] = 0u;
+    ctl[5] = need;
+    if (use_cond) cudaGraphSetConditional(h, need);
 }
 
 // Leaf boxes (p -/+ h) of already sorted Float32 positions.
@@ -152,33 +215,52 @@ __device__ __forceinline__ bool box_overlap(float qmnx, float qmny, float qmnz, 
 // Shared memory: two frontier buffers of fcap entries and the union (upow2).
 __global__ void __launch_bounds__(kBlock)
     k_md_block_union(const float4* __restrict__ keys, const float4* __restrict__ pos,
+                     const int32_t* __restrict__ sid,
                      int32_t n, int32_t nL, int32_t apl, float hq, int32_t fcap, int32_t ucap,
                      int32_t upow2, int32_t* __restrict__ ulist, int32_t* __restrict__ ucount,
                      uint16_t* __restrict__ llist_leaf, int32_t* __restrict__ lcount_leaf,
-                     int32_t lcap_leaf, int32_t* err, int32_t* diag, int32_t sizing) {
+                     int32_t lcap_leaf, int32_t* err, int32_t* diag, int32_t sizing,
+                     unsigned* pressure) {
     extern __shared__ int32_t smem[];
     int32_t* fr[2] = {smem, smem + fcap};
     int32_t* su = smem + 2 * fcap;
     __shared__ int32_t s_cnt[2];
-    __shared__ int32_t s_nu;
-    __shared__ float s_wb[kBlock / 32][6];  // per-warp query boxes (min xyz, max xyz)
+    __shared__ int32_t s_nu, s_nb;
+    // query boxes (min xyz, max xyz): one per warp, two for a warp whose atoms
+    // belong to two systems of a batched ensemble (lanes of lane 0's system,
+    // and the rest)
+    __shared__ float s_wb[2 * (kBlock / 32)][6];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t i = (int64_t)blockIdx.x * kBlock + tid;
-    float mn[3], mx[3];
-    {
-        float4 p = pos[i < n ? i : (int64_t)blockIdx.x * kBlock];
-        mn[0] = mx[0] = p.x; mn[1] = mx[1] = p.y; mn[2] = mx[2] = p.z;
-    }
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-        for (int s = 16; s > 0; s >>= 1) {
-            mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], s));
-            mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], s));
-        }
-    if (lane == 0)
-        for (int d = 0; d < 3; ++d) { s_wb[warp][d] = mn[d] - hq; s_wb[warp][3 + d] = mx[d] + hq; }
-    if (tid == 0) { s_cnt[0] = 1; s_cnt[1] = 0; s_nu = 0; fr[0][0] = (nL + 1) << 1; }
+    if (tid == 0) { s_cnt[0] = 1; s_cnt[1] = 0; s_nu = 0; s_nb = 0; fr[0][0] = (nL + 1) << 1; }
     __syncthreads();
+    {
+        const int64_t ii = i < n ? i : (int64_t)blockIdx.x * kBlock;
+        const float4 p = pos[ii];
+        bool mine = true;
+        if (sid) {
+            const int32_t sv = __ldg(&sid[ii]);
+            mine = sv == __shfl_sync(0xffffffffu, sv, 0);
+        }
+        const bool split = !__all_sync(0xffffffffu, mine);
+        for (int part = 0; part < (split ? 2 : 1); ++part) {
+            const bool in = (part == 0) == mine;
+            float mn[3] = {in ? p.x : INFINITY, in ? p.y : INFINITY, in ? p.z : INFINITY};
+            float mx[3] = {in ? p.x : -INFINITY, in ? p.y : -INFINITY, in ? p.z : -INFINITY};
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                for (int s = 16; s > 0; s >>= 1) {
+                    mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], s));
+                    mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], s));
+                }
+            if (lane == 0) {
+                const int b = atomicAdd(&s_nb, 1);
+                for (int d = 0; d < 3; ++d) { s_wb[b][d] = mn[d] - hq; s_wb[b][3 + d] = mx[d] + hq; }
+            }
+        }
+    }
+    __syncthreads();
+    const int nb = s_nb;
     int cur = 0;
     for (int level = 0; level < 256; ++level) {
         const int32_t nf = min(s_cnt[cur], fcap);
@@ -195,7 +277,7 @@ __global__ void __launch_bounds__(kBlock)
                 if (slot < fcap) fr[cur ^ 1][slot] = skip << 1;
             }
             bool hit = false;
-            for (int w = 0; w < kBlock / 32 && !hit; ++w)
+            for (int w = 0; w < nb && !hit; ++w)
                 hit = box_overlap(s_wb[w][0], s_wb[w][1], s_wb[w][2], s_wb[w][3], s_wb[w][4],
                                   s_wb[w][5], a, b);
             if (hit) {
@@ -219,6 +301,7 @@ __global__ void __launch_bounds__(kBlock)
     }
     const int32_t nu = s_nu;
     if (tid == 0) { atomicMax(&diag[0], nu); atomicAdd(&diag[3], nu); }
+    if (tid == 0 && pressure && 10 * (int64_t)nu > 9 * (int64_t)ucap) atomicOr(pressure, 1u);
     if (nu > ucap) {
         if (tid == 0 && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)blockIdx.x);
         if (tid == 0) ucount[blockIdx.x] = 0;
@@ -303,6 +386,7 @@ __global__ void __launch_bounds__(kBlock)
             if (own < nL) {
                 lcount_leaf[own] = min(mine, lcap_leaf);
                 atomicMax(&diag[2], mine);
+                if (pressure && 10 * mine > 9 * lcap_leaf) atomicOr(pressure, 1u);
                 if (mine > lcap_leaf && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)own);
             }
         }
@@ -323,7 +407,7 @@ __global__ void __launch_bounds__(kBlock)
                      const int32_t* __restrict__ ucount, const uint16_t* __restrict__ llist_leaf,
                      const int32_t* __restrict__ lcount_leaf, int32_t lcap_leaf, int32_t lcap,
                      uint16_t* __restrict__ llist, int32_t* __restrict__ ncount, int32_t* err,
-                     int32_t* diag, int32_t sizing) {
+                     int32_t* diag, int32_t sizing, unsigned* pressure) {
     extern __shared__ float4 spos[];
     const int tid = threadIdx.x;
     const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
@@ -368,27 +452,31 @@ __global__ void __launch_bounds__(kBlock)
     ncount[i] = min(cnt, lcap);
     if (cnt > lcap && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)i);
     atomicMax(&diag[1], cnt);
+    if (pressure && 10 * cnt > 9 * lcap) atomicOr(pressure, 1u);
 }
 
 // Refit: positions changed, order and tree topology kept.  Float32 positions
 // and pair records (and the build records of the skin check) from the FP64
 // state in its current order.
-__global__ void k_md_refit_pos(SetPtrs st, int32_t n, Frame fr, float4* __restrict__ pos32,
-                               int4* __restrict__ rec, int4* __restrict__ recb, int32_t* err) {
+__global__ void k_md_refit_pos(SetPtrs st, int32_t n, Frame fr, const SysRow* __restrict__ sys,
+                               float4* __restrict__ pos32, int4* __restrict__ rec,
+                               int4* __restrict__ recb, int32_t* err, unsigned* counter) {
     int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (counter && k == 0) atomicAdd(counter, 1u);
     if (k >= n) return;
+    const SysRow* r = st.sid ? sys + st.sid[k] : nullptr;
     int32_t f[3];
     float xf[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double xv = st.x[d][k];
-        xf[d] = (float)xv;
-        f[d] = to_fixed(xv, fr.o[d], fr.s, err, k);
+        xf[d] = (float)(r ? xv + r->off[d] : xv);
+        f[d] = to_fixed(xv, r ? r->o[d] : fr.o[d], r ? r->s : fr.s, err, k);
     }
     pos32[k] = make_float4(xf[0], xf[1], xf[2], __int_as_float(k));
-    int4 r = make_int4(f[0], f[1], f[2], __float_as_int((float)st.q[k]));
-    rec[k] = r;
-    recb[k] = r;
+    const int4 rv = make_int4(f[0], f[1], f[2], __float_as_int((float)st.q[k]));
+    rec[k] = rv;
+    recb[k] = rv;
 }
 
 // ------------------------------------------------------------- step kernel
@@ -425,6 +513,20 @@ struct StepArgs {
     double dt;
     double lo[3], hi[3];
     Frame fr;
+    const int32_t* __restrict__ sid;  // batched ensembles: system of each sorted atom
+    const SysRow* __restrict__ sys;   // and the per-system constants
+    int32_t nsys;
+    // early refit: ctl[0] request flag, ctl[1] finished-block tickets; inside a
+    // captured window the last block sets `cond` for the conditional refit node
+    float hsu;  // skin/2 in fixed-point units (early-refit trigger)
+    unsigned* ctl;
+    cudaGraphConditionalHandle cond;
+    int32_t use_cond;
+};
+
+// Pair constants of one system in fixed-point units.
+struct PairK {
+    float rc2u, sig2u, eps24u, eps4, kcu, kceu;
 };
 
 // Pair (i, j) from fixed-point records: the integer difference is exact, its
@@ -432,7 +534,7 @@ struct StepArgs {
 // box size inside the frame.  Constants are pre-scaled, so the force comes out
 // in physical units per fixed-point unit of displacement.
 template <bool COUL, bool ENERGY>
-__device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const StepArgs& a,
+__device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const PairK& a,
                                           float& fx, float& fy, float& fz, float& ue) {
     const float dx = (float)(ri.x - rj.x);
     const float dy = (float)(ri.y - rj.y);
@@ -468,7 +570,9 @@ __device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const
 // One block per 256 atoms.  MODE 0: step (force, pending half kick, kick,
 // drift, reflect, next record).  MODE 1: measure (force, integer-step velocity
 // and energies; state untouched).
-template <bool COUL, bool MASS, bool FIRST, int MODE>
+// BATCH: atoms of several systems; pair constants, walls and the fixed-point
+// origin come from the atom's system (a pair never crosses systems).
+template <bool COUL, bool MASS, bool FIRST, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
     extern __shared__ int4 srec[];
     const int tid = threadIdx.x;
@@ -486,9 +590,28 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         }
     }
     __syncthreads();
-    if (MODE == 0 && !valid) return;
-    if (!valid) i = a.n - 1;  // measure: idle lanes join the warp reduction with zeros
+    // idle lanes (last block) run with an empty list and store nothing; they
+    // join the warp reductions (measure) and the block vote (step)
+    if (!valid) i = a.n - 1;
     const int4 ri = __ldg(&a.rec_in[i]);
+    PairK pk{a.rc2u, a.sig2u, a.eps24u, a.eps4, a.kcu, a.kceu};
+    int32_t sv = 0;
+    const SysRow* __restrict__ row = nullptr;
+    double S = a.fr.s;
+    float hs2u = a.half_skin2u, hsu = a.hsu;
+    if constexpr (BATCH) {
+        sv = __ldg(&a.sid[i]);
+        row = a.sys + sv;
+        pk.sig2u = __ldg(&row->sig2u);
+        pk.eps24u = __ldg(&row->eps24u);
+        pk.eps4 = __ldg(&row->eps4);
+        pk.rc2u = __ldg(&row->rc2u);
+        pk.kcu = __ldg(&row->kcu);
+        pk.kceu = __ldg(&row->kceu);
+        S = __ldg(&row->s);
+        hs2u = __ldg(&row->hs2u);
+        hsu = __ldg(&row->hsu);
+    }
     const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
     auto fetch = [&](int32_t li) -> int4 {
@@ -514,9 +637,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
             for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)(s + 4 + k) * kBlock];
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], a, fx, fy, fz, ue);
+        for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue);
     }
-    for (; s < cnt; ++s) accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), a, fx, fy, fz, ue);
+    for (; s < cnt; ++s) accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), pk, fx, fy, fz, ue);
     if (valid) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
     const double imv = MASS ? a.im[i] : 1.0;
     const float fv[3] = {fx, fy, fz};
@@ -532,13 +655,22 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         double mass = MASS ? 1.0 / imv : 1.0;
         double pe = valid ? 0.5 * (double)ue : 0.0;
         ke = valid ? ke * 0.5 * mass : 0.0;
+        // per-system sums (one system unless batched); a warp spanning two
+        // systems adds lane by lane
+        if (BATCH && !__all_sync(0xffffffffu, sv == __shfl_sync(0xffffffffu, sv, 0))) {
+            if (valid) {
+                atomicAdd(&a.acc[2 * sv], pe);
+                atomicAdd(&a.acc[2 * sv + 1], ke);
+            }
+            return;
+        }
         for (int sh = 16; sh > 0; sh >>= 1) {
             pe += __shfl_xor_sync(0xffffffffu, pe, sh);
             ke += __shfl_xor_sync(0xffffffffu, ke, sh);
         }
         if ((tid & 31) == 0) {
-            atomicAdd(&a.acc[0], pe);
-            atomicAdd(&a.acc[1], ke);
+            atomicAdd(&a.acc[2 * sv], pe);
+            atomicAdd(&a.acc[2 * sv + 1], ke);
         }
         return;
     } else {
@@ -546,17 +678,24 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         // half kick in one add), x += dt v, walls, next record.
         const float kdt = FIRST ? a.hdt : 2.0f * a.hdt;
         int32_t xi[3];
+        bool trig = false;
+        if (valid) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             double v = a.w[d][i] + (double)(kdt * fv[d]) * imv;
             double x = fma(a.dt, v, a.x[d][i]);
-            int32_t q = __double2int_rn(fma(x, a.fr.s, -a.os[d]));
+            const double os = BATCH ? __ldg(&row->os[d]) : a.os[d];
+            int32_t q = __double2int_rn(fma(x, S, -os));
             // integer pre-check; the exact FP64 test of boundary_reflect! runs
             // only for atoms within a grid step of a wall
-            if (q <= a.lo_fp[d] + 1 || q >= a.hi_fp[d] - 1) {
-                if (a.lo[d] > x) { v = -v; x = a.lo[d]; }
-                if (a.hi[d] < x) { v = -v; x = a.hi[d]; }
-                q = __double2int_rn(fma(x, a.fr.s, -a.os[d]));
+            const int32_t lfp = BATCH ? __ldg(&row->lo_fp[d]) : a.lo_fp[d];
+            const int32_t hfp = BATCH ? __ldg(&row->hi_fp[d]) : a.hi_fp[d];
+            if (q <= lfp + 1 || q >= hfp - 1) {
+                const double lo = BATCH ? __ldg(&row->lo[d]) : a.lo[d];
+                const double hi = BATCH ? __ldg(&row->hi[d]) : a.hi[d];
+                if (lo > x) { v = -v; x = lo; }
+                if (hi < x) { v = -v; x = hi; }
+                q = __double2int_rn(fma(x, S, -os));
                 if (!(x == x)) set_error(a.err, ND_ERR_NONFINITE, (int32_t)i);
             }
             a.x[d][i] = x;
@@ -569,7 +708,29 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         const int4 rb = __ldg(&a.rec_build[i]);
         const float ex = (float)(xi[0] - rb.x), ey = (float)(xi[1] - rb.y),
                     ez = (float)(xi[2] - rb.z);
-        if (ex * ex + ey * ey + ez * ez > a.half_skin2u) atomicAdd(a.diag, 1ull);
+        const float e2 = ex * ex + ey * ey + ez * ez;
+        if (e2 > hs2u) atomicAdd(a.diag, 1ull);
+        // Ask for a refit before the next step when this atom could pass the
+        // bound in it: displacement so far + twice this step's move + 5% of
+        // the bound (the velocity may at most double in one step).
+        const float sx = (float)(xi[0] - ri.x), sy = (float)(xi[1] - ri.y),
+                    sz = (float)(xi[2] - ri.z);
+        trig = sqrtf(e2) + 2.0f * sqrtf(sx * sx + sy * sy + sz * sz) > 0.95f * hsu;
+        }
+        // Early refit request: the block votes, and the last block to finish
+        // (a ticket counter, no waiting) publishes the flag to the graph's
+        // conditional node that follows this step.
+        if (__syncthreads_or(trig) && tid == 0) atomicOr(&a.ctl[0], 1u);
+        if (a.use_cond && tid == 0) {
+            __threadfence();
+            const unsigned ticket = atomicAdd(&a.ctl[1], 1u);
+            if (ticket == gridDim.x - 1) {
+                __threadfence();
+                const unsigned f = atomicExch(&a.ctl[0], 0u);
+                atomicExch(&a.ctl[1], 0u);
+                cudaGraphSetConditional(a.cond, f ? 1u : 0u);
+            }
+        }
     }
 }
 
@@ -651,11 +812,26 @@ struct MDEngine {
     int64_t steps = 0, rebuilds = 0;
     Frame fr{};
     DevBuf set_buf[2], rec_buf[2], recb, xyz32, pos32, keys, store, ulist, ucount, llist_leaf,
-        lcount_leaf, llist, ncount, f, vtmp, acc, aos, diag;
+        lcount_leaf, llist, ncount, f, vtmp, acc, aos, diag, sysrow, sid_in;
+    // batched ensemble (nsys > 0): per-system rows and the Hilbert grid whose
+    // level-log2(G) cells are the systems' slots
+    int32_t nsys = 0;
+    float tree_frame[6] = {0, 0, 0, 0, 0, 0};
+    // early refits: ctl = {request flag, block tickets, early refits done};
+    // the first window after an upload is captured too (graph_first), and the
+    // conditional refit bodies are captured on cap_stream
+    DevBuf ctl;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t graph_first = nullptr;
+    int64_t graph_first_launches = 0, refit_kernels = 0;
     SetPtrs set[2];
-    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [refit][set]
-    int32_t resort_every = 5;  // re-sort (new order + topology) every k-th rebuild, refit between
-    int64_t graph_launches[2] = {0, 0};  // kernels per captured window [refit]
+    // one captured window: a device-decided rebuild (re-sort or refit) and R
+    // steps with conditional early refits; the live state is always set 0
+    cudaGraphExec_t graph_main = nullptr;
+    int32_t resort_every = 1;  // re-sort (new order + topology) every k-th window, refit between
+    int64_t graph_main_launches = 0;  // kernel nodes of the window graph outside conditional bodies
+    int64_t resort_kernels = 0;       // kernels of one re-sort rebuild
+    int64_t eager_bodies = 0;         // kernels of rebuild bodies run eagerly (counted by the host)
     size_t step_smem = 0, union_smem = 0, lists_smem = 0;
 };
 
@@ -664,13 +840,14 @@ static nd_status md_alloc(MDEngine* m) {
     const size_t n = (size_t)m->n;
     nd_status st;
     for (int s = 0; s < 2; ++s) {
-        // x[3], w[3], q, im (8 doubles) + orig (int32)
-        if ((st = ensure(c, m->set_buf[s], n * (8 * sizeof(double) + sizeof(int32_t)) + 256))) return st;
+        // x[3], w[3], q, im (8 doubles) + orig (int32) [+ sid (int32)]
+        if ((st = ensure(c, m->set_buf[s], n * (8 * sizeof(double) + 2 * sizeof(int32_t)) + 256))) return st;
         double* b = (double*)m->set_buf[s].p;
         for (int d = 0; d < 3; ++d) { m->set[s].x[d] = b + d * n; m->set[s].w[d] = b + (3 + d) * n; }
         m->set[s].q = b + 6 * n;
         m->set[s].im = b + 7 * n;
         m->set[s].orig = (int32_t*)(b + 8 * n);
+        m->set[s].sid = m->nsys > 0 ? m->set[s].orig + n : nullptr;
         if ((st = ensure(c, m->rec_buf[s], n * sizeof(int4)))) return st;
     }
     if ((st = ensure(c, m->recb, n * sizeof(int4)))) return st;
@@ -683,9 +860,11 @@ static nd_status md_alloc(MDEngine* m) {
     if ((st = ensure(c, m->ncount, sizeof(int32_t) * n))) return st;
     if ((st = ensure(c, m->f, sizeof(float4) * n))) return st;
     if ((st = ensure(c, m->vtmp, 3 * sizeof(double) * n))) return st;
-    if ((st = ensure(c, m->acc, 64))) return st;
+    if ((st = ensure(c, m->acc, std::max<size_t>(64, 2 * sizeof(double) * (size_t)m->nsys)))) return st;
     if ((st = ensure(c, m->diag, 64))) return st;
     if (cudaMemsetAsync(m->diag.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
+    if ((st = ensure(c, m->ctl, 64))) return st;
+    if (cudaMemsetAsync(m->ctl.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
     // rebuild pipeline scratch: codes + perm + sort ping-pong + histograms
     if ((st = ensure(c, c->codes, sizeof(int32_t) * n))) return st;
     if ((st = ensure(c, c->perm, sizeof(int32_t) * n))) return st;
@@ -718,6 +897,10 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     int32_t p2 = 1;
     while (p2 < ucap) p2 <<= 1;
     m->upow2 = p2;
+    int maxsm = 0;
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    // staged records must fit the block's shared memory
+    m->ucap_sm = std::max(0, std::min(m->ucap_sm, (maxsm - 1024) / (16 * m->apl)));
     if ((st = ensure(c, m->ulist, sizeof(int32_t) * (size_t)ucap * m->nblocks))) return st;
     if (lcap > 0 &&
         (st = ensure(c, m->llist, sizeof(uint16_t) * (size_t)lcap * kBlock * m->nblocks)))
@@ -728,8 +911,6 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     m->union_smem = sizeof(int32_t) * (2 * (size_t)fcap + p2);
     m->step_smem = sizeof(int4) * (size_t)m->ucap_sm * m->apl;
     m->lists_smem = sizeof(float4) * (size_t)m->ucap_sm * m->apl;
-    int maxsm = 0;
-    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
     if ((int)m->union_smem + 1024 > maxsm || (lcap > 0 && (int)m->step_smem + 1024 > maxsm)) {
         c->last_error = "neighbour union too large for shared memory";
         return ND_ERR_OVERFLOW;
@@ -745,8 +926,9 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<8>, maxsm);
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<16>, maxsm);
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<32>, maxsm);
-#define ND_SMEM(C, M, F, MODE) \
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE>, maxsm);
+#define ND_SMEM(C, M, F, MODE)                                                                \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false>, maxsm); \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, true>, maxsm);
     ND_SMEM(true, true, true, 0) ND_SMEM(true, true, false, 0) ND_SMEM(true, false, true, 0)
     ND_SMEM(true, false, false, 0) ND_SMEM(false, true, true, 0)
     ND_SMEM(false, true, false, 0) ND_SMEM(false, false, true, 0)
@@ -788,8 +970,20 @@ static StepArgs md_step_args(MDEngine* m, int rec_in) {
     a.diag = (unsigned long long*)m->diag.p;
     a.err = m->sub.d_err;
     const double S = m->fr.s;
-    const float hs = (float)(0.5 * p.skin * S);
+    // The lists are built from Float32 positions; a distance rounded there
+    // errs by a few ulps of the largest coordinate, which the bound on the
+    // displacement gives back.
+    double cmax = 0.0;
+    if (m->nsys > 0) cmax = m->tree_frame[3];
+    else
+        for (int d = 0; d < 3; ++d) cmax = std::max({cmax, std::fabs(p.box_lo[d]), std::fabs(p.box_hi[d])});
+    const double ulp = std::ldexp(1.0, std::ilogb(std::max(cmax, 1.0)) - 23);
+    const float hs = (float)(std::max(0.0, 0.5 * p.skin - 4.0 * ulp) * S);
     a.half_skin2u = hs * hs;
+    a.hsu = hs;
+    a.ctl = (unsigned*)m->ctl.p;
+    a.cond = 0;
+    a.use_cond = 0;
     for (int d = 0; d < 3; ++d) {
         a.os[d] = m->fr.o[d] * S;
         a.lo_fp[d] = (int32_t)std::floor((p.box_lo[d] - m->fr.o[d]) * S);
@@ -804,6 +998,9 @@ static StepArgs md_step_args(MDEngine* m, int rec_in) {
     a.hdt = (float)(0.5 * p.dt);
     a.dt = p.dt;
     a.fr = m->fr;
+    a.sid = m->set[m->cur].sid;
+    a.sys = (const SysRow*)m->sysrow.p;
+    a.nsys = m->nsys;
     return a;
 }
 
@@ -814,7 +1011,20 @@ static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
     const size_t sm = m->step_smem;
     const bool coul = m->has_q && m->p.coulomb_k != 0.0;
     const bool mass = m->has_m;
-#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE><<<grid, kBlock, sm, c->stream>>>(a)
+    if (m->nsys > 0) {
+#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE, true><<<grid, kBlock, sm, c->stream>>>(a)
+        if (coul) {
+            if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
+            else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
+        } else {
+            if (mass) { if (first) ND_STEP(false, true, true); else ND_STEP(false, true, false); }
+            else { if (first) ND_STEP(false, false, true); else ND_STEP(false, false, false); }
+        }
+#undef ND_STEP
+        c->launches++;
+        return;
+    }
+#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE, false><<<grid, kBlock, sm, c->stream>>>(a)
     if (coul) {
         if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
         else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
@@ -826,34 +1036,59 @@ static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
     c->launches++;
 }
 
-// Rebuild: Float32 positions -> codes -> sort -> reorder state -> leaf boxes ->
-// build -> block unions -> per-atom lists; switches the current state set.
-// A refit keeps the order and the sorted codes (so the build reproduces the
-// topology) and only refreshes positions, boxes, unions and lists.
-static nd_status md_rebuild(MDEngine* m, bool sizing = false, bool refit = false) {
+enum { RB_RESORT = 0, RB_REFIT = 1 };
+
+// ctl words: [0] early-refit request, [1] finished-block tickets, [2] early
+// refits done, [3] window counter, [4] capacity pressure, [5] rebuild
+// decision, [6] re-sorts done, [7] scheduled refits done.
+static unsigned* ctl_word(MDEngine* m, int k) { return (unsigned*)m->ctl.p + k; }
+
+// Rebuild of the neighbour lists.
+//   RB_RESORT: Float32 positions -> codes -> sort -> gather the state into the
+//   scratch set and copy it back (the live set keeps its addresses) -> leaf
+//   boxes -> build -> block unions -> per-atom lists.
+//   RB_REFIT: keeps the order and the sorted codes (so the build reproduces
+//   the topology) and refreshes positions, boxes, unions and lists.
+// rec >= 0: a refit inside a window (early refit) whose records go to record
+// buffer `rec`, the one the next step reads; otherwise records go to buffer 0
+// and the step parity restarts.  counter: device count of this kind of
+// rebuild (nullptr: not counted).  sizing: capacity-sizing pass.
+static nd_status md_rebuild(MDEngine* m, int kind, int rec = -1, unsigned* counter = nullptr,
+                            bool sizing = false) {
     Ctx* c = &m->sub;
     const int32_t n = m->n;
     const unsigned g = (unsigned)cdiv(n, 256);
     int32_t* codes = (int32_t*)c->codes.p;
     int32_t* perm = (int32_t*)c->perm.p;
     nd_status st;
-    if (refit) {
-        k_md_refit_pos<<<g, 256, 0, c->stream>>>(m->set[m->cur], n, m->fr, (float4*)m->pos32.p,
-                                                  (int4*)m->rec_buf[0].p, (int4*)m->recb.p,
-                                                  c->d_err);
+    const SysRow* sys = (const SysRow*)m->sysrow.p;
+    SetPtrs& live = m->set[0];
+    // a new list answers any pending early-refit request
+    if (cudaMemsetAsync(m->ctl.p, 0, 2 * sizeof(unsigned), c->stream) != cudaSuccess)
+        return cuda_fail(c, cudaGetLastError(), "md rebuild");
+    if (kind == RB_REFIT) {
+        k_md_refit_pos<<<g, 256, 0, c->stream>>>(
+            live, n, m->fr, sys, (float4*)m->pos32.p, (int4*)m->rec_buf[rec >= 0 ? rec : 0].p,
+            (int4*)m->recb.p, c->d_err, counter);
         c->launches++;
     } else {
-        SetPtrs& s = m->set[m->cur];
-        SetPtrs& t = m->set[m->cur ^ 1];
-        k_md_pos32<<<g, 256, 0, c->stream>>>(s.x[0], s.x[1], s.x[2], n, (float*)m->xyz32.p);
+        SetPtrs& tmp = m->set[1];
+        k_md_pos32<<<g, 256, 0, c->stream>>>(live.x[0], live.x[1], live.x[2], live.sid, sys, n,
+                                             (float*)m->xyz32.p, counter);
         c->launches++;
-        if ((st = morton_codes(c, (const float*)m->xyz32.p, n, m->p.order, codes, perm))) return st;
+        // a batched ensemble sorts on the fixed slot grid, so every system is
+        // one contiguous run of the Hilbert order
+        if ((st = morton_codes(c, (const float*)m->xyz32.p, n, m->p.order, codes, perm,
+                               m->nsys > 0 ? m->tree_frame : nullptr)))
+            return st;
         if ((st = radix_sort_pairs(c, (uint32_t*)codes, perm, n, 30))) return st;
-        k_md_reorder<<<g, 256, 0, c->stream>>>(s, t, perm, (const float*)m->xyz32.p, n, m->fr,
-                                               (float4*)m->pos32.p, (int4*)m->rec_buf[0].p,
-                                               (int4*)m->recb.p, c->d_err);
-        c->launches++;
+        k_md_reorder<<<g, 256, 0, c->stream>>>(live, tmp, perm, (const float*)m->xyz32.p, n,
+                                               m->fr, sys, (float4*)m->pos32.p,
+                                               (int4*)m->rec_buf[0].p, (int4*)m->recb.p, c->d_err);
+        k_md_copy_set<<<g, 256, 0, c->stream>>>(tmp, live, n);
+        c->launches += 2;
     }
+    unsigned* pressure = sizing ? nullptr : ctl_word(m, 4);
     float4* keys = (float4*)m->keys.p;
     const float rl = (float)(m->p.cutoff + m->p.skin);
     k_md_leaf_boxes<<<(unsigned)cdiv(m->nL, 128), 128, 0, c->stream>>>(
@@ -864,17 +1099,17 @@ static nd_status md_rebuild(MDEngine* m, bool sizing = false, bool refit = false
     // the distance test alone decides membership
     const float hq = (rl / 2.0f) * 1.0001f + 1e-6f;
     k_md_block_union<<<(unsigned)m->nblocks, kBlock, m->union_smem, c->stream>>>(
-        keys, (const float4*)m->pos32.p, n, m->nL, m->apl, hq, m->fcap, m->ucap, m->upow2,
-        (int32_t*)m->ulist.p, (int32_t*)m->ucount.p, (uint16_t*)m->llist_leaf.p,
+        keys, (const float4*)m->pos32.p, live.sid, n, m->nL, m->apl, hq, m->fcap, m->ucap,
+        m->upow2, (int32_t*)m->ulist.p, (int32_t*)m->ucount.p, (uint16_t*)m->llist_leaf.p,
         (int32_t*)m->lcount_leaf.p, m->lcap_leaf, c->d_err, (int32_t*)m->diag.p + 2,
-        sizing ? 1 : 0);
+        sizing ? 1 : 0, pressure);
 #define ND_LISTS(A)                                                                             \
     k_md_block_lists<A><<<(unsigned)m->nblocks, kBlock, m->lists_smem, c->stream>>>(            \
         (const float4*)m->pos32.p, n, rl * rl, m->ucap, m->ucap_sm * m->apl,                    \
         (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p,                                \
         (const uint16_t*)m->llist_leaf.p, (const int32_t*)m->lcount_leaf.p, m->lcap_leaf,       \
         m->lcap, (uint16_t*)m->llist.p, (int32_t*)m->ncount.p, c->d_err,                        \
-        (int32_t*)m->diag.p + 2, sizing ? 1 : 0)
+        (int32_t*)m->diag.p + 2, sizing ? 1 : 0, pressure)
     switch (m->apl) {
         case 1: ND_LISTS(1); break;
         case 2: ND_LISTS(2); break;
@@ -885,45 +1120,201 @@ static nd_status md_rebuild(MDEngine* m, bool sizing = false, bool refit = false
     }
 #undef ND_LISTS
     c->launches += 2;
-    if (!refit) m->cur ^= 1;
-    m->rc = 0;
+    if (rec < 0) m->rc = 0;
     return check_launch(c, "md rebuild");
 }
 
-// Enqueue `k` steps inside the current window (no rebuild).
-static void md_steps(MDEngine* m, int32_t k) {
-    for (int32_t s = 0; s < k; ++s) {
-        StepArgs a = md_step_args(m, m->rc);
-        launch_step<0>(m, a, m->first);
-        m->first = false;
-        m->rc ^= 1;
+// Conditional node after the work captured so far on c->stream.  nbody = 1:
+// IF (body 0 runs when the condition is non-zero); nbody = 2: IF/ELSE (body 1
+// runs when it is zero).  Each body is captured on cap_stream by body(k) and
+// its kernels are counted apart (they run only when chosen).
+template <class F>
+static nd_status md_add_cond_node(MDEngine* m, cudaGraphConditionalHandle h, int nbody,
+                                  F&& body) {
+    Ctx* c = &m->sub;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return cuda_fail(c, e, "capture info");
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = (unsigned)nbody;
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+    if (e != cudaSuccess) return cuda_fail(c, e, "conditional node");
+    nd_status st = ND_OK;
+    cudaStream_t main = c->stream;
+    for (int k = 0; k < nbody && st == ND_OK; ++k) {
+        c->stream = m->cap_stream;
+        e = cudaStreamBeginCaptureToGraph(m->cap_stream, np.conditional.phGraph_out[k], nullptr,
+                                          nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { st = cuda_fail(c, e, "body capture"); break; }
+        const int64_t l0 = c->launches;
+        st = body(k);
+        const int64_t nk = c->launches - l0;
+        c->launches = l0;
+        cudaGraph_t out = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(m->cap_stream, &out);
+        if (e2 != cudaSuccess && st == ND_OK) st = cuda_fail(c, e2, "body capture");
+        if (st == ND_OK && nbody == 2) (k == 0 ? m->resort_kernels : m->refit_kernels) = nk;
+        if (st == ND_OK && nbody == 1) m->refit_kernels = nk;
     }
+    c->stream = main;
+    if (st) return st;
+    e = cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return cuda_fail(c, e, "capture dependencies");
+    return ND_OK;
 }
 
-static nd_status md_capture_window(MDEngine* m, int which, int refit) {
-    // Captures (re-sort or refit) rebuild + R steps starting from state set `which`.
+// A conditional handle of the graph being captured on the engine stream; its
+// value resets to 0 at every launch and the kernel before its node sets it.
+static nd_status md_cond_handle(MDEngine* m, cudaGraphConditionalHandle* h) {
     Ctx* c = &m->sub;
-    int save_cur = m->cur, save_rc = m->rc;
-    bool save_first = m->first;
-    int64_t save_launch = c->launches;
-    m->cur = which;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(h, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return cuda_fail(c, e, "conditional handle");
+    return ND_OK;
+}
+
+// Rebuild at the start of a window, re-sort or refit as k_md_window_begin
+// decides on the device: inside a capture an IF/ELSE node, otherwise after
+// reading the decision back.
+static nd_status md_window_begin(MDEngine* m, bool capture) {
+    Ctx* c = &m->sub;
+    nd_status st;
+    cudaGraphConditionalHandle h = 0;
+    if (capture && (st = md_cond_handle(m, &h))) return st;
+    k_md_window_begin<<<1, 32, 0, c->stream>>>((unsigned*)m->ctl.p, m->resort_every, h,
+                                               capture ? 1 : 0);
+    c->launches++;
+    if (capture) {
+        return md_add_cond_node(m, h, 2, [&](int k) {
+            return k == 0 ? md_rebuild(m, RB_RESORT, -1, ctl_word(m, 6))
+                          : md_rebuild(m, RB_REFIT, -1, ctl_word(m, 7));
+        });
+    }
+    unsigned need = 0;
+    cudaError_t e = cudaMemcpyAsync(&need, ctl_word(m, 5), sizeof(need), cudaMemcpyDeviceToHost,
+                                    c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "rebuild decision");
+    const int64_t l0 = c->launches;
+    st = need ? md_rebuild(m, RB_RESORT, -1, ctl_word(m, 6))
+              : md_rebuild(m, RB_REFIT, -1, ctl_word(m, 7));
+    m->eager_bodies += c->launches - l0;
+    return st;
+}
+
+// Enqueue `k` steps of the current window, the first at window position pos0.
+// After every step but the window's last, a refit runs if some atom could pass
+// skin/2 from its list-build position in the next step: inside a capture as a
+// conditional node (one handle per node, set by the step before it),
+// otherwise eagerly after reading the request flag.  ev (eager only): a pair
+// of events per step recorded around the step kernel.
+static nd_status md_steps(MDEngine* m, int32_t k, int32_t pos0, bool capture = false,
+                          cudaEvent_t* ev = nullptr) {
+    Ctx* c = &m->sub;
+    const int32_t R = m->p.rebuild_every;
+    nd_status st;
+    for (int32_t s = 0; s < k; ++s) {
+        const bool tail = (pos0 + s) % R == R - 1;
+        cudaGraphConditionalHandle h = 0;
+        if (capture && !tail && (st = md_cond_handle(m, &h))) return st;
+        StepArgs a = md_step_args(m, m->rc);
+        a.use_cond = capture && !tail ? 1 : 0;
+        a.cond = h;
+        if (ev) cudaEventRecord(ev[2 * s], c->stream);
+        launch_step<0>(m, a, m->first);
+        if (ev) cudaEventRecord(ev[2 * s + 1], c->stream);
+        m->first = false;
+        m->rc ^= 1;
+        if (tail) continue;
+        if (capture) {
+            if ((st = md_add_cond_node(m, h, 1, [&](int) {
+                     return md_rebuild(m, RB_REFIT, m->rc, ctl_word(m, 2));
+                 })))
+                return st;
+        } else {
+            unsigned flag = 0;
+            cudaError_t e = cudaMemcpyAsync(&flag, m->ctl.p, sizeof(flag), cudaMemcpyDeviceToHost,
+                                            c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "refit request");
+            if (flag) {
+                const int64_t l0 = c->launches;
+                if ((st = md_rebuild(m, RB_REFIT, m->rc, ctl_word(m, 2)))) return st;
+                m->eager_bodies += c->launches - l0;
+            }
+        }
+    }
+    return ND_OK;
+}
+
+// The opening window after an upload (no rebuild: the upload built the list;
+// its first step completes only a half kick).
+static nd_status md_capture_first(MDEngine* m) {
+    Ctx* c = &m->sub;
+    const int save_rc = m->rc;
+    const bool save_first = m->first;
+    const int64_t save_launch = c->launches;
+    m->first = true;
+    m->rc = 0;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
+    nd_status st = md_steps(m, m->p.rebuild_every, 0, true);
+    e = cudaStreamEndCapture(c->stream, &g);
+    if (st) { if (g) cudaGraphDestroy(g); return st; }
+    if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
+    e = cudaGraphInstantiate(&m->graph_first, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+    m->graph_first_launches = c->launches - save_launch;
+    c->launches = save_launch;
+    m->rc = save_rc;
+    m->first = save_first;
+    return ND_OK;
+}
+
+// Every later window: device-decided rebuild + R steps.
+static nd_status md_capture_main(MDEngine* m) {
+    Ctx* c = &m->sub;
+    const int save_rc = m->rc;
+    const bool save_first = m->first;
+    const int64_t save_launch = c->launches;
     m->first = false;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
-    nd_status st = md_rebuild(m, false, refit != 0);
-    if (st == ND_OK) md_steps(m, m->p.rebuild_every);
+    nd_status st = md_window_begin(m, true);
+    if (st == ND_OK) st = md_steps(m, m->p.rebuild_every, 0, true);
     e = cudaStreamEndCapture(c->stream, &g);
     if (st) { if (g) cudaGraphDestroy(g); return st; }
     if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
-    e = cudaGraphInstantiate(&m->graph[refit][which], g, 0);
+    e = cudaGraphInstantiate(&m->graph_main, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
-    m->graph_launches[refit] = c->launches - save_launch;
+    m->graph_main_launches = c->launches - save_launch;
     c->launches = save_launch;
-    m->cur = save_cur;
     m->rc = save_rc;
     m->first = save_first;
+    return ND_OK;
+}
+
+// Window counter after an opening build: that build was window 0.
+static nd_status md_opened(MDEngine* m) {
+    const unsigned one = 1u;
+    cudaError_t e = cudaMemcpyAsync(ctl_word(m, 3), &one, sizeof(one), cudaMemcpyHostToDevice,
+                                    m->sub.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->sub.stream);
+    if (e != cudaSuccess) return cuda_fail(&m->sub, e, "window counter");
     return ND_OK;
 }
 
@@ -933,7 +1324,7 @@ static nd_status md_capture_window(MDEngine* m, int which, int refit) {
 static nd_status md_sizing_pass(MDEngine* m, int32_t h[5]) {
     Ctx* c = &m->sub;
     cudaMemsetAsync((int32_t*)m->diag.p + 2, 0, 5 * sizeof(int32_t), c->stream);
-    nd_status st = md_rebuild(m, true);
+    nd_status st = md_rebuild(m, RB_RESORT, -1, nullptr, true);
     if (st) return st;
     cudaError_t e = cudaMemcpyAsync(h, (int32_t*)m->diag.p + 2, 5 * sizeof(int32_t),
                                     cudaMemcpyDeviceToHost, c->stream);
@@ -965,13 +1356,14 @@ static nd_status md_size_lists(MDEngine* m) {
     const int32_t lcap_leaf = std::min(ucap, round_up(max_c * 1.3 + 16, 8));
     // Shared-memory staging sized near the mean union (head-room for drift);
     // a block whose union is larger reads its remaining records from L2.
-    const int32_t ucap_sm = round_up(mean_u * 1.2 + 16, 16);
+    const int32_t ucap_sm = m->p.stage_policy == 1 ? ucap : round_up(mean_u * 1.2 + 16, 16);
     if ((st = md_alloc_lists(m, fcap, ucap, lcap_leaf, 0, ucap_sm))) return st;
     if ((st = md_sizing_pass(m, h))) return st;
     const int32_t max_n = h[1];
     int32_t lcap = m->p.max_neighbors > 0 ? m->p.max_neighbors : round_up(max_n * 1.35 + 16, 8);
     if ((st = md_alloc_lists(m, fcap, ucap, lcap_leaf, lcap, ucap_sm))) return st;
-    if ((st = md_rebuild(m))) return st;
+    if ((st = md_rebuild(m, RB_RESORT))) return st;
+    if ((st = md_opened(m))) return st;
     m->in_window = 0;
     m->rebuild_due = false;
     m->rebuilds = 1;
@@ -1003,10 +1395,12 @@ static nd_status md_upload(MDEngine* m, const double* xd, const double* vd, cons
     SetPtrs& s = m->set[0];
     k_md_split_aos<<<g, 256, 0, c->stream>>>(ax, n, s.x[0], s.x[1], s.x[2]);
     k_md_split_aos<<<g, 256, 0, c->stream>>>(av, n, s.w[0], s.w[1], s.w[2]);
-    k_md_init_scalars<<<g, 256, 0, c->stream>>>(qd ? aq : nullptr, md_ ? am : nullptr, n, s.q, s.im,
-                                                s.orig);
+    k_md_init_scalars<<<g, 256, 0, c->stream>>>(qd ? aq : nullptr, md_ ? am : nullptr,
+                                                (const int32_t*)m->sid_in.p, n, s.q, s.im,
+                                                s.orig, s.sid);
     c->launches += 3;
     if (cudaMemsetAsync(m->diag.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
+    if (cudaMemsetAsync(m->ctl.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
     m->cur = 0;
     m->first = true;
     m->steps = 0;
@@ -1024,7 +1418,8 @@ nd_status md_reset(MDEngine* m, const double* x, const double* v, const double* 
     if ((q != nullptr) != m->has_q || (mass != nullptr) != m->has_m) return ND_ERR_ARG;
     nd_status st = md_upload(m, x, v, q, mass, host);
     if (st) return st;
-    if ((st = md_rebuild(m))) return st;
+    if ((st = md_rebuild(m, RB_RESORT))) return st;
+    if ((st = md_opened(m))) return st;
     m->rebuilds = 1;
     return sync_and_check(&m->sub, "md reset");
 }
@@ -1048,15 +1443,101 @@ static nd_status md_frame(MDEngine* m) {
     return ND_OK;
 }
 
+// Batched ensemble frames.  Slots: a G x G x G grid (G a power of two, G^3 >=
+// nsys) of cubes of side (largest system extent + 2 r_list + 1), system s in
+// slot (s mod G, s/G mod G, s/G^2) with half the gap on every side.  The
+// Hilbert grid spans the slot grid exactly, so each slot is one aligned
+// sub-cube of the curve and each system one contiguous run of the order.
+// Fixed point: per-system origin (walls less 1/16 of the extent), one scale.
+static nd_status md_frame_batch(MDEngine* m, const nd_system* sys) {
+    const int32_t ns = m->nsys;
+    double side_max = 0.0;
+    for (int32_t k = 0; k < ns; ++k)
+        for (int d = 0; d < 3; ++d) {
+            const double e = sys[k].box_hi[d] - sys[k].box_lo[d];
+            if (!(e > 0.0) || !std::isfinite(e)) return ND_ERR_ARG;
+            side_max = std::max(side_max, e);
+        }
+    const double rl = m->p.cutoff + m->p.skin;
+    const double gap = 2.0 * rl + 1.0;
+    const double slot = side_max + gap;
+    int32_t G = 1;
+    while ((int64_t)G * G * G < ns) G *= 2;
+    if (G > 1024) return ND_ERR_ARG;
+    for (int d = 0; d < 3; ++d) { m->tree_frame[d] = 0.0f; m->tree_frame[3 + d] = (float)(G * slot); }
+    m->fr.s = 1.0;  // unused: every system has its own scale
+    for (int d = 0; d < 3; ++d) m->fr.o[d] = 0.0;
+    // the lists come from Float32 tree-frame positions: give back a few ulps
+    // of the largest coordinate from the displacement bound
+    const double ulp = std::ldexp(1.0, std::ilogb(std::max((double)m->tree_frame[3], 1.0)) - 23);
+    const double hs_phys = std::max(0.0, 0.5 * m->p.skin - 4.0 * ulp);
+    std::vector<SysRow> rows(ns);
+    for (int32_t k = 0; k < ns; ++k) {
+        const nd_system& y = sys[k];
+        if (!std::isfinite(y.sigma) || !std::isfinite(y.epsilon) || !(y.sigma > 0)) return ND_ERR_ARG;
+        SysRow& r = rows[k];
+        const int32_t cell[3] = {k % G, (k / G) % G, k / (G * G)};
+        double ext = 0.0;
+        for (int d = 0; d < 3; ++d) ext = std::max(ext, y.box_hi[d] - y.box_lo[d]);
+        const double S = std::ldexp(1.0, (int)std::floor(std::log2(2147480000.0 / (ext * 1.125))));
+        r.s = S;
+        for (int d = 0; d < 3; ++d) {
+            r.o[d] = y.box_lo[d] - ext / 16.0;
+            r.os[d] = r.o[d] * S;
+            r.off[d] = cell[d] * slot + 0.5 * gap - y.box_lo[d];
+            r.lo[d] = y.box_lo[d];
+            r.hi[d] = y.box_hi[d];
+            r.lo_fp[d] = (int32_t)std::floor((y.box_lo[d] - r.o[d]) * S);
+            r.hi_fp[d] = (int32_t)std::ceil((y.box_hi[d] - r.o[d]) * S);
+        }
+        r.sig2u = (float)(y.sigma * y.sigma * S * S);
+        r.eps24u = (float)(24.0 * y.epsilon * S);
+        r.eps4 = (float)(4.0 * y.epsilon);
+        r.rc2u = (float)(m->p.cutoff * m->p.cutoff * S * S);
+        r.kcu = (float)(m->p.coulomb_k * S * S);
+        r.kceu = (float)(m->p.coulomb_k * S);
+        r.hsu = (float)(hs_phys * S);
+        r.hs2u = r.hsu * r.hsu;
+    }
+    Ctx* c = &m->sub;
+    nd_status st = ensure(c, m->sysrow, sizeof(SysRow) * (size_t)ns);
+    if (st) return st;
+    std::vector<int32_t> sid(m->n);
+    int64_t at = 0;
+    for (int32_t k = 0; k < ns; ++k)
+        for (int32_t j = 0; j < sys[k].n_atoms; ++j) sid[at++] = k;
+    if ((st = ensure(c, m->sid_in, sizeof(int32_t) * (size_t)m->n))) return st;
+    cudaError_t e = cudaMemcpy(m->sysrow.p, rows.data(), sizeof(SysRow) * (size_t)ns,
+                               cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(m->sid_in.p, sid.data(), sizeof(int32_t) * (size_t)m->n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "batch tables");
+    return ND_OK;
+}
+
 static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
                                   const double* xd, const double* vd, const double* qd,
-                                  const double* md_, bool host, bool capture, MDEngine** out) {
+                                  const double* md_, bool host, bool capture, MDEngine** out,
+                                  int32_t nsys = 0, const nd_system* sys = nullptr) {
     if (!parent || !p || !out || !xd || !vd || n <= 0) return ND_ERR_ARG;
     if (p->atomsperleaf <= 0 || n % p->atomsperleaf || n / p->atomsperleaf < 2) return ND_ERR_SPEC;
     if (32 % p->atomsperleaf != 0) return ND_ERR_SPEC;  // a warp holds whole leaves
-    if (p->rebuild_every <= 0 || !(p->cutoff > 0) || !(p->skin >= 0) || !(p->dt > 0))
+    if (p->rebuild_every <= 0 || !(p->cutoff > 0) || !(p->skin >= 0) || !(p->dt > 0) ||
+        p->resort_every < 0 || p->stage_policy < 0 || p->stage_policy > 1)
         return ND_ERR_ARG;
+    if (nsys < 0 || (nsys > 0 && !sys)) return ND_ERR_ARG;
+    if (nsys > 0) {
+        int64_t tot = 0;
+        for (int32_t k = 0; k < nsys; ++k) {
+            // a leaf never spans two systems
+            if (sys[k].n_atoms <= 0 || sys[k].n_atoms % p->atomsperleaf) return ND_ERR_SPEC;
+            tot += sys[k].n_atoms;
+        }
+        if (tot != n) return ND_ERR_ARG;
+    }
     MDEngine* m = new MDEngine();
+    m->nsys = nsys;
+    m->resort_every = p->resort_every > 0 ? p->resort_every : 1;
     m->parent = parent;
     m->sub.device = parent->device;
     m->sub.stream = parent->stream;
@@ -1069,7 +1550,7 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     m->nblocks = (int32_t)cdiv(n, kBlock);
     m->has_q = qd != nullptr;
     m->has_m = md_ != nullptr;
-    nd_status st = md_frame(m);
+    nd_status st = nsys > 0 ? md_frame_batch(m, sys) : md_frame(m);
     if (st == ND_OK) st = md_alloc(m);
     if (st) { parent->last_error = m->sub.last_error; md_destroy(m); return st; }
     Ctx* c = &m->sub;
@@ -1077,8 +1558,17 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     m->cur = 0;
     m->first = true;
     if ((st = md_size_lists(m))) { parent->last_error = c->last_error; md_destroy(m); return st; }
-    for (int w = 0; capture && w < 4; ++w)
-        if ((st = md_capture_window(m, w & 1, w >> 1))) { parent->last_error = c->last_error; md_destroy(m); return st; }
+    if (capture && cudaStreamCreateWithFlags(&m->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        st = cuda_fail(c, cudaGetLastError(), "capture stream");
+        parent->last_error = c->last_error;
+        md_destroy(m);
+        return st;
+    }
+    if (capture && ((st = md_capture_main(m)) || (st = md_capture_first(m)))) {
+        parent->last_error = c->last_error;
+        md_destroy(m);
+        return st;
+    }
     parent->launches += c->launches;
     c->launches = 0;
     *out = m;
@@ -1091,20 +1581,134 @@ nd_status md_create(Ctx* parent, const nd_md_params* p, int32_t n, const double*
     return md_create_common(parent, p, n, x, v, q, mass, host, capture, out);
 }
 
+nd_status md_create_batch(Ctx* parent, const nd_md_params* p, int32_t nsys, const nd_system* sys,
+                          const double* x, const double* v, const double* q, const double* mass,
+                          bool host, MDEngine** out) {
+    if (nsys <= 0 || !sys) return ND_ERR_ARG;
+    int64_t n = 0;
+    for (int32_t k = 0; k < nsys; ++k) n += std::max(sys[k].n_atoms, 0);
+    if (n <= 0 || n > INT32_MAX) return ND_ERR_ARG;
+    return md_create_common(parent, p, (int32_t)n, x, v, q, mass, host, true, out, nsys, sys);
+}
+
+// Autotuner.  Each candidate setting runs on a fresh engine from the same
+// host state -- one untimed window, then trial_steps timed with events on the
+// stream, early refits included -- and the settings are tuned one at a time
+// (coordinate descent): skin (the given one and +0.1, +0.2: a longer list
+// against fewer early refits), atoms per leaf (the leaf and traversal width),
+// re-sort interval, shared-memory staging policy.  Candidates that do not fit
+// (shared memory, leaf size not dividing every system) are skipped.
+nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsys,
+                      const nd_system* sys, const double* x, const double* v, const double* q,
+                      const double* mass, int32_t trial_steps, nd_md_params* best,
+                      double* sps) {
+    if (!parent || !p || !best || trial_steps <= 0 || n <= 0) return ND_ERR_ARG;
+    const int32_t R = std::max(p->rebuild_every, 1);
+    const int64_t steps = ((int64_t)trial_steps + R - 1) / R * R;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return cuda_fail(parent, cudaGetLastError(), "autotune events");
+    }
+    // time one setting: seconds per step, < 0 when it does not fit
+    auto trial = [&](const nd_md_params& c, double* t) -> nd_status {
+        *t = -1.0;
+        bool fits = c.atomsperleaf > 0 && 32 % c.atomsperleaf == 0 && n % c.atomsperleaf == 0 &&
+                    n / c.atomsperleaf >= 2;
+        for (int32_t k = 0; fits && k < nsys; ++k) fits = sys[k].n_atoms % c.atomsperleaf == 0;
+        if (!fits) return ND_OK;
+        MDEngine* m = nullptr;
+        nd_status st = nsys > 0 ? md_create_batch(parent, &c, nsys, sys, x, v, q, mass, true, &m)
+                                : md_create(parent, &c, n, x, v, q, mass, true, true, &m);
+        if (st == ND_ERR_OVERFLOW) { parent->last_error.clear(); return ND_OK; }
+        if (st) return st;
+        st = md_run(m, R);
+        if (st == ND_OK) st = md_sync(m);
+        if (st == ND_OK) {
+            cudaEventRecord(e0, m->sub.stream);
+            st = md_run(m, steps);
+            cudaEventRecord(e1, m->sub.stream);
+            if (st == ND_OK) st = md_sync(m);
+        }
+        float ms = 0.0f;
+        if (st == ND_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+            *t = ms * 1e-3 / (double)steps;
+        md_destroy(m);
+        // a setting whose lists outgrow their capacities in the trial is not
+        // a candidate (refit windows on a fast-changing system)
+        if (st == ND_ERR_OVERFLOW) { parent->last_error.clear(); return ND_OK; }
+        return st;
+    };
+    nd_md_params win = *p;
+    if (win.resort_every <= 0) win.resort_every = 1;
+    double best_t = -1.0;
+    nd_status result = ND_OK;
+    auto consider = [&](const nd_md_params& c) -> nd_status {
+        double t = -1.0;
+        nd_status st = trial(c, &t);
+        if (st == ND_OK && t > 0.0 && (best_t < 0.0 || t < best_t)) { best_t = t; win = c; }
+        return st;
+    };
+    {
+        // a starting leaf size that fits
+        const int32_t apls[] = {4, 2, 8, 1};
+        for (int32_t a : apls) {
+            nd_md_params c = win;
+            c.atomsperleaf = a;
+            if ((result = consider(c))) goto done;
+            if (best_t > 0.0) break;
+        }
+        if (best_t < 0.0) { result = ND_ERR_SPEC; parent->last_error = "no autotune candidate fits"; goto done; }
+        const nd_md_params start = win;
+        for (double ds : {0.1, 0.2}) {
+            nd_md_params c = start;
+            c.skin = p->skin + ds;
+            if ((result = consider(c))) goto done;
+        }
+        const nd_md_params s1 = win;
+        for (int32_t a : {2, 4, 8}) {
+            if (a == s1.atomsperleaf) continue;
+            nd_md_params c = s1;
+            c.atomsperleaf = a;
+            if ((result = consider(c))) goto done;
+        }
+        const nd_md_params s2 = win;
+        for (int32_t rs : {1, 5, 10}) {
+            if (rs == s2.resort_every) continue;
+            nd_md_params c = s2;
+            c.resort_every = rs;
+            if ((result = consider(c))) goto done;
+        }
+        const nd_md_params s3 = win;
+        nd_md_params c = s3;
+        c.stage_policy = 1 - s3.stage_policy;
+        if ((result = consider(c))) goto done;
+    }
+done:
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (result == ND_OK) {
+        *best = win;
+        if (sps) *sps = best_t;
+    }
+    return result;
+}
+
 nd_status md_destroy(MDEngine* m) {
     if (!m) return ND_OK;
-    for (int r = 0; r < 2; ++r)
-        for (int w = 0; w < 2; ++w)
-            if (m->graph[r][w]) cudaGraphExecDestroy(m->graph[r][w]);
+    if (m->graph_main) cudaGraphExecDestroy(m->graph_main);
+    if (m->graph_first) cudaGraphExecDestroy(m->graph_first);
     DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->rec_buf[0], &m->rec_buf[1], &m->recb,
                       &m->xyz32, &m->pos32, &m->keys, &m->store, &m->ulist, &m->ucount,
                       &m->llist_leaf, &m->lcount_leaf, &m->llist,
-                      &m->ncount, &m->f, &m->vtmp, &m->acc, &m->aos, &m->diag, &m->sub.codes,
+                      &m->ncount, &m->f, &m->vtmp, &m->acc, &m->aos, &m->diag, &m->sysrow,
+                      &m->sid_in, &m->ctl, &m->sub.codes,
                       &m->sub.codes_alt, &m->sub.perm, &m->sub.perm_alt, &m->sub.hist,
                       &m->sub.misc};
     if (m->sub.stream) cudaStreamSynchronize(m->sub.stream);
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
+    if (m->cap_stream) cudaStreamDestroy(m->cap_stream);
     delete m;
     return ND_OK;
 }
@@ -1117,26 +1721,36 @@ nd_status md_run(MDEngine* m, int64_t steps) {
     nd_status st;
     while (steps > 0) {
         if (m->rebuild_due) {
-            // every resort_every-th rebuild re-sorts; the others refit
-            const int refit = (m->rebuilds % m->resort_every) != 0 ? 1 : 0;
-            if (steps >= R && !m->first && m->graph[refit][m->cur]) {
-                cudaError_t e = cudaGraphLaunch(m->graph[refit][m->cur], c->stream);
+            if (steps >= R && !m->first && m->graph_main) {
+                // a whole window: rebuild (decided on the device) + R steps
+                cudaError_t e = cudaGraphLaunch(m->graph_main, c->stream);
                 if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
-                c->launches += m->graph_launches[refit];
-                if (!refit) m->cur ^= 1;
+                c->launches += m->graph_main_launches;
                 m->rc = R & 1;
                 m->rebuilds++;
                 m->steps += R;
                 steps -= R;
                 continue;
             }
-            if ((st = md_rebuild(m, false, refit != 0))) return st;
+            if ((st = md_window_begin(m, false))) return st;
             m->rebuilds++;
             m->rebuild_due = false;
             m->in_window = 0;
         }
+        if (m->first && m->in_window == 0 && steps >= R && m->graph_first) {
+            // the opening window after an upload
+            cudaError_t e = cudaGraphLaunch(m->graph_first, c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
+            c->launches += m->graph_first_launches;
+            m->first = false;
+            m->rc = R & 1;
+            m->rebuild_due = true;
+            m->steps += R;
+            steps -= R;
+            continue;
+        }
         int32_t k = (int32_t)std::min<int64_t>(steps, R - m->in_window);
-        md_steps(m, k);
+        if ((st = md_steps(m, k, m->in_window))) return st;
         m->in_window += k;
         if (m->in_window == R) { m->in_window = 0; m->rebuild_due = true; }
         m->steps += k;
@@ -1147,9 +1761,47 @@ nd_status md_run(MDEngine* m, int64_t steps) {
     return check_launch(c, "md run");
 }
 
+// Advance `steps` steps eagerly (rebuilds and early refits as usual), timing
+// every step kernel with its own pair of events on the stream: ms[k] is the
+// k-th step kernel's duration.
+nd_status md_step_times(MDEngine* m, int32_t steps, float* ms) {
+    Ctx* c = &m->sub;
+    if (steps <= 0 || !ms) return ND_ERR_ARG;
+    const int32_t R = m->p.rebuild_every;
+    std::vector<cudaEvent_t> ev(2 * (size_t)steps, nullptr);
+    nd_status st = ND_OK;
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) { st = cuda_fail(c, cudaGetLastError(), "events"); break; }
+    int32_t done = 0;
+    while (st == ND_OK && done < steps) {
+        if (m->rebuild_due) {
+            if ((st = md_window_begin(m, false))) break;
+            m->rebuilds++;
+            m->rebuild_due = false;
+            m->in_window = 0;
+        }
+        const int32_t k = std::min(steps - done, R - m->in_window);
+        if ((st = md_steps(m, k, m->in_window, false, ev.data() + 2 * (size_t)done))) break;
+        m->in_window += k;
+        if (m->in_window == R) { m->in_window = 0; m->rebuild_due = true; }
+        m->steps += k;
+        done += k;
+    }
+    if (st == ND_OK) st = sync_and_check(c, "md step times");
+    for (int32_t k = 0; st == ND_OK && k < steps; ++k) {
+        cudaError_t e = cudaEventElapsedTime(&ms[k], ev[2 * k], ev[2 * k + 1]);
+        if (e != cudaSuccess) st = cuda_fail(c, e, "event time");
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    m->parent->launches += c->launches;
+    c->launches = 0;
+    return st;
+}
+
 nd_status md_measure(MDEngine* m) {
     Ctx* c = &m->sub;
-    cudaMemsetAsync(m->acc.p, 0, 2 * sizeof(double), c->stream);
+    cudaMemsetAsync(m->acc.p, 0, 2 * sizeof(double) * (size_t)std::max(m->nsys, 1), c->stream);
     StepArgs a = md_step_args(m, m->rc);
     launch_step<1>(m, a, m->first);
     return check_launch(c, "md measure");
@@ -1194,14 +1846,37 @@ nd_status md_energy(MDEngine* m, double* pot, double* kin) {
     Ctx* c = &m->sub;
     nd_status st = md_measure(m);
     if (st) return st;
-    double h[2];
-    cudaError_t e = cudaMemcpyAsync(h, m->acc.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    const int32_t ns = std::max(m->nsys, 1);
+    std::vector<double> h(2 * (size_t)ns);
+    cudaError_t e = cudaMemcpyAsync(h.data(), m->acc.p, sizeof(double) * h.size(),
+                                    cudaMemcpyDeviceToHost, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "md energy");
     m->parent->launches += c->launches;
     c->launches = 0;
     if ((st = sync_and_check(c, "md energy"))) return st;
-    if (pot) *pot = h[0];
-    if (kin) *kin = h[1];
+    double up = 0.0, uk = 0.0;
+    for (int32_t k = 0; k < ns; ++k) { up += h[2 * k]; uk += h[2 * k + 1]; }
+    if (pot) *pot = up;
+    if (kin) *kin = uk;
+    return ND_OK;
+}
+
+nd_status md_energies(MDEngine* m, double* pot, double* kin) {
+    Ctx* c = &m->sub;
+    if (m->nsys <= 0) return ND_ERR_ARG;
+    nd_status st = md_measure(m);
+    if (st) return st;
+    std::vector<double> h(2 * (size_t)m->nsys);
+    cudaError_t e = cudaMemcpyAsync(h.data(), m->acc.p, sizeof(double) * h.size(),
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "batch energies");
+    m->parent->launches += c->launches;
+    c->launches = 0;
+    if ((st = sync_and_check(c, "batch energies"))) return st;
+    for (int32_t k = 0; k < m->nsys; ++k) {
+        if (pot) pot[k] = h[2 * k];
+        if (kin) kin[k] = h[2 * k + 1];
+    }
     return ND_OK;
 }
 
@@ -1225,22 +1900,33 @@ nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list
     return ND_OK;
 }
 
-nd_status md_diagnostics(MDEngine* m, int64_t* skin_violations, int32_t* max_neighbors) {
+nd_status md_diagnostics(MDEngine* m, nd_md_diag* out) {
     Ctx* c = &m->sub;
     unsigned long long d[2] = {0, 0};
+    unsigned ctl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     cudaError_t e = cudaMemcpyAsync(d, m->diag.p, sizeof(d), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, m->ctl.p, sizeof(ctl), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "md diagnostics");
-    if (skin_violations) *skin_violations = (int64_t)d[0];
+    *out = nd_md_diag{};
+    out->skin_violations = (int64_t)d[0];
     // diag int32 words 2 and 3 hold the largest union and list seen
-    if (max_neighbors) *max_neighbors = (int32_t)(d[1] >> 32);
+    out->max_neighbors = (int32_t)(d[1] >> 32);
+    out->resorts = ctl[6];
+    out->refits = ctl[7];
+    out->early_refits = ctl[2];
+    out->resort_kernels = m->resort_kernels;
+    out->refit_kernels = m->refit_kernels;
+    // kernels run inside conditional bodies of graphs: all bodies run, less
+    // those the host ran (and counted) itself
+    out->body_kernels = (int64_t)ctl[6] * m->resort_kernels +
+                        ((int64_t)ctl[7] + ctl[2]) * m->refit_kernels - m->eager_bodies;
     return ND_OK;
 }
 
 int64_t md_launches_per_run(MDEngine* m, int64_t steps) {
     const int64_t R = m->p.rebuild_every;
-    const int64_t w = steps / R, full = (w + m->resort_every - 1) / m->resort_every;
-    return full * m->graph_launches[0] + (w - full) * m->graph_launches[1] + (steps % R);
+    return (steps / R) * m->graph_main_launches + (steps % R);
 }
 
 nd_status md_sync(MDEngine* m) { return sync_and_check(&m->sub, "md sync"); }

@@ -13,7 +13,7 @@ from .bvh import (SpheresBVHSpecs, APointPrimitive, leafTreeData, TreeData,
                   neighbor_pairs_dev, pair_hash_dev)
 from .dynamics import (ForceField, md_params, force_lennardjones_, force_coulomb_, sum_forces_,
                        forces, SimSpec, GenericObjectCollection, GenericRandomCollector,
-                       simulate_, MDEngine)
+                       simulate_, MDEngine, Ensemble, systems_table, autotune)
 from . import synth
 
 _lib.lib()  # load now: no CPU fallback exists

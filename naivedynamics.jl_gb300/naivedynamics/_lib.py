@@ -66,7 +66,24 @@ class MDParams(ctypes.Structure):
                 ("skin", ctypes.c_double), ("dt", ctypes.c_double),
                 ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3),
                 ("atomsperleaf", ctypes.c_int32), ("rebuild_every", ctypes.c_int32),
-                ("order", ctypes.c_int32), ("max_neighbors", ctypes.c_int32)]
+                ("order", ctypes.c_int32), ("max_neighbors", ctypes.c_int32),
+                ("resort_every", ctypes.c_int32), ("stage_policy", ctypes.c_int32)]
+
+
+class MDDiag(ctypes.Structure):
+    """nd_md_diag."""
+    _fields_ = [("skin_violations", ctypes.c_int64), ("max_neighbors", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("resorts", ctypes.c_int64),
+                ("refits", ctypes.c_int64), ("early_refits", ctypes.c_int64),
+                ("resort_kernels", ctypes.c_int64), ("refit_kernels", ctypes.c_int64),
+                ("body_kernels", ctypes.c_int64)]
+
+
+class System(ctypes.Structure):
+    """nd_system: one member of a batched ensemble."""
+    _fields_ = [("n_atoms", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("sigma", ctypes.c_double), ("epsilon", ctypes.c_double),
+                ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3)]
 
 
 _i32 = ctypes.c_int32
@@ -115,7 +132,16 @@ SIGNATURES = {
     "nd_md_stats": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                            ctypes.POINTER(_i32)]),
     "nd_md_launches_per_run": (_i64, [_vp, _i64]),
-    "nd_md_diagnostics": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i32)]),
+    "nd_md_step_times": (_i32, [_vp, _i32, _vp]),
+    "nd_batch_create": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, ctypes.POINTER(System), _vp,
+                               _vp, _vp, _vp, _pp]),
+    "nd_batch_create_dev": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, ctypes.POINTER(System),
+                                   _vp, _vp, _vp, _vp, _pp]),
+    "nd_batch_energies": (_i32, [_vp, _vp, _vp]),
+    "nd_md_autotune": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _i32, ctypes.POINTER(System),
+                              _vp, _vp, _vp, _vp, _i32, ctypes.POINTER(MDParams),
+                              ctypes.POINTER(_d)]),
+    "nd_md_diagnostics": (_i32, [_vp, ctypes.POINTER(MDDiag)]),
     "nd_simulate": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _vp, _i64]),
     "nd_synth_uniform": (_i32, [_u64, _i32, _d, _d, _vp]),
     "nd_synth_uniform_mindist": (_i32, [_u64, _i32, _d, _d, _vp]),

@@ -25,7 +25,7 @@ from ._lib import MDParams, ND_ORDER_SPATIAL, default_context, ptr
 
 __all__ = ["ForceField", "md_params", "force_lennardjones_", "force_coulomb_", "sum_forces_",
            "forces", "SimSpec", "GenericObjectCollection", "GenericRandomCollector", "simulate_",
-           "MDEngine"]
+           "MDEngine", "Ensemble", "systems_table", "autotune"]
 
 
 @dataclass
@@ -38,7 +38,8 @@ class ForceField:
 
 def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e-3,
               box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), atomsperleaf=4, rebuild_every=10,
-              order=ND_ORDER_SPATIAL, max_neighbors=0) -> MDParams:
+              order=ND_ORDER_SPATIAL, max_neighbors=0, resort_every=0,
+              stage_policy=0) -> MDParams:
     p = MDParams()
     p.sigma, p.epsilon, p.coulomb_k, p.cutoff, p.skin, p.dt = (float(sigma), float(epsilon),
                                                                float(coulomb_k), float(cutoff),
@@ -49,6 +50,7 @@ def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e
     p.atomsperleaf, p.rebuild_every, p.order, p.max_neighbors = (int(atomsperleaf),
                                                                  int(rebuild_every), int(order),
                                                                  int(max_neighbors))
+    p.resort_every, p.stage_policy = int(resort_every), int(stage_policy)
     return p
 
 
@@ -257,10 +259,94 @@ class MDEngine:
         return dict(steps=s.value, rebuilds=r.value, list_pairs=p.value, capacity=cap.value)
 
     def diagnostics(self):
-        v, mx = ctypes.c_int64(), ctypes.c_int32()
-        self.ctx.check(_lib.lib().nd_md_diagnostics(self.handle, ctypes.byref(v), ctypes.byref(mx)),
+        d = _lib.MDDiag()
+        self.ctx.check(_lib.lib().nd_md_diagnostics(self.handle, ctypes.byref(d)),
                        "nd_md_diagnostics")
-        return dict(skin_violations=v.value, max_neighbors=mx.value)
+        return {name: getattr(d, name) for name, _ in d._fields_ if name != "reserved"}
+
+    def step_times(self, steps: int):
+        """Advance `steps` steps eagerly, timing each step kernel with CUDA
+        events on the context stream; returns the durations in ms."""
+        ms = np.empty(int(steps), np.float32)
+        self.ctx.check(_lib.lib().nd_md_step_times(self.handle, int(steps), ptr(ms)),
+                       "nd_md_step_times")
+        return ms
 
     def launches_per_run(self, steps: int) -> int:
         return int(_lib.lib().nd_md_launches_per_run(self.handle, int(steps)))
+
+
+def systems_table(n_atoms, sigma, epsilon, box_lo, box_hi):
+    """ctypes array of nd_system rows from per-system sequences (box_lo/box_hi:
+    nsys x 3)."""
+    n_atoms = np.asarray(n_atoms)
+    ns = len(n_atoms)
+    arr = (_lib.System * ns)()
+    lo = np.asarray(box_lo, np.float64).reshape(ns, 3)
+    hi = np.asarray(box_hi, np.float64).reshape(ns, 3)
+    for k in range(ns):
+        r = arr[k]
+        r.n_atoms = int(n_atoms[k])
+        r.sigma = float(sigma[k])
+        r.epsilon = float(epsilon[k])
+        for d in range(3):
+            r.box_lo[d] = float(lo[k, d])
+            r.box_hi[d] = float(hi[k, d])
+    return arr
+
+
+class Ensemble(MDEngine):
+    """Batched ensemble (nd_batch_create): independent systems of uneven sizes
+    advanced together, one launch per step over all of them.  x, v are the
+    systems' (N_s x 3) arrays concatenated in order; `systems` is the table from
+    systems_table().  run/get/energy/diagnostics behave as for MDEngine
+    (energy() sums the systems); energies() gives per-system values."""
+
+    def __init__(self, params: MDParams, systems, x, v, q=None, m=None, device=False, ctx=None):
+        self.ctx = ctx or default_context()
+        self.params = params
+        self.systems = systems
+        self.nsys = len(systems)
+        self.offsets = np.concatenate([[0], np.cumsum([r.n_atoms for r in systems])])
+        h = ctypes.c_void_p()
+        if device:
+            st = _lib.lib().nd_batch_create_dev(self.ctx.handle, ctypes.byref(params), self.nsys,
+                                                systems, ptr(x), ptr(v), ptr(q), ptr(m),
+                                                ctypes.byref(h))
+        else:
+            x = _f64(x, (-1, 3))
+            v = _f64(v, (-1, 3))
+            qq = None if q is None else _f64(q)
+            mm = None if m is None else _f64(m)
+            st = _lib.lib().nd_batch_create(self.ctx.handle, ctypes.byref(params), self.nsys,
+                                            systems, ptr(x), ptr(v), ptr(qq), ptr(mm),
+                                            ctypes.byref(h))
+        self.ctx.check(st, "nd_batch_create")
+        self.handle = h.value
+        self.n = int(self.offsets[-1])
+
+    def energies(self):
+        pe = np.empty(self.nsys, np.float64)
+        ke = np.empty(self.nsys, np.float64)
+        self.ctx.check(_lib.lib().nd_batch_energies(self.handle, ptr(pe), ptr(ke)),
+                       "nd_batch_energies")
+        return pe, ke
+
+
+def autotune(params: MDParams, x, v, q=None, m=None, systems=None, trial_steps=20, ctx=None):
+    """nd_md_autotune: the fastest (atomsperleaf, resort_every, stage_policy)
+    for this state, as a new MDParams, and its time per MD step in seconds.
+    systems=None tunes a plain engine."""
+    ctx = ctx or default_context()
+    x = _f64(x, (-1, 3))
+    v = _f64(v, (-1, 3))
+    qq = None if q is None else _f64(q)
+    mm = None if m is None else _f64(m)
+    best = MDParams()
+    sps = ctypes.c_double()
+    ns = 0 if systems is None else len(systems)
+    st = _lib.lib().nd_md_autotune(ctx.handle, ctypes.byref(params), x.shape[0], ns, systems,
+                                   ptr(x), ptr(v), ptr(qq), ptr(mm), int(trial_steps),
+                                   ctypes.byref(best), ctypes.byref(sps))
+    ctx.check(st, "nd_md_autotune")
+    return best, sps.value

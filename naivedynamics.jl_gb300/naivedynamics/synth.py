@@ -67,3 +67,28 @@ def lj_system(seed: int, n: int, side: float, dmin: float = 0.8, charges: bool =
     v = normal(seed ^ 0x5EED0001, (n, 3), 1.0)
     q = charges_pm1(seed ^ 0x5EED0002, n) if charges else None
     return x, v, q
+
+
+def ensemble(seed: int = SEED_ENSEMBLE, nsys: int = 512, nmin: int = 256, nmax: int = 16384,
+             rho=(0.6, 0.9), sigma=(0.9, 1.1), eps=(0.8, 1.2), dmin_sigma: float = 0.8):
+    """Batched LJ ensemble: N_s = 4 round(exp(U[ln nmin, ln nmax]) / 4) atoms,
+    density rho_s ~ U[rho], cube side L_s = (N_s / rho_s)^(1/3) with walls
+    [0, L_s]^3, sigma_s ~ U[sigma], eps_s ~ U[eps]; positions with minimum
+    separation dmin_sigma * sigma_s, velocities N(0, 1).  Returns a dict with
+    the per-system arrays and the concatenated x, v."""
+    g = np.random.default_rng(seed)
+    n = (4 * np.round(np.exp(g.uniform(np.log(nmin), np.log(nmax), nsys)) / 4)).astype(np.int64)
+    n = np.clip(n, 4 * ((nmin + 3) // 4), nmax)
+    r = g.uniform(rho[0], rho[1], nsys)
+    side = (n / r) ** (1.0 / 3.0)
+    sg = g.uniform(sigma[0], sigma[1], nsys)
+    ep = g.uniform(eps[0], eps[1], nsys)
+    xs, vs = [], []
+    for k in range(nsys):
+        sk = (seed * 1000003 + k) & 0xFFFFFFFFFFFFFFFF
+        xs.append(uniform_positions_mindist(sk, int(n[k]), float(side[k]), dmin_sigma * sg[k]))
+        vs.append(normal(sk ^ 0x5EED0001, (int(n[k]), 3), 1.0))
+    lo = np.zeros((nsys, 3))
+    hi = np.repeat(side[:, None], 3, axis=1)
+    return dict(n_atoms=n, rho=r, side=side, sigma=sg, epsilon=ep, box_lo=lo, box_hi=hi,
+                x=np.concatenate(xs), v=np.concatenate(vs))

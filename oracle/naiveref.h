@@ -130,7 +130,8 @@ typedef struct {
 int64_t ref_forces(const ref_md_params* p, int32_t n, const double* x, const double* q,
                    double* f, double* energy);
 
-/* Per-system sigma/epsilon variant used by the ensemble checks. */
+/* Ensemble checks call ref_forces / ref_md_run once per system (systems are
+ * independent), with that system's sigma, epsilon and walls. */
 
 /*
  * Kick-drift-kick velocity Verlet with reflecting walls:

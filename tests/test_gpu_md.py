@@ -104,6 +104,50 @@ def test_md_trajectory_vs_fp64(nd, oracle):
     assert eng.diagnostics()["skin_violations"] == 0
 
 
+def test_md_early_refit_keeps_lists_valid(nd, oracle):
+    # A hot start (velocities N(0, 15^2)) moves atoms more than skin/4 inside a
+    # rebuild window: early refits must keep every atom within skin/2 of its
+    # list-build position (no skin violation), the trajectory must follow the
+    # FP64 one, and eager (partial-window) runs must refit at the same steps as
+    # the captured windows.
+    x0, v0, _ = _config1(nd, n=2048, side=13.5)
+    v0 = v0 * 15.0
+    a = nd.MDEngine(_params(nd, 13.5), x0, v0)
+    a.run(60)
+    a.sync()
+    xa, va, fa = a.get()
+    d = a.diagnostics()
+    print(f"early refits {d['early_refits']} ({d['refit_kernels']} kernels each), "
+          f"skin violations {d['skin_violations']}")
+    assert d["early_refits"] > 0
+    assert d["skin_violations"] == 0
+    p = oracle.md_params(cutoff=2.5, box_hi=(13.5, 13.5, 13.5), dt=1e-3)
+    xr, vr, _ = oracle.md_run(p, x0, v0, steps=60)
+    assert np.abs(xa - xr).max() < 1e-5
+    f64, _, _ = oracle.forces(p, xa)
+    assert force_errors(fa, f64)[1] <= F_L2_TOL
+    b = nd.MDEngine(_params(nd, 13.5), x0, v0)
+    for k in (7, 3, 11, 9, 10, 20):
+        b.run(k)
+    xb, vb, _ = b.get()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    assert b.diagnostics()["early_refits"] == d["early_refits"]
+
+
+def test_md_refit_windows_match_resorting(nd):
+    # Re-sorting at every rebuild and refitting the kept tree in between give
+    # the same dynamics up to force summation order.
+    x0, v0, q = _config1(nd, charges=True, n=2048, side=13.5)
+    out = []
+    for rs in (1, 5):
+        eng = nd.MDEngine(_params(nd, 13.5, coulomb=1.0, resort_every=rs), x0, v0, q)
+        eng.run(60)
+        out.append(eng.get())
+        assert eng.diagnostics()["skin_violations"] == 0
+    assert np.abs(out[0][0] - out[1][0]).max() < 2e-6
+    assert force_errors(out[1][2], np.asarray(out[0][2], np.float64))[1] < 1e-5
+
+
 def test_md_neighbor_list_pair_set(nd, oracle):
     # The engine's list at a rebuild equals every pair with d^2 < r_list^2 on
     # the Float32 positions (full list: each pair twice).
