@@ -252,6 +252,71 @@ def batched_leg(nd, ctx, ext, flush):
             "plain_path": "512 nd_md engines run one after another on one stream (graphs)"}
 
 
+ADJ_N = 32768
+ADJ_STEPS = 1000
+
+
+def adjoint_leg(nd, ctx, ext, flush):
+    """Differentiable trajectory: 32,768 LJ atoms at density 0.83 (cube side
+    (N/0.83)^(1/3), min separation 0.8), 1000 steps dt 1e-3, loss = squared
+    deviation of the Gaussian-smoothed pair-distance histogram (64 bins on
+    [0, 2.5]) from the histogram of the same seed run at sigma 1.05, eps 0.9;
+    gradient wrt sigma, eps, x0, v0 with checkpoints every 50 steps.  Forward
+    and backward passes timed with CUDA events on the library's stream (one
+    captured graph each); the plain engine's 1000 steps on the same state are
+    timed beside them."""
+    import numpy as np
+    import torch
+
+    side = (ADJ_N / 0.83) ** (1.0 / 3.0)
+    x, v, _ = nd.synth.lj_system(nd.synth.SEED_ADJOINT, ADJ_N, side, 0.8)
+    mp = nd.md_params(sigma=1.05, epsilon=0.9, cutoff=2.5, skin=0.3, dt=1e-3,
+                      box_hi=(side,) * 3, atomsperleaf=4, rebuild_every=REBUILD, resort_every=5)
+    adj = nd.Adjoint(mp, nd.adj_spec(ADJ_STEPS, checkpoint_every=50), x, v, ctx=ctx)
+    _, target = adj.forward()
+    adj.set_params(1.0, 1.0)
+    adj.set_target(target)
+    adj.forward()
+    adj.backward()  # captures both graphs
+    fwd, bwd = [], []
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        loss, _ = adj.forward()
+        g = adj.backward()
+        f_ms, b_ms = adj.times()
+        fwd.append(f_ms)
+        bwd.append(b_ms)
+    adj.close()
+    mp.sigma, mp.epsilon = 1.0, 1.0
+    eng = nd.MDEngine(mp, x, v, ctx=ctx)
+    eng.run(REBUILD)
+    eng.sync()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(ext):
+        a.record(ext)
+        eng.run(ADJ_STEPS)
+        b.record(ext)
+    eng.sync()
+    plain_ms = a.elapsed_time(b)
+    eng.close()
+    f_ms, b_ms = float(np.median(fwd)), float(np.median(bwd))
+    return {"metric": "adjoint step time / forward step time", "unit": "ratio",
+            "workload": (f"adjoint_32768: N={ADJ_N} LJ, cube side {side:.2f} (density 0.83), "
+                         f"{ADJ_STEPS} steps dt 1e-3, histogram loss (64 bins on [0, 2.5], "
+                         "Gaussian width = bin width) vs the sigma 1.05 / eps 0.9 run, "
+                         "checkpoints every 50 steps, skin 0.3, rebuild every 10"),
+            "value": b_ms / f_ms, "forward_ms_per_step": f_ms / ADJ_STEPS,
+            "adjoint_ms_per_step": b_ms / ADJ_STEPS,
+            "plain_engine_ms_per_step": plain_ms / ADJ_STEPS,
+            "adjoint_over_plain_forward": (b_ms / ADJ_STEPS) / (plain_ms / ADJ_STEPS),
+            "loss": loss, "dL_dsigma": g["sigma"], "dL_depsilon": g["epsilon"],
+            "dL_dx0_norm": float(np.linalg.norm(g["x0"])),
+            "target": "<= 3 (adjoint step vs forward step)"}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -402,6 +467,8 @@ def run_gb300(args):
     eng.close()
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_leg(nd, ctx, ext, flush)
+    if rank == 0 and not args.no_adjoint:
+        line["adjoint"] = adjoint_leg(nd, ctx, ext, flush)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(steps=10)
     if rank == 0:
@@ -420,6 +487,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the adjoint (differentiable trajectory) measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -343,6 +343,59 @@ nd_status nd_md_autotune(nd_ctx* ctx, const nd_md_params* p, int32_t n, int32_t 
 nd_status nd_simulate(nd_ctx* ctx, const nd_md_params* p, int32_t n, double* x, double* v,
                       float* f, const double* q, const double* m, int64_t steps);
 
+/* ------------------------------------------------------------------ adjoint */
+
+/*
+ * Differentiable trajectory: `steps` kick-drift-kick steps of the engine from
+ * (x0, v0), then the Gaussian-smoothed pair-distance histogram of the final
+ * positions,
+ *   h_b = (1/N) sum_{i<j, r_ij < r_max} s(r_ij) exp(-(r_ij - c_b)^2 / (2 width^2)),
+ *   c_b = (b + 1/2) r_max / bins,  s = 1 below r_switch, a C2 switch to 0 at r_max,
+ * and the loss L = sum_b (h_b - target_b)^2.  The backward pass is the
+ * hand-written adjoint of that program (reverse steps over the same
+ * neighbour lists, segments of checkpoint_every steps recomputed from their
+ * checkpoints): dL/dx0, dL/dv0, dL/dsigma, dL/depsilon.  Wall clamps and the
+ * force cutoff are differentiated as the piecewise program they are.
+ * Rebuilds: a re-sort every resort_every windows (0 = 5), refits between, and
+ * early refits decided on the device in the forward pass (as nd_md_run does)
+ * and replayed from its record in the backward pass.  Results do not depend
+ * on checkpoint_every: every interval gives the same bits.  A forward pass in
+ * which an atom still moved more than skin/2 from its list-build position
+ * returns ND_ERR_OVERFLOW.  No counterpart in the reference (it has no
+ * derivative code); the Julia side is a ChainRulesCore.rrule over these calls.
+ */
+typedef struct nd_adj nd_adj;
+typedef struct {
+    int32_t steps;            /* K: a multiple of checkpoint_every */
+    int32_t checkpoint_every; /* a multiple of resort_every * rebuild_every; 0 = 50 */
+    int32_t bins;             /* 1..1024 */
+    int32_t reserved;
+    double r_max;             /* histogram range [0, r_max], r_max <= cutoff */
+    double width;             /* Gaussian width; 0 = r_max / bins */
+    double r_switch;          /* start of the pair-weight switch; < 0 = r_max - 0.25 */
+} nd_adj_spec;
+
+/* x0, v0: N x 3 FP64 host arrays; q, m: N or NULL.  p as for nd_md_create. */
+nd_status nd_adj_create(nd_ctx* ctx, const nd_md_params* p, int32_t n, const double* x0,
+                        const double* v0, const double* q, const double* m,
+                        const nd_adj_spec* spec, nd_adj** out);
+nd_status nd_adj_destroy(nd_adj* adj);
+/* Lennard-Jones parameters of later passes. */
+nd_status nd_adj_set_params(nd_adj* adj, double sigma, double epsilon);
+/* Target histogram (bins values, host; NULL = zeros). */
+nd_status nd_adj_set_target(nd_adj* adj, const double* target);
+/* Forward pass: hist (bins) and loss out (either may be NULL). */
+nd_status nd_adj_forward(nd_adj* adj, double* hist, double* loss);
+/* Backward pass after a forward pass: dL/dx0, dL/dv0 (N x 3, caller order),
+ * dL/dsigma, dL/depsilon (each may be NULL). */
+nd_status nd_adj_backward(nd_adj* adj, double* dx0, double* dv0, double* dsigma,
+                          double* depsilon);
+/* Final positions x_K (N x 3, caller order) of the last forward pass. */
+nd_status nd_adj_final(nd_adj* adj, double* x);
+/* Device durations (CUDA events on the context stream) of the last forward
+ * and backward passes, in ms (either may be NULL; -1 for a pass not run yet). */
+nd_status nd_adj_times(nd_adj* adj, float* forward_ms, float* backward_ms);
+
 /* ------------------------------------------------------------ synthetic inputs */
 
 /* Seeded host-side generators for benchmark and test inputs (splitmix64). */

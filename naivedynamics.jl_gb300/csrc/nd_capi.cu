@@ -17,14 +17,22 @@ struct nd_md;
 // device state first and leaves the handles orphaned (every call on them then
 // returns ND_ERR_ARG and nd_md_destroy only frees the handle), so the two may
 // be destroyed in either order.
+struct nd_adj;
+
 struct nd_ctx {
     nd::Ctx c;
     std::set<nd_md*> engines;
+    std::set<nd_adj*> adjoints;
 };
 
 struct nd_md {
     nd_ctx* ctx;
     nd::MDEngine* e;
+};
+
+struct nd_adj {
+    nd_ctx* ctx;
+    nd::AdjEngine* e;
 };
 
 static nd_md* md_register(nd_ctx* h, nd::MDEngine* e) {
@@ -284,6 +292,12 @@ nd_status nd_ctx_destroy(nd_ctx* h) {
         md->ctx = nullptr;
     }
     h->engines.clear();
+    for (nd_adj* a : h->adjoints) {
+        nd::adj_destroy(a->e);
+        a->e = nullptr;
+        a->ctx = nullptr;
+    }
+    h->adjoints.clear();
     if (c->sim_cache) nd::md_destroy(c->sim_cache);
     c->sim_cache = nullptr;
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -620,6 +634,75 @@ nd_status nd_simulate(nd_ctx* h, const nd_md_params* p, int32_t n, double* x, do
         c->sim_cache = nullptr;
     }
     return st;
+}
+
+// ------------------------------------------------------------------ adjoint
+
+static bool adj_live(const nd_adj* a) { return a && a->ctx && a->e; }
+
+static nd_status adj_wrap(nd_adj* a, nd_status st) {
+    if (st) a->ctx->c.last_error = nd::adj_last_error(a->e);
+    return st;
+}
+
+nd_status nd_adj_create(nd_ctx* h, const nd_md_params* p, int32_t n, const double* x0,
+                        const double* v0, const double* q, const double* m,
+                        const nd_adj_spec* spec, nd_adj** out) {
+    if (!h || !out) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    nd::AdjEngine* e = nullptr;
+    if ((st = nd::adj_create(&h->c, p, n, x0, v0, q, m, spec, &e))) return st;
+    nd_adj* a = new nd_adj{h, e};
+    h->adjoints.insert(a);
+    *out = a;
+    return ND_OK;
+}
+
+nd_status nd_adj_destroy(nd_adj* a) {
+    if (!a) return ND_OK;
+    if (adj_live(a)) {
+        nd::set_device(&a->ctx->c);
+        a->ctx->adjoints.erase(a);
+        nd::adj_destroy(a->e);
+    }
+    delete a;
+    return ND_OK;
+}
+
+nd_status nd_adj_set_params(nd_adj* a, double sigma, double epsilon) {
+    if (!adj_live(a)) return ND_ERR_ARG;
+    return adj_wrap(a, nd::adj_set_params(a->e, sigma, epsilon));
+}
+
+nd_status nd_adj_set_target(nd_adj* a, const double* target) {
+    if (!adj_live(a)) return ND_ERR_ARG;
+    nd::set_device(&a->ctx->c);
+    return adj_wrap(a, nd::adj_set_target(a->e, target));
+}
+
+nd_status nd_adj_forward(nd_adj* a, double* hist, double* loss) {
+    if (!adj_live(a)) return ND_ERR_ARG;
+    nd::set_device(&a->ctx->c);
+    return adj_wrap(a, nd::adj_forward(a->e, hist, loss));
+}
+
+nd_status nd_adj_backward(nd_adj* a, double* dx0, double* dv0, double* dsigma,
+                          double* depsilon) {
+    if (!adj_live(a)) return ND_ERR_ARG;
+    nd::set_device(&a->ctx->c);
+    return adj_wrap(a, nd::adj_backward(a->e, dx0, dv0, dsigma, depsilon));
+}
+
+nd_status nd_adj_final(nd_adj* a, double* x) {
+    if (!adj_live(a) || !x) return ND_ERR_ARG;
+    nd::set_device(&a->ctx->c);
+    return adj_wrap(a, nd::adj_final(a->e, x));
+}
+
+nd_status nd_adj_times(nd_adj* a, float* forward_ms, float* backward_ms) {
+    if (!adj_live(a)) return ND_ERR_ARG;
+    return adj_wrap(a, nd::adj_times(a->e, forward_ms, backward_ms));
 }
 
 // ------------------------------------------------------------ synthetic inputs

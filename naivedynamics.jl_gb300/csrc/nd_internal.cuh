@@ -228,4 +228,18 @@ nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int32_t* 
 // One pass (apl == 4, leaf path): writes at most capacity pairs, *total = all pairs.
 nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int32_t* pj,
                          float* pd, int64_t capacity, int64_t* total);
+
+// ------------------------------------------------------------- adjoint
+struct AdjEngine;
+nd_status adj_create(Ctx* parent, const nd_md_params* p, int32_t n, const double* x0,
+                     const double* v0, const double* q, const double* mass, const nd_adj_spec* s,
+                     AdjEngine** out);
+nd_status adj_destroy(AdjEngine* A);
+nd_status adj_set_params(AdjEngine* A, double sigma, double epsilon);
+nd_status adj_set_target(AdjEngine* A, const double* target);
+nd_status adj_forward(AdjEngine* A, double* hist, double* loss);
+nd_status adj_backward(AdjEngine* A, double* dx0, double* dv0, double* dsigma, double* deps);
+nd_status adj_times(AdjEngine* A, float* fwd_ms, float* bwd_ms);
+nd_status adj_final(AdjEngine* A, double* x);
+const char* adj_last_error(AdjEngine* A);
 }  // namespace nd

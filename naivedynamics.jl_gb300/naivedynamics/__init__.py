@@ -14,6 +14,7 @@ from .bvh import (SpheresBVHSpecs, APointPrimitive, leafTreeData, TreeData,
 from .dynamics import (ForceField, md_params, force_lennardjones_, force_coulomb_, sum_forces_,
                        forces, SimSpec, GenericObjectCollection, GenericRandomCollector,
                        simulate_, MDEngine, Ensemble, systems_table, autotune)
+from .adjoint import Adjoint, adj_spec, histogram_loss_function
 from . import synth
 
 _lib.lib()  # load now: no CPU fallback exists

@@ -86,6 +86,14 @@ class System(ctypes.Structure):
                 ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3)]
 
 
+class AdjSpec(ctypes.Structure):
+    """nd_adj_spec: differentiable trajectory and histogram loss."""
+    _fields_ = [("steps", ctypes.c_int32), ("checkpoint_every", ctypes.c_int32),
+                ("bins", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("r_max", ctypes.c_double), ("width", ctypes.c_double),
+                ("r_switch", ctypes.c_double)]
+
+
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
 _u64 = ctypes.c_uint64
@@ -143,6 +151,15 @@ SIGNATURES = {
                               ctypes.POINTER(_d)]),
     "nd_md_diagnostics": (_i32, [_vp, ctypes.POINTER(MDDiag)]),
     "nd_simulate": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _vp, _i64]),
+    "nd_adj_create": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp,
+                             ctypes.POINTER(AdjSpec), _pp]),
+    "nd_adj_destroy": (_i32, [_vp]),
+    "nd_adj_set_params": (_i32, [_vp, _d, _d]),
+    "nd_adj_set_target": (_i32, [_vp, _vp]),
+    "nd_adj_forward": (_i32, [_vp, _vp, ctypes.POINTER(_d)]),
+    "nd_adj_backward": (_i32, [_vp, _vp, _vp, ctypes.POINTER(_d), ctypes.POINTER(_d)]),
+    "nd_adj_final": (_i32, [_vp, _vp]),
+    "nd_adj_times": (_i32, [_vp, ctypes.POINTER(_f), ctypes.POINTER(_f)]),
     "nd_synth_uniform": (_i32, [_u64, _i32, _d, _d, _vp]),
     "nd_synth_uniform_mindist": (_i32, [_u64, _i32, _d, _d, _vp]),
     "nd_synth_clusters": (_i32, [_u64, _i32, _i32, _d, _d, _d, _vp]),

@@ -155,6 +155,31 @@ int64_t ref_md_run_bvh(const ref_md_params* p, int32_t n, double* x, double* v, 
 
 int ref_num_threads(void);
 
+/* ------------------------------------------------ differentiable trajectory */
+
+/* Loss of a trajectory: steps of kick-drift-kick, then the Gaussian-smoothed
+ * pair-distance histogram of the final positions (bins on [0, r_max], width
+ * `width`, pair weights switched to 0 between r_switch and r_max) against a
+ * target, L = sum_b (h_b - target_b)^2.  See naiveadj.c. */
+typedef struct {
+    int32_t steps;
+    int32_t bins;
+    double r_max;
+    double width;
+    double r_switch;
+} ref_adj_spec;
+
+/*
+ * Forward-mode (dual-number) evaluation of the loss: value and its derivatives
+ * dloss[0] = dL/dsigma, dloss[1] = dL/depsilon, dloss[2] = the directional
+ * derivative along (dx0, dv0) (either may be NULL = 0).  target may be NULL
+ * (zeros).  hist (bins), x_out, v_out (N x 3), events (2) may be NULL.
+ */
+int ref_adj_dual(const ref_md_params* p, const ref_adj_spec* s, int32_t n, const double* x0,
+                 const double* v0, const double* q, const double* m, const double* dx0,
+                 const double* dv0, const double* target, double* hist, double* loss,
+                 double dloss[3], double* x_out, double* v_out, uint64_t events[2]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,12 @@ class OracleError(RuntimeError):
     pass
 
 
+class RefAdjSpec(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int32), ("bins", ctypes.c_int32),
+                ("r_max", ctypes.c_double), ("width", ctypes.c_double),
+                ("r_switch", ctypes.c_double)]
+
+
 class RefMDParams(ctypes.Structure):
     _fields_ = [("sigma", ctypes.c_double), ("epsilon", ctypes.c_double),
                 ("coulomb_k", ctypes.c_double), ("cutoff", ctypes.c_double),
@@ -101,6 +107,10 @@ def lib():
                                          f64p, f64p, f64p, f64p, ctypes.c_int64, ctypes.c_int32,
                                          ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
             L.ref_md_run_bvh.restype = ctypes.c_int64
+            L.ref_adj_dual.argtypes = [ctypes.POINTER(RefMDParams), ctypes.POINTER(RefAdjSpec),
+                                       ctypes.c_int32, f64p, f64p, f64p, f64p, f64p, f64p, f64p,
+                                       f64p, f64p, f64p, f64p, f64p, u64p]
+            L.ref_adj_dual.restype = ctypes.c_int
             L.ref_num_threads.argtypes = []
             L.ref_num_threads.restype = ctypes.c_int
             _lib = L
@@ -290,3 +300,37 @@ def md_run_bvh(p, x, v, q=None, m=None, steps=1, rebuild=10, skin=0.3, apl=4,
 
 def num_threads():
     return int(lib().ref_num_threads())
+
+
+def adj_spec(steps, bins=64, r_max=2.5, width=None, r_switch=None):
+    """Histogram-loss specification: width defaults to the bin width, the pair
+    weight switch starts at r_max - 0.25 (r_max - 4 widths at most)."""
+    s = RefAdjSpec()
+    s.steps, s.bins, s.r_max = steps, bins, r_max
+    s.width = r_max / bins if width is None else width
+    s.r_switch = (r_max - 0.25) if r_switch is None else r_switch
+    return s
+
+
+def adj_dual(p, s, x0, v0, q=None, m=None, dx0=None, dv0=None, target=None):
+    """Forward-mode FP64 loss of a trajectory (dual numbers).  Returns dict with
+    loss, dloss = (dL/dsigma, dL/depsilon, directional derivative along
+    (dx0, dv0)), hist, x, v (final state) and events (branch signature)."""
+    x0 = np.ascontiguousarray(x0, np.float64).reshape(-1, 3)
+    v0 = np.ascontiguousarray(v0, np.float64).reshape(-1, 3)
+    n = x0.shape[0]
+    c = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+    q, m, dx0, dv0, target = c(q), c(m), c(dx0), c(dv0), c(target)
+    hist = np.empty(s.bins, np.float64)
+    loss = ctypes.c_double()
+    dl = np.empty(3, np.float64)
+    xo = np.empty_like(x0)
+    vo = np.empty_like(v0)
+    ev = np.zeros(2, np.uint64)
+    f64 = ctypes.c_double
+    _check(lib().ref_adj_dual(ctypes.byref(p), ctypes.byref(s), n, _p(x0, f64), _p(v0, f64),
+                              _p(q, f64), _p(m, f64), _p(dx0, f64), _p(dv0, f64),
+                              _p(target, f64), _p(hist, f64), ctypes.byref(loss), _p(dl, f64),
+                              _p(xo, f64), _p(vo, f64), _p(ev, ctypes.c_uint64)))
+    return dict(loss=loss.value, dloss=dl, hist=hist, x=xo, v=vo,
+                events=(int(ev[0]), int(ev[1])))
