@@ -252,11 +252,69 @@ def batched_leg(nd, ctx, ext, flush):
             "plain_path": "512 nd_md engines run one after another on one stream (graphs)"}
 
 
+STRESS_N = 4194304
+
+
+def stress_leg(nd, ctx, ext, flush, steps=3, cpu=True, points=STRESS_N):
+    """Neighbour-search stress: 4,194,304 Float32 points in 64 isotropic
+    Gaussian clusters (centres uniform in a cube of side 400, sigma U[2, 10]),
+    r = 2.5, LBVH build + traversal + emission of the half pair list (i, j, d)
+    into device memory (nd_leaf_pairs_dev, spatial order, one-pass emission),
+    inputs resident, L2 flushed before each call.  cpu: the oracle's leaf-BVH
+    build + order-free hash traversal of the same points on all host cores."""
+    import numpy as np
+    import torch
+
+    x = nd.synth.cluster_positions(nd.synth.SEED_NS_STRESS, points, 64, 400.0, 2.0, 10.0)
+    spec = nd.SpheresBVHSpecs(2.5, points, 4)
+    xt = torch.from_numpy(x).cuda()
+    st, cnt = nd.neighbor_pairs_dev(xt, spec, None, None, None, 0, ctx=ctx)
+    pi = torch.empty(cnt, dtype=torch.int32, device="cuda")
+    pj = torch.empty(cnt, dtype=torch.int32, device="cuda")
+    pd = torch.empty(cnt, dtype=torch.float32, device="cuda")
+    times = []
+    for k in range(steps + 1):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            a.record(ext)
+            st, c2 = nd.neighbor_pairs_dev(xt, spec, pi, pj, pd, cnt, ctx=ctx)
+            b.record(ext)
+        torch.cuda.synchronize()
+        assert st == 0 and c2 == cnt
+        if k > 0:
+            times.append(a.elapsed_time(b))
+    h = nd.pair_hash_dev(pi, pj, pd, cnt, ctx=ctx)
+    del pi, pj, pd
+    torch.cuda.empty_cache()
+    ms = float(np.median(times))
+    out = {"metric": "neighbour-search pairs/s (LBVH build + traversal + emission)",
+           "unit": "pairs/s",
+           "workload": (f"ns_stress_{points}: 64 Gaussian clusters x {points // 64} Float32 points, "
+                        "centres U[0,400)^3, sigma U[2,10], r 2.5, atomsperleaf 4, spatial order, "
+                        "half list (i, j, d) written to device memory"),
+           "value": cnt / (ms * 1e-3), "pairs": cnt, "ms_per_call": ms,
+           "bytes_written_per_pair": 12, "pair_hash": [str(h[0]), str(h[1])]}
+    if cpu:
+        from oracle import naiveref as R
+        t0 = time.perf_counter()
+        t = R.tree(x, 2.5, 4, order=1)
+        cnt_ref, h_ref = R.leaf_traverse_hash(t, 2.5, 4)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": cnt_ref / cs, "unit": "pairs/s", "cores": R.num_threads(),
+                               "kind": "port",
+                               "sample": (f"oracle leafTreeData + leafneighbor_traverse of the same "
+                                          f"{points} points (pairs hashed, not stored), {cs:.2f} s")}
+        out["pairs_and_hash_equal_cpu"] = bool(cnt_ref == cnt and tuple(h_ref) == tuple(h))
+    return out
+
+
 ADJ_N = 32768
 ADJ_STEPS = 1000
 
 
-def adjoint_leg(nd, ctx, ext, flush):
+def adjoint_leg(nd, ctx, ext, flush, steps=ADJ_STEPS):
     """Differentiable trajectory: 32,768 LJ atoms at density 0.83 (cube side
     (N/0.83)^(1/3), min separation 0.8), 1000 steps dt 1e-3, loss = squared
     deviation of the Gaussian-smoothed pair-distance histogram (64 bins on
@@ -272,7 +330,7 @@ def adjoint_leg(nd, ctx, ext, flush):
     x, v, _ = nd.synth.lj_system(nd.synth.SEED_ADJOINT, ADJ_N, side, 0.8)
     mp = nd.md_params(sigma=1.05, epsilon=0.9, cutoff=2.5, skin=0.3, dt=1e-3,
                       box_hi=(side,) * 3, atomsperleaf=4, rebuild_every=REBUILD, resort_every=5)
-    adj = nd.Adjoint(mp, nd.adj_spec(ADJ_STEPS, checkpoint_every=50), x, v, ctx=ctx)
+    adj = nd.Adjoint(mp, nd.adj_spec(steps, checkpoint_every=50), x, v, ctx=ctx)
     _, target = adj.forward()
     adj.set_params(1.0, 1.0)
     adj.set_target(target)
@@ -297,7 +355,7 @@ def adjoint_leg(nd, ctx, ext, flush):
     torch.cuda.synchronize()
     with torch.cuda.stream(ext):
         a.record(ext)
-        eng.run(ADJ_STEPS)
+        eng.run(steps)
         b.record(ext)
     eng.sync()
     plain_ms = a.elapsed_time(b)
@@ -305,13 +363,13 @@ def adjoint_leg(nd, ctx, ext, flush):
     f_ms, b_ms = float(np.median(fwd)), float(np.median(bwd))
     return {"metric": "adjoint step time / forward step time", "unit": "ratio",
             "workload": (f"adjoint_32768: N={ADJ_N} LJ, cube side {side:.2f} (density 0.83), "
-                         f"{ADJ_STEPS} steps dt 1e-3, histogram loss (64 bins on [0, 2.5], "
+                         f"{steps} steps dt 1e-3, histogram loss (64 bins on [0, 2.5], "
                          "Gaussian width = bin width) vs the sigma 1.05 / eps 0.9 run, "
                          "checkpoints every 50 steps, skin 0.3, rebuild every 10"),
-            "value": b_ms / f_ms, "forward_ms_per_step": f_ms / ADJ_STEPS,
-            "adjoint_ms_per_step": b_ms / ADJ_STEPS,
-            "plain_engine_ms_per_step": plain_ms / ADJ_STEPS,
-            "adjoint_over_plain_forward": (b_ms / ADJ_STEPS) / (plain_ms / ADJ_STEPS),
+            "value": b_ms / f_ms, "forward_ms_per_step": f_ms / steps,
+            "adjoint_ms_per_step": b_ms / steps,
+            "plain_engine_ms_per_step": plain_ms / steps,
+            "adjoint_over_plain_forward": (b_ms / steps) / (plain_ms / steps),
             "loss": loss, "dL_dsigma": g["sigma"], "dL_depsilon": g["epsilon"],
             "dL_dx0_norm": float(np.linalg.norm(g["x0"])),
             "target": "<= 3 (adjoint step vs forward step)"}
@@ -468,7 +526,9 @@ def run_gb300(args):
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_leg(nd, ctx, ext, flush)
     if rank == 0 and not args.no_adjoint:
-        line["adjoint"] = adjoint_leg(nd, ctx, ext, flush)
+        line["adjoint"] = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps)
+    if rank == 0 and not args.no_stress:
+        line["ns_stress"] = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(steps=10)
     if rank == 0:
@@ -476,6 +536,25 @@ def run_gb300(args):
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_only(args):
+    import torch
+    import naivedynamics as nd
+
+    torch.cuda.set_device(0)
+    ctx = nd.Context(0)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    if args.only == "batched":
+        out = batched_leg(nd, ctx, ext, flush)
+    elif args.only == "adjoint":
+        out = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps)
+    else:
+        out = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline,
+                         points=args.stress_points)
+    print(json.dumps(out), flush=True)
+    ctx.close()
 
 
 def main():
@@ -489,11 +568,22 @@ def main():
                     help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the adjoint (differentiable trajectory) measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=ADJ_STEPS,
+                    help="MD steps of the adjoint measurement (a multiple of 50)")
+    ap.add_argument("--no-stress", action="store_true",
+                    help="skip the neighbour-search stress measurement")
+    ap.add_argument("--stress-points", type=int, default=STRESS_N,
+                    help="points of the stress measurement with --only stress (64 clusters)")
+    ap.add_argument("--only", choices=["batched", "adjoint", "stress"],
+                    help="run one secondary measurement alone and print its JSON object "
+                         "(for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.only:
+        run_only(args)
     else:
         run_gb300(args)
 

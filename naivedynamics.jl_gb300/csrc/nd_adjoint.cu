@@ -41,6 +41,7 @@
 namespace nd {
 
 constexpr int kHistChunk = 16;  // histogram bins a thread accumulates per pass
+constexpr int kAdjTPA = 4;      // threads per atom in the reverse step
 
 struct AdjArgs {
     int32_t n, apl, ucap, smrec;
@@ -49,8 +50,8 @@ struct AdjArgs {
     const uint16_t* __restrict__ llist;
     const int32_t* __restrict__ ncount;
     int32_t lcap;
-    const double* xt[3];  // positions of the step (sorted order)
-    const double* __restrict__ q;
+    const double* xt[3];  // positions of the step (sorted order; the wall masks)
+    const int4* __restrict__ recs;  // their fixed-point records (x, y, z, charge bits)
     const double* __restrict__ im;
     const float4* __restrict__ g4_in;
     float4* __restrict__ g4_out;
@@ -59,8 +60,6 @@ struct AdjArgs {
     double* lx0[3];  // last reverse step: dL/dx0, dL/dv0 (sorted order)
     double* lv0[3];
     double* __restrict__ gpart;  // per block: [0] dL/dsigma, [1] dL/deps partial sums
-    double o[3];
-    double S;
     float invS;
     double lo[3], hi[3];
     float rc2, sig2, eps24, kc;
@@ -75,15 +74,6 @@ struct AdjArgs {
     const float* __restrict__ cb;   // bins: 2 (h_b - target_b) / N
     int32_t* err;
 };
-
-__device__ __forceinline__ int4 adj_rec(const AdjArgs& a, int64_t k) {
-    int4 r;
-    r.x = to_fixed(a.xt[0][k], a.o[0], a.S, a.err, (int32_t)k);
-    r.y = to_fixed(a.xt[1][k], a.o[1], a.S, a.err, (int32_t)k);
-    r.z = to_fixed(a.xt[2][k], a.o[2], a.S, a.err, (int32_t)k);
-    r.w = __float_as_int(a.q ? (float)a.q[k] : 0.0f);
-    return r;
-}
 
 // Atom index (sorted) of union entry li of the block's union U.
 __device__ __forceinline__ int64_t adj_atom(const int32_t* __restrict__ U, int32_t li, int32_t apl) {
@@ -126,10 +116,12 @@ __device__ __forceinline__ void hvp_pair(const AdjArgs& a, const int4& ri, const
     hv.z += g * ez + rd * dz;
 }
 
-// Fixed-order block sum of two values; thread 0 adds them to this block's
-// partials (one writer per block and launches in stream order: deterministic).
+// Fixed-order block sum of two values over NT threads; thread 0 adds them to
+// this block's partials (one writer per block and launches in stream order:
+// deterministic).
+template <int NT>
 __device__ __forceinline__ void block_add2(double v0, double v1, double* part) {
-    __shared__ double s[2][kBlock / 32];
+    __shared__ double s[2][NT / 32];
     for (int sh = 16; sh > 0; sh >>= 1) {
         v0 += __shfl_xor_sync(0xffffffffu, v0, sh);
         v1 += __shfl_xor_sync(0xffffffffu, v1, sh);
@@ -139,7 +131,7 @@ __device__ __forceinline__ void block_add2(double v0, double v1, double* part) {
     __syncthreads();
     if (threadIdx.x == 0) {
         double t0 = 0.0, t1 = 0.0;
-        for (int w = 0; w < kBlock / 32; ++w) { t0 += s[0][w]; t1 += s[1][w]; }
+        for (int w = 0; w < NT / 32; ++w) { t0 += s[0][w]; t1 += s[1][w]; }
         part[2 * blockIdx.x] += t0;
         part[2 * blockIdx.x + 1] += t1;
     }
@@ -166,37 +158,43 @@ __device__ __forceinline__ void adj_prepare(const AdjArgs& a, int64_t i, const d
     a.g4_out[i] = g4;
 }
 
-// One reverse step.  One block per 256 atoms, the forward step's union is
-// staged (fixed-point position records of x_t and the Float32 velocity
-// adjoints) and each thread gathers over its atom's list.
+// One reverse step.  One block per 256 atoms and kAdjTPA threads per atom:
+// the forward step's union is staged (the step's fixed-point position records
+// and the Float32 velocity adjoints), thread p of an atom gathers over list
+// slots p, p + kAdjTPA, ..., and the slices are added in a fixed order.
 template <bool COUL>
-__global__ void __launch_bounds__(kBlock, 2) k_adj_reverse(AdjArgs a) {
+__global__ void __launch_bounds__(kBlock * kAdjTPA) k_adj_reverse(AdjArgs a) {
     extern __shared__ int4 adj_smem[];
     int4* srec = adj_smem;
     float4* sg = reinterpret_cast<float4*>(adj_smem + a.smrec);
+    __shared__ float spart[kAdjTPA - 1][5][kBlock];
     const int tid = threadIdx.x;
-    int64_t i = (int64_t)blockIdx.x * kBlock + tid;
+    const int al = tid & (kBlock - 1);  // atom within the block
+    const int part = tid / kBlock;      // list slice
+    int64_t i = (int64_t)blockIdx.x * kBlock + al;
     const bool valid = i < a.n;
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
     {
         const int32_t nu = min(__ldg(&a.ucount[blockIdx.x]), a.ucap);
         const int32_t m = min(nu * a.apl, a.smrec);
-        for (int32_t k = tid; k < m; k += kBlock) {
+        for (int32_t k = tid; k < m; k += kBlock * kAdjTPA) {
             const int64_t at = adj_atom(U, k, a.apl);
-            srec[k] = adj_rec(a, at);
+            srec[k] = __ldg(&a.recs[at]);
             sg[k] = a.g4_in[at];
         }
     }
     __syncthreads();
     if (!valid) i = a.n - 1;
-    const int4 ri = adj_rec(a, i);
+    const int4 ri = __ldg(&a.recs[i]);
     const float4 gi = a.g4_in[i];
     const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
-    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
+    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + al;
     float3 hv = make_float3(0.f, 0.f, 0.f);
     float eacc = 0.f, sacc = 0.f;
-    for (int32_t s = 0; s < cnt; ++s) {
-        const int32_t li = L[(int64_t)s * kBlock];
+    int32_t li = part < cnt ? L[(int64_t)part * kBlock] : 0;
+    for (int32_t s = part; s < cnt; s += kAdjTPA) {
+        const int32_t sn = s + kAdjTPA;
+        const int32_t next = sn < cnt ? L[(int64_t)sn * kBlock] : 0;
         int4 rj;
         float4 gj;
         if (li < a.smrec) {
@@ -204,13 +202,30 @@ __global__ void __launch_bounds__(kBlock, 2) k_adj_reverse(AdjArgs a) {
             gj = sg[li];
         } else {
             const int64_t at = adj_atom(U, li, a.apl);
-            rj = adj_rec(a, at);
+            rj = __ldg(&a.recs[at]);
             gj = a.g4_in[at];
         }
         hvp_pair<COUL>(a, ri, gi, rj, gj, hv, eacc, sacc);
+        li = next;
     }
+    if (part > 0) {
+        spart[part - 1][0][al] = hv.x;
+        spart[part - 1][1][al] = hv.y;
+        spart[part - 1][2][al] = hv.z;
+        spart[part - 1][3][al] = eacc;
+        spart[part - 1][4][al] = sacc;
+    }
+    __syncthreads();
     double te = 0.0, ts = 0.0;
-    if (valid) {
+    if (part == 0 && valid) {
+#pragma unroll
+        for (int p = 0; p < kAdjTPA - 1; ++p) {
+            hv.x += spart[p][0][al];
+            hv.y += spart[p][1][al];
+            hv.z += spart[p][2][al];
+            eacc += spart[p][3][al];
+            sacc += spart[p][4][al];
+        }
         const double k = a.ckdt * a.im[i];
         const double lx[3] = {a.abar[0][i] + k * (double)hv.x, a.abar[1][i] + k * (double)hv.y,
                               a.abar[2][i] + k * (double)hv.z};
@@ -224,7 +239,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_adj_reverse(AdjArgs a) {
             adj_prepare(a, i, lx, lu);
         }
     }
-    block_add2(ts, te, a.gpart);
+    block_add2<kBlock * kAdjTPA>(ts, te, a.gpart);
 }
 
 // Smooth pair weight of the histogram: 1 below r_switch, C2 switch to 0 at r_max.
@@ -246,7 +261,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_hist(AdjArgs a) {
     const int64_t i = (int64_t)blockIdx.x * kBlock + tid;
     if (i >= a.n) return;
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
-    const int4 ri = adj_rec(a, i);
+    const int4 ri = __ldg(&a.recs[i]);
     const int32_t cnt = __ldg(&a.ncount[i]);
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
     for (int32_t b0 = 0; b0 < a.bins; b0 += kHistChunk) {
@@ -256,7 +271,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_hist(AdjArgs a) {
         for (int32_t s = 0; s < cnt; ++s) {
             const int64_t j = adj_atom(U, L[(int64_t)s * kBlock], a.apl);
             if (j <= i) continue;
-            const int4 rj = adj_rec(a, j);
+            const int4 rj = __ldg(&a.recs[j]);
             const float dx = (float)(ri.x - rj.x) * a.invS;
             const float dy = (float)(ri.y - rj.y) * a.invS;
             const float dz = (float)(ri.z - rj.z) * a.invS;
@@ -317,13 +332,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_terminal(AdjArgs a) {
     const int64_t i = (int64_t)blockIdx.x * kBlock + tid;
     if (i >= a.n) return;
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
-    const int4 ri = adj_rec(a, i);
+    const int4 ri = __ldg(&a.recs[i]);
     const int32_t cnt = __ldg(&a.ncount[i]);
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
     float gx = 0.f, gy = 0.f, gz = 0.f;
     for (int32_t s = 0; s < cnt; ++s) {
         const int64_t j = adj_atom(U, L[(int64_t)s * kBlock], a.apl);
-        const int4 rj = adj_rec(a, j);
+        const int4 rj = __ldg(&a.recs[j]);
         const float dx = (float)(ri.x - rj.x) * a.invS;
         const float dy = (float)(ri.y - rj.y) * a.invS;
         const float dz = (float)(ri.z - rj.z) * a.invS;
@@ -407,7 +422,7 @@ struct AdjEngine {
     int32_t n = 0, K = 0, C = 0, R = 0, Q = 0, nseg = 0, nsort = 0;
     int32_t smrec = 0;
     size_t rev_smem = 0, ckpt_bytes = 0;
-    DevBuf ckpt, perms, codes, statics, traj, lam, lam_tmp, g4[2], gpart, xK, hatom, hist, target,
+    DevBuf ckpt, perms, codes, statics, traj, trajrec, recK, lam, lam_tmp, g4[2], gpart, xK, hatom, hist, target,
         cb, scal, outs, flags;
     bool timed[2] = {false, false};  // forward / backward events recorded
     bool have_forward = false;
@@ -419,7 +434,11 @@ struct AdjEngine {
 
 static double* lam_p(AdjEngine* A) { return (double*)A->lam.p; }
 
-static AdjArgs adj_args(AdjEngine* A, const double* xt) {
+static bool adj_coulomb(const AdjEngine* A) {
+    return A->m->has_q && A->m->p.coulomb_k != 0.0;
+}
+
+static AdjArgs adj_args(AdjEngine* A, const double* xt, const int4* recs) {
     MDEngine* m = A->m;
     AdjArgs a{};
     a.n = m->n;
@@ -433,7 +452,7 @@ static AdjArgs adj_args(AdjEngine* A, const double* xt) {
     a.lcap = m->lcap;
     const size_t n = (size_t)m->n;
     for (int d = 0; d < 3; ++d) a.xt[d] = xt + d * n;
-    a.q = m->has_q && m->p.coulomb_k != 0.0 ? m->set[0].q : nullptr;
+    a.recs = recs;
     a.im = m->set[0].im;
     double* L = lam_p(A);
     for (int d = 0; d < 3; ++d) {
@@ -444,11 +463,9 @@ static AdjArgs adj_args(AdjEngine* A, const double* xt) {
     }
     a.gpart = (double*)A->gpart.p;
     for (int d = 0; d < 3; ++d) {
-        a.o[d] = m->fr.o[d];
         a.lo[d] = m->p.box_lo[d];
         a.hi[d] = m->p.box_hi[d];
     }
-    a.S = m->fr.s;
     a.invS = (float)(1.0 / m->fr.s);
     const nd_md_params& p = m->p;
     a.rc2 = (float)(p.cutoff * p.cutoff);
@@ -557,8 +574,10 @@ static nd_status adj_enqueue_forward(AdjEngine* A) {
              })))
             return st;
     }
-    if ((st = adj_copy(A, A->xK.p, live_set(A), 3 * sizeof(double) * n, "x_K"))) return st;
-    AdjArgs a = adj_args(A, (const double*)A->xK.p);
+    if ((st = adj_copy(A, A->xK.p, live_set(A), 3 * sizeof(double) * n, "x_K")) ||
+        (st = adj_copy(A, A->recK.p, m->rec_buf[m->rc].p, sizeof(int4) * n, "x_K records")))
+        return st;
+    AdjArgs a = adj_args(A, (const double*)A->xK.p, (const int4*)A->recK.p);
     const unsigned nb = (unsigned)m->nblocks;
     k_adj_hist<<<nb, kBlock, 0, c->stream>>>(a);
     k_adj_hist_reduce<<<(unsigned)A->s.bins, 256, 0, c->stream>>>((const float*)A->hatom.p, A->n,
@@ -581,11 +600,12 @@ static nd_status adj_enqueue_backward(AdjEngine* A) {
     const unsigned g256 = (unsigned)cdiv(A->n, 256);
     char* ck = (char*)A->ckpt.p;
     double* traj = (double*)A->traj.p;
+    int4* trec = (int4*)A->trajrec.p;
     const std::vector<uint8_t>& sched = A->sched;
     cudaMemsetAsync(A->gpart.p, 0, 2 * sizeof(double) * nb, c->stream);
     int gc = 0;  // g4 buffer holding g of the next reverse step
     {
-        AdjArgs a = adj_args(A, (const double*)A->xK.p);
+        AdjArgs a = adj_args(A, (const double*)A->xK.p, (const int4*)A->recK.p);
         a.g4_out = (float4*)A->g4[gc].p;
         k_adj_terminal<<<nb, kBlock, sizeof(float) * (size_t)A->s.bins, c->stream>>>(a);
         c->launches++;
@@ -597,7 +617,8 @@ static nd_status adj_enqueue_backward(AdjEngine* A) {
             const int32_t t = t0 + k;
             if ((st = adj_rebuild_before(A, t, false))) return st;
             if (t % A->R != 0 && sched[t - 1] && (st = md_rebuild(m, RB_REFIT, m->rc))) return st;
-            if ((st = adj_copy(A, traj + k * 3 * n, live_set(A), 3 * sizeof(double) * n, "trajectory")))
+            if ((st = adj_copy(A, traj + k * 3 * n, live_set(A), 3 * sizeof(double) * n, "trajectory")) ||
+                (st = adj_copy(A, trec + k * n, m->rec_buf[m->rc].p, sizeof(int4) * n, "records")))
                 return st;
             if (k < A->C - 1) adj_step(A, t == 0);
         }
@@ -620,13 +641,14 @@ static nd_status adj_enqueue_backward(AdjEngine* A) {
                     return st;
                 if ((st = md_rebuild(m, RB_REFIT))) return st;
                 for (int32_t t = e - 1; t >= s; --t) {
-                    AdjArgs a = adj_args(A, traj + (t - t0) * 3 * n);
+                    AdjArgs a = adj_args(A, traj + (t - t0) * 3 * n, trec + (t - t0) * n);
                     a.g4_in = (const float4*)A->g4[gc].p;
                     a.g4_out = (float4*)A->g4[gc ^ 1].p;
                     a.ckdt = (t == 0 ? 0.5 : 1.0) * m->p.dt;
                     a.last = t == 0 ? 1 : 0;
-                    if (a.q) k_adj_reverse<true><<<nb, kBlock, A->rev_smem, c->stream>>>(a);
-                    else k_adj_reverse<false><<<nb, kBlock, A->rev_smem, c->stream>>>(a);
+                    const unsigned nt = kBlock * kAdjTPA;
+                    if (adj_coulomb(A)) k_adj_reverse<true><<<nb, nt, A->rev_smem, c->stream>>>(a);
+                    else k_adj_reverse<false><<<nb, nt, A->rev_smem, c->stream>>>(a);
                     c->launches++;
                     gc ^= 1;
                 }
@@ -686,7 +708,7 @@ nd_status adj_destroy(AdjEngine* A) {
     adj_drop_graphs(A);
     for (cudaEvent_t e : A->ev)
         if (e) cudaEventDestroy(e);
-    DevBuf* bufs[] = {&A->ckpt, &A->perms, &A->codes, &A->statics, &A->traj, &A->lam, &A->lam_tmp, &A->g4[0],
+    DevBuf* bufs[] = {&A->ckpt, &A->perms, &A->codes, &A->statics, &A->traj, &A->trajrec, &A->recK, &A->lam, &A->lam_tmp, &A->g4[0],
                       &A->g4[1], &A->gpart, &A->xK, &A->hatom, &A->hist, &A->target, &A->cb,
                       &A->scal, &A->outs, &A->flags};
     for (DevBuf* b : bufs)
@@ -730,7 +752,10 @@ nd_status adj_create(Ctx* parent, const nd_md_params* p, int32_t n, const double
     A->ckpt_bytes = (A->ckpt_bytes + 255) / 256 * 256;
     int maxsm = 0;
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-    A->smrec = std::max(0, std::min(m->ucap_sm * m->apl, (maxsm - 2048) / 32));
+    // dynamic: 32 B per staged union atom; static: the slice partials and the
+    // block reduction
+    const int static_sm = (int)(sizeof(float) * 5 * kBlock * (kAdjTPA - 1)) + 2048;
+    A->smrec = std::max(0, std::min(m->ucap_sm * m->apl, (maxsm - static_sm) / 32));
     A->rev_smem = 32 * (size_t)A->smrec;
     cudaError_t e = cudaFuncSetAttribute((const void*)k_adj_reverse<true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A->rev_smem);
@@ -744,6 +769,8 @@ nd_status adj_create(Ctx* parent, const nd_md_params* p, int32_t n, const double
         (st = ensure(c, A->codes, sizeof(int32_t) * nn * A->nsort)) ||
         (st = ensure(c, A->statics, adj_statics_bytes(A) * A->nsort)) ||
         (st = ensure(c, A->traj, 3 * sizeof(double) * nn * A->C)) ||
+        (st = ensure(c, A->trajrec, sizeof(int4) * nn * A->C)) ||
+        (st = ensure(c, A->recK, sizeof(int4) * nn)) ||
         (st = ensure(c, A->lam, 6 * sizeof(double) * nn)) ||
         (st = ensure(c, A->lam_tmp, 6 * sizeof(double) * nn)) ||
         (st = ensure(c, A->g4[0], sizeof(float4) * nn)) ||

@@ -763,74 +763,146 @@ __global__ void __launch_bounds__(128)
     leaf_query<APL>(q, keys, pos, apl, r2, 2 * nL - 1, err, s);
 }
 
-// One-pass emission: pairs of one leaf-vs-leaf test are staged in registers
-// and a warp-aggregated atomicAdd reserves their slots.
-struct SinkStage {
-    int32_t i[16], j[16];
-    float d[16];
-    int n = 0;
-    __device__ __forceinline__ void push(int32_t a, int32_t b, float dd) {
-        i[n] = a; j[n] = b; d[n] = dd; ++n;
-    }
-};
+// One-pass emission, warp-cooperative (atomsperleaf 4; the pair multiset of
+// leafneighbor_traverse in an order decided at run time).  A warp
+// takes 32 consecutive query leaves and walks the tree ONCE, from the skip
+// rope of its first leaf, pruning with the union of its lanes' boxes; at
+// every leaf t it reaches, each lane runs leafneighbor_traverse's leaf test
+// for its own leaf q (t > q, strict box overlap -- the leaves a rope walk
+// from q's skip would accept, since a box overlapping t overlaps all of t's
+// ancestors) and the 4 x 4 distance tests.  Lanes stay converged, node loads
+// are broadcast, and the pairs are ballot-compacted into a shared-memory
+// buffer per warp that is written out with one atomic reservation and
+// coalesced stores.
+constexpr int kWarpBuf = 1024;  // buffered pairs per warp
 
-__device__ __forceinline__ void flush_stage(SinkStage& s, unsigned long long* cursor,
-                                            int64_t cap, int32_t* pi, int32_t* pj, float* pd) {
-    // Counts are <= 16, so the exclusive prefix over the active lanes is the sum
-    // of five ballot bit-planes; valid for any set of converged lanes.
-    const unsigned m = __activemask();
+__device__ __forceinline__ void warp_buf_flush(int32_t* bi, int32_t* bj, float* bd, int& nb,
+                                               unsigned long long* cursor, int64_t cap,
+                                               int32_t* pi, int32_t* pj, float* pd) {
     const int lane = threadIdx.x & 31;
-    const unsigned below = m & ((1u << lane) - 1u);
-    const unsigned cnt = (unsigned)s.n;
+    unsigned long long base = 0;
+    if (lane == 0 && nb) base = atomicAdd(cursor, (unsigned long long)nb);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (int k = lane; k < nb; k += 32) {
+        const unsigned long long w = base + (unsigned long long)k;
+        if ((int64_t)w < cap) { pi[w] = bi[k]; pj[w] = bj[k]; pd[w] = bd[k]; }
+    }
+    __syncwarp();
+    nb = 0;
+}
+
+// Appends this lane's hits (bit k of mask = pair (qa[k / 4], tb[k % 4]), d2[k]
+// its squared distance) to the warp's buffer: the lanes' offsets are the
+// exclusive prefix of their hit counts (<= 16, so five ballot bit planes).
+__device__ __forceinline__ void warp_emit16(unsigned mask, const float4 (&qa)[4],
+                                            const float4 (&tb)[4], const float (&d2)[16],
+                                            int32_t* bi, int32_t* bj, float* bd, int& nb,
+                                            unsigned long long* cursor, int64_t cap, int32_t* pi,
+                                            int32_t* pj, float* pd) {
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const unsigned cnt = (unsigned)__popc(mask);
     unsigned pre = 0, total = 0;
 #pragma unroll
     for (int b = 0; b < 5; ++b) {
-        unsigned plane = __ballot_sync(m, (cnt >> b) & 1u);
+        const unsigned plane = __ballot_sync(0xffffffffu, (cnt >> b) & 1u);
         pre += (unsigned)__popc(plane & below) << b;
         total += (unsigned)__popc(plane) << b;
     }
-    const int leader = __ffs(m) - 1;
-    unsigned long long base = 0;
-    if (lane == leader && total) base = atomicAdd(cursor, (unsigned long long)total);
-    base = __shfl_sync(m, base, leader);
-    unsigned long long w = base + pre;
-    for (int k = 0; k < s.n; ++k, ++w) {
-        if ((int64_t)w < cap) { pi[w] = s.i[k]; pj[w] = s.j[k]; pd[w] = s.d[k]; }
+    if (total == 0) return;
+    if (nb + (int)total > kWarpBuf) warp_buf_flush(bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+    int at = nb + (int)pre;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        if (mask & (1u << k)) {
+            bi[at] = __float_as_int(qa[k >> 2].w);
+            bj[at] = __float_as_int(tb[k & 3].w);
+            bd[at] = __fsqrt_rn(d2[k]);
+            ++at;
+        }
     }
-    s.n = 0;
+    __syncwarp();
+    nb += (int)total;
 }
 
 __global__ void __launch_bounds__(128)
-    k_leaf_unordered4(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
-                      float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
-                      float* pd, int32_t* err) {
-    int32_t q = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (q > nL) return;
+    k_leaf_warp4(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
+                 float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
+                 float* pd, int32_t* err) {
     constexpr int APL = 4;
-    Node ql = load_node(keys, q);
-    int64_t A = (int64_t)(q - 1) * APL;
+    __shared__ int32_t sbi[4][kWarpBuf], sbj[4][kWarpBuf];
+    __shared__ float sbd[4][kWarpBuf];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int32_t q0 = (int32_t)((blockIdx.x * 4 + w) * 32) + 1;
+    if (q0 > nL) return;  // whole warp
+    int32_t* bi = sbi[w];
+    int32_t* bj = sbj[w];
+    float* bd = sbd[w];
+    const int32_t q = q0 + lane;
+    const bool valid = q <= nL;
+    Node ql;
     float4 qa[APL];
+    if (valid) {
+        ql = load_node(keys, q);
+        const int64_t A = (int64_t)(q - 1) * APL;
 #pragma unroll
-    for (int i = 0; i < APL; ++i) qa[i] = __ldg(&pos[A + i]);
-    SinkStage s;
+        for (int i = 0; i < APL; ++i) qa[i] = __ldg(&pos[A + i]);
+    } else {
+        ql.mnx = ql.mny = ql.mnz = INFINITY;
+        ql.mxx = ql.mxy = ql.mxz = -INFINITY;
+        ql.left = ql.skip = 0;
 #pragma unroll
-    for (int i = 0; i < APL - 1; ++i)
+        for (int i = 0; i < APL; ++i) qa[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    int nb = 0;
+    float d2[16];
+    unsigned mask = 0;
+    // intra-leaf pairs (a before b in the leaf)
 #pragma unroll
-        for (int j = i + 1; j < APL; ++j) {
-            float d2 = dist2_ref(qa[i].x, qa[i].y, qa[i].z, qa[j].x, qa[j].y, qa[j].z);
-            if (d2 < r2) s.push(__float_as_int(qa[i].w), __float_as_int(qa[j].w), __fsqrt_rn(d2));
+    for (int k = 0; k < 16; ++k) {
+        const int i = k >> 2, j = k & 3;
+        d2[k] = 0.0f;
+        if (j > i) {
+            d2[k] = dist2_ref(qa[i].x, qa[i].y, qa[i].z, qa[j].x, qa[j].y, qa[j].z);
+            if (valid && d2[k] < r2) mask |= 1u << k;
         }
-    flush_stage(s, cursor, cap, pi, pj, pd);
-    int32_t t = ql.skip;
+    }
+    warp_emit16(mask, qa, qa, d2, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+    // the warp's union box (invalid lanes contribute the empty box)
+    Node un = ql;
+    for (int sh = 16; sh > 0; sh >>= 1) {
+        un.mnx = fminf(un.mnx, __shfl_xor_sync(0xffffffffu, un.mnx, sh));
+        un.mny = fminf(un.mny, __shfl_xor_sync(0xffffffffu, un.mny, sh));
+        un.mnz = fminf(un.mnz, __shfl_xor_sync(0xffffffffu, un.mnz, sh));
+        un.mxx = fmaxf(un.mxx, __shfl_xor_sync(0xffffffffu, un.mxx, sh));
+        un.mxy = fmaxf(un.mxy, __shfl_xor_sync(0xffffffffu, un.mxy, sh));
+        un.mxz = fmaxf(un.mxz, __shfl_xor_sync(0xffffffffu, un.mxz, sh));
+    }
+    int32_t t = __shfl_sync(0xffffffffu, ql.skip, 0);
     int32_t visits = 0;
     const int32_t nnodes = 2 * nL - 1;
     while (t != 0) {
-        ND_WALK_GUARD(t, nnodes, visits, err, q)
-        Node nd_ = load_node(keys, t);
-        if (overlap(ql, nd_)) {
+        if (t < 1 || t > nnodes || ++visits > nnodes) {
+            if (lane == 0) set_error(err, ND_ERR_INTERNAL, q0);
+            break;
+        }
+        const Node nd_ = load_node(keys, t);
+        if (overlap(un, nd_)) {
             if (nd_.left == 0) {
-                leaf_pairs_fixed<APL>(qa, pos, (int64_t)(t - 1) * APL, r2, s);
-                flush_stage(s, cursor, cap, pi, pj, pd);
+                mask = 0;
+                float4 tb[APL];
+                if (valid && t > q && overlap(ql, nd_)) {
+                    const int64_t B = (int64_t)(t - 1) * APL;
+#pragma unroll
+                    for (int j = 0; j < APL; ++j) tb[j] = __ldg(&pos[B + j]);
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const int i = k >> 2, j = k & 3;
+                        d2[k] = dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z);
+                        if (d2[k] < r2) mask |= 1u << k;
+                    }
+                }
+                warp_emit16(mask, qa, tb, d2, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
                 t = nd_.skip;
             } else {
                 t = nd_.left;
@@ -839,6 +911,7 @@ __global__ void __launch_bounds__(128)
             t = nd_.skip;
         }
     }
+    warp_buf_flush(bi, bj, bd, nb, cursor, cap, pi, pj, pd);
 }
 
 __global__ void __launch_bounds__(128)
@@ -869,7 +942,7 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
     if ((st = ensure(c, c->misc, 64))) return st;
     unsigned long long* cursor = (unsigned long long*)c->misc.p;
     cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
-    k_leaf_unordered4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
+    k_leaf_warp4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
         t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd, c->d_err);
     c->launches++;
     if ((st = check_launch(c, "leaf pairs (unordered)"))) return st;

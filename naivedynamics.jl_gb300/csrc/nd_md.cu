@@ -487,8 +487,10 @@ __device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const
 }
 
 // One block per 256 atoms.  MODE 0: step (force, pending half kick, kick,
-// drift, reflect, next record).  MODE 1: measure (force, integer-step velocity
-// and energies; state untouched).
+// drift, reflect, next record).  MODE 2: the same step inside a captured
+// window, whose last block also sets the early-refit condition of the graph
+// node after it.  MODE 1: measure (force, integer-step velocity and
+// energies; state untouched).
 // BATCH: atoms of several systems; pair constants, walls and the fixed-point
 // origin come from the atom's system (a pair never crosses systems).
 template <bool COUL, bool MASS, bool FIRST, int MODE, bool BATCH>
@@ -640,14 +642,16 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         // (a ticket counter, no waiting) publishes the flag to the graph's
         // conditional node that follows this step.
         if (__syncthreads_or(trig) && tid == 0) atomicOr(&a.ctl[0], 1u);
-        if (a.use_cond && tid == 0) {
-            __threadfence();
-            const unsigned ticket = atomicAdd(&a.ctl[1], 1u);
-            if (ticket == gridDim.x - 1) {
+        if constexpr (MODE == 2) {
+            if (tid == 0) {
                 __threadfence();
-                const unsigned f = atomicExch(&a.ctl[0], 0u);
-                atomicExch(&a.ctl[1], 0u);
-                cudaGraphSetConditional(a.cond, f ? 1u : 0u);
+                const unsigned ticket = atomicAdd(&a.ctl[1], 1u);
+                if (ticket == gridDim.x - 1) {
+                    __threadfence();
+                    const unsigned f = atomicExch(&a.ctl[0], 0u);
+                    atomicExch(&a.ctl[1], 0u);
+                    cudaGraphSetConditional(a.cond, f ? 1u : 0u);
+                }
             }
         }
     }
@@ -818,7 +822,11 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     ND_SMEM(true, true, false, 1) ND_SMEM(true, false, true, 1)
     ND_SMEM(true, false, false, 1) ND_SMEM(false, true, true, 1)
     ND_SMEM(false, true, false, 1) ND_SMEM(false, false, true, 1)
-    ND_SMEM(false, false, false, 1)
+    ND_SMEM(false, false, false, 1) ND_SMEM(true, true, true, 2)
+    ND_SMEM(true, true, false, 2) ND_SMEM(true, false, true, 2)
+    ND_SMEM(true, false, false, 2) ND_SMEM(false, true, true, 2)
+    ND_SMEM(false, true, false, 2) ND_SMEM(false, false, true, 2)
+    ND_SMEM(false, false, false, 2)
 #undef ND_SMEM
     if (e != cudaSuccess) return cuda_fail(c, e, "shared memory opt-in");
     return ND_OK;
@@ -887,7 +895,7 @@ StepArgs md_step_args(MDEngine* m, int rec_in) {
 }
 
 template <int MODE>
-static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
+static void launch_step_impl(MDEngine* m, const StepArgs& a, bool first) {
     Ctx* c = &m->sub;
     const unsigned grid = (unsigned)m->nblocks;
     const size_t sm = m->step_smem;
@@ -918,6 +926,13 @@ static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
     c->launches++;
 }
 
+// MODE 0 steps inside a captured window publish their early-refit vote to the
+// conditional node after them (MODE 2); the others are plain kernels.
+template <int MODE>
+static void launch_step(MDEngine* m, const StepArgs& a, bool first) {
+    if (MODE == 0 && a.use_cond) launch_step_impl<2>(m, a, first);
+    else launch_step_impl<MODE>(m, a, first);
+}
 
 void md_launch_step(MDEngine* m, const StepArgs& a, bool first) { launch_step<0>(m, a, first); }
 

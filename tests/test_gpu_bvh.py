@@ -244,3 +244,28 @@ def test_ns_stress_reduced(nd, oracle):
     tl = oracle.leaf_traverse(t, 2.5, 4)
     mr = np.isin(np.minimum(tl[0], tl[1]), sel)
     assert np.array_equal(canon(a[m], b[m], d[m]), canon(tl[0][mr], tl[1][mr], tl[2][mr]))
+
+
+def test_ns_stress_full(nd, oracle):
+    # The neighbour-search stress configuration at full size: 4,194,304 points
+    # (64 clusters x 65,536), r = 2.5, ~2.6e9 half pairs written to device
+    # memory (31 GB); exact pair count and order-free 128-bit hash of every
+    # canonical (min, max, bits(d)) triple against the oracle's traversal.
+    import torch
+    n = 64 * 65536
+    x = nd.synth.cluster_positions(0x4E440003, n, 64, 400.0, 2.0, 10.0)
+    t = oracle.tree(x, 2.5, 4, order=1)
+    cnt_ref, h_ref = oracle.leaf_traverse_hash(t, 2.5, 4)
+    del t
+    spec = nd.SpheresBVHSpecs(2.5, n, 4)
+    xt = torch.from_numpy(x).cuda()
+    st, cnt = nd.neighbor_pairs_dev(xt, spec, None, None, None, 0, order=1)
+    assert st == nd._lib.ND_NEED_REALLOC and cnt == cnt_ref
+    pi = torch.empty(cnt, dtype=torch.int32, device="cuda")
+    pj = torch.empty_like(pi)
+    pd = torch.empty(cnt, dtype=torch.float32, device="cuda")
+    st, cnt2 = nd.neighbor_pairs_dev(xt, spec, pi, pj, pd, cnt, order=1)
+    assert st == 0 and cnt2 == cnt_ref
+    assert nd.pair_hash_dev(pi, pj, pd, cnt2) == h_ref
+    del pi, pj, pd
+    torch.cuda.empty_cache()
