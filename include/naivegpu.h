@@ -295,6 +295,29 @@ nd_status nd_md_diagnostics(nd_md* md, nd_md_diag* out);
  * its own pair of CUDA events on the context stream: ms[k] (host array of
  * `steps`) receives the k-th step kernel's duration.  Synchronises. */
 nd_status nd_md_step_times(nd_md* md, int32_t steps, float* ms);
+/*
+ * rescale_velocity!(velocity, Tf, gamma, mass, objectcount) (Simulator.jl:119-144),
+ * which simulate! applies every 10 steps (Simulator.jl:241-243): after every
+ * `every`-th step, on the integer-step velocities,
+ *   Ti = sum_i (2 / (3 N kb)) |v_i| m_i / 2   (kb = 1; the reference sums |v|, not v^2),
+ *   beta = (1 + gamma (Tf / Ti - 1))^0.5,   v_i *= beta.
+ * Ti <= 0 leaves the velocities unchanged; a negative radicand (the
+ * reference's DomainError) leaves them unchanged and the next sync returns
+ * ND_ERR_ARG.  every = 0 switches it off.  Single-system engines only.
+ */
+nd_status nd_md_set_thermostat(nd_md* md, double temperature, double gamma, int32_t every);
+/*
+ * The position log of simulate! (poslog, Simulator.jl:167,245), kept on the
+ * device: after every `every`-th step the positions (caller order, N x 3 FP64)
+ * go into a ring of `frames` frames.  every = 0 switches it off.  Setting it
+ * restarts the frame count.
+ */
+nd_status nd_md_set_log(nd_md* md, int32_t every, int32_t frames);
+/* Frames logged so far (including frames the ring has overwritten). */
+nd_status nd_md_log_count(nd_md* md, int64_t* count);
+/* Copy frames [first, first + nframes) (frame k = the k-th logged step) to a host
+ * array of nframes x N x 3 FP64; frames no longer in the ring are ND_ERR_ARG. */
+nd_status nd_md_log_read(nd_md* md, int64_t first, int64_t nframes, double* out);
 /* Number of kernel launches one nd_md_run(steps) enqueues (for diagnostics). */
 int64_t nd_md_launches_per_run(nd_md* md, int64_t steps);
 

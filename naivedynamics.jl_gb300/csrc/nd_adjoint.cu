@@ -188,13 +188,13 @@ __global__ void __launch_bounds__(kBlock * kAdjTPA) k_adj_reverse(AdjArgs a) {
     const int4 ri = __ldg(&a.recs[i]);
     const float4 gi = a.g4_in[i];
     const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
-    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + al;
+    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock;
     float3 hv = make_float3(0.f, 0.f, 0.f);
     float eacc = 0.f, sacc = 0.f;
-    int32_t li = part < cnt ? L[(int64_t)part * kBlock] : 0;
+    int32_t li = part < cnt ? L[llist_at(part, al)] : 0;
     for (int32_t s = part; s < cnt; s += kAdjTPA) {
         const int32_t sn = s + kAdjTPA;
-        const int32_t next = sn < cnt ? L[(int64_t)sn * kBlock] : 0;
+        const int32_t next = sn < cnt ? L[llist_at(sn, al)] : 0;
         int4 rj;
         float4 gj;
         if (li < a.smrec) {
@@ -263,13 +263,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_hist(AdjArgs a) {
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
     const int4 ri = __ldg(&a.recs[i]);
     const int32_t cnt = __ldg(&a.ncount[i]);
-    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
+    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock;
     for (int32_t b0 = 0; b0 < a.bins; b0 += kHistChunk) {
         float acc[kHistChunk];
 #pragma unroll
         for (int k = 0; k < kHistChunk; ++k) acc[k] = 0.0f;
         for (int32_t s = 0; s < cnt; ++s) {
-            const int64_t j = adj_atom(U, L[(int64_t)s * kBlock], a.apl);
+            const int64_t j = adj_atom(U, L[llist_at(s, tid)], a.apl);
             if (j <= i) continue;
             const int4 rj = __ldg(&a.recs[j]);
             const float dx = (float)(ri.x - rj.x) * a.invS;
@@ -334,10 +334,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_terminal(AdjArgs a) {
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
     const int4 ri = __ldg(&a.recs[i]);
     const int32_t cnt = __ldg(&a.ncount[i]);
-    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
+    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock;
     float gx = 0.f, gy = 0.f, gz = 0.f;
     for (int32_t s = 0; s < cnt; ++s) {
-        const int64_t j = adj_atom(U, L[(int64_t)s * kBlock], a.apl);
+        const int64_t j = adj_atom(U, L[llist_at(s, tid)], a.apl);
         const int4 rj = __ldg(&a.recs[j]);
         const float dx = (float)(ri.x - rj.x) * a.invS;
         const float dy = (float)(ri.y - rj.y) * a.invS;

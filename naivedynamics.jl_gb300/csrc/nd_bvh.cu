@@ -774,7 +774,7 @@ __global__ void __launch_bounds__(128)
 // are broadcast, and the pairs are ballot-compacted into a shared-memory
 // buffer per warp that is written out with one atomic reservation and
 // coalesced stores.
-constexpr int kWarpBuf = 1024;  // buffered pairs per warp
+constexpr int kWarpBuf = 512;  // buffered pairs per warp (one leaf visit adds at most 512)
 
 __device__ __forceinline__ void warp_buf_flush(int32_t* bi, int32_t* bj, float* bd, int& nb,
                                                unsigned long long* cursor, int64_t cap,
@@ -791,12 +791,12 @@ __device__ __forceinline__ void warp_buf_flush(int32_t* bi, int32_t* bj, float* 
     nb = 0;
 }
 
-// Appends this lane's hits (bit k of mask = pair (qa[k / 4], tb[k % 4]), d2[k]
-// its squared distance) to the warp's buffer: the lanes' offsets are the
-// exclusive prefix of their hit counts (<= 16, so five ballot bit planes).
+// Appends this lane's hits (bit k of mask = pair (qa[k / 4], tb[k % 4])) to
+// the warp's buffer: the lanes' offsets are the exclusive prefix of their hit
+// counts (<= 16, so five ballot bit planes); distances are recomputed with the
+// same operations as the test, so they are the tested values.
 __device__ __forceinline__ void warp_emit16(unsigned mask, const float4 (&qa)[4],
-                                            const float4 (&tb)[4], const float (&d2)[16],
-                                            int32_t* bi, int32_t* bj, float* bd, int& nb,
+                                            const float4 (&tb)[4], int32_t* bi, int32_t* bj, float* bd, int& nb,
                                             unsigned long long* cursor, int64_t cap, int32_t* pi,
                                             int32_t* pj, float* pd) {
     const int lane = threadIdx.x & 31;
@@ -817,7 +817,8 @@ __device__ __forceinline__ void warp_emit16(unsigned mask, const float4 (&qa)[4]
         if (mask & (1u << k)) {
             bi[at] = __float_as_int(qa[k >> 2].w);
             bj[at] = __float_as_int(tb[k & 3].w);
-            bd[at] = __fsqrt_rn(d2[k]);
+            const float4 a = qa[k >> 2], b = tb[k & 3];
+            bd[at] = __fsqrt_rn(dist2_ref(a.x, a.y, a.z, b.x, b.y, b.z));
             ++at;
         }
     }
@@ -825,7 +826,7 @@ __device__ __forceinline__ void warp_emit16(unsigned mask, const float4 (&qa)[4]
     nb += (int)total;
 }
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 8)
     k_leaf_warp4(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
                  float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
                  float* pd, int32_t* err) {
@@ -855,19 +856,16 @@ __global__ void __launch_bounds__(128)
         for (int i = 0; i < APL; ++i) qa[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     int nb = 0;
-    float d2[16];
     unsigned mask = 0;
     // intra-leaf pairs (a before b in the leaf)
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
         const int i = k >> 2, j = k & 3;
-        d2[k] = 0.0f;
-        if (j > i) {
-            d2[k] = dist2_ref(qa[i].x, qa[i].y, qa[i].z, qa[j].x, qa[j].y, qa[j].z);
-            if (valid && d2[k] < r2) mask |= 1u << k;
-        }
+        if (j > i && valid &&
+            dist2_ref(qa[i].x, qa[i].y, qa[i].z, qa[j].x, qa[j].y, qa[j].z) < r2)
+            mask |= 1u << k;
     }
-    warp_emit16(mask, qa, qa, d2, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+    warp_emit16(mask, qa, qa, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
     // the warp's union box (invalid lanes contribute the empty box)
     Node un = ql;
     for (int sh = 16; sh > 0; sh >>= 1) {
@@ -898,11 +896,11 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
                         const int i = k >> 2, j = k & 3;
-                        d2[k] = dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z);
-                        if (d2[k] < r2) mask |= 1u << k;
+                        if (dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z) < r2)
+                            mask |= 1u << k;
                     }
                 }
-                warp_emit16(mask, qa, tb, d2, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+                warp_emit16(mask, qa, tb, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
                 t = nd_.skip;
             } else {
                 t = nd_.left;

@@ -601,6 +601,29 @@ nd_status nd_md_step_times(nd_md* md, int32_t steps, float* ms) {
     return md_wrap(md, nd::md_step_times(md->e, steps, ms));
 }
 
+nd_status nd_md_set_thermostat(nd_md* md, double temperature, double gamma, int32_t every) {
+    if (!md_live(md)) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_set_thermostat(md->e, temperature, gamma, every));
+}
+
+nd_status nd_md_set_log(nd_md* md, int32_t every, int32_t frames) {
+    if (!md_live(md)) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_set_log(md->e, every, frames));
+}
+
+nd_status nd_md_log_count(nd_md* md, int64_t* count) {
+    if (!md_live(md) || !count) return ND_ERR_ARG;
+    return md_wrap(md, nd::md_log_count(md->e, count));
+}
+
+nd_status nd_md_log_read(nd_md* md, int64_t first, int64_t nframes, double* out) {
+    if (!md_live(md) || (nframes > 0 && !out)) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_log_read(md->e, first, nframes, out));
+}
+
 int64_t nd_md_launches_per_run(nd_md* md, int64_t steps) {
     return md_live(md) ? nd::md_launches_per_run(md->e, steps) : 0;
 }

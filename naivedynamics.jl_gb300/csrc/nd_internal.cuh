@@ -217,6 +217,10 @@ nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list
                    int32_t* capacity);
 int64_t md_launches_per_run(MDEngine* m, int64_t steps);
 nd_status md_diagnostics(MDEngine* m, nd_md_diag* out);
+nd_status md_set_thermostat(MDEngine* m, double temperature, double gamma, int32_t every);
+nd_status md_set_log(MDEngine* m, int32_t every, int32_t frames);
+nd_status md_log_count(MDEngine* m, int64_t* count);
+nd_status md_log_read(MDEngine* m, int64_t first, int64_t nframes, double* out);
 const char* md_last_error(MDEngine* m);
 nd_status forces_pairs(Ctx* c, const nd_md_params* p, int32_t n, const double* x,
                        const double* q, const int32_t* pi, const int32_t* pj, int64_t np,

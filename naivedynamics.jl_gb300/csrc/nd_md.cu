@@ -751,6 +751,9 @@ static nd_status md_alloc(MDEngine* m) {
     if (cudaMemsetAsync(m->diag.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
     if ((st = ensure(c, m->ctl, 64))) return st;
     if (cudaMemsetAsync(m->ctl.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
+    if ((st = ensure(c, m->obs, 64))) return st;
+    if (cudaMemsetAsync(m->obs.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
+    if ((st = ensure(c, m->obs_part, sizeof(double) * (size_t)cdiv(m->n, 256)))) return st;
     // rebuild pipeline scratch: codes + perm + sort ping-pong + histograms
     if ((st = ensure(c, c->codes, sizeof(int32_t) * n))) return st;
     if ((st = ensure(c, c->perm, sizeof(int32_t) * n))) return st;
@@ -1033,10 +1036,16 @@ static nd_status md_window_begin(MDEngine* m, bool capture) {
                                                capture ? 1 : 0);
     c->launches++;
     if (capture) {
-        return md_add_cond_node(m, h, 2, [&](int k) {
-            return k == 0 ? md_rebuild(m, RB_RESORT, -1, ctl_word(m, 6))
-                          : md_rebuild(m, RB_REFIT, -1, ctl_word(m, 7));
-        });
+        int64_t nk[2] = {0, 0};
+        nd_status s2 = md_add_cond_node(
+            m, h, 2,
+            [&](int k) {
+                return k == 0 ? md_rebuild(m, RB_RESORT, -1, ctl_word(m, 6))
+                              : md_rebuild(m, RB_REFIT, -1, ctl_word(m, 7));
+            },
+            nk);
+        if (s2 == ND_OK) { m->resort_kernels = nk[0]; m->refit_kernels = nk[1]; }
+        return s2;
     }
     unsigned need = 0;
     cudaError_t e = cudaMemcpyAsync(&need, ctl_word(m, 5), sizeof(need), cudaMemcpyDeviceToHost,
@@ -1048,6 +1057,164 @@ static nd_status md_window_begin(MDEngine* m, bool capture) {
               : md_rebuild(m, RB_REFIT, -1, ctl_word(m, 7));
     m->eager_bodies += c->launches - l0;
     return st;
+}
+
+// ---------------------------------------------------------- observers
+// The step loop of simulate! (Simulator.jl:241-245) rescales the velocities
+// every 10 steps (rescale_velocity!, :119-144) and appends the positions to
+// its log after every step.  Here both are optional, run after the steps
+// whose global index they divide, and inside captured windows are IF nodes
+// whose conditions k_md_due sets from the device's window counter.
+
+__global__ void k_md_due(const unsigned* __restrict__ ctl, int32_t R, int32_t p, int32_t every_t,
+                         int32_t every_l, cudaGraphConditionalHandle ht,
+                         cudaGraphConditionalHandle hl) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    // ctl[3] is the current window's number + 1
+    const long long g = (long long)(ctl[3] - 1u) * R + p + 1;
+    if (every_t > 0) cudaGraphSetConditional(ht, g % every_t == 0 ? 1u : 0u);
+    if (every_l > 0) cudaGraphSetConditional(hl, g % every_l == 0 ? 1u : 0u);
+}
+
+// rescale_velocity!, 1: per block of 256 atoms the sum of |v_i| m_i / 2 over
+// the integer-step velocities v (component-major, 3 x n), fixed order.
+__global__ void __launch_bounds__(256) k_md_thermo_part(const double* __restrict__ v,
+                                                        const double* __restrict__ im, int32_t n,
+                                                        double* __restrict__ part) {
+    __shared__ double s[256];
+    const int32_t i = blockIdx.x * 256 + threadIdx.x;
+    double t = 0.0;
+    if (i < n) {
+        const double a = v[i], b = v[(int64_t)n + i], c = v[2 * (int64_t)n + i];
+        t = sqrt(a * a + b * b + c * c) / im[i] / 2.0;
+    }
+    s[threadIdx.x] = t;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+
+// 2: Ti = 2 / (3 N kb) * sum (kb = 1), beta = (1 + gamma (Tf / Ti - 1))^0.5.
+// Ti <= 0 keeps beta = 1; a negative radicand (the reference's DomainError)
+// keeps beta = 1 and reports ND_ERR_ARG.  obs: [0] frames logged,
+// [1] thermostat applications (uint64), [2] the last beta (double).
+__global__ void k_md_thermo_beta(const double* __restrict__ part, int32_t nb, int32_t n,
+                                 double Tf, double gamma, unsigned long long* obs, int32_t* err) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double sum = 0.0;
+    for (int32_t b = 0; b < nb; ++b) sum += part[b];
+    const double Ti = 2.0 / (3.0 * (double)n) * sum;
+    double beta = 1.0;
+    if (Ti > 0.0) {
+        const double r = 1.0 + gamma * (Tf / Ti - 1.0);
+        if (r >= 0.0) beta = sqrt(r);
+        else set_error(err, ND_ERR_ARG, 0);
+    }
+    reinterpret_cast<double*>(obs)[2] = beta;
+    obs[1] += 1ull;
+}
+
+// 3: v <- beta v on the half-step state: u = beta v - dt/2 F/m, so the next
+// step's two half kicks continue from the rescaled integer-step velocity.
+__global__ void k_md_thermo_scale(double* w0, double* w1, double* w2, const double* __restrict__ v,
+                                  const float4* __restrict__ f, const double* __restrict__ im,
+                                  int32_t n, float hdt, const unsigned long long* obs) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double beta = reinterpret_cast<const double*>(obs)[2];
+    const float4 g = f[i];
+    const double imv = im[i];
+    w0[i] = beta * v[i] - (double)(hdt * g.x) * imv;
+    w1[i] = beta * v[(int64_t)n + i] - (double)(hdt * g.y) * imv;
+    w2[i] = beta * v[2 * (int64_t)n + i] - (double)(hdt * g.z) * imv;
+}
+
+// Position log: frame (frames logged mod ring size) <- positions in the
+// caller's order; k_md_log_advance counts the frame afterwards.
+__global__ void k_md_log(const double* __restrict__ x0, const double* __restrict__ x1,
+                         const double* __restrict__ x2, const int32_t* __restrict__ orig, int32_t n,
+                         double* __restrict__ ring, int64_t frames,
+                         const unsigned long long* __restrict__ obs) {
+    const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int64_t slot = (int64_t)(obs[0] % (unsigned long long)frames);
+    double* fr = ring + slot * 3 * (int64_t)n;
+    const int64_t o = orig[k];
+    fr[3 * o] = x0[k];
+    fr[3 * o + 1] = x1[k];
+    fr[3 * o + 2] = x2[k];
+}
+
+__global__ void k_md_log_advance(unsigned long long* obs) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) obs[0] += 1ull;
+}
+
+static nd_status md_thermo_body(MDEngine* m) {
+    Ctx* c = &m->sub;
+    const unsigned g = (unsigned)cdiv(m->n, 256);
+    StepArgs a = md_step_args(m, m->rc);
+    launch_step<1>(m, a, false);  // integer-step velocities and forces
+    const double* vt = (const double*)m->vtmp.p;
+    SetPtrs& s = m->set[0];
+    k_md_thermo_part<<<g, 256, 0, c->stream>>>(vt, s.im, m->n, (double*)m->obs_part.p);
+    k_md_thermo_beta<<<1, 32, 0, c->stream>>>((const double*)m->obs_part.p, (int32_t)g, m->n,
+                                              m->thermo_T, m->thermo_gamma,
+                                              (unsigned long long*)m->obs.p, c->d_err);
+    k_md_thermo_scale<<<g, 256, 0, c->stream>>>(s.w[0], s.w[1], s.w[2], vt, (const float4*)m->f.p,
+                                                s.im, m->n, (float)(0.5 * m->p.dt),
+                                                (const unsigned long long*)m->obs.p);
+    c->launches += 3;
+    return check_launch(c, "thermostat");
+}
+
+static nd_status md_log_body(MDEngine* m) {
+    Ctx* c = &m->sub;
+    SetPtrs& s = m->set[0];
+    k_md_log<<<(unsigned)cdiv(m->n, 256), 256, 0, c->stream>>>(
+        s.x[0], s.x[1], s.x[2], s.orig, m->n, (double*)m->logbuf.p, m->log_frames,
+        (const unsigned long long*)m->obs.p);
+    k_md_log_advance<<<1, 32, 0, c->stream>>>((unsigned long long*)m->obs.p);
+    c->launches += 2;
+    return check_launch(c, "position log");
+}
+
+static int32_t gcd32(int32_t a, int32_t b) {
+    while (b) { const int32_t t = a % b; a = b; b = t; }
+    return a;
+}
+
+// Observers after the step at window position p (global step g on the host).
+static nd_status md_observe(MDEngine* m, int32_t p, bool capture, int64_t g) {
+    if (m->thermo_every <= 0 && m->log_every <= 0) return ND_OK;
+    Ctx* c = &m->sub;
+    const int32_t R = m->p.rebuild_every;
+    auto possible = [&](int32_t every) { return every > 0 && (p + 1) % gcd32(every, R) == 0; };
+    const bool pt = possible(m->thermo_every), pl = possible(m->log_every);
+    if (!pt && !pl) return ND_OK;
+    nd_status st;
+    if (!capture) {
+        const int64_t l0 = c->launches;
+        if (pt && g % m->thermo_every == 0 && (st = md_thermo_body(m))) return st;
+        if (pl && g % m->log_every == 0 && (st = md_log_body(m))) return st;
+        m->eager_bodies += c->launches - l0;
+        return ND_OK;
+    }
+    cudaGraphConditionalHandle ht = 0, hl = 0;
+    if (pt && (st = md_cond_handle(m, &ht))) return st;
+    if (pl && (st = md_cond_handle(m, &hl))) return st;
+    k_md_due<<<1, 32, 0, c->stream>>>((const unsigned*)m->ctl.p, R, p, pt ? m->thermo_every : 0,
+                                      pl ? m->log_every : 0, ht, hl);
+    c->launches++;
+    if (pt && (st = md_add_cond_node(m, ht, 1, [&](int) { return md_thermo_body(m); },
+                                     &m->thermo_kernels)))
+        return st;
+    if (pl && (st = md_add_cond_node(m, hl, 1, [&](int) { return md_log_body(m); },
+                                     &m->log_kernels)))
+        return st;
+    return ND_OK;
 }
 
 // Enqueue `k` steps of the current window, the first at window position pos0.
@@ -1073,13 +1240,12 @@ static nd_status md_steps(MDEngine* m, int32_t k, int32_t pos0, bool capture = f
         if (ev) cudaEventRecord(ev[2 * s + 1], c->stream);
         m->first = false;
         m->rc ^= 1;
-        if (tail) continue;
-        if (capture) {
-            if ((st = md_add_cond_node(m, h, 1, [&](int) {
-                     return md_rebuild(m, RB_REFIT, m->rc, ctl_word(m, 2));
-                 })))
+        if (!tail && capture) {
+            if ((st = md_add_cond_node(
+                     m, h, 1, [&](int) { return md_rebuild(m, RB_REFIT, m->rc, ctl_word(m, 2)); },
+                     &m->refit_kernels)))
                 return st;
-        } else {
+        } else if (!tail) {
             unsigned flag = 0;
             cudaError_t e = cudaMemcpyAsync(&flag, m->ctl.p, sizeof(flag), cudaMemcpyDeviceToHost,
                                             c->stream);
@@ -1091,6 +1257,7 @@ static nd_status md_steps(MDEngine* m, int32_t k, int32_t pos0, bool capture = f
                 m->eager_bodies += c->launches - l0;
             }
         }
+        if ((st = md_observe(m, pos0 + s, capture, m->steps + s + 1))) return st;
     }
     return ND_OK;
 }
@@ -1198,7 +1365,8 @@ static nd_status md_size_lists(MDEngine* m) {
     if ((st = md_alloc_lists(m, fcap, ucap, lcap_leaf, 0, ucap_sm))) return st;
     if ((st = md_sizing_pass(m, h))) return st;
     const int32_t max_n = h[1];
-    int32_t lcap = m->p.max_neighbors > 0 ? m->p.max_neighbors : round_up(max_n * 1.35 + 16, 8);
+    int32_t lcap = m->p.max_neighbors > 0 ? round_up(m->p.max_neighbors, 8)
+                                          : round_up(max_n * 1.35 + 16, 8);
     if ((st = md_alloc_lists(m, fcap, ucap, lcap_leaf, lcap, ucap_sm))) return st;
     if ((st = md_rebuild(m, RB_RESORT))) return st;
     if ((st = md_opened(m))) return st;
@@ -1239,6 +1407,7 @@ nd_status md_upload(MDEngine* m, const double* xd, const double* vd, const doubl
     c->launches += 3;
     if (cudaMemsetAsync(m->diag.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
     if (cudaMemsetAsync(m->ctl.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
+    if (m->obs.p && cudaMemsetAsync(m->obs.p, 0, 64, c->stream) != cudaSuccess) return ND_ERR_CUDA;
     m->cur = 0;
     m->first = true;
     m->steps = 0;
@@ -1540,7 +1709,7 @@ nd_status md_destroy(MDEngine* m) {
                       &m->xyz32, &m->pos32, &m->keys, &m->store, &m->ulist, &m->ucount,
                       &m->llist_leaf, &m->lcount_leaf, &m->llist,
                       &m->ncount, &m->f, &m->vtmp, &m->acc, &m->aos, &m->diag, &m->sysrow,
-                      &m->sid_in, &m->ctl, &m->sub.codes,
+                      &m->sid_in, &m->ctl, &m->obs, &m->obs_part, &m->logbuf, &m->sub.codes,
                       &m->sub.codes_alt, &m->sub.perm, &m->sub.perm_alt, &m->sub.hist,
                       &m->sub.misc};
     if (m->sub.stream) cudaStreamSynchronize(m->sub.stream);
@@ -1742,7 +1911,9 @@ nd_status md_diagnostics(MDEngine* m, nd_md_diag* out) {
     Ctx* c = &m->sub;
     unsigned long long d[2] = {0, 0};
     unsigned ctl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long ob[2] = {0, 0};
     cudaError_t e = cudaMemcpyAsync(d, m->diag.p, sizeof(d), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ob, m->obs.p, sizeof(ob), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, m->ctl.p, sizeof(ctl), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "md diagnostics");
@@ -1758,7 +1929,9 @@ nd_status md_diagnostics(MDEngine* m, nd_md_diag* out) {
     // kernels run inside conditional bodies of graphs: all bodies run, less
     // those the host ran (and counted) itself
     out->body_kernels = (int64_t)ctl[6] * m->resort_kernels +
-                        ((int64_t)ctl[7] + ctl[2]) * m->refit_kernels - m->eager_bodies;
+                        ((int64_t)ctl[7] + ctl[2]) * m->refit_kernels +
+                        (int64_t)ob[1] * m->thermo_kernels + (int64_t)ob[0] * m->log_kernels -
+                        m->eager_bodies;
     return ND_OK;
 }
 
@@ -1768,6 +1941,75 @@ int64_t md_launches_per_run(MDEngine* m, int64_t steps) {
 }
 
 nd_status md_sync(MDEngine* m) { return sync_and_check(&m->sub, "md sync"); }
+
+// Re-capture the window graphs after a change of the observers.
+static nd_status md_recapture(MDEngine* m) {
+    if (!m->cap_stream) return ND_OK;
+    Ctx* c = &m->sub;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "recapture");
+    if (m->graph_main) { cudaGraphExecDestroy(m->graph_main); m->graph_main = nullptr; }
+    if (m->graph_first) { cudaGraphExecDestroy(m->graph_first); m->graph_first = nullptr; }
+    nd_status st = md_capture_main(m);
+    if (st == ND_OK) st = md_capture_first(m);
+    return st;
+}
+
+nd_status md_set_thermostat(MDEngine* m, double temperature, double gamma, int32_t every) {
+    if (every < 0 || !std::isfinite(temperature) || !std::isfinite(gamma)) return ND_ERR_ARG;
+    if (every > 0 && m->nsys > 0) {
+        m->sub.last_error = "the thermostat applies to single-system engines";
+        return ND_ERR_ARG;
+    }
+    m->thermo_T = temperature;
+    m->thermo_gamma = gamma;
+    m->thermo_every = every;
+    return md_recapture(m);
+}
+
+nd_status md_set_log(MDEngine* m, int32_t every, int32_t frames) {
+    if (every < 0 || (every > 0 && frames <= 0)) return ND_ERR_ARG;
+    Ctx* c = &m->sub;
+    if (every > 0) {
+        nd_status st = ensure(c, m->logbuf, sizeof(double) * 3 * (size_t)m->n * (size_t)frames);
+        if (st) return st;
+    }
+    m->log_every = every;
+    m->log_frames = every > 0 ? frames : 0;
+    if (cudaMemsetAsync(m->obs.p, 0, sizeof(unsigned long long), c->stream) != cudaSuccess)
+        return cuda_fail(c, cudaGetLastError(), "position log");
+    return md_recapture(m);
+}
+
+nd_status md_log_count(MDEngine* m, int64_t* count) {
+    unsigned long long v = 0;
+    Ctx* c = &m->sub;
+    cudaError_t e = cudaMemcpyAsync(&v, m->obs.p, sizeof(v), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "position log");
+    *count = (int64_t)v;
+    return ND_OK;
+}
+
+nd_status md_log_read(MDEngine* m, int64_t first, int64_t nframes, double* out) {
+    Ctx* c = &m->sub;
+    int64_t count = 0;
+    nd_status st = md_log_count(m, &count);
+    if (st) return st;
+    if (m->log_frames <= 0 || first < 0 || nframes < 0 || first + nframes > count ||
+        first < count - m->log_frames) {
+        c->last_error = "frames outside the position log";
+        return ND_ERR_ARG;
+    }
+    const size_t fb = sizeof(double) * 3 * (size_t)m->n;
+    for (int64_t k = 0; k < nframes; ++k) {
+        const int64_t slot = (first + k) % m->log_frames;
+        cudaError_t e = cudaMemcpyAsync((char*)out + k * fb, (const char*)m->logbuf.p + slot * fb,
+                                        fb, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "position log");
+    }
+    return sync_and_check(c, "position log");
+}
 
 const char* md_last_error(MDEngine* m) { return m->sub.last_error.c_str(); }
 

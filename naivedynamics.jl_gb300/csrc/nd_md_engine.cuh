@@ -128,9 +128,23 @@ struct MDEngine {
     int64_t resort_kernels = 0;       // kernels of one re-sort rebuild
     int64_t eager_bodies = 0;         // kernels of rebuild bodies run eagerly (counted by the host)
     size_t step_smem = 0, union_smem = 0, lists_smem = 0;
+    // observers of the step loop: thermostat (rescale_velocity!) and position log
+    double thermo_T = 0.0, thermo_gamma = 0.0;
+    int32_t thermo_every = 0, log_every = 0;
+    int64_t log_frames = 0;
+    DevBuf obs, obs_part, logbuf;  // obs: frames logged, thermostat runs, last beta
+    int64_t thermo_kernels = 0, log_kernels = 0;
 };
 
 enum { RB_RESORT = 0, RB_REFIT = 1 };
+
+// Per-atom neighbour lists (uint16 indices into the block's union), per block
+// of kBlock atoms, slot-major: entry s of the block's thread t is element
+// s * kBlock + t, so a warp reading its atoms' s-th entries reads 64
+// contiguous bytes.
+__device__ __forceinline__ int64_t llist_at(int32_t s, int32_t t) {
+    return (int64_t)s * kBlock + t;
+}
 
 // Rebuild of the neighbour lists (re-sort or refit; see nd_md.cu).
 nd_status md_rebuild(MDEngine* m, int kind, int rec = -1, unsigned* counter = nullptr,
@@ -145,11 +159,12 @@ nd_status md_upload(MDEngine* m, const double* xd, const double* vd, const doubl
 
 // Conditional node after the work captured so far on c->stream.  nbody = 1:
 // IF (body 0 runs when the condition is non-zero); nbody = 2: IF/ELSE (body 1
-// runs when it is zero).  Each body is captured on cap_stream by body(k) and
-// its kernels are counted apart (they run only when chosen).
+// runs when it is zero).  Each body is captured on cap_stream by body(k); its
+// kernels are counted apart (they run only when chosen) into nk_out[k] when
+// nk_out is given.
 template <class F>
 inline nd_status md_add_cond_node(MDEngine* m, cudaGraphConditionalHandle h, int nbody,
-                                  F&& body) {
+                                  F&& body, int64_t* nk_out = nullptr) {
     Ctx* c = &m->sub;
     cudaStreamCaptureStatus cs;
     cudaGraph_t g = nullptr;
@@ -179,8 +194,7 @@ inline nd_status md_add_cond_node(MDEngine* m, cudaGraphConditionalHandle h, int
         cudaGraph_t out = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(m->cap_stream, &out);
         if (e2 != cudaSuccess && st == ND_OK) st = cuda_fail(c, e2, "body capture");
-        if (st == ND_OK && nbody == 2) (k == 0 ? m->resort_kernels : m->refit_kernels) = nk;
-        if (st == ND_OK && nbody == 1) m->refit_kernels = nk;
+        if (st == ND_OK && nk_out) nk_out[k] = nk;
     }
     c->stream = main;
     if (st) return st;

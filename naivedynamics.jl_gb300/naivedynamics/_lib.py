@@ -150,6 +150,10 @@ SIGNATURES = {
                               _vp, _vp, _vp, _vp, _i32, ctypes.POINTER(MDParams),
                               ctypes.POINTER(_d)]),
     "nd_md_diagnostics": (_i32, [_vp, ctypes.POINTER(MDDiag)]),
+    "nd_md_set_thermostat": (_i32, [_vp, _d, _d, _i32]),
+    "nd_md_set_log": (_i32, [_vp, _i32, _i32]),
+    "nd_md_log_count": (_i32, [_vp, ctypes.POINTER(_i64)]),
+    "nd_md_log_read": (_i32, [_vp, _i64, _i64, _vp]),
     "nd_simulate": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _vp, _i64]),
     "nd_adj_create": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp,
                              ctypes.POINTER(AdjSpec), _pp]),

@@ -168,12 +168,17 @@ class GenericObjectCollection:
 
 def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCollector,
               ff: ForceField | None = None, skin=0.3, atomsperleaf=4, rebuild_every=10,
-              order=ND_ORDER_SPATIAL, ctx=None):
+              order=ND_ORDER_SPATIAL, log_every: int | None = None, ctx=None):
     """simulate!(sys, spec, clct) (Simulator.jl:154-256) on the GPU.
 
     Advances sys.position / sys.velocity in place by spec.duration steps of
     kick-drift-kick velocity Verlet with reflecting walls at clct.minDim /
-    clct.maxDim, and stores the final forces in sys.force."""
+    clct.maxDim, and stores the final forces in sys.force.  As in the
+    reference step loop, a non-zero spec.vDamp applies rescale_velocity!
+    towards clct.temperature every 10 steps (Simulator.jl:241-243).  With
+    log_every, the positions after every log_every-th step are logged on the
+    device and returned, the initial positions first -- the poslog that
+    simulate! returns (log_every = 1); otherwise sys is returned."""
     ff = ff or ForceField()
     ctx = ctx or default_context()
     n = sys.position.shape[0]
@@ -183,11 +188,32 @@ def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCo
                   coulomb_k=ff.coulomb_k if q is not None else 0.0, cutoff=ff.cutoff, skin=skin,
                   dt=spec.stepwidth, box_lo=clct.minDim, box_hi=clct.maxDim,
                   atomsperleaf=atomsperleaf, rebuild_every=rebuild_every, order=order)
-    f = np.empty((n, 3), np.float32)
-    st = _lib.lib().nd_simulate(ctx.handle, ctypes.byref(p), n, ptr(sys.position),
-                                ptr(sys.velocity), ptr(f), ptr(q), ptr(m), int(spec.duration))
-    ctx.check(st, "nd_simulate")
+    if not log_every and not spec.vDamp:
+        f = np.empty((n, 3), np.float32)
+        st = _lib.lib().nd_simulate(ctx.handle, ctypes.byref(p), n, ptr(sys.position),
+                                    ptr(sys.velocity), ptr(f), ptr(q), ptr(m),
+                                    int(spec.duration))
+        ctx.check(st, "nd_simulate")
+        sys.force = f
+        return sys
+    x0 = sys.position.copy()
+    eng = MDEngine(p, sys.position, sys.velocity, q, m, ctx=ctx)
+    try:
+        if spec.vDamp:
+            eng.set_thermostat(clct.temperature, spec.vDamp, 10)
+        frames = int(spec.duration) // log_every if log_every else 0
+        if frames:
+            eng.set_log(log_every, frames)
+        eng.run(int(spec.duration))
+        x, v, f = eng.get()
+        poslog = eng.log_read(0, frames) if frames else None
+    finally:
+        eng.close()
+    sys.position[...] = x
+    sys.velocity[...] = v
     sys.force = f
+    if log_every:
+        return np.concatenate([x0[None], poslog]) if frames else x0[None]
     return sys
 
 
@@ -250,6 +276,30 @@ class MDEngine:
         self.ctx.check(_lib.lib().nd_md_energy(self.handle, ctypes.byref(pe), ctypes.byref(ke)),
                        "nd_md_energy")
         return pe.value, ke.value
+
+    def set_thermostat(self, temperature: float, gamma: float, every: int = 10):
+        """rescale_velocity! (Simulator.jl:119-144) after every `every`-th step;
+        every = 0 switches it off."""
+        self.ctx.check(_lib.lib().nd_md_set_thermostat(self.handle, float(temperature),
+                                                       float(gamma), int(every)),
+                       "nd_md_set_thermostat")
+
+    def set_log(self, every: int, frames: int):
+        """Position log (simulate!'s poslog) after every `every`-th step into a
+        device ring of `frames` frames; every = 0 switches it off."""
+        self.ctx.check(_lib.lib().nd_md_set_log(self.handle, int(every), int(frames)),
+                       "nd_md_set_log")
+
+    def log_count(self) -> int:
+        c = ctypes.c_int64()
+        self.ctx.check(_lib.lib().nd_md_log_count(self.handle, ctypes.byref(c)), "nd_md_log_count")
+        return c.value
+
+    def log_read(self, first: int, nframes: int) -> np.ndarray:
+        out = np.empty((nframes, self.n, 3), np.float64)
+        self.ctx.check(_lib.lib().nd_md_log_read(self.handle, int(first), int(nframes), ptr(out)),
+                       "nd_md_log_read")
+        return out
 
     def stats(self):
         s, r, p = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -600,6 +600,56 @@ int ref_md_run(const ref_md_params* p, int32_t n, double* x, double* v, double* 
     return REF_OK;
 }
 
+/* rescale_velocity! (Simulator.jl:119-144): Ti = sum_i (2/(3 N kb)) |v_i| m_i/2
+ * with kb = 1 (the reference sums the speed, not its square), then
+ * beta = (1 + gamma (Tf/Ti - 1))^0.5 and every velocity scaled by beta.
+ * Ti <= 0 leaves the velocities unchanged. */
+static void rescale_velocity(int32_t n, double* v, const double* m, double Tf, double gamma) {
+    double Ti = 0.0;
+    const double c = 2.0 / (3.0 * (double)n * 1.0);
+    for (int32_t i = 0; i < n; ++i) {
+        const double s = sqrt(v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] +
+                              v[3 * i + 2] * v[3 * i + 2]);
+        Ti += c * s * (m ? m[i] : 1.0) / 2.0;
+    }
+    if (!(Ti > 0.0)) return;
+    const double beta = sqrt(1.0 + gamma * (Tf / Ti - 1.0));
+    for (int64_t k = 0; k < 3 * (int64_t)n; ++k) v[k] *= beta;
+}
+
+int ref_md_run_observed(const ref_md_params* p, int32_t n, double* x, double* v, double* f,
+                        const double* q, const double* m, int64_t steps, double thermo_T,
+                        double thermo_gamma, int32_t thermo_every, int32_t log_every,
+                        double* poslog) {
+    const double h = 0.5 * p->dt;
+    int64_t frame = 0;
+    for (int64_t s = 1; s <= steps; ++s) {
+        for (int32_t i = 0; i < n; ++i) {
+            double im = m ? 1.0 / m[i] : 1.0;
+            for (int d = 0; d < 3; ++d) {
+                v[3 * i + d] += h * f[3 * i + d] * im;
+                x[3 * i + d] += p->dt * v[3 * i + d];
+            }
+        }
+        reflect(p, n, x, v);
+        int64_t st = ref_forces(p, n, x, q, f, NULL);
+        if (st < 0) return (int)st;
+        for (int32_t i = 0; i < n; ++i) {
+            double im = m ? 1.0 / m[i] : 1.0;
+            for (int d = 0; d < 3; ++d) v[3 * i + d] += h * f[3 * i + d] * im;
+        }
+        /* simulate! (Simulator.jl:241-245): rescale every thermo_every steps,
+         * then log the positions */
+        if (thermo_every > 0 && s % thermo_every == 0)
+            rescale_velocity(n, v, m, thermo_T, thermo_gamma);
+        if (log_every > 0 && s % log_every == 0 && poslog) {
+            memcpy(poslog + frame * 3 * (int64_t)n, x, sizeof(double) * 3 * (size_t)n);
+            ++frame;
+        }
+    }
+    return REF_OK;
+}
+
 /* CPU baseline: leaf BVH every `rebuild` steps + FP64 forces over the half list. */
 typedef struct { int32_t* i; int32_t* j; int64_t n, cap; } pairbuf;
 

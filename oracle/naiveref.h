@@ -143,6 +143,18 @@ int ref_md_run(const ref_md_params* p, int32_t n, double* x, double* v, double* 
                const double* q, const double* m, int64_t steps);
 
 /*
+ * ref_md_run with the step loop's observers of simulate! (Simulator.jl:241-245):
+ * after every thermo_every-th step rescale_velocity! (Simulator.jl:119-144)
+ * with temperature thermo_T and damping thermo_gamma (0 = off), and after
+ * every log_every-th step the positions appended to poslog (frames x N x 3;
+ * 0 or poslog NULL = off).
+ */
+int ref_md_run_observed(const ref_md_params* p, int32_t n, double* x, double* v, double* f,
+                        const double* q, const double* m, int64_t steps, double thermo_T,
+                        double thermo_gamma, int32_t thermo_every, int32_t log_every,
+                        double* poslog);
+
+/*
  * CPU baseline: the reference path timed on host cores.  Every `rebuild`
  * steps the leaf BVH (reference order, leafTreeData + leafneighbor_traverse)
  * is rebuilt at radius cutoff + skin from Float32 positions; forces are

@@ -103,6 +103,11 @@ def lib():
             L.ref_md_run.argtypes = [ctypes.POINTER(RefMDParams), ctypes.c_int32, f64p, f64p,
                                      f64p, f64p, f64p, ctypes.c_int64]
             L.ref_md_run.restype = ctypes.c_int
+            L.ref_md_run_observed.argtypes = [ctypes.POINTER(RefMDParams), ctypes.c_int32, f64p,
+                                              f64p, f64p, f64p, f64p, ctypes.c_int64,
+                                              ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                              ctypes.c_int32, f64p]
+            L.ref_md_run_observed.restype = ctypes.c_int
             L.ref_md_run_bvh.argtypes = [ctypes.POINTER(RefMDParams), ctypes.c_int32, f64p,
                                          f64p, f64p, f64p, f64p, ctypes.c_int64, ctypes.c_int32,
                                          ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
@@ -279,6 +284,24 @@ def md_run(p, x, v, q=None, m=None, steps=1):
                             _p(v, ctypes.c_double), _p(f, ctypes.c_double),
                             _p(qq, ctypes.c_double), _p(mm, ctypes.c_double), steps))
     return x, v, f
+
+
+def md_run_observed(p, x, v, q=None, m=None, steps=1, thermo=None, log_every=0):
+    """FP64 KDK run with simulate!'s observers: thermo = (T, gamma, every) for
+    rescale_velocity!, log_every for the position log.  Returns (x, v, f, poslog)."""
+    x = np.array(x, np.float64).reshape(-1, 3)
+    v = np.array(v, np.float64).reshape(-1, 3)
+    qq = None if q is None else np.ascontiguousarray(q, np.float64)
+    mm = None if m is None else np.ascontiguousarray(m, np.float64)
+    f, _, _ = forces(p, x, qq)
+    T, g, every = thermo if thermo else (0.0, 0.0, 0)
+    nf = steps // log_every if log_every > 0 else 0
+    log = np.zeros((max(nf, 1), x.shape[0], 3), np.float64)
+    _check(lib().ref_md_run_observed(ctypes.byref(p), x.shape[0], _p(x, ctypes.c_double),
+                                     _p(v, ctypes.c_double), _p(f, ctypes.c_double),
+                                     _p(qq, ctypes.c_double), _p(mm, ctypes.c_double), steps,
+                                     T, g, every, log_every, _p(log, ctypes.c_double)))
+    return x, v, f, log[:nf]
 
 
 def md_run_bvh(p, x, v, q=None, m=None, steps=1, rebuild=10, skin=0.3, apl=4,
