@@ -252,6 +252,51 @@ def batched_leg(nd, ctx, ext, flush):
             "plain_path": "512 nd_md engines run one after another on one stream (graphs)"}
 
 
+def plain_leg(nd, ctx, ext, flush):
+    """Plain LJ velocity Verlet at 4,096 atoms (cube side 17, min separation
+    0.8, v ~ N(0,1), sigma = eps = 1, r_c 2.5, dt 1e-3, rebuild every 10):
+    100 steps through the captured graphs, CUDA events on the library's
+    stream, 3 untimed repetitions first; the oracle's FP64 KDK loop with its
+    leaf BVH on the host cores beside it."""
+    import numpy as np
+    import torch
+
+    n, side, steps = 4096, 17.0, 100
+    x, v, _ = nd.synth.lj_system(nd.synth.SEED_PLAIN_LJ, n, side, 0.8)
+    p = nd.md_params(cutoff=2.5, skin=0.3, dt=1e-3, box_hi=(side,) * 3, atomsperleaf=4,
+                     rebuild_every=REBUILD)
+    eng = nd.MDEngine(p, x, v, ctx=ctx)
+    times = []
+    for k in range(6):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            a.record(ext)
+            eng.run(steps)
+            b.record(ext)
+        eng.sync()
+        if k >= 3:
+            times.append(a.elapsed_time(b))
+    eng.close()
+    ms = float(np.median(times))
+    out = {"metric": "plain LJ atom-steps/s @4096", "unit": UNIT,
+           "workload": "plain_lj_4096: N=4096 uniform cube side 17 (min separation 0.8), "
+                       "sigma=eps=1, r_c 2.5, skin 0.3, dt 1e-3, rebuild every 10, 100 steps",
+           "value": n * steps / (ms * 1e-3), "ms_per_100_steps": ms}
+    from oracle import naiveref as R
+    pr = R.md_params(cutoff=2.5, box_hi=(side,) * 3, dt=1e-3)
+    t0 = time.perf_counter()
+    R.md_run_bvh(pr, x, v, steps=steps, rebuild=REBUILD, skin=0.3, apl=4,
+                 order=R.REF_ORDER_REFERENCE)
+    cs = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": n * steps / cs, "unit": UNIT, "cores": R.num_threads(),
+                           "kind": "port",
+                           "sample": f"the same 100 steps (leaf BVH in reference order every 10 "
+                                     f"steps, FP64 forces, OpenMP), {cs:.2f} s"}
+    return out
+
+
 STRESS_N = 4194304
 
 
@@ -528,6 +573,8 @@ def run_gb300(args):
     eng.close()
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_leg(nd, ctx, ext, flush)
+    if rank == 0 and not args.no_plain:
+        line["plain_lj_4096"] = plain_leg(nd, ctx, ext, flush)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps)
     if rank == 0 and not args.no_stress:
@@ -549,13 +596,29 @@ def md_eager_leg(nd, ctx):
     builds), then per window a rebuild and ten steps."""
     import numpy as np
 
+    import torch
+
     x, v, q = nd.synth.lj_system(SEED, N_ATOMS, SIDE, 0.8, charges=True)
     p = _md_params(nd)
     p.skin, p.atomsperleaf, p.resort_every = 0.4, 8, 10
     eng = nd.MDEngine(p, x, v, q, ctx=ctx)
     ms = eng.step_times(10 * REBUILD)
+    # then the same settings through the captured graphs, CUDA events
+    ext = torch.cuda.ExternalStream(ctx.stream)
+    graph_ms = []
+    for k in range(4):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            a.record(ext)
+            eng.run(MD_PER_STEP)
+            b.record(ext)
+        eng.sync()
+        if k > 0:
+            graph_ms.append(a.elapsed_time(b))
     eng.close()
-    return {"workload": WORKLOAD + " (eager, fixed settings)", "step_kernel_ms_mean": float(np.mean(ms))}
+    return {"workload": WORKLOAD + " (fixed settings)", "step_kernel_ms_mean": float(np.mean(ms)),
+            "graph_ms_per_100_steps": float(np.median(graph_ms)),
+            "atom_steps_per_s": N_ATOMS * MD_PER_STEP / (float(np.median(graph_ms)) * 1e-3)}
 
 
 def run_only(args):
@@ -592,6 +655,8 @@ def main():
                     help="skip the adjoint (differentiable trajectory) measurement")
     ap.add_argument("--adjoint-steps", type=int, default=ADJ_STEPS,
                     help="MD steps of the adjoint measurement (a multiple of 50)")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the 4,096-atom plain LJ measurement")
     ap.add_argument("--no-stress", action="store_true",
                     help="skip the neighbour-search stress measurement")
     ap.add_argument("--stress-points", type=int, default=STRESS_N,

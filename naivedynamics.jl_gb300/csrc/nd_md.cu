@@ -177,8 +177,9 @@ __device__ __forceinline__ bool box_overlap(float qmnx, float qmny, float qmnz, 
 __global__ void __launch_bounds__(kBlock)
     k_md_block_union(const float4* __restrict__ keys, const float4* __restrict__ pos,
                      const int32_t* __restrict__ sid,
-                     int32_t n, int32_t nL, int32_t apl, float hq, int32_t fcap, int32_t ucap,
-                     int32_t upow2, int32_t* __restrict__ ulist, int32_t* __restrict__ ucount,
+                     int32_t n, int32_t nL, int32_t apl, float hq, float rl, int32_t fcap,
+                     int32_t ucap, int32_t upow2, int32_t* __restrict__ ulist,
+                     int32_t* __restrict__ ucount,
                      uint16_t* __restrict__ llist_leaf, int32_t* __restrict__ lcount_leaf,
                      int32_t lcap_leaf, int32_t* err, int32_t* diag, int32_t sizing,
                      unsigned* pressure) {
@@ -295,9 +296,14 @@ __global__ void __launch_bounds__(kBlock)
     // Per-leaf candidate lists: for each of its leaves a warp keeps the union
     // positions whose leaf box overlaps that leaf's box (the leaf-leaf test of
     // leafneighbor_traverse, BVHTraverse.jl:1282), ballot-compacted in union
-    // order.  A lane loads one union box per chunk and tests it against up to
-    // eight own leaves.  The own boxes are widened by a few ulps so no pair is
-    // lost to rounding; the atom distance test decides.
+    // order, and whose atoms can be within r_list of that leaf's atoms at all:
+    // leaf boxes are atom boxes -/+ r_list/2, so overlapping boxes only say the
+    // atom boxes are within r_list on each axis; the Euclidean gap of the atom
+    // boxes (sqrt of the summed squared per-axis gaps) must be below r_list too,
+    // which drops the candidates diagonally off the leaf.  A lane loads one
+    // union box per chunk and tests it against up to eight own leaves.  The own
+    // boxes are widened by a few ulps so no pair is lost to rounding; the atom
+    // distance test decides.
     __shared__ float s_own[kBlock / 32][8][6];
     const unsigned below = (1u << lane) - 1u;
     const int32_t leaves_per_warp = 32 / apl;
@@ -329,7 +335,14 @@ __global__ void __launch_bounds__(kBlock)
             for (int kl = 0; kl < 8; ++kl) {
                 if (kl >= nown) break;
                 const float* o = s_own[warp][kl];
-                const bool hit = (u < nu) && box_overlap(o[0], o[1], o[2], o[3], o[4], o[5], a, b);
+                bool hit = (u < nu) && box_overlap(o[0], o[1], o[2], o[3], o[4], o[5], a, b);
+                if (hit) {
+                    // per-axis gap of the atom boxes = key-box gap + r_list
+                    const float gx = fmaxf(fmaxf(o[0] - a.w, a.x - o[3]) + rl, 0.0f);
+                    const float gy = fmaxf(fmaxf(o[1] - b.x, a.y - o[4]) + rl, 0.0f);
+                    const float gz = fmaxf(fmaxf(o[2] - b.y, a.z - o[5]) + rl, 0.0f);
+                    hit = gx * gx + gy * gy + gz * gz < rl * rl * 1.0002f;
+                }
                 const unsigned m = __ballot_sync(0xffffffffu, hit);
                 if (hit) {
                     const int32_t pos = lc[kl] + __popc(m & below);
@@ -999,7 +1012,7 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
     // the distance test alone decides membership
     const float hq = (rl / 2.0f) * 1.0001f + 1e-6f;
     k_md_block_union<<<(unsigned)m->nblocks, kBlock, m->union_smem, c->stream>>>(
-        keys, (const float4*)m->pos32.p, live.sid, n, m->nL, m->apl, hq, m->fcap, m->ucap,
+        keys, (const float4*)m->pos32.p, live.sid, n, m->nL, m->apl, hq, rl, m->fcap, m->ucap,
         m->upow2, (int32_t*)m->ulist.p, (int32_t*)m->ucount.p, (uint16_t*)m->llist_leaf.p,
         (int32_t*)m->lcount_leaf.p, m->lcap_leaf, c->d_err, (int32_t*)m->diag.p + 2,
         sizing ? 1 : 0, pressure);
