@@ -631,6 +631,8 @@ def run_only(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.only == "md":
         out = md_eager_leg(nd, ctx)
+    elif args.only == "plain":
+        out = plain_leg(nd, ctx, ext, flush)
     elif args.only == "batched":
         out = batched_leg(nd, ctx, ext, flush)
     elif args.only == "adjoint":
@@ -661,7 +663,7 @@ def main():
                     help="skip the neighbour-search stress measurement")
     ap.add_argument("--stress-points", type=int, default=STRESS_N,
                     help="points of the stress measurement with --only stress (64 clusters)")
-    ap.add_argument("--only", choices=["md", "batched", "adjoint", "stress"],
+    ap.add_argument("--only", choices=["md", "plain", "batched", "adjoint", "stress"],
                     help="run one secondary measurement alone and print its JSON object "
                          "(for profiling)")
     args = ap.parse_args()

@@ -30,6 +30,7 @@
 
 namespace nd {
 
+constexpr int kSmallTPA = 4;         // threads per atom of the step kernel for small systems
 constexpr int kSizingFcap = 8192;    // BFS frontier entries per buffer in the sizing build
 constexpr int kSizingUcap = 8192;    // union capacity of the sizing build
 
@@ -506,19 +507,24 @@ __device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const
 // energies; state untouched).
 // BATCH: atoms of several systems; pair constants, walls and the fixed-point
 // origin come from the atom's system (a pair never crosses systems).
-template <bool COUL, bool MASS, bool FIRST, int MODE, bool BATCH>
-__global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
+// TPA: threads per atom.  With TPA > 1 (small systems, whose grid is under a
+// couple of waves) thread p of an atom sums list entries p, p + TPA, ... and
+// the slices are added in a fixed order before the atom's update.
+template <bool COUL, bool MASS, bool FIRST, int MODE, bool BATCH, int TPA = 1>
+__global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(StepArgs a) {
     extern __shared__ int4 srec[];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x & (kBlock - 1);  // the atom within the block
+    const int part = threadIdx.x / kBlock;       // its list slice
     int64_t i = (int64_t)blockIdx.x * kBlock + tid;
     const bool valid = i < a.n;
+    const bool own = part == 0;  // the thread that updates the atom
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
     // stage the block's union: record of atom (leaf * apl + e) at u * apl + e,
     // up to the shared-memory capacity; larger unions read the rest from L2
     {
         const int32_t nu = min(__ldg(&a.ucount[blockIdx.x]), a.ucap);
         const int32_t m = min(nu * a.apl, a.smrec);
-        for (int32_t k = tid; k < m; k += kBlock) {
+        for (int32_t k = threadIdx.x; k < m; k += kBlock * TPA) {
             const int32_t u = k / a.apl, e = k - u * a.apl;
             srec[k] = __ldg(&a.rec_in[(int64_t)__ldg(&U[u]) * a.apl + e]);
         }
@@ -554,27 +560,56 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         return __ldg(&a.rec_in[(int64_t)__ldg(&U[u]) * a.apl + e]);
     };
     float fx = 0.f, fy = 0.f, fz = 0.f, ue = 0.f;
-    // groups of four neighbours; the next group's indices are loaded while the
-    // current group is computed
-    int32_t s = 0;
-    int32_t li[4];
-    if (cnt >= 4) {
+    if constexpr (TPA == 1) {
+        // groups of four neighbours; the next group's indices are loaded
+        // while the current group is computed
+        int32_t s = 0;
+        int32_t li[4];
+        if (cnt >= 4) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)k * kBlock];
-    }
-    for (; s + 4 <= cnt; s += 4) {
-        int4 rj[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
-        if (s + 8 <= cnt) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)(s + 4 + k) * kBlock];
+            for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)k * kBlock];
         }
+        for (; s + 4 <= cnt; s += 4) {
+            int4 rj[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue);
+            for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
+            if (s + 8 <= cnt) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)(s + 4 + k) * kBlock];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue);
+        }
+        for (; s < cnt; ++s)
+            accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), pk, fx, fy, fz, ue);
+    } else {
+        // slice `part` of the list, the next index loaded ahead
+        int32_t li = part < cnt ? L[(int64_t)part * kBlock] : 0;
+        for (int32_t s = part; s < cnt; s += TPA) {
+            const int32_t sn = s + TPA;
+            const int32_t next = sn < cnt ? L[(int64_t)sn * kBlock] : 0;
+            accum_pair<COUL, MODE == 1>(ri, fetch(li), pk, fx, fy, fz, ue);
+            li = next;
+        }
+        __shared__ float spart[TPA > 1 ? TPA - 1 : 1][4][kBlock];
+        if (part > 0) {
+            spart[part - 1][0][tid] = fx;
+            spart[part - 1][1][tid] = fy;
+            spart[part - 1][2][tid] = fz;
+            spart[part - 1][3][tid] = ue;
+        }
+        __syncthreads();
+        if (own) {
+#pragma unroll
+            for (int p = 0; p < TPA - 1; ++p) {
+                fx += spart[p][0][tid];
+                fy += spart[p][1][tid];
+                fz += spart[p][2][tid];
+                ue += spart[p][3][tid];
+            }
+        }
     }
-    for (; s < cnt; ++s) accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), pk, fx, fy, fz, ue);
-    if (valid) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
+    if (valid && own) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
     const double imv = MASS ? a.im[i] : 1.0;
     const float fv[3] = {fx, fy, fz};
     if constexpr (MODE == 1) {
@@ -583,12 +618,12 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         for (int d = 0; d < 3; ++d) {
             double kick = (double)(a.hdt * fv[d]) * imv;
             double v = FIRST ? a.w[d][i] : a.w[d][i] + kick;
-            if (valid) a.v_out[d][i] = v;
+            if (valid && own) a.v_out[d][i] = v;
             ke += v * v;
         }
         double mass = MASS ? 1.0 / imv : 1.0;
-        double pe = valid ? 0.5 * (double)ue : 0.0;
-        ke = valid ? ke * 0.5 * mass : 0.0;
+        double pe = valid && own ? 0.5 * (double)ue : 0.0;
+        ke = valid && own ? ke * 0.5 * mass : 0.0;
         // per-system sums (one system unless batched); a warp spanning two
         // systems adds lane by lane
         if (BATCH && !__all_sync(0xffffffffu, sv == __shfl_sync(0xffffffffu, sv, 0))) {
@@ -613,7 +648,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         const float kdt = FIRST ? a.hdt : 2.0f * a.hdt;
         int32_t xi[3];
         bool trig = false;
-        if (valid) {
+        if (valid && own) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             double v = a.w[d][i] + (double)(kdt * fv[d]) * imv;
@@ -654,9 +689,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_md_step(StepArgs a) {
         // Early refit request: the block votes, and the last block to finish
         // (a ticket counter, no waiting) publishes the flag to the graph's
         // conditional node that follows this step.
-        if (__syncthreads_or(trig) && tid == 0) atomicOr(&a.ctl[0], 1u);
+        if (__syncthreads_or(trig) && threadIdx.x == 0) atomicOr(&a.ctl[0], 1u);
         if constexpr (MODE == 2) {
-            if (tid == 0) {
+            if (threadIdx.x == 0) {
                 __threadfence();
                 const unsigned ticket = atomicAdd(&a.ctl[1], 1u);
                 if (ticket == gridDim.x - 1) {
@@ -813,6 +848,16 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     m->union_smem = sizeof(int32_t) * (2 * (size_t)fcap + p2);
     m->step_smem = sizeof(int4) * (size_t)m->ucap_sm * m->apl;
     m->lists_smem = sizeof(float4) * (size_t)m->ucap_sm * m->apl;
+    // threads per atom of the step kernel: more than one for grids under two
+    // waves of one block per SM, when the slice partials fit beside the
+    // staged union
+    {
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+        const size_t part_sm = sizeof(float) * 4 * kBlock * (kSmallTPA - 1);
+        m->tpa = (m->nsys == 0 && m->nblocks < 2 * nsm &&
+                  (int)(m->step_smem + part_sm) + 1024 <= maxsm) ? kSmallTPA : 1;
+    }
     if ((int)m->union_smem + 1024 > maxsm || (lcap > 0 && (int)m->step_smem + 1024 > maxsm)) {
         c->last_error = "neighbour union too large for shared memory";
         return ND_ERR_OVERFLOW;
@@ -843,6 +888,18 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     ND_SMEM(true, false, false, 2) ND_SMEM(false, true, true, 2)
     ND_SMEM(false, true, false, 2) ND_SMEM(false, false, true, 2)
     ND_SMEM(false, false, false, 2)
+#undef ND_SMEM
+#define ND_SMEM(C, M, F, MODE) \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false, kSmallTPA>, maxsm);
+    ND_SMEM(true, true, true, 0) ND_SMEM(true, true, false, 0) ND_SMEM(true, false, true, 0)
+    ND_SMEM(true, false, false, 0) ND_SMEM(false, true, true, 0) ND_SMEM(false, true, false, 0)
+    ND_SMEM(false, false, true, 0) ND_SMEM(false, false, false, 0)
+    ND_SMEM(true, true, true, 1) ND_SMEM(true, true, false, 1) ND_SMEM(true, false, true, 1)
+    ND_SMEM(true, false, false, 1) ND_SMEM(false, true, true, 1) ND_SMEM(false, true, false, 1)
+    ND_SMEM(false, false, true, 1) ND_SMEM(false, false, false, 1)
+    ND_SMEM(true, true, true, 2) ND_SMEM(true, true, false, 2) ND_SMEM(true, false, true, 2)
+    ND_SMEM(true, false, false, 2) ND_SMEM(false, true, true, 2) ND_SMEM(false, true, false, 2)
+    ND_SMEM(false, false, true, 2) ND_SMEM(false, false, false, 2)
 #undef ND_SMEM
     if (e != cudaSuccess) return cuda_fail(c, e, "shared memory opt-in");
     return ND_OK;
@@ -919,6 +976,20 @@ static void launch_step_impl(MDEngine* m, const StepArgs& a, bool first) {
     const bool mass = m->has_m;
     if (m->nsys > 0) {
 #define ND_STEP(C, M, F) k_md_step<C, M, F, MODE, true><<<grid, kBlock, sm, c->stream>>>(a)
+        if (coul) {
+            if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
+            else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
+        } else {
+            if (mass) { if (first) ND_STEP(false, true, true); else ND_STEP(false, true, false); }
+            else { if (first) ND_STEP(false, false, true); else ND_STEP(false, false, false); }
+        }
+#undef ND_STEP
+        c->launches++;
+        return;
+    }
+    if (m->tpa > 1) {
+#define ND_STEP(C, M, F) \
+    k_md_step<C, M, F, MODE, false, kSmallTPA><<<grid, kBlock * kSmallTPA, sm, c->stream>>>(a)
         if (coul) {
             if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
             else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }

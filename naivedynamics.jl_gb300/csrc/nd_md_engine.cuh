@@ -128,6 +128,7 @@ struct MDEngine {
     int64_t resort_kernels = 0;       // kernels of one re-sort rebuild
     int64_t eager_bodies = 0;         // kernels of rebuild bodies run eagerly (counted by the host)
     size_t step_smem = 0, union_smem = 0, lists_smem = 0;
+    int32_t tpa = 1;  // threads per atom of the step kernel
     // observers of the step loop: thermostat (rescale_velocity!) and position log
     double thermo_T = 0.0, thermo_gamma = 0.0;
     int32_t thermo_every = 0, log_every = 0;
