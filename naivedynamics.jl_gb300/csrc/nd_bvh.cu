@@ -932,6 +932,134 @@ __global__ void __launch_bounds__(128)
     atom_query(qi, keys, pos, apl, r2, 2 * (n / apl) - 1, err, s);
 }
 
+// Two-phase form of the one-pass emission, for callers that allow scratch
+// memory.  Broad phase: the warp's union walk of k_leaf_warp4 records the
+// candidate leaf pairs (q, t) -- t > q with overlapping boxes, and (q, q) for
+// the pairs inside q -- through a per-warp shared buffer; the walk's work per
+// visited leaf is one box test.  Narrow phase: one thread per candidate leaf
+// pair runs the 4 x 4 distance tests and emits through the warp buffers of
+// k_leaf_warp4.  The distance tests, most of the work, are then spread evenly
+// over the GPU however dense the points are, instead of following the walks
+// of the densest regions.
+constexpr int kLeafBuf = 256;  // candidate leaf pairs buffered per warp
+
+__device__ __forceinline__ void lp_flush(int2* buf, int& nb, unsigned long long* cursor, int64_t cap,
+                                         int2* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0 && nb) base = atomicAdd(cursor, (unsigned long long)nb);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (int k = lane; k < nb; k += 32) {
+        const unsigned long long w = base + (unsigned long long)k;
+        if ((int64_t)w < cap) out[w] = buf[k];
+    }
+    __syncwarp();
+    nb = 0;
+}
+
+__device__ __forceinline__ void lp_append(bool want, int32_t q, int32_t t, int2* buf, int& nb,
+                                          unsigned long long* cursor, int64_t cap,
+                                          int2* __restrict__ out) {
+    const unsigned bal = __ballot_sync(0xffffffffu, want);
+    if (!bal) return;
+    const int total = __popc(bal);
+    if (nb + total > kLeafBuf) lp_flush(buf, nb, cursor, cap, out);
+    if (want) buf[nb + __popc(bal & ((1u << (threadIdx.x & 31)) - 1u))] = make_int2(q, t);
+    __syncwarp();
+    nb += total;
+}
+
+__global__ void __launch_bounds__(128)
+    k_leaf_broad4(const float4* __restrict__ keys, int32_t nL, unsigned long long* cursor,
+                  int64_t cap, int2* __restrict__ out, int32_t* err) {
+    __shared__ int2 sbuf[4][kLeafBuf];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int32_t q0 = (int32_t)((blockIdx.x * 4 + w) * 32) + 1;
+    if (q0 > nL) return;  // whole warp
+    int2* buf = sbuf[w];
+    const int32_t q = q0 + lane;
+    const bool valid = q <= nL;
+    Node ql;
+    if (valid) {
+        ql = load_node(keys, q);
+    } else {
+        ql.mnx = ql.mny = ql.mnz = INFINITY;
+        ql.mxx = ql.mxy = ql.mxz = -INFINITY;
+        ql.left = ql.skip = 0;
+    }
+    int nb = 0;
+    lp_append(valid, q, q, buf, nb, cursor, cap, out);  // pairs inside the leaf
+    Node un = ql;
+    for (int sh = 16; sh > 0; sh >>= 1) {
+        un.mnx = fminf(un.mnx, __shfl_xor_sync(0xffffffffu, un.mnx, sh));
+        un.mny = fminf(un.mny, __shfl_xor_sync(0xffffffffu, un.mny, sh));
+        un.mnz = fminf(un.mnz, __shfl_xor_sync(0xffffffffu, un.mnz, sh));
+        un.mxx = fmaxf(un.mxx, __shfl_xor_sync(0xffffffffu, un.mxx, sh));
+        un.mxy = fmaxf(un.mxy, __shfl_xor_sync(0xffffffffu, un.mxy, sh));
+        un.mxz = fmaxf(un.mxz, __shfl_xor_sync(0xffffffffu, un.mxz, sh));
+    }
+    int32_t t = __shfl_sync(0xffffffffu, ql.skip, 0);
+    int32_t visits = 0;
+    const int32_t nnodes = 2 * nL - 1;
+    while (t != 0) {
+        if (t < 1 || t > nnodes || ++visits > nnodes) {
+            if (lane == 0) set_error(err, ND_ERR_INTERNAL, q0);
+            break;
+        }
+        const Node nd_ = load_node(keys, t);
+        if (overlap(un, nd_)) {
+            if (nd_.left == 0) {
+                lp_append(valid && t > q && overlap(ql, nd_), q, t, buf, nb, cursor, cap, out);
+                t = nd_.skip;
+            } else {
+                t = nd_.left;
+            }
+        } else {
+            t = nd_.skip;
+        }
+    }
+    lp_flush(buf, nb, cursor, cap, out);
+}
+
+__global__ void __launch_bounds__(256)
+    k_leaf_narrow4(const int2* __restrict__ lp, int64_t nlp, const float4* __restrict__ pos,
+                   float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
+                   float* pd) {
+    constexpr int APL = 4;
+    __shared__ int32_t sbi[8][kWarpBuf], sbj[8][kWarpBuf];
+    __shared__ float sbd[8][kWarpBuf];
+    const int w = threadIdx.x >> 5;
+    int32_t* bi = sbi[w];
+    int32_t* bj = sbj[w];
+    float* bd = sbd[w];
+    int nb = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // warp-uniform trip count: lanes past the end test nothing but join the ballots
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+         __any_sync(0xffffffffu, k < nlp); k += stride) {
+        unsigned mask = 0;
+        float4 qa[APL], tb[APL];
+        if (k < nlp) {
+            const int2 e = __ldg(&lp[k]);
+            const int64_t A = (int64_t)(e.x - 1) * APL, B = (int64_t)(e.y - 1) * APL;
+#pragma unroll
+            for (int i = 0; i < APL; ++i) qa[i] = __ldg(&pos[A + i]);
+#pragma unroll
+            for (int j = 0; j < APL; ++j) tb[j] = __ldg(&pos[B + j]);
+            const bool self = e.x == e.y;
+#pragma unroll
+            for (int m = 0; m < 16; ++m) {
+                const int i = m >> 2, j = m & 3;
+                if ((!self || j > i) &&
+                    dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z) < r2)
+                    mask |= 1u << m;
+            }
+        }
+        warp_emit16(mask, qa, tb, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+    }
+    warp_buf_flush(bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+}
+
 nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int32_t* pj,
                          float* pd, int64_t capacity, int64_t* total) {
     const float r2 = r * r;  // (neighbor_distance)^2 in Float32
@@ -939,13 +1067,47 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
     nd_status st;
     if ((st = ensure(c, c->misc, 64))) return st;
     unsigned long long* cursor = (unsigned long long*)c->misc.p;
-    cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
-    k_leaf_warp4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
-        t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd, c->d_err);
-    c->launches++;
-    if ((st = check_launch(c, "leaf pairs (unordered)"))) return st;
     unsigned long long tot = 0;
-    cudaError_t e = cudaMemcpyAsync(&tot, cursor, sizeof(tot), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e;
+    if (c->no_alloc) {
+        // no scratch for candidate pairs: the one-pass walk
+        cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
+        k_leaf_warp4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
+            t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd, c->d_err);
+        c->launches++;
+    } else {
+        // broad phase, re-run once with a larger buffer if it overflowed
+        unsigned long long nlp = 0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            int64_t lcap = (int64_t)(c->leafpairs.bytes / sizeof(int2));
+            if (lcap < 16 * (int64_t)t.nL) {
+                if ((st = ensure(c, c->leafpairs, sizeof(int2) * 16 * (size_t)t.nL))) return st;
+                lcap = 16 * (int64_t)t.nL;
+            }
+            cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
+            k_leaf_broad4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
+                t.keys, t.nL, cursor, lcap, (int2*)c->leafpairs.p, c->d_err);
+            c->launches++;
+            if ((st = check_launch(c, "leaf pairs (broad phase)"))) return st;
+            e = cudaMemcpyAsync(&nlp, cursor, sizeof(nlp), cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "candidate leaf pairs");
+            if ((int64_t)nlp <= lcap) break;
+            if ((st = ensure(c, c->leafpairs, sizeof(int2) * (size_t)(nlp + nlp / 4)))) return st;
+        }
+        cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+        const int64_t blocks = std::min<int64_t>(cdiv((int64_t)nlp, 256), (int64_t)nsm * 32);
+        if (nlp > 0) {
+            k_leaf_narrow4<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, c->stream>>>(
+                (const int2*)c->leafpairs.p, (int64_t)nlp, t.pos4, r2, cursor, capacity, pi, pj,
+                pd);
+            c->launches++;
+        }
+    }
+    if ((st = check_launch(c, "leaf pairs (unordered)"))) return st;
+    e = cudaMemcpyAsync(&tot, cursor, sizeof(tot), cudaMemcpyDeviceToHost, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "pair count");
     if ((st = sync_and_check(c, "leaf pairs (unordered)"))) return st;
     *total = (int64_t)tot;

@@ -303,7 +303,8 @@ nd_status nd_ctx_destroy(nd_ctx* h) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     nd::DevBuf* bufs[] = {&c->xyz, &c->codes, &c->codes_alt, &c->perm, &c->perm_alt, &c->pos4,
                           &c->idx, &c->keys, &c->store, &c->hist, &c->counts, &c->offsets,
-                          &c->partial, &c->pairs_i, &c->pairs_j, &c->pairs_d, &c->misc, &c->hash};
+                          &c->partial, &c->pairs_i, &c->pairs_j, &c->pairs_d, &c->misc, &c->hash,
+                          &c->leafpairs};
     for (nd::DevBuf* b : bufs) nd::free_buf(*b);
     if (c->d_err) cudaFree(c->d_err);
     if (c->h_err) cudaFreeHost(c->h_err);

@@ -136,7 +136,7 @@ struct Ctx {
     std::string last_error;
     // scratch buffers of the neighbour-search pipeline, grown on demand
     DevBuf xyz, codes, codes_alt, perm, perm_alt, pos4, idx, keys, store, hist, counts, offsets,
-        partial, pairs_i, pairs_j, pairs_d, misc, hash;
+        partial, pairs_i, pairs_j, pairs_d, misc, hash, leafpairs;
     struct MDEngine* sim_cache = nullptr;  // engine re-used by nd_simulate
     bool no_alloc = false;                 // buffers are fixed slices: never grow them
 };

@@ -48,6 +48,24 @@ def test_thermostat_matches_oracle(nd, oracle, every):
     assert np.abs(vg - vr).max() < TOL
 
 
+def test_thermostat_with_masses_and_charges(nd, oracle):
+    # Ti weights |v_i| by m_i (rescale_velocity!, Simulator.jl:130); the
+    # rescaled half-step velocity keeps the per-atom dt/2 F/m of the next kick
+    x, v, q = nd.synth.lj_system(0x4E440001, N, SIDE, 0.8, charges=True)
+    m = 1.0 + np.random.default_rng(3).random(N)
+    p = nd.md_params(coulomb_k=1.0, cutoff=2.5, skin=0.3, dt=1e-3, box_hi=(SIDE,) * 3,
+                     rebuild_every=10)
+    eng = nd.MDEngine(p, x, v, q, m)
+    eng.set_thermostat(0.8, 0.7, 10)
+    eng.run(40)
+    xg, vg, _ = eng.get()
+    eng.close()
+    pr = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(SIDE,) * 3, dt=1e-3)
+    xr, vr, _, _ = oracle.md_run_observed(pr, x, v, q=q, m=m, steps=40, thermo=(0.8, 0.7, 10))
+    assert np.abs(xg - xr).max() < TOL
+    assert np.abs(vg - vr).max() < TOL
+
+
 @pytest.mark.parametrize("every", [5, 15])
 def test_position_log_matches_oracle(nd, oracle, every):
     x, v, _ = _state(nd)
