@@ -304,7 +304,7 @@ def stress_leg(nd, ctx, ext, flush, steps=3, cpu=True, points=STRESS_N):
     """Neighbour-search stress: 4,194,304 Float32 points in 64 isotropic
     Gaussian clusters (centres uniform in a cube of side 400, sigma U[2, 10]),
     r = 2.5, LBVH build + traversal + emission of the half pair list (i, j, d)
-    into device memory (nd_leaf_pairs_dev, spatial order, one-pass emission),
+    into device memory (nd_leaf_pairs_dev, spatial order, two-phase emission),
     inputs resident, L2 flushed before each call.  cpu: the oracle's leaf-BVH
     build + order-free hash traversal of the same points on all host cores."""
     import numpy as np
