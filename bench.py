@@ -33,6 +33,7 @@ N_ATOMS = 262144
 SIDE = 68.0
 MD_PER_STEP = 100
 REBUILD = 10
+UNION_NAMES = {0: "blocks", 1: "tree"}
 SEED = 0x4E440002
 METRIC = "LJ+Coulomb atom-steps/s @262k (FP32 forces, FP64 x/v, rebuild every 10)"
 UNIT = "atom-steps/s"
@@ -223,7 +224,8 @@ def batched_leg(nd, ctx, ext, flush):
         p = nd.md_params(sigma=float(e["sigma"][k]), epsilon=float(e["epsilon"][k]), cutoff=2.5,
                          skin=tuned.skin, dt=1e-3, box_lo=(0, 0, 0), box_hi=(side, side, side),
                          atomsperleaf=tuned.atomsperleaf, rebuild_every=REBUILD,
-                         resort_every=tuned.resort_every, stage_policy=tuned.stage_policy)
+                         resort_every=tuned.resort_every, stage_policy=tuned.stage_policy,
+                         union_search=tuned.union_search)
         eng = nd.MDEngine(p, e["x"][sl], e["v"][sl], ctx=ctx)
         _, _, fp = eng.get()
         f_err = max(f_err, float(np.linalg.norm(f_bat[sl] - fp) / np.linalg.norm(fp)))
@@ -248,7 +250,9 @@ def batched_leg(nd, ctx, ext, flush):
             "early_refits": bat_diag["early_refits"],
             "tuned": {"skin": tuned.skin, "atomsperleaf": tuned.atomsperleaf,
                       "resort_every": tuned.resort_every,
-                      "stage_policy": tuned.stage_policy, "autotune_s": round(tune_s, 2)},
+                      "stage_policy": tuned.stage_policy,
+                      "union_search": UNION_NAMES[tuned.union_search],
+                      "autotune_s": round(tune_s, 2)},
             "plain_path": "512 nd_md engines run one after another on one stream (graphs)"}
 
 
@@ -547,7 +551,9 @@ def run_gb300(args):
                                  "refit between",
                    "tuned": {"skin": params.skin, "atomsperleaf": params.atomsperleaf,
                              "resort_every": params.resort_every,
-                             "stage_policy": params.stage_policy, "autotune_s": round(tune_s, 2)},
+                             "stage_policy": params.stage_policy,
+                             "union_search": UNION_NAMES[params.union_search],
+                             "autotune_s": round(tune_s, 2)},
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "512 MB buffer written before every timed step (outside the events)",
                    "neighbours_per_atom": round(nbr, 2),
@@ -588,12 +594,12 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
-def md_eager_leg(nd, ctx):
+def md_eager_leg(nd, ctx, union_search="blocks"):
     """The headline workload with the settings the autotuner picks for it
-    (skin 0.4, 8 atoms per leaf, re-sort every 10th window), created and run
-    for ten windows eagerly (nd_md_step_times), so that every kernel is a
-    plain launch in a known order for profiling: engine creation (three
-    builds), then per window a rebuild and ten steps."""
+    (skin 0.4, 8 atoms per leaf, re-sort every 10th window; the given union
+    search), created and run for ten windows eagerly (nd_md_step_times), so
+    that every kernel is a plain launch in a known order for profiling: engine
+    creation (three builds), then per window a rebuild and ten steps."""
     import numpy as np
 
     import torch
@@ -601,6 +607,7 @@ def md_eager_leg(nd, ctx):
     x, v, q = nd.synth.lj_system(SEED, N_ATOMS, SIDE, 0.8, charges=True)
     p = _md_params(nd)
     p.skin, p.atomsperleaf, p.resort_every = 0.4, 8, 10
+    p.union_search = {v_: k for k, v_ in UNION_NAMES.items()}[union_search]
     eng = nd.MDEngine(p, x, v, q, ctx=ctx)
     ms = eng.step_times(10 * REBUILD)
     # then the same settings through the captured graphs, CUDA events
@@ -616,7 +623,8 @@ def md_eager_leg(nd, ctx):
         if k > 0:
             graph_ms.append(a.elapsed_time(b))
     eng.close()
-    return {"workload": WORKLOAD + " (fixed settings)", "step_kernel_ms_mean": float(np.mean(ms)),
+    return {"workload": WORKLOAD + f" (fixed settings, union search {union_search})",
+            "step_kernel_ms_mean": float(np.mean(ms)),
             "graph_ms_per_100_steps": float(np.median(graph_ms)),
             "atom_steps_per_s": N_ATOMS * MD_PER_STEP / (float(np.median(graph_ms)) * 1e-3)}
 
@@ -630,7 +638,7 @@ def run_only(args):
     ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.only == "md":
-        out = md_eager_leg(nd, ctx)
+        out = md_eager_leg(nd, ctx, union_search=args.union_search)
     elif args.only == "plain":
         out = plain_leg(nd, ctx, ext, flush)
     elif args.only == "batched":
@@ -663,6 +671,8 @@ def main():
                     help="skip the neighbour-search stress measurement")
     ap.add_argument("--stress-points", type=int, default=STRESS_N,
                     help="points of the stress measurement with --only stress (64 clusters)")
+    ap.add_argument("--union-search", choices=["blocks", "tree"], default="blocks",
+                    help="union search of the fixed-settings engine of --only md")
     ap.add_argument("--only", choices=["md", "plain", "batched", "adjoint", "stress"],
                     help="run one secondary measurement alone and print its JSON object "
                          "(for profiling)")

@@ -97,7 +97,15 @@ typedef struct {
                               kept tree; 0 = 1 (always re-sort) */
     int32_t stage_policy;  /* shared-memory staging of a block's neighbour records:
                               0 = sized near the mean union, 1 = the largest union */
+    int32_t union_search;  /* how a block of 256 atoms finds the leaves near it (the same
+                              leaves either way): ND_UNION_BLOCKS = boxes of the blocks of
+                              the kept order, ND_UNION_TREE = breadth-first walk of the
+                              LBVH built (re-sort) or refitted (refit) at every rebuild */
+    int32_t reserved;      /* 0 */
 } nd_md_params;
+
+#define ND_UNION_BLOCKS 0
+#define ND_UNION_TREE   1
 
 /* One system of a batched ensemble: its atom count (a multiple of atomsperleaf),
  * Lennard-Jones parameters and reflecting walls.  Systems never interact. */
@@ -346,7 +354,7 @@ nd_status nd_batch_energies(nd_md* md, double* potential, double* kinetic);
  * Autotuner: times short runs of candidate engine settings on copies of the
  * given state (host arrays; the state is not advanced) and writes the fastest
  * into *best (skin -- p->skin, +0.1 or +0.2 --, atomsperleaf -- the
- * leaf/traversal width --, resort_every and stage_policy; every other field
+ * leaf/traversal width --, resort_every, stage_policy and union_search; every other field
  * copied from *p), tuning one setting at a time.  nsys == 0 tunes a plain
  * engine (sys ignored).  Candidates change only the summation order of the
  * forces, not which pairs interact.  trial_steps: timed steps per candidate

@@ -169,14 +169,102 @@ __device__ __forceinline__ bool box_overlap(float qmnx, float qmny, float qmnz, 
            (qmxz > a.z);
 }
 
-// One block per 256 atoms: the boxes of its eight warps (their atoms -/+ hq)
-// are tested against the tree breadth-first -- all 256 threads expand the
-// current level together, a node's children being (left, skip of left) in the
-// rope layout -- and every leaf overlapping any of them joins the union.  The union is sorted (bitonic)
-// so list order, and hence force summation order, is deterministic.
-// Shared memory: two frontier buffers of fcap entries and the union (upow2).
+// Boxes of the blocks of kBlock atoms (the union of their leaves' key boxes,
+// exact: min / max only) and of the super-blocks of 32 blocks, stored like
+// tree nodes (min xyz, max x), (max y, max z, 0, 0): blocks at [0, nblocks),
+// super-blocks after them.  One thread block of 32 warps per super-block,
+// one warp per block.
+__global__ void __launch_bounds__(1024)
+    k_md_block_boxes(const float4* __restrict__ keys, int32_t nL, int32_t nblocks, int32_t lpb,
+                     float4* __restrict__ bbox) {
+    __shared__ float s_b[32][6];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int32_t b = blockIdx.x * 32 + w;
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (b < nblocks) {
+        const int32_t l1 = min((b + 1) * lpb, nL);
+        for (int32_t l = b * lpb + lane; l < l1; l += 32) {
+            const float4 a = __ldg(&keys[2 * (int64_t)l]), c = __ldg(&keys[2 * (int64_t)l + 1]);
+            mn[0] = fminf(mn[0], a.x); mn[1] = fminf(mn[1], a.y); mn[2] = fminf(mn[2], a.z);
+            mx[0] = fmaxf(mx[0], a.w); mx[1] = fmaxf(mx[1], c.x); mx[2] = fmaxf(mx[2], c.y);
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        for (int s = 16; s > 0; s >>= 1) {
+            mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], s));
+            mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], s));
+        }
+    if (lane == 0) {
+        if (b < nblocks) {
+            bbox[2 * (int64_t)b] = make_float4(mn[0], mn[1], mn[2], mx[0]);
+            bbox[2 * (int64_t)b + 1] = make_float4(mx[1], mx[2], 0.f, 0.f);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { s_b[w][d] = mn[d]; s_b[w][3 + d] = mx[d]; }
+    }
+    __syncthreads();
+    if (w == 0) {
+        float v[6];
+#pragma unroll
+        for (int d = 0; d < 6; ++d) v[d] = s_b[lane][d];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            for (int s = 16; s > 0; s >>= 1) {
+                v[d] = fminf(v[d], __shfl_xor_sync(0xffffffffu, v[d], s));
+                v[3 + d] = fmaxf(v[3 + d], __shfl_xor_sync(0xffffffffu, v[3 + d], s));
+            }
+        if (lane == 0) {
+            const int64_t sb = nblocks + (int64_t)blockIdx.x;
+            bbox[2 * sb] = make_float4(v[0], v[1], v[2], v[3]);
+            bbox[2 * sb + 1] = make_float4(v[4], v[5], 0.f, 0.f);
+        }
+    }
+}
+
+// Order-keeping compaction over the whole thread block: threads with `keep`
+// write `value` to out[base + rank], rank counted in thread order.  Returns
+// the number kept (the same in every thread).  Every thread must call it.
+__device__ __forceinline__ int32_t block_compact(bool keep, int32_t value, int32_t* out,
+                                                 int32_t base, int32_t cap, int32_t* s_w) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) s_w[warp] = __popc(bal);
+    __syncthreads();
+    int32_t off = base, total = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) {
+        const int32_t c = s_w[w];
+        off += w < warp ? c : 0;
+        total += c;
+    }
+    if (keep) {
+        const int32_t at = off + __popc(bal & ((1u << lane) - 1u));
+        if (at < cap) out[at] = value;
+    }
+    __syncthreads();
+    return total;
+}
+
+// One block per 256 atoms: every leaf whose box overlaps one of the block's
+// eight warp boxes (their atoms -/+ hq) joins the block's union, sorted by
+// leaf index so list order, and hence force summation order, is
+// deterministic.  Two searches give the same union:
+//  - blocks (tree == 0): the super-block boxes, then the boxes of the blocks
+//    of overlapping super-blocks, are tested against the union of the warp
+//    boxes (a leaf overlapping a warp box lies in a block and a super-block
+//    whose boxes overlap that union); the leaves of the candidate blocks are
+//    tested against the warp boxes.  Enumerating in index order at every
+//    level leaves the union sorted.
+//  - tree (tree == 1): the warp boxes are tested against the tree
+//    breadth-first -- all 256 threads expand the current level together, a
+//    node's children being (left, skip of left) in the rope layout -- and the
+//    union is sorted (bitonic) afterwards.
+// Shared memory: two buffers of fcap entries (BFS frontiers, or candidate
+// super-blocks and blocks) and the union (upow2).
 __global__ void __launch_bounds__(kBlock)
-    k_md_block_union(const float4* __restrict__ keys, const float4* __restrict__ pos,
+    k_md_block_union(const float4* __restrict__ keys, const float4* __restrict__ bbox,
+                     int32_t nblocks, int32_t tree, const float4* __restrict__ pos,
                      const int32_t* __restrict__ sid,
                      int32_t n, int32_t nL, int32_t apl, float hq, float rl, int32_t fcap,
                      int32_t ucap, int32_t upow2, int32_t* __restrict__ ulist,
@@ -189,6 +277,8 @@ __global__ void __launch_bounds__(kBlock)
     int32_t* su = smem + 2 * fcap;
     __shared__ int32_t s_cnt[2];
     __shared__ int32_t s_nu, s_nb;
+    __shared__ int32_t s_w[kBlock / 32];
+    __shared__ float s_ub[6];
     // query boxes (min xyz, max xyz): one per warp, two for a warp whose atoms
     // belong to two systems of a batched ensemble (lanes of lane 0's system,
     // and the rest)
@@ -224,45 +314,100 @@ __global__ void __launch_bounds__(kBlock)
     }
     __syncthreads();
     const int nb = s_nb;
-    int cur = 0;
-    for (int level = 0; level < 256; ++level) {
-        const int32_t nf = min(s_cnt[cur], fcap);
-        if (nf == 0) break;
-        for (int32_t k = tid; k < nf; k += kBlock) {
-            const int32_t e = fr[cur][k];
-            const int32_t t = e >> 1;
-            if (t < 1 || t > 2 * nL - 1) { set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x); continue; }
-            const float4 a = __ldg(&keys[2 * (int64_t)(t - 1)]);
-            const float4 b = __ldg(&keys[2 * (int64_t)(t - 1) + 1]);
-            const int32_t left = __float_as_int(b.z), skip = __float_as_int(b.w);
-            if (e & 1) {  // a left child: its skip rope is its right sibling
-                int32_t slot = atomicAdd(&s_cnt[cur ^ 1], 1);
-                if (slot < fcap) fr[cur ^ 1][slot] = skip << 1;
-            }
+    int32_t nu;
+    if (!tree) {
+        if (tid < 6) {
+            float v = tid < 3 ? INFINITY : -INFINITY;
+            for (int w = 0; w < nb; ++w) v = tid < 3 ? fminf(v, s_wb[w][tid]) : fmaxf(v, s_wb[w][tid]);
+            s_ub[tid] = v;
+        }
+        __syncthreads();
+        const float u0 = s_ub[0], u1 = s_ub[1], u2 = s_ub[2], u3 = s_ub[3], u4 = s_ub[4],
+                    u5 = s_ub[5];
+        int32_t* csb = fr[0];
+        int32_t* cb = fr[1];
+        const int32_t nsb = (nblocks + 31) >> 5;
+        int32_t ncs = 0;
+        for (int32_t base = 0; base < nsb; base += kBlock) {
+            const int32_t s = base + tid;
+            const bool keep = s < nsb && box_overlap(u0, u1, u2, u3, u4, u5,
+                                                     __ldg(&bbox[2 * ((int64_t)nblocks + s)]),
+                                                     __ldg(&bbox[2 * ((int64_t)nblocks + s) + 1]));
+            ncs += block_compact(keep, s, csb, ncs, fcap, s_w);
+        }
+        int32_t ncb = 0;
+        const int32_t ks = min(ncs, fcap) * 32;
+        for (int32_t base = 0; base < ks; base += kBlock) {
+            const int32_t k = base + tid;
+            const int32_t b = k < ks ? csb[k >> 5] * 32 + (k & 31) : nblocks;
+            const bool keep = b < nblocks && box_overlap(u0, u1, u2, u3, u4, u5,
+                                                         __ldg(&bbox[2 * (int64_t)b]),
+                                                         __ldg(&bbox[2 * (int64_t)b + 1]));
+            ncb += block_compact(keep, b, cb, ncb, fcap, s_w);
+        }
+        if (tid == 0) {
+            const int32_t mc = max(ncs, ncb);
+            atomicMax(&diag[4], mc);
+            if (pressure && 10 * mc > 9 * fcap) atomicOr(pressure, 1u);
+            if (mc > fcap && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)blockIdx.x);
+        }
+        const int32_t lpb = kBlock / apl, lsh = __ffs(lpb) - 1;  // leaves per block (2^lsh)
+        const int32_t kl = min(ncb, fcap) << lsh;
+        nu = 0;
+        for (int32_t base = 0; base < kl; base += kBlock) {
+            const int32_t k = base + tid;
+            const int32_t leaf = k < kl ? (cb[k >> lsh] << lsh) + (k & (lpb - 1)) : nL;
             bool hit = false;
-            for (int w = 0; w < nb && !hit; ++w)
-                hit = box_overlap(s_wb[w][0], s_wb[w][1], s_wb[w][2], s_wb[w][3], s_wb[w][4],
-                                  s_wb[w][5], a, b);
-            if (hit) {
-                if (left == 0) {
-                    int32_t slot = atomicAdd(&s_nu, 1);
-                    if (slot < upow2) su[slot] = t - 1;
-                } else {
+            if (leaf < nL) {
+                const float4 a = __ldg(&keys[2 * (int64_t)leaf]);
+                const float4 b = __ldg(&keys[2 * (int64_t)leaf + 1]);
+                for (int w = 0; w < nb && !hit; ++w)
+                    hit = box_overlap(s_wb[w][0], s_wb[w][1], s_wb[w][2], s_wb[w][3], s_wb[w][4],
+                                      s_wb[w][5], a, b);
+            }
+            nu += block_compact(hit, leaf, su, nu, upow2, s_w);
+        }
+    } else {
+        int cur = 0;
+        for (int level = 0; level < 256; ++level) {
+            const int32_t nf = min(s_cnt[cur], fcap);
+            if (nf == 0) break;
+            for (int32_t k = tid; k < nf; k += kBlock) {
+                const int32_t e = fr[cur][k];
+                const int32_t t = e >> 1;
+                if (t < 1 || t > 2 * nL - 1) { set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x); continue; }
+                const float4 a = __ldg(&keys[2 * (int64_t)(t - 1)]);
+                const float4 b = __ldg(&keys[2 * (int64_t)(t - 1) + 1]);
+                const int32_t left = __float_as_int(b.z), skip = __float_as_int(b.w);
+                if (e & 1) {  // a left child: its skip rope is its right sibling
                     int32_t slot = atomicAdd(&s_cnt[cur ^ 1], 1);
-                    if (slot < fcap) fr[cur ^ 1][slot] = (left << 1) | 1;
+                    if (slot < fcap) fr[cur ^ 1][slot] = skip << 1;
+                }
+                bool hit = false;
+                for (int w = 0; w < nb && !hit; ++w)
+                    hit = box_overlap(s_wb[w][0], s_wb[w][1], s_wb[w][2], s_wb[w][3], s_wb[w][4],
+                                      s_wb[w][5], a, b);
+                if (hit) {
+                    if (left == 0) {
+                        int32_t slot = atomicAdd(&s_nu, 1);
+                        if (slot < upow2) su[slot] = t - 1;
+                    } else {
+                        int32_t slot = atomicAdd(&s_cnt[cur ^ 1], 1);
+                        if (slot < fcap) fr[cur ^ 1][slot] = (left << 1) | 1;
+                    }
                 }
             }
+            __syncthreads();
+            if (tid == 0) {
+                atomicMax(&diag[4], s_cnt[cur ^ 1]);
+                if (s_cnt[cur ^ 1] > fcap && !sizing) set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x);
+                s_cnt[cur] = 0;
+            }
+            cur ^= 1;
+            __syncthreads();
         }
-        __syncthreads();
-        if (tid == 0) {
-            atomicMax(&diag[4], s_cnt[cur ^ 1]);
-            if (s_cnt[cur ^ 1] > fcap && !sizing) set_error(err, ND_ERR_INTERNAL, (int32_t)blockIdx.x);
-            s_cnt[cur] = 0;
-        }
-        cur ^= 1;
-        __syncthreads();
+        nu = s_nu;
     }
-    const int32_t nu = s_nu;
     if (tid == 0) { atomicMax(&diag[0], nu); atomicAdd(&diag[3], nu); }
     if (tid == 0 && pressure && 10 * (int64_t)nu > 9 * (int64_t)ucap) atomicOr(pressure, 1u);
     if (nu > ucap) {
@@ -274,21 +419,24 @@ __global__ void __launch_bounds__(kBlock)
         }
         return;
     }
-    // bitonic sort of the union (padded to a power of two)
-    int32_t p2 = 1;
-    while (p2 < nu) p2 <<= 1;
-    for (int32_t k = nu + tid; k < p2; k += kBlock) su[k] = INT32_MAX;
-    __syncthreads();
-    for (int32_t size = 2; size <= p2; size <<= 1) {
-        for (int32_t stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int32_t k = tid; k < p2 / 2; k += kBlock) {
-                int32_t lo = 2 * k - (k & (stride - 1));
-                int32_t hi = lo + stride;
-                bool up = ((lo & size) == 0);
-                int32_t a = su[lo], b = su[hi];
-                if ((a > b) == up) { su[lo] = b; su[hi] = a; }
+    // bitonic sort of the union (padded to a power of two); the block search
+    // enumerates it in order
+    if (tree) {
+        int32_t p2 = 1;
+        while (p2 < nu) p2 <<= 1;
+        for (int32_t k = nu + tid; k < p2; k += kBlock) su[k] = INT32_MAX;
+        __syncthreads();
+        for (int32_t size = 2; size <= p2; size <<= 1) {
+            for (int32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int32_t k = tid; k < p2 / 2; k += kBlock) {
+                    int32_t lo = 2 * k - (k & (stride - 1));
+                    int32_t hi = lo + stride;
+                    bool up = ((lo & size) == 0);
+                    int32_t a = su[lo], b = su[hi];
+                    if ((a > b) == up) { su[lo] = b; su[hi] = a; }
+                }
+                __syncthreads();
             }
-            __syncthreads();
         }
     }
     int32_t* dst = ulist + (int64_t)blockIdx.x * ucap;
@@ -790,6 +938,8 @@ static nd_status md_alloc(MDEngine* m) {
     if ((st = ensure(c, m->pos32, n * sizeof(float4)))) return st;
     if ((st = ensure(c, m->keys, 32 * (size_t)(2 * m->nL)))) return st;
     if ((st = ensure(c, m->store, sizeof(int32_t) * (size_t)m->nL))) return st;
+    if ((st = ensure(c, m->bbox, 32 * ((size_t)m->nblocks + (size_t)cdiv(m->nblocks, 32)))))
+        return st;
     if ((st = ensure(c, m->ucount, sizeof(int32_t) * (size_t)m->nblocks))) return st;
     if ((st = ensure(c, m->ncount, sizeof(int32_t) * n))) return st;
     if ((st = ensure(c, m->f, sizeof(float4) * n))) return st;
@@ -1078,12 +1228,21 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
     k_md_leaf_boxes<<<(unsigned)cdiv(m->nL, 128), 128, 0, c->stream>>>(
         (const float4*)m->pos32.p, m->nL, m->apl, rl / 2.0f, keys);
     c->launches++;
-    if ((st = build_internal_nodes(c, keys, (int32_t*)m->store.p, codes, m->nL, m->apl))) return st;
+    const bool tree = m->p.union_search == ND_UNION_TREE;
+    if (tree) {
+        if ((st = build_internal_nodes(c, keys, (int32_t*)m->store.p, codes, m->nL, m->apl)))
+            return st;
+    } else {
+        k_md_block_boxes<<<(unsigned)cdiv(m->nblocks, 32), 1024, 0, c->stream>>>(
+            keys, m->nL, m->nblocks, kBlock / m->apl, (float4*)m->bbox.p);
+        c->launches++;
+    }
     // query boxes slightly above r_list/2 so the box tests never drop a pair;
     // the distance test alone decides membership
     const float hq = (rl / 2.0f) * 1.0001f + 1e-6f;
     k_md_block_union<<<(unsigned)m->nblocks, kBlock, m->union_smem, c->stream>>>(
-        keys, (const float4*)m->pos32.p, live.sid, n, m->nL, m->apl, hq, rl, m->fcap, m->ucap,
+        keys, (const float4*)m->bbox.p, m->nblocks, tree ? 1 : 0, (const float4*)m->pos32.p,
+        live.sid, n, m->nL, m->apl, hq, rl, m->fcap, m->ucap,
         m->upow2, (int32_t*)m->ulist.p, (int32_t*)m->ucount.p, (uint16_t*)m->llist_leaf.p,
         (int32_t*)m->lcount_leaf.p, m->lcap_leaf, c->d_err, (int32_t*)m->diag.p + 2,
         sizing ? 1 : 0, pressure);
@@ -1614,7 +1773,8 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     if (p->atomsperleaf <= 0 || n % p->atomsperleaf || n / p->atomsperleaf < 2) return ND_ERR_SPEC;
     if (32 % p->atomsperleaf != 0) return ND_ERR_SPEC;  // a warp holds whole leaves
     if (p->rebuild_every <= 0 || !(p->cutoff > 0) || !(p->skin >= 0) || !(p->dt > 0) ||
-        p->resort_every < 0 || p->stage_policy < 0 || p->stage_policy > 1)
+        p->resort_every < 0 || p->stage_policy < 0 || p->stage_policy > 1 ||
+        (p->union_search != ND_UNION_BLOCKS && p->union_search != ND_UNION_TREE))
         return ND_ERR_ARG;
     if (nsys < 0 || (nsys > 0 && !sys)) return ND_ERR_ARG;
     if (nsys > 0) {
@@ -1687,7 +1847,7 @@ nd_status md_create_batch(Ctx* parent, const nd_md_params* p, int32_t nsys, cons
 // stream, early refits included -- and the settings are tuned one at a time
 // (coordinate descent): skin (the given one and +0.1, +0.2: a longer list
 // against fewer early refits), atoms per leaf (the leaf and traversal width),
-// re-sort interval, shared-memory staging policy.  Candidates that do not fit
+// re-sort interval, shared-memory staging policy, union search.  Candidates that do not fit
 // (shared memory, leaf size not dividing every system) are skipped.
 nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsys,
                       const nd_system* sys, const double* x, const double* v, const double* q,
@@ -1774,6 +1934,10 @@ nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsy
         nd_md_params c = s3;
         c.stage_policy = 1 - s3.stage_policy;
         if ((result = consider(c))) goto done;
+        const nd_md_params s4 = win;
+        c = s4;
+        c.union_search = s4.union_search == ND_UNION_TREE ? ND_UNION_BLOCKS : ND_UNION_TREE;
+        if ((result = consider(c))) goto done;
     }
 done:
     cudaEventDestroy(e0);
@@ -1790,7 +1954,7 @@ nd_status md_destroy(MDEngine* m) {
     if (m->graph_main) cudaGraphExecDestroy(m->graph_main);
     if (m->graph_first) cudaGraphExecDestroy(m->graph_first);
     DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->rec_buf[0], &m->rec_buf[1], &m->recb,
-                      &m->xyz32, &m->pos32, &m->keys, &m->store, &m->ulist, &m->ucount,
+                      &m->xyz32, &m->pos32, &m->keys, &m->store, &m->bbox, &m->ulist, &m->ucount,
                       &m->llist_leaf, &m->lcount_leaf, &m->llist,
                       &m->ncount, &m->f, &m->vtmp, &m->acc, &m->aos, &m->diag, &m->sysrow,
                       &m->sid_in, &m->ctl, &m->obs, &m->obs_part, &m->logbuf, &m->sub.codes,

@@ -106,7 +106,7 @@ struct MDEngine {
     bool rebuild_due = false;
     int64_t steps = 0, rebuilds = 0;
     Frame fr{};
-    DevBuf set_buf[2], rec_buf[2], recb, xyz32, pos32, keys, store, ulist, ucount, llist_leaf,
+    DevBuf set_buf[2], rec_buf[2], recb, xyz32, pos32, keys, store, bbox, ulist, ucount, llist_leaf,
         lcount_leaf, llist, ncount, f, vtmp, acc, aos, diag, sysrow, sid_in;
     // batched ensemble (nsys > 0): per-system rows and the Hilbert grid whose
     // level-log2(G) cells are the systems' slots

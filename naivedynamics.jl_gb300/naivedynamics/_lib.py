@@ -32,6 +32,8 @@ ND_BOX_LEAF = 0
 ND_BOX_ATOM = 1
 ND_PAIRS_ORDERED = 0
 ND_PAIRS_UNORDERED = 1
+ND_UNION_BLOCKS = 0
+ND_UNION_TREE = 1
 
 GRIDKEY_DTYPE = np.dtype([("min", np.float32, 3), ("max", np.float32, 3),
                           ("left", np.int32), ("skip", np.int32)])
@@ -67,7 +69,8 @@ class MDParams(ctypes.Structure):
                 ("box_lo", ctypes.c_double * 3), ("box_hi", ctypes.c_double * 3),
                 ("atomsperleaf", ctypes.c_int32), ("rebuild_every", ctypes.c_int32),
                 ("order", ctypes.c_int32), ("max_neighbors", ctypes.c_int32),
-                ("resort_every", ctypes.c_int32), ("stage_policy", ctypes.c_int32)]
+                ("resort_every", ctypes.c_int32), ("stage_policy", ctypes.c_int32),
+                ("union_search", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class MDDiag(ctypes.Structure):

@@ -128,6 +128,21 @@ def test_batch_resort_schedules_agree(nd):
     assert np.abs(out[0] - out[1]).max() < 2e-6
 
 
+def test_batch_union_searches_agree(nd):
+    # blocks of 256 atoms straddle systems here; both union searches must
+    # still find the same leaves
+    e = _ensemble(nd, nsys=20, nmax=1500, seed=0x4E440044)
+    out = []
+    for us in (nd.ND_UNION_BLOCKS, nd.ND_UNION_TREE):
+        eng = nd.Ensemble(_params(nd, union_search=us, resort_every=2), _table(nd, e), e["x"],
+                          e["v"])
+        eng.run(40)
+        out.append(eng.get())
+        eng.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+
+
 def test_batch_errors(nd):
     e = _ensemble(nd, nsys=4, nmax=512)
     t = _table(nd, e)
@@ -147,7 +162,7 @@ def test_autotune_plain_and_batch(nd):
     p = _params(nd, box_lo=(0, 0, 0), box_hi=(17, 17, 17))
     best, sps = nd.autotune(p, x0, v0, trial_steps=20)
     assert best.atomsperleaf in (2, 4, 8) and best.resort_every in (1, 5, 10)
-    assert best.stage_policy in (0, 1) and sps > 0
+    assert best.stage_policy in (0, 1) and best.union_search in (0, 1) and sps > 0
     assert abs(best.skin - p.skin) < 0.25 and best.skin >= p.skin
     assert best.cutoff == p.cutoff and best.rebuild_every == p.rebuild_every
     e = _ensemble(nd, nsys=16, nmax=1024)

@@ -68,9 +68,9 @@ def test_force_calls_with_pair_list(nd, oracle):
     assert abs((ulj + uc) - u64) <= 1e-6 * abs(u64)
 
 
-def _params(nd, side, coulomb=0.0, rebuild=10, order=1, skin=0.3, **kw):
+def _params(nd, side, coulomb=0.0, rebuild=10, order=1, skin=0.3, atomsperleaf=4, **kw):
     return nd.md_params(sigma=1.0, epsilon=1.0, coulomb_k=coulomb, cutoff=2.5, skin=skin, dt=1e-3,
-                        box_lo=(0, 0, 0), box_hi=(side, side, side), atomsperleaf=4,
+                        box_lo=(0, 0, 0), box_hi=(side, side, side), atomsperleaf=atomsperleaf,
                         rebuild_every=rebuild, order=order, **kw)
 
 
@@ -146,6 +146,26 @@ def test_md_refit_windows_match_resorting(nd):
         assert eng.diagnostics()["skin_violations"] == 0
     assert np.abs(out[0][0] - out[1][0]).max() < 2e-6
     assert force_errors(out[1][2], np.asarray(out[0][2], np.float64))[1] < 1e-5
+
+
+@pytest.mark.parametrize("apl", [1, 4, 8])
+def test_md_union_searches_agree(nd, apl):
+    # The block-box search and the tree walk find the same sorted union, so
+    # lists, summation order and every bit of the trajectory agree, through
+    # re-sorts, refits and (at a small skin) early refits.
+    x0, v0, q = _config1(nd, charges=True, n=4096, side=17.0)
+    out = []
+    for us in (nd.ND_UNION_BLOCKS, nd.ND_UNION_TREE):
+        eng = nd.MDEngine(_params(nd, 17.0, coulomb=1.0, skin=0.05, resort_every=3,
+                                  union_search=us, atomsperleaf=apl), x0, v0, q)
+        eng.run(70)
+        out.append((eng.get(), eng.stats()["list_pairs"], eng.diagnostics()))
+        eng.close()
+    (xa, va, fa), la, da = out[0]
+    (xb, vb, fb), lb, db = out[1]
+    assert da["early_refits"] > 0 and da["resorts"] > 0 and da["refits"] > 0
+    assert la == lb and da["early_refits"] == db["early_refits"]
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
 
 
 def test_md_neighbor_list_pair_set(nd, oracle):
