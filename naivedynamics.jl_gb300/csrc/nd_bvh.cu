@@ -357,9 +357,10 @@ __device__ __forceinline__ void load_box_cg(const float4* keys, int32_t node /*1
 // publishes this thread's node writes; the fence after a successful read of a
 // non-zero slot orders the sibling-box loads, which bypass L1 (ld.cg).  No
 // thread ever waits on another, so the kernel cannot hang; a climb longer than
-// nL levels flags ND_ERR_INTERNAL.
+// nL levels flags ND_ERR_INTERNAL.  ranges (may be null): leaf range
+// [first, last] of internal node nL + q at ranges[q - 1].
 __global__ void k_bvh_build(float4* keys, int32_t* store, const int32_t* __restrict__ code,
-                            int32_t nL, int32_t apl, int32_t* err) {
+                            int32_t nL, int32_t apl, int2* ranges, int32_t* err) {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (i > nL) return;
     int32_t rangel = i, ranger = i;
@@ -409,6 +410,7 @@ __global__ void k_bvh_build(float4* keys, int32_t* store, const int32_t* __restr
         }
         int32_t q = (delr < dell) ? ranger : rangel;
         int32_t parent = nL + q;
+        if (ranges) ranges[q - 1] = make_int2(rangel, ranger);
         int32_t skip;
         if (ranger == nL) {
             skip = 0;
@@ -433,10 +435,11 @@ __global__ void k_root_overwrite(float4* keys, int32_t nL) {
 }
 
 nd_status build_internal_nodes(Ctx* c, float4* keys, int32_t* store, const int32_t* codes,
-                               int32_t nL, int32_t apl) {
+                               int32_t nL, int32_t apl, int2* ranges) {
     cudaError_t e = cudaMemsetAsync(store, 0, sizeof(int32_t) * (size_t)(nL - 1), c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "store reset");
-    k_bvh_build<<<(int)cdiv(nL, 256), 256, 0, c->stream>>>(keys, store, codes, nL, apl, c->d_err);
+    k_bvh_build<<<(int)cdiv(nL, 256), 256, 0, c->stream>>>(keys, store, codes, nL, apl, ranges,
+                                                            c->d_err);
     c->launches++;
     return check_launch(c, "bvh build");
 }
@@ -465,7 +468,15 @@ nd_status build_tree(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t a
                                                            (int32_t*)c->idx.p, keys);
     c->launches++;
     if ((st = check_launch(c, "leaf boxes"))) return st;
-    if ((st = build_internal_nodes(c, keys, (int32_t*)c->store.p, codes, nL, apl))) return st;
+    // leaf ranges of the internal nodes, for the split walks of the two-phase
+    // emission (not kept by the allocation-free entry point)
+    int2* ranges = nullptr;
+    if (!c->no_alloc) {
+        if ((st = ensure(c, c->ranges, sizeof(int2) * (size_t)std::max(nL - 1, 1)))) return st;
+        ranges = (int2*)c->ranges.p;
+    }
+    if ((st = build_internal_nodes(c, keys, (int32_t*)c->store.p, codes, nL, apl, ranges)))
+        return st;
     if (overwrite_root) {
         k_root_overwrite<<<1, 1, 0, c->stream>>>(keys, nL);
         c->launches++;
@@ -478,6 +489,7 @@ nd_status build_tree(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t a
     out->pos4 = (const float4*)c->pos4.p;
     out->idx = (const int32_t*)c->idx.p;
     out->keys = keys;
+    out->ranges = ranges;
     out->nkeys = nkeys;
     return check_launch(c, "tree");
 }
@@ -776,7 +788,7 @@ __global__ void __launch_bounds__(128)
 // coalesced stores.
 constexpr int kWarpBuf = 512;  // buffered pairs per warp (one leaf visit adds at most 512)
 
-__device__ __forceinline__ void warp_buf_flush(int32_t* bi, int32_t* bj, float* bd, int& nb,
+__device__ __forceinline__ void warp_buf_flush(int2* bij, float* bd, int& nb,
                                                unsigned long long* cursor, int64_t cap,
                                                int32_t* pi, int32_t* pj, float* pd) {
     const int lane = threadIdx.x & 31;
@@ -785,59 +797,72 @@ __device__ __forceinline__ void warp_buf_flush(int32_t* bi, int32_t* bj, float* 
     base = __shfl_sync(0xffffffffu, base, 0);
     for (int k = lane; k < nb; k += 32) {
         const unsigned long long w = base + (unsigned long long)k;
-        if ((int64_t)w < cap) { pi[w] = bi[k]; pj[w] = bj[k]; pd[w] = bd[k]; }
+        if ((int64_t)w < cap) {
+            const int2 ij = bij[k];
+            pi[w] = ij.x;
+            pj[w] = ij.y;
+            pd[w] = __fsqrt_rn(bd[k]);
+        }
     }
     __syncwarp();
     nb = 0;
 }
 
-// Appends this lane's hits (bit k of mask = pair (qa[k / 4], tb[k % 4])) to
-// the warp's buffer: the lanes' offsets are the exclusive prefix of their hit
-// counts (<= 16, so five ballot bit planes); distances are recomputed with the
-// same operations as the test, so they are the tested values.
-__device__ __forceinline__ void warp_emit16(unsigned mask, const float4 (&qa)[4],
-                                            const float4 (&tb)[4], int32_t* bi, int32_t* bj, float* bd, int& nb,
+// Appends this lane's hits (bit k of mask = pair (ia[k / 4], ib[k % 4]) at
+// squared distance d2[k], the value the test compared) to the warp's buffer
+// in bit-major order: for each k, the lanes holding bit k take consecutive
+// slots, so every store of the warp is contiguous (no shared-memory bank
+// conflicts).  The buffer holds squared distances; the flush writes their
+// square roots, every lane of the flush taking one.
+__device__ __forceinline__ void warp_emit16(unsigned mask, const float (&d2)[16],
+                                            const int32_t (&ia)[4], const int32_t (&ib)[4],
+                                            int2* bij, float* bd, int& nb,
                                             unsigned long long* cursor, int64_t cap, int32_t* pi,
                                             int32_t* pj, float* pd) {
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    const unsigned cnt = (unsigned)__popc(mask);
-    unsigned pre = 0, total = 0;
-#pragma unroll
-    for (int b = 0; b < 5; ++b) {
-        const unsigned plane = __ballot_sync(0xffffffffu, (cnt >> b) & 1u);
-        pre += (unsigned)__popc(plane & below) << b;
-        total += (unsigned)__popc(plane) << b;
-    }
+    const unsigned total = __reduce_add_sync(0xffffffffu, (unsigned)__popc(mask));
     if (total == 0) return;
-    if (nb + (int)total > kWarpBuf) warp_buf_flush(bi, bj, bd, nb, cursor, cap, pi, pj, pd);
-    int at = nb + (int)pre;
+    if (nb + (int)total > kWarpBuf) warp_buf_flush(bij, bd, nb, cursor, cap, pi, pj, pd);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        if (mask & (1u << k)) {
-            bi[at] = __float_as_int(qa[k >> 2].w);
-            bj[at] = __float_as_int(tb[k & 3].w);
-            const float4 a = qa[k >> 2], b = tb[k & 3];
-            bd[at] = __fsqrt_rn(dist2_ref(a.x, a.y, a.z, b.x, b.y, b.z));
-            ++at;
+        const bool hit = (mask >> k) & 1u;
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int at = nb + __popc(bal & below);
+            bij[at] = make_int2(ia[k >> 2], ib[k & 3]);
+            bd[at] = d2[k];
         }
+        nb += __popc(bal);
     }
     __syncwarp();
-    nb += (int)total;
 }
 
-__global__ void __launch_bounds__(128, 8)
+// The 16 tests of leaf pair (a, b) (a == b: the six pairs inside the leaf):
+// squared distances and the hit mask.
+__device__ __forceinline__ unsigned leaf_tests16(const float4 (&qa)[4], const float4 (&tb)[4],
+                                                 bool self, float r2, float (&d2)[16]) {
+    unsigned mask = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        const int i = k >> 2, j = k & 3;
+        d2[k] = dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z);
+        if ((!self || j > i) && d2[k] < r2) mask |= 1u << k;
+    }
+    return mask;
+}
+
+__global__ void __launch_bounds__(128, 6)
     k_leaf_warp4(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
                  float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
                  float* pd, int32_t* err) {
     constexpr int APL = 4;
-    __shared__ int32_t sbi[4][kWarpBuf], sbj[4][kWarpBuf];
+    __shared__ int2 sbij[4][kWarpBuf];
     __shared__ float sbd[4][kWarpBuf];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int32_t q0 = (int32_t)((blockIdx.x * 4 + w) * 32) + 1;
     if (q0 > nL) return;  // whole warp
-    int32_t* bi = sbi[w];
-    int32_t* bj = sbj[w];
+    int2* bij = sbij[w];
     float* bd = sbd[w];
     const int32_t q = q0 + lane;
     const bool valid = q <= nL;
@@ -856,16 +881,16 @@ __global__ void __launch_bounds__(128, 8)
         for (int i = 0; i < APL; ++i) qa[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     int nb = 0;
-    unsigned mask = 0;
-    // intra-leaf pairs (a before b in the leaf)
+    int32_t ia[APL];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        const int i = k >> 2, j = k & 3;
-        if (j > i && valid &&
-            dist2_ref(qa[i].x, qa[i].y, qa[i].z, qa[j].x, qa[j].y, qa[j].z) < r2)
-            mask |= 1u << k;
+    for (int i = 0; i < APL; ++i) ia[i] = __float_as_int(qa[i].w);
+    {
+        // intra-leaf pairs (a before b in the leaf)
+        float d2[16];
+        unsigned mask = leaf_tests16(qa, qa, true, r2, d2);
+        if (!valid) mask = 0;
+        warp_emit16(mask, d2, ia, ia, bij, bd, nb, cursor, cap, pi, pj, pd);
     }
-    warp_emit16(mask, qa, qa, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
     // the warp's union box (invalid lanes contribute the empty box)
     Node un = ql;
     for (int sh = 16; sh > 0; sh >>= 1) {
@@ -887,20 +912,19 @@ __global__ void __launch_bounds__(128, 8)
         const Node nd_ = load_node(keys, t);
         if (overlap(un, nd_)) {
             if (nd_.left == 0) {
-                mask = 0;
-                float4 tb[APL];
+                unsigned mask = 0;
+                float d2[16];
+                int32_t ib[APL] = {0, 0, 0, 0};
                 if (valid && t > q && overlap(ql, nd_)) {
                     const int64_t B = (int64_t)(t - 1) * APL;
+                    float4 tb[APL];
 #pragma unroll
                     for (int j = 0; j < APL; ++j) tb[j] = __ldg(&pos[B + j]);
+                    mask = leaf_tests16(qa, tb, false, r2, d2);
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const int i = k >> 2, j = k & 3;
-                        if (dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z) < r2)
-                            mask |= 1u << k;
-                    }
+                    for (int j = 0; j < APL; ++j) ib[j] = __float_as_int(tb[j].w);
                 }
-                warp_emit16(mask, qa, tb, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+                warp_emit16(mask, d2, ia, ib, bij, bd, nb, cursor, cap, pi, pj, pd);
                 t = nd_.skip;
             } else {
                 t = nd_.left;
@@ -909,7 +933,7 @@ __global__ void __launch_bounds__(128, 8)
             t = nd_.skip;
         }
     }
-    warp_buf_flush(bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+    warp_buf_flush(bij, bd, nb, cursor, cap, pi, pj, pd);
 }
 
 __global__ void __launch_bounds__(128)
@@ -933,15 +957,21 @@ __global__ void __launch_bounds__(128)
 }
 
 // Two-phase form of the one-pass emission, for callers that allow scratch
-// memory.  Broad phase: the warp's union walk of k_leaf_warp4 records the
-// candidate leaf pairs (q, t) -- t > q with overlapping boxes, and (q, q) for
-// the pairs inside q -- through a per-warp shared buffer; the walk's work per
-// visited leaf is one box test.  Narrow phase: one thread per candidate leaf
-// pair runs the 4 x 4 distance tests and emits through the warp buffers of
-// k_leaf_warp4.  The distance tests, most of the work, are then spread evenly
-// over the GPU however dense the points are, instead of following the walks
-// of the densest regions.
-constexpr int kLeafBuf = 256;  // candidate leaf pairs buffered per warp
+// memory.  Broad phase: the candidate leaf pairs (q, t) -- t > q with
+// overlapping boxes, and (q, q) for the pairs inside q -- are recorded through
+// per-warp shared buffers; the work per visited leaf is one box test.  Narrow
+// phase: one thread per candidate leaf pair runs the 4 x 4 distance tests and
+// emits through the warp buffers of k_leaf_warp4.  The distance tests, most of
+// the work, are then spread evenly over the GPU however dense the points are.
+//
+// The broad phase itself is split in two so that no walk is long: the union
+// walk of a warp's 32 query leaves (as in k_leaf_warp4) stops at subtrees of
+// at most kTaskLeaves leaves and records each overlapping one as a task
+// (group, subtree root); a flat pool of warps then walks the tasks' subtrees.
+// In a dense cluster one warp's union overlaps thousands of leaves; its walk
+// becomes a few hundred steps plus many short walks on other warps.
+constexpr int kLeafBuf = 256;    // candidate leaf pairs buffered per warp
+constexpr int kTaskLeaves = 64;  // largest subtree recorded as one task
 
 __device__ __forceinline__ void lp_flush(int2* buf, int& nb, unsigned long long* cursor, int64_t cap,
                                          int2* __restrict__ out) {
@@ -969,27 +999,18 @@ __device__ __forceinline__ void lp_append(bool want, int32_t q, int32_t t, int2*
     nb += total;
 }
 
-__global__ void __launch_bounds__(128)
-    k_leaf_broad4(const float4* __restrict__ keys, int32_t nL, unsigned long long* cursor,
-                  int64_t cap, int2* __restrict__ out, int32_t* err) {
-    __shared__ int2 sbuf[4][kLeafBuf];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int32_t q0 = (int32_t)((blockIdx.x * 4 + w) * 32) + 1;
-    if (q0 > nL) return;  // whole warp
-    int2* buf = sbuf[w];
-    const int32_t q = q0 + lane;
-    const bool valid = q <= nL;
-    Node ql;
-    if (valid) {
+// The query group of a warp: leaves q0 .. q0 + 31 (lane's own leaf, empty box
+// past nL) and the union of their boxes.
+__device__ __forceinline__ void group_boxes(const float4* __restrict__ keys, int32_t nL,
+                                            int32_t q, Node& ql, Node& un) {
+    if (q <= nL) {
         ql = load_node(keys, q);
     } else {
         ql.mnx = ql.mny = ql.mnz = INFINITY;
         ql.mxx = ql.mxy = ql.mxz = -INFINITY;
         ql.left = ql.skip = 0;
     }
-    int nb = 0;
-    lp_append(valid, q, q, buf, nb, cursor, cap, out);  // pairs inside the leaf
-    Node un = ql;
+    un = ql;
     for (int sh = 16; sh > 0; sh >>= 1) {
         un.mnx = fminf(un.mnx, __shfl_xor_sync(0xffffffffu, un.mnx, sh));
         un.mny = fminf(un.mny, __shfl_xor_sync(0xffffffffu, un.mny, sh));
@@ -998,6 +1019,39 @@ __global__ void __launch_bounds__(128)
         un.mxy = fmaxf(un.mxy, __shfl_xor_sync(0xffffffffu, un.mxy, sh));
         un.mxz = fmaxf(un.mxz, __shfl_xor_sync(0xffffffffu, un.mxz, sh));
     }
+}
+
+// Broad phase, first half: one warp per group of 32 query leaves.  The pairs
+// inside each leaf go to the candidate list; the union walk from the skip rope
+// of the group's first leaf records (group, node) for every overlapping node
+// of at most kTaskLeaves leaves instead of descending into it.  Tasks are
+// warp-uniform: lane k holds the k-th pending one, 32 are written at a time.
+__global__ void __launch_bounds__(128)
+    k_leaf_tasks4(const float4* __restrict__ keys, const int2* __restrict__ ranges, int32_t nL,
+                  unsigned long long* cursor, int64_t cap, int2* __restrict__ out,
+                  unsigned long long* tcursor, int64_t tcap, int2* __restrict__ tasks,
+                  int32_t* err) {
+    __shared__ int2 sbuf[4][kLeafBuf];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int32_t g = (int32_t)(blockIdx.x * 4 + w);
+    const int32_t q0 = g * 32 + 1;
+    if (q0 > nL) return;  // whole warp
+    int2* buf = sbuf[w];
+    const int32_t q = q0 + lane;
+    Node ql, un;
+    group_boxes(keys, nL, q, ql, un);
+    int nb = 0;
+    lp_append(q <= nL, q, q, buf, nb, cursor, cap, out);  // pairs inside the leaf
+    lp_flush(buf, nb, cursor, cap, out);
+    int2 mine = make_int2(0, 0);
+    int npend = 0;
+    auto flush_tasks = [&]() {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(tcursor, (unsigned long long)npend);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane < npend && (int64_t)(base + lane) < tcap) tasks[base + lane] = mine;
+        npend = 0;
+    };
     int32_t t = __shfl_sync(0xffffffffu, ql.skip, 0);
     int32_t visits = 0;
     const int32_t nnodes = 2 * nL - 1;
@@ -1007,15 +1061,70 @@ __global__ void __launch_bounds__(128)
             break;
         }
         const Node nd_ = load_node(keys, t);
+        int32_t size = 1;
+        if (t > nL) {
+            const int2 rg = __ldg(&ranges[t - nL - 1]);
+            size = rg.y - rg.x + 1;
+        }
         if (overlap(un, nd_)) {
-            if (nd_.left == 0) {
-                lp_append(valid && t > q && overlap(ql, nd_), q, t, buf, nb, cursor, cap, out);
+            if (size <= kTaskLeaves) {
+                if (lane == npend) mine = make_int2(g, t);
+                if (++npend == 32) flush_tasks();
                 t = nd_.skip;
             } else {
                 t = nd_.left;
             }
         } else {
             t = nd_.skip;
+        }
+    }
+    if (npend) flush_tasks();
+}
+
+// Broad phase, second half: warps stride over the tasks; each walks its
+// subtree (from the root to the root's skip rope) with its group's union box
+// and records, at every leaf t it reaches, (q, t) for the lanes whose own leaf
+// q < t overlaps t.
+__global__ void __launch_bounds__(128)
+    k_leaf_subwalk4(const float4* __restrict__ keys, int32_t nL,
+                    const unsigned long long* __restrict__ tcount, int64_t tcap,
+                    const int2* __restrict__ tasks, unsigned long long* cursor, int64_t cap,
+                    int2* __restrict__ out, int32_t* err) {
+    __shared__ int2 sbuf[4][kLeafBuf];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int2* buf = sbuf[w];
+    int nb = 0;
+    const int64_t ntask = min((int64_t)*tcount, tcap);
+    const int32_t nnodes = 2 * nL - 1;
+    for (int64_t k = (int64_t)blockIdx.x * 4 + w; k < ntask; k += (int64_t)gridDim.x * 4) {
+        const int2 tk = __ldg(&tasks[k]);
+        const int32_t q = tk.x * 32 + 1 + lane;
+        const bool valid = q <= nL;
+        Node ql, un;
+        group_boxes(keys, nL, q, ql, un);
+        if (tk.y < 1 || tk.y > nnodes) {
+            if (lane == 0) set_error(err, ND_ERR_INTERNAL, tk.x);
+            continue;
+        }
+        const int32_t end = load_node(keys, tk.y).skip;
+        int32_t t = tk.y;
+        int32_t visits = 0;
+        while (t != end) {
+            if (t < 1 || t > nnodes || ++visits > 2 * kTaskLeaves) {
+                if (lane == 0) set_error(err, ND_ERR_INTERNAL, tk.x);
+                break;
+            }
+            const Node nd_ = load_node(keys, t);
+            if (overlap(un, nd_)) {
+                if (nd_.left == 0) {
+                    lp_append(valid && t > q && overlap(ql, nd_), q, t, buf, nb, cursor, cap, out);
+                    t = nd_.skip;
+                } else {
+                    t = nd_.left;
+                }
+            } else {
+                t = nd_.skip;
+            }
         }
     }
     lp_flush(buf, nb, cursor, cap, out);
@@ -1026,11 +1135,10 @@ __global__ void __launch_bounds__(256)
                    float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
                    float* pd) {
     constexpr int APL = 4;
-    __shared__ int32_t sbi[8][kWarpBuf], sbj[8][kWarpBuf];
+    __shared__ int2 sbij[8][kWarpBuf];
     __shared__ float sbd[8][kWarpBuf];
     const int w = threadIdx.x >> 5;
-    int32_t* bi = sbi[w];
-    int32_t* bj = sbj[w];
+    int2* bij = sbij[w];
     float* bd = sbd[w];
     int nb = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -1038,26 +1146,26 @@ __global__ void __launch_bounds__(256)
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
          __any_sync(0xffffffffu, k < nlp); k += stride) {
         unsigned mask = 0;
-        float4 qa[APL], tb[APL];
+        float d2[16];
+        int32_t ia[APL] = {0, 0, 0, 0}, ib[APL] = {0, 0, 0, 0};
         if (k < nlp) {
             const int2 e = __ldg(&lp[k]);
             const int64_t A = (int64_t)(e.x - 1) * APL, B = (int64_t)(e.y - 1) * APL;
+            float4 qa[APL], tb[APL];
 #pragma unroll
             for (int i = 0; i < APL; ++i) qa[i] = __ldg(&pos[A + i]);
 #pragma unroll
             for (int j = 0; j < APL; ++j) tb[j] = __ldg(&pos[B + j]);
-            const bool self = e.x == e.y;
+            mask = leaf_tests16(qa, tb, e.x == e.y, r2, d2);
 #pragma unroll
-            for (int m = 0; m < 16; ++m) {
-                const int i = m >> 2, j = m & 3;
-                if ((!self || j > i) &&
-                    dist2_ref(qa[i].x, qa[i].y, qa[i].z, tb[j].x, tb[j].y, tb[j].z) < r2)
-                    mask |= 1u << m;
+            for (int i = 0; i < APL; ++i) {
+                ia[i] = __float_as_int(qa[i].w);
+                ib[i] = __float_as_int(tb[i].w);
             }
         }
-        warp_emit16(mask, qa, tb, bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+        warp_emit16(mask, d2, ia, ib, bij, bd, nb, cursor, cap, pi, pj, pd);
     }
-    warp_buf_flush(bi, bj, bd, nb, cursor, cap, pi, pj, pd);
+    warp_buf_flush(bij, bd, nb, cursor, cap, pi, pj, pd);
 }
 
 nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int32_t* pj,
@@ -1076,28 +1184,54 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
             t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd, c->d_err);
         c->launches++;
     } else {
-        // broad phase, re-run once with a larger buffer if it overflowed
-        unsigned long long nlp = 0;
-        for (int attempt = 0; attempt < 2; ++attempt) {
+        // broad phase: tasks, then the tasks' subtree walks; re-run with
+        // larger buffers while either list overflowed
+        if (!t.ranges) return ND_ERR_INTERNAL;
+        unsigned long long* tcursor = cursor + 1;
+        unsigned long long nlp = 0, ntask = 0;
+        int nsm = 0, occ = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_leaf_subwalk4, 128, 0);
+        const int64_t ngroups = cdiv(t.nL, 32);
+        for (int attempt = 0;; ++attempt) {
             int64_t lcap = (int64_t)(c->leafpairs.bytes / sizeof(int2));
             if (lcap < 16 * (int64_t)t.nL) {
                 if ((st = ensure(c, c->leafpairs, sizeof(int2) * 16 * (size_t)t.nL))) return st;
                 lcap = 16 * (int64_t)t.nL;
             }
-            cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
-            k_leaf_broad4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
-                t.keys, t.nL, cursor, lcap, (int2*)c->leafpairs.p, c->d_err);
-            c->launches++;
+            int64_t tcap = (int64_t)(c->tasks.bytes / sizeof(int2));
+            if (tcap < 16 * ngroups) {
+                if ((st = ensure(c, c->tasks, sizeof(int2) * 16 * (size_t)ngroups))) return st;
+                tcap = 16 * ngroups;
+            }
+            cudaMemsetAsync(cursor, 0, 2 * sizeof(unsigned long long), c->stream);
+            k_leaf_tasks4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
+                t.keys, t.ranges, t.nL, cursor, lcap, (int2*)c->leafpairs.p, tcursor, tcap,
+                (int2*)c->tasks.p, c->d_err);
+            k_leaf_subwalk4<<<(unsigned)(nsm * std::max(occ, 1)), 128, 0, c->stream>>>(
+                t.keys, t.nL, tcursor, tcap, (const int2*)c->tasks.p, cursor, lcap,
+                (int2*)c->leafpairs.p, c->d_err);
+            c->launches += 2;
             if ((st = check_launch(c, "leaf pairs (broad phase)"))) return st;
-            e = cudaMemcpyAsync(&nlp, cursor, sizeof(nlp), cudaMemcpyDeviceToHost, c->stream);
+            unsigned long long h[2] = {0, 0};
+            e = cudaMemcpyAsync(h, cursor, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
             if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
             if (e != cudaSuccess) return cuda_fail(c, e, "candidate leaf pairs");
-            if ((int64_t)nlp <= lcap) break;
-            if ((st = ensure(c, c->leafpairs, sizeof(int2) * (size_t)(nlp + nlp / 4)))) return st;
+            nlp = h[0];
+            ntask = h[1];
+            if ((int64_t)nlp <= lcap && (int64_t)ntask <= tcap) break;
+            if (attempt == 2) {
+                c->last_error = "candidate leaf pairs: buffers kept overflowing";
+                return ND_ERR_INTERNAL;
+            }
+            if ((int64_t)ntask > tcap &&
+                (st = ensure(c, c->tasks, sizeof(int2) * (size_t)(ntask + ntask / 4))))
+                return st;
+            if ((int64_t)nlp > lcap &&
+                (st = ensure(c, c->leafpairs, sizeof(int2) * (size_t)(nlp + nlp / 4))))
+                return st;
         }
         cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
-        int nsm = 0;
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
         const int64_t blocks = std::min<int64_t>(cdiv((int64_t)nlp, 256), (int64_t)nsm * 32);
         if (nlp > 0) {
             k_leaf_narrow4<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, c->stream>>>(

@@ -304,7 +304,7 @@ nd_status nd_ctx_destroy(nd_ctx* h) {
     nd::DevBuf* bufs[] = {&c->xyz, &c->codes, &c->codes_alt, &c->perm, &c->perm_alt, &c->pos4,
                           &c->idx, &c->keys, &c->store, &c->hist, &c->counts, &c->offsets,
                           &c->partial, &c->pairs_i, &c->pairs_j, &c->pairs_d, &c->misc, &c->hash,
-                          &c->leafpairs};
+                          &c->leafpairs, &c->ranges, &c->tasks};
     for (nd::DevBuf* b : bufs) nd::free_buf(*b);
     if (c->d_err) cudaFree(c->d_err);
     if (c->h_err) cudaFreeHost(c->h_err);

@@ -136,7 +136,7 @@ struct Ctx {
     std::string last_error;
     // scratch buffers of the neighbour-search pipeline, grown on demand
     DevBuf xyz, codes, codes_alt, perm, perm_alt, pos4, idx, keys, store, hist, counts, offsets,
-        partial, pairs_i, pairs_j, pairs_d, misc, hash, leafpairs;
+        partial, pairs_i, pairs_j, pairs_d, misc, hash, leafpairs, ranges, tasks;
     struct MDEngine* sim_cache = nullptr;  // engine re-used by nd_simulate
     bool no_alloc = false;                 // buffers are fixed slices: never grow them
 };
@@ -157,6 +157,7 @@ struct TreeBuffers {
     const float4* pos4 = nullptr;    // sorted positions, w = bits of 1-based index (n)
     const int32_t* idx = nullptr;    // sorted 1-based original index (n)
     float4* keys = nullptr;          // 2 float4 per node, nd_gridkey layout (nkeys)
+    const int2* ranges = nullptr;    // leaf range of internal node nL + q at q - 1 (or null)
     int64_t nkeys = 0;
 };
 
@@ -185,7 +186,7 @@ nd_status pair_hash(Ctx* c, const int32_t* pi, const int32_t* pj, const float* p
 
 // Apetrei bottom-up build over already prepared leaf keys (used by the MD engine).
 nd_status build_internal_nodes(Ctx* c, float4* keys, int32_t* store, const int32_t* codes_sorted,
-                               int32_t nL, int32_t apl);
+                               int32_t nL, int32_t apl, int2* ranges = nullptr);
 
 inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

@@ -546,28 +546,39 @@ __global__ void __launch_bounds__(kBlock)
     const int64_t own = (valid ? i : (int64_t)blockIdx.x * kBlock) / APL;
     const float4 p = __ldg(&pos[valid ? i : (int64_t)blockIdx.x * kBlock]);
     const int32_t nc = valid ? min(__ldg(&lcount_leaf[own]), lcap_leaf) : 0;
-    const uint16_t* __restrict__ C = llist_leaf + own * lcap_leaf;
+    // candidate entries eight at a time (a leaf's list starts on a 16-byte
+    // boundary: lcap_leaf is a multiple of 8), the next eight loaded while the
+    // current ones are tested
+    const uint4* __restrict__ C = reinterpret_cast<const uint4*>(llist_leaf + own * lcap_leaf);
     uint16_t* __restrict__ L = llist + (int64_t)blockIdx.x * lcap * kBlock + tid;
     const int32_t self = (int32_t)i;
     int32_t cnt = 0;
-    for (int32_t k = 0; k < nc; ++k) {
-        const int32_t u = __ldg(&C[k]);
-        float4 q[APL];
-        if ((u + 1) * APL <= smpos) {
+    uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
+    for (int32_t k0 = 0; k0 < nc; k0 += 8) {
+        const uint4 cur = nxt;
+        if (k0 + 8 < nc) nxt = __ldg(&C[(k0 >> 3) + 1]);
+        const uint32_t cw[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
-            for (int e = 0; e < APL; ++e) q[e] = spos[u * APL + e];
-        } else {
-            const int64_t base = (int64_t)__ldg(&U[u]) * APL;
+        for (int h = 0; h < 8; ++h) {
+            if (k0 + h >= nc) break;
+            const int32_t u = (int32_t)((cw[h >> 1] >> (16 * (h & 1))) & 0xffffu);
+            float4 q[APL];
+            if ((u + 1) * APL <= smpos) {
 #pragma unroll
-            for (int e = 0; e < APL; ++e) q[e] = __ldg(&pos[base + e]);
-        }
+                for (int e = 0; e < APL; ++e) q[e] = spos[u * APL + e];
+            } else {
+                const int64_t base = (int64_t)__ldg(&U[u]) * APL;
 #pragma unroll
-        for (int e = 0; e < APL; ++e) {
-            const bool hit = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z) < rl2 &&
-                             __float_as_int(q[e].w) != self;
-            if (hit) {
-                if (cnt < lcap) L[(int64_t)cnt * kBlock] = (uint16_t)(u * APL + e);
-                ++cnt;
+                for (int e = 0; e < APL; ++e) q[e] = __ldg(&pos[base + e]);
+            }
+#pragma unroll
+            for (int e = 0; e < APL; ++e) {
+                const bool hit = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z) < rl2 &&
+                                 __float_as_int(q[e].w) != self;
+                if (hit) {
+                    if (cnt < lcap) L[cnt * kBlock] = (uint16_t)(u * APL + e);
+                    ++cnt;
+                }
             }
         }
     }

@@ -66,6 +66,39 @@ def test_no_alloc_matches_allocating_entry_point(nd):
         assert st == _lib.ND_NEED_REALLOC and c0 == cnt
 
 
+def test_no_alloc_unordered_pair_set(nd):
+    # unordered mode (one-pass emission here, two-phase in the allocating
+    # entry point): the same pairs, each with the same distance bits
+    import torch
+    from naivedynamics import _lib
+    L = _lib.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    x = uniform(103, 16384)
+    xt = torch.from_numpy(x).cuda()
+    spec = nd.SpheresBVHSpecs(0.08, len(x), 4)
+    dummy = torch.empty(1, dtype=torch.int32, device="cuda")
+    st, cnt = nd.neighbor_pairs_dev(xt, spec, dummy, dummy, dummy.float(), 0,
+                                    order=nd.ND_ORDER_SPATIAL, mode=nd.ND_PAIRS_UNORDERED)
+    assert cnt > 0
+    outs = []
+    for noalloc in (False, True):
+        o = [torch.empty(cnt, dtype=torch.int32, device="cuda") for _ in range(2)]
+        o.append(torch.empty(cnt, dtype=torch.float32, device="cuda"))
+        if noalloc:
+            st, c = _noalloc(L, xt, spec.c_spec(), nd.ND_ORDER_SPATIAL, nd.ND_PAIRS_UNORDERED,
+                             *o, cnt, stream)
+        else:
+            st, c = nd.neighbor_pairs_dev(xt, spec, *o, cnt, order=nd.ND_ORDER_SPATIAL,
+                                          mode=nd.ND_PAIRS_UNORDERED)
+        torch.cuda.synchronize()
+        assert st == 0 and c == cnt
+        i, j, d = (t.cpu().numpy() for t in o)
+        k = np.lexsort((j, i))
+        outs.append((i[k], j[k], d[k].view(np.int32)))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
 def test_no_alloc_rejects_oversize(nd):
     import torch
     from naivedynamics import _lib
