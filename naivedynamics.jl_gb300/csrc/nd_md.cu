@@ -659,6 +659,82 @@ __device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const
     }
 }
 
+// Packed single precision (sm_100 and later): one instruction applies the
+// operation to both halves of a 64-bit register pair, so two list entries
+// share each instruction of the pair arithmetic.  Every half is rounded as
+// the scalar instruction would round it.
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// Pair constants of PairK, each in both halves.
+struct PairK2 {
+    uint64_t rc2u, sig2u, eps24u, kcu, two, mone, half_neg, three_half;
+    __device__ __forceinline__ explicit PairK2(const PairK& a)
+        : rc2u(pk2(a.rc2u, a.rc2u)), sig2u(pk2(a.sig2u, a.sig2u)),
+          eps24u(pk2(a.eps24u, a.eps24u)), kcu(pk2(a.kcu, a.kcu)), two(pk2(2.0f, 2.0f)),
+          mone(pk2(-1.0f, -1.0f)), half_neg(pk2(-0.5f, -0.5f)), three_half(pk2(1.5f, 1.5f)) {}
+};
+
+// Forces of the pairs (i, a) and (i, b) together (no energies): the same
+// terms as accum_pair, the pair outside the cutoff contributing zero.  The
+// accumulators hold the running sums of the a-entries and the b-entries
+// separately; the caller adds the halves at the end.
+template <bool COUL>
+__device__ __forceinline__ void accum_pair2(const int4& ri, const int4& ra, const int4& rb,
+                                           const PairK& k1, const PairK2& k, uint64_t& fx,
+                                           uint64_t& fy, uint64_t& fz) {
+    const uint64_t dx = pk2((float)(ri.x - ra.x), (float)(ri.x - rb.x));
+    const uint64_t dy = pk2((float)(ri.y - ra.y), (float)(ri.y - rb.y));
+    const uint64_t dz = pk2((float)(ri.z - ra.z), (float)(ri.z - rb.z));
+    const uint64_t r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+    float r2a, r2b;
+    upk2(r2, r2a, r2b);
+    const bool ina = r2a < k1.rc2u, inb = r2b < k1.rc2u;
+    if (!(ina | inb)) return;
+    uint64_t inv_r = 0, inv_r2;
+    if (COUL) {
+        inv_r = pk2(rsqrtf(r2a), rsqrtf(r2b));
+        // one Newton step: inv_r (1.5 - 0.5 r2 inv_r^2)
+        const uint64_t t = fma2(k.half_neg, mul2(r2, mul2(inv_r, inv_r)), k.three_half);
+        inv_r = mul2(inv_r, t);
+        inv_r2 = mul2(inv_r, inv_r);
+    } else {
+        inv_r2 = pk2(__fdividef(1.0f, r2a), __fdividef(1.0f, r2b));
+        // one Newton step: inv_r2 (2 - r2 inv_r2)
+        inv_r2 = mul2(inv_r2, fma2(mul2(r2, inv_r2), k.mone, k.two));
+    }
+    const uint64_t s2 = mul2(k.sig2u, inv_r2);
+    const uint64_t s6 = mul2(mul2(s2, s2), s2);
+    uint64_t fmag = mul2(mul2(mul2(k.eps24u, inv_r2), s6), fma2(k.two, s6, k.mone));
+    if (COUL) {
+        const float qi = __int_as_float(ri.w);
+        const uint64_t qq = pk2(qi * __int_as_float(ra.w), qi * __int_as_float(rb.w));
+        fmag = fma2(mul2(k.kcu, qq), mul2(inv_r, inv_r2), fmag);
+    }
+    float fa, fb;
+    upk2(fmag, fa, fb);
+    fmag = pk2(ina ? fa : 0.0f, inb ? fb : 0.0f);
+    fx = fma2(fmag, dx, fx);
+    fy = fma2(fmag, dy, fy);
+    fz = fma2(fmag, dz, fz);
+}
+
 // One block per 256 atoms.  MODE 0: step (force, pending half kick, kick,
 // drift, reflect, next record).  MODE 2: the same step inside a captured
 // window, whose last block also sets the early-refit condition of the graph
@@ -722,6 +798,8 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     if constexpr (TPA == 1) {
         // groups of four neighbours; the next group's indices are loaded
         // while the current group is computed
+        const PairK2 pk2c(pk);
+        uint64_t fx2 = 0, fy2 = 0, fz2 = 0;  // packed (0.0f, 0.0f)
         int32_t s = 0;
         int32_t li[4];
         if (cnt >= 4) {
@@ -736,8 +814,20 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
 #pragma unroll
                 for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)(s + 4 + k) * kBlock];
             }
+            if constexpr (MODE == 1) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue);
+                for (int k = 0; k < 4; ++k) accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue);
+            } else {
+                // two entries per packed instruction
+                accum_pair2<COUL>(ri, rj[0], rj[1], pk, pk2c, fx2, fy2, fz2);
+                accum_pair2<COUL>(ri, rj[2], rj[3], pk, pk2c, fx2, fy2, fz2);
+            }
+        }
+        if constexpr (MODE != 1) {
+            float a, b;
+            upk2(fx2, a, b); fx = a + b;
+            upk2(fy2, a, b); fy = a + b;
+            upk2(fz2, a, b); fz = a + b;
         }
         for (; s < cnt; ++s)
             accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), pk, fx, fy, fz, ue);
