@@ -225,7 +225,8 @@ def batched_leg(nd, ctx, ext, flush):
                          skin=tuned.skin, dt=1e-3, box_lo=(0, 0, 0), box_hi=(side, side, side),
                          atomsperleaf=tuned.atomsperleaf, rebuild_every=REBUILD,
                          resort_every=tuned.resort_every, stage_policy=tuned.stage_policy,
-                         union_search=tuned.union_search)
+                         union_search=tuned.union_search,
+                         refit_check_every=tuned.refit_check_every)
         eng = nd.MDEngine(p, e["x"][sl], e["v"][sl], ctx=ctx)
         _, _, fp = eng.get()
         f_err = max(f_err, float(np.linalg.norm(f_bat[sl] - fp) / np.linalg.norm(fp)))
@@ -252,6 +253,7 @@ def batched_leg(nd, ctx, ext, flush):
                       "resort_every": tuned.resort_every,
                       "stage_policy": tuned.stage_policy,
                       "union_search": UNION_NAMES[tuned.union_search],
+                      "refit_check_every": max(tuned.refit_check_every, 1),
                       "autotune_s": round(tune_s, 2)},
             "plain_path": "512 nd_md engines run one after another on one stream (graphs)"}
 
@@ -553,6 +555,7 @@ def run_gb300(args):
                              "resort_every": params.resort_every,
                              "stage_policy": params.stage_policy,
                              "union_search": UNION_NAMES[params.union_search],
+                             "refit_check_every": max(params.refit_check_every, 1),
                              "autotune_s": round(tune_s, 2)},
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "512 MB buffer written before every timed step (outside the events)",
@@ -594,12 +597,13 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
-def md_eager_leg(nd, ctx, union_search="blocks"):
+def md_eager_leg(nd, ctx, union_search="blocks", check_every=3):
     """The headline workload with the settings the autotuner picks for it
     (skin 0.4, 8 atoms per leaf, re-sort every 10th window; the given union
-    search), created and run for ten windows eagerly (nd_md_step_times), so
-    that every kernel is a plain launch in a known order for profiling: engine
-    creation (three builds), then per window a rebuild and ten steps."""
+    search and early-refit check interval), created and run for ten windows
+    eagerly (nd_md_step_times), so that every kernel is a plain launch in a
+    known order for profiling: engine creation (three builds), then per window
+    a rebuild and ten steps."""
     import numpy as np
 
     import torch
@@ -608,6 +612,7 @@ def md_eager_leg(nd, ctx, union_search="blocks"):
     p = _md_params(nd)
     p.skin, p.atomsperleaf, p.resort_every = 0.4, 8, 10
     p.union_search = {v_: k for k, v_ in UNION_NAMES.items()}[union_search]
+    p.refit_check_every = check_every
     eng = nd.MDEngine(p, x, v, q, ctx=ctx)
     ms = eng.step_times(10 * REBUILD)
     # then the same settings through the captured graphs, CUDA events
@@ -622,8 +627,11 @@ def md_eager_leg(nd, ctx, union_search="blocks"):
         eng.sync()
         if k > 0:
             graph_ms.append(a.elapsed_time(b))
+    d = eng.diagnostics()
     eng.close()
-    return {"workload": WORKLOAD + f" (fixed settings, union search {union_search})",
+    return {"workload": WORKLOAD + f" (fixed settings, union search {union_search}, "
+                                   f"early-refit checks every {check_every} steps)",
+            "early_refits": d["early_refits"], "skin_violations": d["skin_violations"],
             "step_kernel_ms_mean": float(np.mean(ms)),
             "graph_ms_per_100_steps": float(np.median(graph_ms)),
             "atom_steps_per_s": N_ATOMS * MD_PER_STEP / (float(np.median(graph_ms)) * 1e-3)}
@@ -638,7 +646,8 @@ def run_only(args):
     ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.only == "md":
-        out = md_eager_leg(nd, ctx, union_search=args.union_search)
+        out = md_eager_leg(nd, ctx, union_search=args.union_search,
+                           check_every=args.check_every)
     elif args.only == "plain":
         out = plain_leg(nd, ctx, ext, flush)
     elif args.only == "batched":
@@ -673,6 +682,8 @@ def main():
                     help="points of the stress measurement with --only stress (64 clusters)")
     ap.add_argument("--union-search", choices=["blocks", "tree"], default="blocks",
                     help="union search of the fixed-settings engine of --only md")
+    ap.add_argument("--check-every", type=int, default=3,
+                    help="early-refit check interval of the fixed-settings engine of --only md")
     ap.add_argument("--only", choices=["md", "plain", "batched", "adjoint", "stress"],
                     help="run one secondary measurement alone and print its JSON object "
                          "(for profiling)")

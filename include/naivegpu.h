@@ -101,7 +101,11 @@ typedef struct {
                               leaves either way): ND_UNION_BLOCKS = boxes of the blocks of
                               the kept order, ND_UNION_TREE = breadth-first walk of the
                               LBVH built (re-sort) or refitted (refit) at every rebuild */
-    int32_t reserved;      /* 0 */
+    int32_t refit_check_every; /* steps between the early-refit checks inside a window (0 = 1):
+                              after every k-th step the engine refits if some atom could pass
+                              skin/2 from its list-build position within the next k steps
+                              (assuming no step moves an atom more than twice as far as the
+                              step before the check) */
 } nd_md_params;
 
 #define ND_UNION_BLOCKS 0
@@ -279,14 +283,16 @@ nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* lis
                       int32_t* capacity);
 /* Engine diagnostics (nd_md_diagnostics). */
 typedef struct {
-    int64_t skin_violations; /* atom-steps in which an atom had moved more than skin/2
-                                since its list was built: the list may then miss pairs */
+    int64_t skin_violations; /* atom-steps computed with a list from which an atom had
+                                moved more than skin/2: the list may then miss pairs (none
+                                with a check after every step; with sparser checks, a
+                                system moving too fast for them) */
     int32_t max_neighbors;   /* largest per-atom neighbour count of any build */
     int32_t reserved;
     int64_t resorts;         /* window rebuilds that re-sorted the atoms */
     int64_t refits;          /* window rebuilds that refitted the kept tree */
-    int64_t early_refits;    /* refits inside a window: after a step that left some atom
-                                able to pass skin/2 in the next step */
+    int64_t early_refits;    /* refits inside a window: at a check that found some atom
+                                able to pass skin/2 before the next check */
     int64_t resort_kernels;  /* kernels of one re-sort rebuild */
     int64_t refit_kernels;   /* kernels of one refit */
     int64_t body_kernels;    /* kernels run so far inside captured conditional nodes
@@ -354,10 +360,11 @@ nd_status nd_batch_energies(nd_md* md, double* potential, double* kinetic);
  * Autotuner: times short runs of candidate engine settings on copies of the
  * given state (host arrays; the state is not advanced) and writes the fastest
  * into *best (skin -- p->skin, +0.1 or +0.2 --, atomsperleaf -- the
- * leaf/traversal width --, resort_every, stage_policy and union_search; every other field
- * copied from *p), tuning one setting at a time.  nsys == 0 tunes a plain
- * engine (sys ignored).  Candidates change only the summation order of the
- * forces, not which pairs interact.  trial_steps: timed steps per candidate
+ * leaf/traversal width --, resort_every, stage_policy, union_search and
+ * refit_check_every -- 1, 2 or 3; every other field copied from *p), tuning one
+ * setting at a time.  nsys == 0 tunes a plain engine (sys ignored).  Candidates
+ * change only the summation order of the forces and the steps at which early
+ * refits may run, not which pairs interact.  trial_steps: timed steps per candidate
  * (rounded up to whole rebuild windows).  seconds_per_step (may be NULL)
  * receives the winner's time per MD step.
  */

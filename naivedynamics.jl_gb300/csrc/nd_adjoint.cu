@@ -504,18 +504,21 @@ static nd_status adj_copy(AdjEngine* A, void* dst, const void* src, size_t bytes
 
 // One forward step of the engine (records ping-pong as in the plain engine).
 static void adj_step(AdjEngine* A, bool first, int use_cond = 0,
-                     cudaGraphConditionalHandle h = 0) {
+                     cudaGraphConditionalHandle h = 0, int unchecked = 0) {
     MDEngine* m = A->m;
     StepArgs a = md_step_args(m, m->rc);
     a.use_cond = use_cond;
+    a.vote = use_cond;
+    a.unchecked = unchecked;
     a.cond = h;
     md_launch_step(m, a, first);
     m->rc ^= 1;
 }
 
-// Whether an early refit may follow step t (not before a scheduled rebuild).
+// Whether an early refit may follow step t: after the window's steps 0, M,
+// 2M, ... (M = the engine's check interval), not before a scheduled rebuild.
 static bool adj_cond_after(const AdjEngine* A, int32_t t) {
-    return (t + 1) % A->R != 0 && t + 1 < A->K;
+    return (t + 1) % A->R != 0 && t + 1 < A->K && (t % A->R) % A->m->check_every == 0;
 }
 
 // Rebuild before step t of the static schedule (re-sort, refit, or the early
@@ -562,7 +565,10 @@ static nd_status adj_enqueue_forward(AdjEngine* A) {
         const bool cond = adj_cond_after(A, t);
         cudaGraphConditionalHandle h = 0;
         if (cond && (st = md_cond_handle(m, &h))) return st;
-        adj_step(A, t == 0, cond ? 1 : 0, h);
+        // the list is used unchecked after this step when no check follows
+        // and no scheduled rebuild comes first (the loss at x_K included)
+        const bool unchecked = !cond && ((t + 1) % A->R != 0 || t + 1 == A->K);
+        adj_step(A, t == 0, cond ? 1 : 0, h, unchecked ? 1 : 0);
         if (cond &&
             (st = md_add_cond_node(m, h, 1, [&](int) {
                  nd_status s2 = md_rebuild(m, RB_REFIT, m->rc);

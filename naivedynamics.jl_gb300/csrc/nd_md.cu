@@ -922,18 +922,23 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         }
         a.rec_out[i] = make_int4(xi[0], xi[1], xi[2], ri.w);
         // A list built at r_c + skin stays valid while no atom moved more than
-        // skin/2 since the build; count the atom-steps that broke that bound.
+        // skin/2 since the build; count the atom-steps that broke that bound
+        // where the next step keeps the list without a check.
         const int4 rb = __ldg(&a.rec_build[i]);
         const float ex = (float)(xi[0] - rb.x), ey = (float)(xi[1] - rb.y),
                     ez = (float)(xi[2] - rb.z);
         const float e2 = ex * ex + ey * ey + ez * ez;
-        if (e2 > hs2u) atomicAdd(a.diag, 1ull);
+        if (a.unchecked && e2 > hs2u) atomicAdd(a.diag, 1ull);
         // Ask for a refit before the next step when this atom could pass the
-        // bound in it: displacement so far + twice this step's move + 5% of
-        // the bound (the velocity may at most double in one step).
-        const float sx = (float)(xi[0] - ri.x), sy = (float)(xi[1] - ri.y),
-                    sz = (float)(xi[2] - ri.z);
-        trig = sqrtf(e2) + 2.0f * sqrtf(sx * sx + sy * sy + sz * sz) > 0.95f * hsu;
+        // bound before the next check: displacement so far + trig_k times this
+        // step's move + 5% of the bound (no step until the next check moves
+        // it more than twice as far as this one; with a check after every
+        // step, trig_k = 2 still covers one step more).
+        if (a.vote) {
+            const float sx = (float)(xi[0] - ri.x), sy = (float)(xi[1] - ri.y),
+                        sz = (float)(xi[2] - ri.z);
+            trig = sqrtf(e2) + a.trig_k * sqrtf(sx * sx + sy * sy + sz * sz) > 0.95f * hsu;
+        }
         }
         // Early refit request: the block votes, and the last block to finish
         // (a ticket counter, no waiting) publishes the flag to the graph's
@@ -1198,6 +1203,9 @@ StepArgs md_step_args(MDEngine* m, int rec_in) {
     a.ctl = (unsigned*)m->ctl.p;
     a.cond = 0;
     a.use_cond = 0;
+    a.vote = 1;
+    a.trig_k = 2.0f * (float)std::max(m->check_every - 1, 1);
+    a.unchecked = 0;
     for (int d = 0; d < 3; ++d) {
         a.os[d] = m->fr.o[d] * S;
         a.lo_fp[d] = (int32_t)std::floor((p.box_lo[d] - m->fr.o[d]) * S);
@@ -1562,10 +1570,11 @@ static nd_status md_observe(MDEngine* m, int32_t p, bool capture, int64_t g) {
 }
 
 // Enqueue `k` steps of the current window, the first at window position pos0.
-// After every step but the window's last, a refit runs if some atom could pass
-// skin/2 from its list-build position in the next step: inside a capture as a
-// conditional node (one handle per node, set by the step before it),
-// otherwise eagerly after reading the request flag.  ev (eager only): a pair
+// After the window's steps 0, M, 2M, ... (M = check_every) but not its last, a
+// refit runs if some atom could pass skin/2 from its list-build position
+// before the next check: inside a capture as a conditional node (one handle
+// per node, set by the step before it), otherwise eagerly after reading the
+// request flag.  ev (eager only): a pair
 // of events per step recorded around the step kernel.
 static nd_status md_steps(MDEngine* m, int32_t k, int32_t pos0, bool capture = false,
                           cudaEvent_t* ev = nullptr) {
@@ -1573,23 +1582,27 @@ static nd_status md_steps(MDEngine* m, int32_t k, int32_t pos0, bool capture = f
     const int32_t R = m->p.rebuild_every;
     nd_status st;
     for (int32_t s = 0; s < k; ++s) {
-        const bool tail = (pos0 + s) % R == R - 1;
+        // a check follows the window's steps 0, M, 2M, ... but not its last
+        const int32_t p = (pos0 + s) % R;
+        const bool check = p != R - 1 && p % m->check_every == 0;
         cudaGraphConditionalHandle h = 0;
-        if (capture && !tail && (st = md_cond_handle(m, &h))) return st;
+        if (capture && check && (st = md_cond_handle(m, &h))) return st;
         StepArgs a = md_step_args(m, m->rc);
-        a.use_cond = capture && !tail ? 1 : 0;
+        a.use_cond = capture && check ? 1 : 0;
+        a.vote = check ? 1 : 0;
+        a.unchecked = !check && p != R - 1 ? 1 : 0;
         a.cond = h;
         if (ev) cudaEventRecord(ev[2 * s], c->stream);
         launch_step<0>(m, a, m->first);
         if (ev) cudaEventRecord(ev[2 * s + 1], c->stream);
         m->first = false;
         m->rc ^= 1;
-        if (!tail && capture) {
+        if (check && capture) {
             if ((st = md_add_cond_node(
                      m, h, 1, [&](int) { return md_rebuild(m, RB_REFIT, m->rc, ctl_word(m, 2)); },
                      &m->refit_kernels)))
                 return st;
-        } else if (!tail) {
+        } else if (check) {
             unsigned flag = 0;
             cudaError_t e = cudaMemcpyAsync(&flag, m->ctl.p, sizeof(flag), cudaMemcpyDeviceToHost,
                                             c->stream);
@@ -1875,7 +1888,8 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     if (32 % p->atomsperleaf != 0) return ND_ERR_SPEC;  // a warp holds whole leaves
     if (p->rebuild_every <= 0 || !(p->cutoff > 0) || !(p->skin >= 0) || !(p->dt > 0) ||
         p->resort_every < 0 || p->stage_policy < 0 || p->stage_policy > 1 ||
-        (p->union_search != ND_UNION_BLOCKS && p->union_search != ND_UNION_TREE))
+        (p->union_search != ND_UNION_BLOCKS && p->union_search != ND_UNION_TREE) ||
+        p->refit_check_every < 0)
         return ND_ERR_ARG;
     if (nsys < 0 || (nsys > 0 && !sys)) return ND_ERR_ARG;
     if (nsys > 0) {
@@ -1890,6 +1904,7 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     MDEngine* m = new MDEngine();
     m->nsys = nsys;
     m->resort_every = p->resort_every > 0 ? p->resort_every : 1;
+    m->check_every = p->refit_check_every > 0 ? p->refit_check_every : 1;
     m->parent = parent;
     m->sub.device = parent->device;
     m->sub.stream = parent->stream;
@@ -1948,7 +1963,8 @@ nd_status md_create_batch(Ctx* parent, const nd_md_params* p, int32_t nsys, cons
 // stream, early refits included -- and the settings are tuned one at a time
 // (coordinate descent): skin (the given one and +0.1, +0.2: a longer list
 // against fewer early refits), atoms per leaf (the leaf and traversal width),
-// re-sort interval, shared-memory staging policy, union search.  Candidates that do not fit
+// re-sort interval, shared-memory staging policy, union search, early-refit
+// check interval.  Candidates that do not fit
 // (shared memory, leaf size not dividing every system) are skipped.
 nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsys,
                       const nd_system* sys, const double* x, const double* v, const double* q,
@@ -2039,6 +2055,13 @@ nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsy
         c = s4;
         c.union_search = s4.union_search == ND_UNION_TREE ? ND_UNION_BLOCKS : ND_UNION_TREE;
         if ((result = consider(c))) goto done;
+        const nd_md_params s5 = win;
+        for (int32_t ce : {1, 2, 3}) {
+            if (ce == std::max(s5.refit_check_every, 1)) continue;
+            c = s5;
+            c.refit_check_every = ce;
+            if ((result = consider(c))) goto done;
+        }
     }
 done:
     cudaEventDestroy(e0);

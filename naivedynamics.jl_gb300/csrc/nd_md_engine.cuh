@@ -90,6 +90,13 @@ struct StepArgs {
     unsigned* ctl;
     cudaGraphConditionalHandle cond;
     int32_t use_cond;
+    // this step votes for an early refit (a check follows it); the vote
+    // covers the next trig_k / 2 + 1 steps
+    int32_t vote;
+    float trig_k;
+    // the next step uses this step's list unchecked: an atom past skin/2 is a
+    // skin violation
+    int32_t unchecked;
 };
 
 struct MDEngine {
@@ -124,6 +131,7 @@ struct MDEngine {
     // steps with conditional early refits; the live state is always set 0
     cudaGraphExec_t graph_main = nullptr;
     int32_t resort_every = 1;  // re-sort (new order + topology) every k-th window, refit between
+    int32_t check_every = 1;   // steps between early-refit checks
     int64_t graph_main_launches = 0;  // kernel nodes of the window graph outside conditional bodies
     int64_t resort_kernels = 0;       // kernels of one re-sort rebuild
     int64_t eager_bodies = 0;         // kernels of rebuild bodies run eagerly (counted by the host)

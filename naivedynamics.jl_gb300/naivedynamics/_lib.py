@@ -70,7 +70,7 @@ class MDParams(ctypes.Structure):
                 ("atomsperleaf", ctypes.c_int32), ("rebuild_every", ctypes.c_int32),
                 ("order", ctypes.c_int32), ("max_neighbors", ctypes.c_int32),
                 ("resort_every", ctypes.c_int32), ("stage_policy", ctypes.c_int32),
-                ("union_search", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("union_search", ctypes.c_int32), ("refit_check_every", ctypes.c_int32)]
 
 
 class MDDiag(ctypes.Structure):

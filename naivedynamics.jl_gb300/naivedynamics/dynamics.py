@@ -40,7 +40,7 @@ class ForceField:
 def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e-3,
               box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), atomsperleaf=4, rebuild_every=10,
               order=ND_ORDER_SPATIAL, max_neighbors=0, resort_every=0,
-              stage_policy=0, union_search=ND_UNION_BLOCKS) -> MDParams:
+              stage_policy=0, union_search=ND_UNION_BLOCKS, refit_check_every=1) -> MDParams:
     p = MDParams()
     p.sigma, p.epsilon, p.coulomb_k, p.cutoff, p.skin, p.dt = (float(sigma), float(epsilon),
                                                                float(coulomb_k), float(cutoff),
@@ -52,7 +52,7 @@ def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e
                                                                  int(rebuild_every), int(order),
                                                                  int(max_neighbors))
     p.resort_every, p.stage_policy = int(resort_every), int(stage_policy)
-    p.union_search, p.reserved = int(union_search), 0
+    p.union_search, p.refit_check_every = int(union_search), int(refit_check_every)
     return p
 
 
@@ -387,7 +387,7 @@ class Ensemble(MDEngine):
 
 def autotune(params: MDParams, x, v, q=None, m=None, systems=None, trial_steps=20, ctx=None):
     """nd_md_autotune: the fastest (skin, atomsperleaf, resort_every,
-    stage_policy, union_search) for this state, as a new MDParams, and its time per MD step in seconds.
+    stage_policy, union_search, refit_check_every) for this state, as a new MDParams, and its time per MD step in seconds.
     systems=None tunes a plain engine."""
     ctx = ctx or default_context()
     x = _f64(x, (-1, 3))

@@ -121,8 +121,9 @@ def test_backward_needs_forward(nd, oracle):
 
 
 def test_skin_violation_is_reported(nd, oracle):
-    # no skin: every step moves atoms past skin/2 = 0 before any refit can
-    # follow it, so the forward pass reports the invalid lists
+    # no skin: every step moves atoms past skin/2 = 0, so every check refits,
+    # but the last step's positions (where the loss is evaluated) are never
+    # checked against their list: the forward pass reports the invalid list
     adj, _ = _case(nd, oracle, 256, 50, skin=0.0)
     with pytest.raises(nd.NDError) as e:
         adj.forward()

@@ -104,15 +104,18 @@ def test_md_trajectory_vs_fp64(nd, oracle):
     assert eng.diagnostics()["skin_violations"] == 0
 
 
-def test_md_early_refit_keeps_lists_valid(nd, oracle):
-    # A hot start (velocities N(0, 15^2)) moves atoms more than skin/4 inside a
-    # rebuild window: early refits must keep every atom within skin/2 of its
-    # list-build position (no skin violation), the trajectory must follow the
-    # FP64 one, and eager (partial-window) runs must refit at the same steps as
-    # the captured windows.
+@pytest.mark.parametrize("check_every,vscale", [(1, 15.0), (3, 5.0)])
+def test_md_early_refit_keeps_lists_valid(nd, oracle, check_every, vscale):
+    # A hot start (velocities N(0, vscale^2)) moves atoms more than skin/4
+    # inside a rebuild window: early refits must keep every atom within skin/2
+    # of its list-build position (no skin violation), the trajectory must
+    # follow the FP64 one, and eager (partial-window) runs must refit at the
+    # same steps as the captured windows -- with a check after every step, and
+    # after every third step of a window (for atoms slow enough that three
+    # steps stay well inside skin/2).
     x0, v0, _ = _config1(nd, n=2048, side=13.5)
-    v0 = v0 * 15.0
-    a = nd.MDEngine(_params(nd, 13.5), x0, v0)
+    v0 = v0 * vscale
+    a = nd.MDEngine(_params(nd, 13.5, refit_check_every=check_every), x0, v0)
     a.run(60)
     a.sync()
     xa, va, fa = a.get()
@@ -126,7 +129,7 @@ def test_md_early_refit_keeps_lists_valid(nd, oracle):
     assert np.abs(xa - xr).max() < 1e-5
     f64, _, _ = oracle.forces(p, xa)
     assert force_errors(fa, f64)[1] <= F_L2_TOL
-    b = nd.MDEngine(_params(nd, 13.5), x0, v0)
+    b = nd.MDEngine(_params(nd, 13.5, refit_check_every=check_every), x0, v0)
     for k in (7, 3, 11, 9, 10, 20):
         b.run(k)
     xb, vb, _ = b.get()
@@ -240,12 +243,20 @@ def test_md_walls(nd, oracle):
 
 
 def test_md_skin_violations_counted(nd):
-    # Atoms moving ~0.05 per step cross skin/2 = 0.15 within a 10-step window.
+    # Atoms moving up to ~0.2 per step cross skin/2 = 0.15 in one step.  With
+    # a check after every step each such step is followed by a refit (no step
+    # runs on a stale list); with a check after every third step the steps in
+    # between run on lists some atoms have left, and those are counted.
     x0, v0, _ = _config1(nd, n=512, side=8.5)
-    eng = nd.MDEngine(_params(nd, 8.5), x0, v0 * 50.0)
-    eng.run(10)
-    eng.sync()
-    assert eng.diagnostics()["skin_violations"] > 0
+    d = {}
+    for ce in (1, 3):
+        eng = nd.MDEngine(_params(nd, 8.5, refit_check_every=ce), x0, v0 * 50.0)
+        eng.run(10)
+        eng.sync()
+        d[ce] = eng.diagnostics()
+        eng.close()
+    assert d[1]["skin_violations"] == 0 and d[1]["early_refits"] > 0
+    assert d[3]["skin_violations"] > 0
 
 
 def test_simulate_drop_in(nd, oracle):
