@@ -365,7 +365,7 @@ ADJ_N = 32768
 ADJ_STEPS = 1000
 
 
-def adjoint_leg(nd, ctx, ext, flush, steps=ADJ_STEPS):
+def adjoint_leg(nd, ctx, ext, flush, steps=ADJ_STEPS, check_every=1):
     """Differentiable trajectory: 32,768 LJ atoms at density 0.83 (cube side
     (N/0.83)^(1/3), min separation 0.8), 1000 steps dt 1e-3, loss = squared
     deviation of the Gaussian-smoothed pair-distance histogram (64 bins on
@@ -373,14 +373,16 @@ def adjoint_leg(nd, ctx, ext, flush, steps=ADJ_STEPS):
     gradient wrt sigma, eps, x0, v0 with checkpoints every 50 steps.  Forward
     and backward passes timed with CUDA events on the library's stream (one
     captured graph each); the plain engine's 1000 steps on the same state are
-    timed beside them."""
+    timed beside them.  check_every: early-refit check interval of the
+    forward pass."""
     import numpy as np
     import torch
 
     side = (ADJ_N / 0.83) ** (1.0 / 3.0)
     x, v, _ = nd.synth.lj_system(nd.synth.SEED_ADJOINT, ADJ_N, side, 0.8)
     mp = nd.md_params(sigma=1.05, epsilon=0.9, cutoff=2.5, skin=0.3, dt=1e-3,
-                      box_hi=(side,) * 3, atomsperleaf=4, rebuild_every=REBUILD, resort_every=5)
+                      box_hi=(side,) * 3, atomsperleaf=4, rebuild_every=REBUILD, resort_every=5,
+                      refit_check_every=check_every)
     adj = nd.Adjoint(mp, nd.adj_spec(steps, checkpoint_every=50), x, v, ctx=ctx)
     _, target = adj.forward()
     adj.set_params(1.0, 1.0)
@@ -417,6 +419,7 @@ def adjoint_leg(nd, ctx, ext, flush, steps=ADJ_STEPS):
                          f"{steps} steps dt 1e-3, histogram loss (64 bins on [0, 2.5], "
                          "Gaussian width = bin width) vs the sigma 1.05 / eps 0.9 run, "
                          "checkpoints every 50 steps, skin 0.3, rebuild every 10"),
+            "refit_check_every": check_every,
             "value": b_ms / f_ms, "forward_ms_per_step": f_ms / steps,
             "adjoint_ms_per_step": b_ms / steps,
             "plain_engine_ms_per_step": plain_ms / steps,
@@ -585,7 +588,8 @@ def run_gb300(args):
     if rank == 0 and not args.no_plain:
         line["plain_lj_4096"] = plain_leg(nd, ctx, ext, flush)
     if rank == 0 and not args.no_adjoint:
-        line["adjoint"] = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps)
+        line["adjoint"] = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps,
+                                      check_every=args.adjoint_check_every)
     if rank == 0 and not args.no_stress:
         line["ns_stress"] = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -653,7 +657,8 @@ def run_only(args):
     elif args.only == "batched":
         out = batched_leg(nd, ctx, ext, flush)
     elif args.only == "adjoint":
-        out = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps)
+        out = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps,
+                          check_every=args.adjoint_check_every)
     else:
         out = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline,
                          points=args.stress_points)
@@ -674,6 +679,8 @@ def main():
                     help="skip the adjoint (differentiable trajectory) measurement")
     ap.add_argument("--adjoint-steps", type=int, default=ADJ_STEPS,
                     help="MD steps of the adjoint measurement (a multiple of 50)")
+    ap.add_argument("--adjoint-check-every", type=int, default=1,
+                    help="early-refit check interval of the adjoint's forward pass")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the 4,096-atom plain LJ measurement")
     ap.add_argument("--no-stress", action="store_true",
