@@ -1081,12 +1081,15 @@ __global__ void __launch_bounds__(128)
     if (npend) flush_tasks();
 }
 
-// Broad phase, second half: warps stride over the tasks; each walks its
-// subtree (from the root to the root's skip rope) with its group's union box
-// and records, at every leaf t it reaches, (q, t) for the lanes whose own leaf
-// q < t overlaps t.
+// Broad phase, second half: warps stride over the tasks.  A task's subtree
+// holds the leaves of one contiguous range (at most kTaskLeaves); the warp
+// scans them in order, four node loads in flight at a time, and records
+// (q, t) for the lanes whose own leaf q < t overlaps t.  That is the walk's
+// candidate set: a leaf overlapping q overlaps every ancestor (they contain
+// it), so a walk pruning with the group's union box reaches it; the scan
+// needs no dependent loads.
 __global__ void __launch_bounds__(128)
-    k_leaf_subwalk4(const float4* __restrict__ keys, int32_t nL,
+    k_leaf_subwalk4(const float4* __restrict__ keys, const int2* __restrict__ ranges, int32_t nL,
                     const unsigned long long* __restrict__ tcount, int64_t tcap,
                     const int2* __restrict__ tasks, unsigned long long* cursor, int64_t cap,
                     int2* __restrict__ out, int32_t* err) {
@@ -1098,32 +1101,37 @@ __global__ void __launch_bounds__(128)
     const int32_t nnodes = 2 * nL - 1;
     for (int64_t k = (int64_t)blockIdx.x * 4 + w; k < ntask; k += (int64_t)gridDim.x * 4) {
         const int2 tk = __ldg(&tasks[k]);
-        const int32_t q = tk.x * 32 + 1 + lane;
+        const int32_t q0 = tk.x * 32 + 1;
+        const int32_t q = q0 + lane;
         const bool valid = q <= nL;
         Node ql, un;
         group_boxes(keys, nL, q, ql, un);
-        if (tk.y < 1 || tk.y > nnodes) {
+        const int32_t root = tk.y;
+        if (root < 1 || root > nnodes) {
             if (lane == 0) set_error(err, ND_ERR_INTERNAL, tk.x);
             continue;
         }
-        const int32_t end = load_node(keys, tk.y).skip;
-        int32_t t = tk.y;
-        int32_t visits = 0;
-        while (t != end) {
-            if (t < 1 || t > nnodes || ++visits > 2 * kTaskLeaves) {
-                if (lane == 0) set_error(err, ND_ERR_INTERNAL, tk.x);
-                break;
-            }
-            const Node nd_ = load_node(keys, t);
-            if (overlap(un, nd_)) {
-                if (nd_.left == 0) {
-                    lp_append(valid && t > q && overlap(ql, nd_), q, t, buf, nb, cursor, cap, out);
-                    t = nd_.skip;
-                } else {
-                    t = nd_.left;
-                }
-            } else {
-                t = nd_.skip;
+        int32_t la = root, lb = root;  // leaf range of the subtree
+        if (root > nL) {
+            const int2 rg = __ldg(&ranges[root - nL - 1]);
+            la = rg.x;
+            lb = rg.y;
+        }
+        if (la < 1 || lb > nL || lb - la + 1 > kTaskLeaves) {
+            if (lane == 0) set_error(err, ND_ERR_INTERNAL, tk.x);
+            continue;
+        }
+        // leaves after the group's first only (t > q for some lane)
+        for (int32_t t0 = max(la, q0 + 1); t0 <= lb; t0 += 4) {
+            Node nd4[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (t0 + u <= lb) nd4[u] = load_node(keys, t0 + u);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int32_t t = t0 + u;
+                if (t > lb) break;  // warp-uniform
+                lp_append(valid && t > q && overlap(ql, nd4[u]), q, t, buf, nb, cursor, cap, out);
             }
         }
     }
@@ -1209,7 +1217,7 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
                 t.keys, t.ranges, t.nL, cursor, lcap, (int2*)c->leafpairs.p, tcursor, tcap,
                 (int2*)c->tasks.p, c->d_err);
             k_leaf_subwalk4<<<(unsigned)(nsm * std::max(occ, 1)), 128, 0, c->stream>>>(
-                t.keys, t.nL, tcursor, tcap, (const int2*)c->tasks.p, cursor, lcap,
+                t.keys, t.ranges, t.nL, tcursor, tcap, (const int2*)c->tasks.p, cursor, lcap,
                 (int2*)c->leafpairs.p, c->d_err);
             c->launches += 2;
             if ((st = check_launch(c, "leaf pairs (broad phase)"))) return st;
