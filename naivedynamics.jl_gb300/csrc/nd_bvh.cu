@@ -1084,15 +1084,21 @@ __global__ void __launch_bounds__(128)
 // Broad phase, second half: warps stride over the tasks.  A task's subtree
 // holds the leaves of one contiguous range (at most kTaskLeaves); the warp
 // scans them in order, four node loads in flight at a time, and records
-// (q, t) for the lanes whose own leaf q < t overlaps t.  That is the walk's
-// candidate set: a leaf overlapping q overlaps every ancestor (they contain
-// it), so a walk pruning with the group's union box reaches it; the scan
-// needs no dependent loads.
+// (q, t) for the lanes whose own leaf q < t overlaps t (a leaf overlapping q
+// overlaps every ancestor, so these are the candidates a walk pruning with
+// the group's union box would find) and whose atoms can be within r at all:
+// leaf boxes are atom boxes -/+ r/2, so overlapping boxes only bound the atom
+// boxes' gap on each axis by r; the Euclidean gap (per-axis gaps, each
+// lowered by a few ulps of the coordinates for the rounding of the -/+ r/2)
+// must be below r too.  That drops the candidates diagonally off q, about
+// 40 % of them in dense clusters, and every pair of a dropped leaf pair is
+// farther apart than r.
 __global__ void __launch_bounds__(128)
     k_leaf_subwalk4(const float4* __restrict__ keys, const int2* __restrict__ ranges, int32_t nL,
-                    const unsigned long long* __restrict__ tcount, int64_t tcap,
+                    float r, const unsigned long long* __restrict__ tcount, int64_t tcap,
                     const int2* __restrict__ tasks, unsigned long long* cursor, int64_t cap,
                     int2* __restrict__ out, int32_t* err) {
+    const float r2g = r * r * 1.0001f;  // the gap test is a filter: the distance test decides
     __shared__ int2 sbuf[4][kLeafBuf];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int2* buf = sbuf[w];
@@ -1121,6 +1127,11 @@ __global__ void __launch_bounds__(128)
             if (lane == 0) set_error(err, ND_ERR_INTERNAL, tk.x);
             continue;
         }
+        // rounding slack of this lane's coordinates: 8 ulps of the largest
+        const float mag = fmaxf(fmaxf(fmaxf(fabsf(ql.mnx), fabsf(ql.mxx)),
+                                      fmaxf(fabsf(ql.mny), fabsf(ql.mxy))),
+                                fmaxf(fabsf(ql.mnz), fabsf(ql.mxz)));
+        const float slack = valid ? mag * 9.5367431640625e-7f + 1e-30f : 0.0f;  // 8 * 2^-23
         // leaves after the group's first only (t > q for some lane)
         for (int32_t t0 = max(la, q0 + 1); t0 <= lb; t0 += 4) {
             Node nd4[4];
@@ -1131,7 +1142,16 @@ __global__ void __launch_bounds__(128)
             for (int u = 0; u < 4; ++u) {
                 const int32_t t = t0 + u;
                 if (t > lb) break;  // warp-uniform
-                lp_append(valid && t > q && overlap(ql, nd4[u]), q, t, buf, nb, cursor, cap, out);
+                const Node& b = nd4[u];
+                bool want = valid && t > q && overlap(ql, b);
+                if (want) {
+                    // atom-box gap per axis = key-box gap + r (r/2 on each box)
+                    const float gx = fmaxf(fmaxf(ql.mnx - b.mxx, b.mnx - ql.mxx) + r - slack, 0.0f);
+                    const float gy = fmaxf(fmaxf(ql.mny - b.mxy, b.mny - ql.mxy) + r - slack, 0.0f);
+                    const float gz = fmaxf(fmaxf(ql.mnz - b.mxz, b.mnz - ql.mxz) + r - slack, 0.0f);
+                    want = gx * gx + gy * gy + gz * gz < r2g;
+                }
+                lp_append(want, q, t, buf, nb, cursor, cap, out);
             }
         }
     }
@@ -1217,7 +1237,7 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
                 t.keys, t.ranges, t.nL, cursor, lcap, (int2*)c->leafpairs.p, tcursor, tcap,
                 (int2*)c->tasks.p, c->d_err);
             k_leaf_subwalk4<<<(unsigned)(nsm * std::max(occ, 1)), 128, 0, c->stream>>>(
-                t.keys, t.ranges, t.nL, tcursor, tcap, (const int2*)c->tasks.p, cursor, lcap,
+                t.keys, t.ranges, t.nL, r, tcursor, tcap, (const int2*)c->tasks.p, cursor, lcap,
                 (int2*)c->leafpairs.p, c->d_err);
             c->launches += 2;
             if ((st = check_launch(c, "leaf pairs (broad phase)"))) return st;
