@@ -535,10 +535,29 @@ __global__ void __launch_bounds__(kBlock)
     const int tid = threadIdx.x;
     const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
     {
+        // four positions per thread in flight: their leaf indices, then the
+        // positions
         const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
         const int32_t m = min(nu * APL, smpos);
-        for (int32_t k = tid; k < m; k += kBlock)
-            spos[k] = __ldg(&pos[(int64_t)__ldg(&U[k / APL]) * APL + (k % APL)]);
+        for (int32_t k = tid; k < m; k += 4 * kBlock) {
+            int32_t lf[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int32_t kk = k + j * kBlock;
+                lf[j] = kk < m ? __ldg(&U[kk / APL]) : 0;
+            }
+            float4 r[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int32_t kk = k + j * kBlock;
+                if (kk < m) r[j] = __ldg(&pos[(int64_t)lf[j] * APL + (kk % APL)]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int32_t kk = k + j * kBlock;
+                if (kk < m) spos[kk] = r[j];
+            }
+        }
     }
     __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * kBlock + tid;
@@ -757,11 +776,30 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     // stage the block's union: record of atom (leaf * apl + e) at u * apl + e,
     // up to the shared-memory capacity; larger unions read the rest from L2
     {
+        // four records per thread in flight: their leaf indices, then the
+        // records (apl is a power of two)
         const int32_t nu = min(__ldg(&a.ucount[blockIdx.x]), a.ucap);
         const int32_t m = min(nu * a.apl, a.smrec);
-        for (int32_t k = threadIdx.x; k < m; k += kBlock * TPA) {
-            const int32_t u = k / a.apl, e = k - u * a.apl;
-            srec[k] = __ldg(&a.rec_in[(int64_t)__ldg(&U[u]) * a.apl + e]);
+        const int32_t lsh = __ffs(a.apl) - 1, emask = a.apl - 1;
+        constexpr int32_t NT = kBlock * TPA;
+        for (int32_t k = threadIdx.x; k < m; k += 4 * NT) {
+            int32_t lf[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int32_t kk = k + j * NT;
+                lf[j] = kk < m ? __ldg(&U[kk >> lsh]) : 0;
+            }
+            int4 r[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int32_t kk = k + j * NT;
+                if (kk < m) r[j] = __ldg(&a.rec_in[((int64_t)lf[j] << lsh) + (kk & emask)]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int32_t kk = k + j * NT;
+                if (kk < m) srec[kk] = r[j];
+            }
         }
     }
     __syncthreads();
