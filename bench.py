@@ -181,11 +181,17 @@ def batched_leg(nd, ctx, ext, flush):
     density U[0.6, 0.9], sigma U[0.9, 1.1], eps U[0.8, 1.2], r_c 2.5, dt 1e-3,
     rebuild every 10, 200 steps) through one autotuned engine, against the same
     systems run one by one through the plain engine.  Both timed with CUDA
-    events on the library's stream, inputs resident, L2 flushed before each."""
+    events on the library's stream, inputs resident, L2 flushed before each.
+    On N GPUs every rank runs its share of the systems (greedy balance of the
+    atom counts; no exchange): atom-steps summed over ranks over the slowest
+    rank's time."""
     import numpy as np
     import torch
+    from naivedynamics import replicas
 
-    e = nd.synth.ensemble(nd.synth.SEED_ENSEMBLE)
+    ws, rank = replicas.world()
+    e_all = nd.synth.ensemble(nd.synth.SEED_ENSEMBLE)
+    e = replicas.take_systems(e_all, replicas.shard_systems(e_all["n_atoms"], ws)[rank])
     table = nd.systems_table(e["n_atoms"], e["sigma"], e["epsilon"], e["box_lo"], e["box_hi"])
     base = nd.md_params(cutoff=2.5, skin=0.3, dt=1e-3, atomsperleaf=4, rebuild_every=REBUILD)
     t0 = time.perf_counter()
@@ -236,11 +242,15 @@ def batched_leg(nd, ctx, ext, flush):
     t_plain = timed(lambda: [eng.run(ENSEMBLE_STEPS) for eng in plain])
     for eng in plain:
         eng.close()
-    v_bat = n_tot * ENSEMBLE_STEPS / t_bat
-    v_plain = n_tot * ENSEMBLE_STEPS / t_plain
+    work = replicas.sum_over_ranks(n_tot * ENSEMBLE_STEPS)
+    t_bat = replicas.max_over_ranks(t_bat)
+    t_plain = replicas.max_over_ranks(t_plain)
+    v_bat = work / t_bat
+    v_plain = work / t_plain
+    n_all = int(e_all["n_atoms"].sum())
     return {"metric": "ensemble atom-steps/s, batched vs plain", "unit": UNIT,
-            "workload": (f"ensemble_512: {len(e['n_atoms'])} LJ systems, {n_tot} atoms "
-                         f"(N_s {int(e['n_atoms'].min())}..{int(e['n_atoms'].max())}), "
+            "workload": (f"ensemble_512: {len(e_all['n_atoms'])} LJ systems, {n_all} atoms "
+                         f"(N_s {int(e_all['n_atoms'].min())}..{int(e_all['n_atoms'].max())}), "
                          "rho U[0.6,0.9], sigma U[0.9,1.1], eps U[0.8,1.2], r_c 2.5, "
                          f"skin {tuned.skin:.1f} (autotuned), "
                          f"dt 1e-3, rebuild every 10, {ENSEMBLE_STEPS} steps"),
@@ -255,7 +265,8 @@ def batched_leg(nd, ctx, ext, flush):
                       "union_search": UNION_NAMES[tuned.union_search],
                       "refit_check_every": max(tuned.refit_check_every, 1),
                       "autotune_s": round(tune_s, 2)},
-            "plain_path": "512 nd_md engines run one after another on one stream (graphs)"}
+            "plain_path": "512 nd_md engines run one after another on one stream (graphs)",
+            "sharding": f"{ws} rank(s), greedy balance of the systems' atom counts"}
 
 
 def plain_leg(nd, ctx, ext, flush):
@@ -442,6 +453,8 @@ def run_gb300(args):
     import torch
     import naivedynamics as nd
 
+    from naivedynamics import replicas
+
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     if ws > 1:
@@ -496,11 +509,7 @@ def run_gb300(args):
     # rebuild bodies that ran
     launches = (ctx.launch_count() - launches0 + diag["body_kernels"] - diag0["body_kernels"])
     t_ms = sum(s.elapsed_time(e) for (s, e) in events)
-    t_max = t_ms
-    if ws > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = replicas.max_over_ranks(t_ms)  # the job's time: its slowest replica's
     stats = eng.stats()
 
     # ---- roofline of the dominant kernel: k_md_step launches each bracketed
@@ -545,11 +554,7 @@ def run_gb300(args):
         t0 = time.perf_counter()
         e2e_call()
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_t)
-    if ws > 1:
-        tt = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = replicas.max_over_ranks(sum(e2e_t))
 
     total_atom_steps = ws * N_ATOMS * MD_PER_STEP * args.steps
     value = total_atom_steps / (t_max * 1e-3)
@@ -591,8 +596,10 @@ def run_gb300(args):
     if clocks:
         line["clocks"] = clocks
     eng.close()
-    if rank == 0 and not args.no_batched:
-        line["batched"] = batched_leg(nd, ctx, ext, flush)
+    if not args.no_batched:
+        b = batched_leg(nd, ctx, ext, flush)  # every rank runs its share of the systems
+        if rank == 0:
+            line["batched"] = b
     if rank == 0 and not args.no_plain:
         line["plain_lj_4096"] = plain_leg(nd, ctx, ext, flush)
     if rank == 0 and not args.no_adjoint:
