@@ -607,6 +607,27 @@ __device__ __forceinline__ bool overlap(const Node& a, const Node& b) {
            (a.mnz < b.mxz) & (a.mxz > b.mnz);
 }
 
+// Rounding slack of leaf a's box coordinates: 8 ulps of the largest.
+__device__ __forceinline__ float leaf_slack(const Node& a) {
+    const float mag = fmaxf(fmaxf(fmaxf(fabsf(a.mnx), fabsf(a.mxx)), fmaxf(fabsf(a.mny), fabsf(a.mxy))),
+                            fmaxf(fabsf(a.mnz), fabsf(a.mxz)));
+    return mag * 9.5367431640625e-7f;  // 8 * 2^-23
+}
+
+// Whether two leaves whose key boxes (atom boxes -/+ r/2) overlap can hold a
+// pair within r: the per-axis gaps of the atom boxes (key-box gap + r, each
+// lowered by the rounding slack of the -/+ r/2) must have a Euclidean norm
+// below r (r2g = r^2 widened a little: a filter, the distance test decides).
+// Boxes that overlap on every axis only bound each gap by r; this drops the
+// leaf pairs diagonally apart.
+__device__ __forceinline__ bool leaf_gap_ok(const Node& a, const Node& b, float r, float r2g,
+                                            float slack) {
+    const float gx = fmaxf(fmaxf(a.mnx - b.mxx, b.mnx - a.mxx) + r - slack, 0.0f);
+    const float gy = fmaxf(fmaxf(a.mny - b.mxy, b.mny - a.mxy) + r - slack, 0.0f);
+    const float gz = fmaxf(fmaxf(a.mnz - b.mxz, b.mnz - a.mxz) + r - slack, 0.0f);
+    return gx * gx + gy * gy + gz * gz < r2g;
+}
+
 // Emission sinks.  COUNT counts; WRITE writes at a running cursor; ATOMIC
 // reserves chunks of a global cursor (warp-aggregated) as pairs appear.
 struct SinkCount {
@@ -854,9 +875,10 @@ __device__ __forceinline__ unsigned leaf_tests16(const float4 (&qa)[4], const fl
 
 __global__ void __launch_bounds__(128, 6)
     k_leaf_warp4(const float4* __restrict__ keys, const float4* __restrict__ pos, int32_t nL,
-                 float r2, unsigned long long* cursor, int64_t cap, int32_t* pi, int32_t* pj,
-                 float* pd, int32_t* err) {
+                 float r, float r2, unsigned long long* cursor, int64_t cap, int32_t* pi,
+                 int32_t* pj, float* pd, int32_t* err) {
     constexpr int APL = 4;
+    const float r2g = r * r * 1.0001f;
     __shared__ int2 sbij[4][kWarpBuf];
     __shared__ float sbd[4][kWarpBuf];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -880,6 +902,7 @@ __global__ void __launch_bounds__(128, 6)
 #pragma unroll
         for (int i = 0; i < APL; ++i) qa[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    const float slack = valid ? leaf_slack(ql) : 0.0f;
     int nb = 0;
     int32_t ia[APL];
 #pragma unroll
@@ -915,7 +938,7 @@ __global__ void __launch_bounds__(128, 6)
                 unsigned mask = 0;
                 float d2[16];
                 int32_t ib[APL] = {0, 0, 0, 0};
-                if (valid && t > q && overlap(ql, nd_)) {
+                if (valid && t > q && overlap(ql, nd_) && leaf_gap_ok(ql, nd_, r, r2g, slack)) {
                     const int64_t B = (int64_t)(t - 1) * APL;
                     float4 tb[APL];
 #pragma unroll
@@ -1086,13 +1109,9 @@ __global__ void __launch_bounds__(128)
 // scans them in order, four node loads in flight at a time, and records
 // (q, t) for the lanes whose own leaf q < t overlaps t (a leaf overlapping q
 // overlaps every ancestor, so these are the candidates a walk pruning with
-// the group's union box would find) and whose atoms can be within r at all:
-// leaf boxes are atom boxes -/+ r/2, so overlapping boxes only bound the atom
-// boxes' gap on each axis by r; the Euclidean gap (per-axis gaps, each
-// lowered by a few ulps of the coordinates for the rounding of the -/+ r/2)
-// must be below r too.  That drops the candidates diagonally off q, about
-// 40 % of them in dense clusters, and every pair of a dropped leaf pair is
-// farther apart than r.
+// the group's union box would find) and whose atoms can be within r at all
+// (leaf_gap_ok: about 40 % of the overlapping leaves in dense clusters are
+// not).
 __global__ void __launch_bounds__(128)
     k_leaf_subwalk4(const float4* __restrict__ keys, const int2* __restrict__ ranges, int32_t nL,
                     float r, const unsigned long long* __restrict__ tcount, int64_t tcap,
@@ -1127,11 +1146,7 @@ __global__ void __launch_bounds__(128)
             if (lane == 0) set_error(err, ND_ERR_INTERNAL, tk.x);
             continue;
         }
-        // rounding slack of this lane's coordinates: 8 ulps of the largest
-        const float mag = fmaxf(fmaxf(fmaxf(fabsf(ql.mnx), fabsf(ql.mxx)),
-                                      fmaxf(fabsf(ql.mny), fabsf(ql.mxy))),
-                                fmaxf(fabsf(ql.mnz), fabsf(ql.mxz)));
-        const float slack = valid ? mag * 9.5367431640625e-7f + 1e-30f : 0.0f;  // 8 * 2^-23
+        const float slack = valid ? leaf_slack(ql) : 0.0f;
         // leaves after the group's first only (t > q for some lane)
         for (int32_t t0 = max(la, q0 + 1); t0 <= lb; t0 += 4) {
             Node nd4[4];
@@ -1143,14 +1158,8 @@ __global__ void __launch_bounds__(128)
                 const int32_t t = t0 + u;
                 if (t > lb) break;  // warp-uniform
                 const Node& b = nd4[u];
-                bool want = valid && t > q && overlap(ql, b);
-                if (want) {
-                    // atom-box gap per axis = key-box gap + r (r/2 on each box)
-                    const float gx = fmaxf(fmaxf(ql.mnx - b.mxx, b.mnx - ql.mxx) + r - slack, 0.0f);
-                    const float gy = fmaxf(fmaxf(ql.mny - b.mxy, b.mny - ql.mxy) + r - slack, 0.0f);
-                    const float gz = fmaxf(fmaxf(ql.mnz - b.mxz, b.mnz - ql.mxz) + r - slack, 0.0f);
-                    want = gx * gx + gy * gy + gz * gz < r2g;
-                }
+                const bool want =
+                    valid && t > q && overlap(ql, b) && leaf_gap_ok(ql, b, r, r2g, slack);
                 lp_append(want, q, t, buf, nb, cursor, cap, out);
             }
         }
@@ -1209,7 +1218,7 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
         // no scratch for candidate pairs: the one-pass walk
         cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), c->stream);
         k_leaf_warp4<<<(unsigned)cdiv(t.nL, 128), 128, 0, c->stream>>>(
-            t.keys, t.pos4, t.nL, r2, cursor, capacity, pi, pj, pd, c->d_err);
+            t.keys, t.pos4, t.nL, r, r2, cursor, capacity, pi, pj, pd, c->d_err);
         c->launches++;
     } else {
         // broad phase: tasks, then the tasks' subtree walks; re-run with
