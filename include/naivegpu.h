@@ -57,6 +57,10 @@ typedef int32_t nd_status;
 #define ND_PAIRS_ORDERED   0  /* exactly the reference's single-thread emission order */
 #define ND_PAIRS_UNORDERED 1  /* same multiset, order decided at run time (one pass)  */
 
+/* Pair criterion on the Float32 squared distance d2 (d = sqrt(d2), rounded). */
+#define ND_CRIT_SQUARED 0  /* d2 < r^2: leafneighbor_traverse (BVHTraverse.jl:1048)        */
+#define ND_CRIT_SQRT    1  /* d < r: simdneighbor_traverse (ext/NaiveSIMD.jl:529,589)      */
+
 typedef struct nd_ctx nd_ctx;
 typedef struct nd_md nd_md;
 
@@ -185,6 +189,19 @@ nd_status nd_leaf_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, 
 nd_status nd_leaf_pairs_dev(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec,
                             int32_t order, int32_t mode, int32_t* pi, int32_t* pj, float* pd,
                             int64_t capacity, int64_t* count);
+
+/*
+ * simdbuild_traverse_bvh(position, spec) (ext/NaiveSIMD.jl:706-710) =
+ * simdTreeData (:424-480, the leafTreeData tree; atomsperleaf must be 4, else
+ * ND_ERR_SPEC) + simdneighbor_traverse (:610-704): the traversal and emission
+ * order of leafneighbor_traverse with the SIMD twin's criterion sqrt(d^2) < r
+ * (:529,589; the pairs on the boundary can differ from d^2 < r^2).  The
+ * reference splits query leaves over threads; ND_PAIRS_ORDERED is its order on
+ * one thread.  Same buffer protocol as nd_leaf_pairs.
+ */
+nd_status nd_simd_leaf_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec,
+                             int32_t order, int32_t mode, int32_t* pi, int32_t* pj, float* pd,
+                             int64_t capacity, int64_t* count);
 
 /*
  * build_traverse_bvh(position, spec) (BVHTraverse.jl:1416-1421) = TreeData +

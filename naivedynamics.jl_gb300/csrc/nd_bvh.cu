@@ -10,6 +10,7 @@
 // exact single-precision operation order (no FMA contraction, IEEE division and
 // square root) so that codes, order, tree and pair list are bit-identical.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <utility>
 
@@ -1205,9 +1206,22 @@ __global__ void __launch_bounds__(256)
     warp_buf_flush(bij, bd, nb, cursor, cap, pi, pj, pd);
 }
 
-nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int32_t* pj,
-                         float* pd, int64_t capacity, int64_t* total) {
-    const float r2 = r * r;  // (neighbor_distance)^2 in Float32
+// The pair criterion as a threshold on the Float32 squared distance d2:
+// ND_CRIT_SQUARED: d2 < r^2 (leafneighbor_traverse, BVHTraverse.jl:1048), the
+// threshold fl(r * r); ND_CRIT_SQRT: sqrt(d2) < r (simdneighbor_traverse,
+// ext/NaiveSIMD.jl:529,589), the smallest float T with sqrtf(T) >= r -- the
+// square root is correctly rounded, hence monotonic, so sqrt(d2) < r exactly
+// when d2 < T.  The kernels compare d2 with the threshold either way.
+float pair_threshold(float r, int32_t criterion) {
+    float t = r * r;
+    if (criterion != ND_CRIT_SQRT) return t;
+    while (t > 0.0f && std::sqrt(std::nextafter(t, 0.0f)) >= r) t = std::nextafter(t, 0.0f);
+    while (std::sqrt(t) < r) t = std::nextafter(t, INFINITY);
+    return t;
+}
+
+nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, float r2, int32_t* pi,
+                         int32_t* pj, float* pd, int64_t capacity, int64_t* total) {
     if (t.apl != 4) return ND_ERR_ARG;
     nd_status st;
     if ((st = ensure(c, c->misc, 64))) return st;
@@ -1285,8 +1299,7 @@ nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int
     return ND_OK;
 }
 
-nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int64_t* total) {
-    const float r2 = r * r;
+nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int64_t* total) {
     nd_status st;
     int64_t nq = (kind == 0) ? t.nL : t.n;
     if ((st = ensure(c, c->counts, sizeof(int64_t) * (size_t)(nq + 1)))) return st;
@@ -1314,9 +1327,8 @@ nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int64_t* 
     return ND_OK;
 }
 
-nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int32_t* pi, int32_t* pj,
+nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int32_t* pi, int32_t* pj,
                       float* pd) {
-    const float r2 = r * r;
     int64_t nq = (kind == 0) ? t.nL : t.n;
     const int64_t* offsets = (const int64_t*)c->offsets.p;
     unsigned grid = (unsigned)cdiv(nq, 128);

@@ -153,9 +153,10 @@ static nd_status tree_from_host(Ctx* c, const float* xyz, const nd_bvh_spec* s, 
 
 nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode, int kind,
                        const float* xyz, bool host, int32_t* pi, int32_t* pj, float* pd,
-                       int64_t capacity, int64_t* count) {
+                       int64_t capacity, int64_t* count, int32_t criterion) {
     nd_status st = spec_ok(s);
     if (st) return st;
+    if (criterion != ND_CRIT_SQUARED && criterion != ND_CRIT_SQRT) return ND_ERR_ARG;
     if (!xyz || !count || capacity < 0) return ND_ERR_ARG;
     if (capacity > 0 && (!pi || !pj || !pd)) return ND_ERR_ARG;
     if (order != ND_ORDER_REFERENCE && order != ND_ORDER_SPATIAL) return ND_ERR_ARG;
@@ -172,12 +173,13 @@ nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode
     }
     if (st) return st;
     const float r = s->neighbor_distance;
+    const float r2 = pair_threshold(r, criterion);
     int64_t total = 0;
     if (kind == 0 && mode == ND_PAIRS_UNORDERED && s->atomsperleaf == 4) {
         if (host) {
             int64_t devcap = (int64_t)(c->pairs_i.bytes / sizeof(int32_t));
             devcap = std::min(devcap, (int64_t)(c->pairs_d.bytes / sizeof(float)));
-            if ((st = emit_unordered(c, t, r, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
+            if ((st = emit_unordered(c, t, r, r2, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
                                      (float*)c->pairs_d.p, devcap, &total)))
                 return st;
             *count = total;
@@ -187,17 +189,17 @@ nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode
                 if ((st = ensure(c, c->pairs_j, sizeof(int32_t) * (size_t)total))) return st;
                 if ((st = ensure(c, c->pairs_d, sizeof(float) * (size_t)total))) return st;
                 int64_t again = 0;
-                if ((st = emit_unordered(c, t, r, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
+                if ((st = emit_unordered(c, t, r, r2, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
                                          (float*)c->pairs_d.p, total, &again)))
                     return st;
             }
         } else {
-            if ((st = emit_unordered(c, t, r, pi, pj, pd, capacity, &total))) return st;
+            if ((st = emit_unordered(c, t, r, r2, pi, pj, pd, capacity, &total))) return st;
             *count = total;
             return total > capacity ? ND_NEED_REALLOC : ND_OK;
         }
     } else {
-        if ((st = count_pairs(c, t, r, kind, &total))) return st;
+        if ((st = count_pairs(c, t, r2, kind, &total))) return st;
         *count = total;
         if (total > capacity) return ND_NEED_REALLOC;
         if (total == 0) return ND_OK;
@@ -205,11 +207,11 @@ nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode
             if ((st = ensure(c, c->pairs_i, sizeof(int32_t) * (size_t)total))) return st;
             if ((st = ensure(c, c->pairs_j, sizeof(int32_t) * (size_t)total))) return st;
             if ((st = ensure(c, c->pairs_d, sizeof(float) * (size_t)total))) return st;
-            if ((st = write_pairs(c, t, r, kind, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
+            if ((st = write_pairs(c, t, r2, kind, (int32_t*)c->pairs_i.p, (int32_t*)c->pairs_j.p,
                                   (float*)c->pairs_d.p)))
                 return st;
         } else {
-            if ((st = write_pairs(c, t, r, kind, pi, pj, pd))) return st;
+            if ((st = write_pairs(c, t, r2, kind, pi, pj, pd))) return st;
             return sync_and_check(c, "pair write");
         }
     }
@@ -424,6 +426,15 @@ nd_status nd_leaf_pairs_dev(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, i
                             int64_t* count) {
     if (!h) return ND_ERR_ARG;
     return nd::pairs_common(&h->c, s, order, mode, 0, xyz, false, pi, pj, pd, capacity, count);
+}
+
+nd_status nd_simd_leaf_pairs(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, int32_t order,
+                             int32_t mode, int32_t* pi, int32_t* pj, float* pd,
+                             int64_t capacity, int64_t* count) {
+    if (!h || !s) return ND_ERR_ARG;
+    if (s->atomsperleaf != 4) return ND_ERR_SPEC;  // simdTreeData asserts atomsperleaf == 4
+    return nd::pairs_common(&h->c, s, order, mode, 0, xyz, true, pi, pj, pd, capacity, count,
+                            ND_CRIT_SQRT);
 }
 
 nd_status nd_atom_pairs(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, int32_t order,

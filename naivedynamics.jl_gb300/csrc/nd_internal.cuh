@@ -180,7 +180,7 @@ nd_status scan_exclusive(Ctx* c, const int64_t* in, int64_t* out, int64_t n, int
 // pipeline on the context's buffers (host or device positions and outputs).
 nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode, int kind,
                        const float* xyz, bool host, int32_t* pi, int32_t* pj, float* pd,
-                       int64_t capacity, int64_t* count);
+                       int64_t capacity, int64_t* count, int32_t criterion = ND_CRIT_SQUARED);
 nd_status pair_hash(Ctx* c, const int32_t* pi, const int32_t* pj, const float* pd, int64_t np,
                     uint64_t out[2]);
 
@@ -227,12 +227,13 @@ nd_status forces_pairs(Ctx* c, const nd_md_params* p, int32_t n, const double* x
                        const double* q, const int32_t* pi, const int32_t* pj, int64_t np,
                        float* f, double* energy);
 // Two-phase ordered emission: count (computes per-query offsets, syncs) then write.
-nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int64_t* total);
-nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r, int kind, int32_t* pi, int32_t* pj,
+// Squared-distance threshold of a pair criterion (ND_CRIT_*).
+float pair_threshold(float r, int32_t criterion);
+nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int64_t* total);
+nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int32_t* pi, int32_t* pj,
                       float* pd);
-// One pass (apl == 4, leaf path): writes at most capacity pairs, *total = all pairs.
-nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, int32_t* pi, int32_t* pj,
-                         float* pd, int64_t capacity, int64_t* total);
+nd_status emit_unordered(Ctx* c, const TreeBuffers& t, float r, float r2, int32_t* pi,
+                         int32_t* pj, float* pd, int64_t capacity, int64_t* total);
 
 // ------------------------------------------------------------- adjoint
 struct AdjEngine;

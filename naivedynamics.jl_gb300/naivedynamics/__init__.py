@@ -7,10 +7,11 @@ the library and fails loudly if it has not been built.
 from . import _lib
 from ._lib import (Context, NDError, SpecError, InexactError, default_context,
                    ND_ORDER_REFERENCE, ND_ORDER_SPATIAL, ND_PAIRS_ORDERED, ND_PAIRS_UNORDERED,
-                   ND_UNION_BLOCKS, ND_UNION_TREE, GRIDKEY_DTYPE, PAIR_DTYPE)
+                   ND_CRIT_SQUARED, ND_CRIT_SQRT, ND_UNION_BLOCKS, ND_UNION_TREE,
+                   GRIDKEY_DTYPE, PAIR_DTYPE)
 from .bvh import (SpheresBVHSpecs, APointPrimitive, leafTreeData, TreeData,
-                  leafbuild_traverse_bvh, build_traverse_bvh, gpubvh_neighborlist,
-                  neighbor_pairs_dev, pair_hash_dev)
+                  leafbuild_traverse_bvh, simdbuild_traverse_bvh, build_traverse_bvh,
+                  gpubvh_neighborlist, neighbor_pairs_dev, pair_hash_dev)
 from .dynamics import (ForceField, md_params, force_lennardjones_, force_coulomb_, sum_forces_,
                        forces, SimSpec, GenericObjectCollection, GenericRandomCollector,
                        simulate_, MDEngine, Ensemble, systems_table, autotune)

@@ -32,6 +32,8 @@ ND_BOX_LEAF = 0
 ND_BOX_ATOM = 1
 ND_PAIRS_ORDERED = 0
 ND_PAIRS_UNORDERED = 1
+ND_CRIT_SQUARED = 0
+ND_CRIT_SQRT = 1
 ND_UNION_BLOCKS = 0
 ND_UNION_TREE = 1
 
@@ -123,6 +125,8 @@ SIGNATURES = {
                              ctypes.POINTER(_i64)]),
     "nd_leaf_pairs_dev": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _i32, _i32, _vp, _vp, _vp,
                                  _i64, ctypes.POINTER(_i64)]),
+    "nd_simd_leaf_pairs": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _i32, _i32, _vp, _vp, _vp,
+                                  _i64, ctypes.POINTER(_i64)]),
     "nd_atom_pairs": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _i32, _vp, _vp, _vp, _i64,
                              ctypes.POINTER(_i64)]),
     "nd_pair_hash_dev": (_i32, [_vp, _vp, _vp, _vp, _i64, ctypes.POINTER(_u64)]),

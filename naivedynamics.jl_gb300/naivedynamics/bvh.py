@@ -23,9 +23,10 @@ from ._lib import (GRIDKEY_DTYPE, ND_BOX_ATOM, ND_BOX_LEAF, ND_NEED_REALLOC, ND_
                    PAIR_DTYPE, SpecError, default_context, ptr)
 
 __all__ = ["SpheresBVHSpecs", "APointPrimitive", "leafTreeData", "TreeData",
-           "leafbuild_traverse_bvh", "build_traverse_bvh", "gpubvh_neighborlist",
-           "neighbor_pairs_dev", "pair_hash_dev", "GRIDKEY_DTYPE", "PAIR_DTYPE",
-           "ND_ORDER_REFERENCE", "ND_ORDER_SPATIAL", "ND_PAIRS_ORDERED", "ND_PAIRS_UNORDERED"]
+           "leafbuild_traverse_bvh", "simdbuild_traverse_bvh", "build_traverse_bvh",
+           "gpubvh_neighborlist", "neighbor_pairs_dev", "pair_hash_dev", "GRIDKEY_DTYPE",
+           "PAIR_DTYPE", "ND_ORDER_REFERENCE", "ND_ORDER_SPATIAL", "ND_PAIRS_ORDERED",
+           "ND_PAIRS_UNORDERED"]
 
 
 @dataclass(frozen=True)
@@ -144,6 +145,21 @@ def leafbuild_traverse_bvh(position, spec: SpheresBVHSpecs, order: int = ND_ORDE
     x = _positions(position)
     cs = spec.c_spec()
     fn = lambda h, *a: _lib.lib().nd_leaf_pairs(h, ptr(x), ctypes.byref(cs), order, mode, *a)
+    return _pairs(fn, ctx, capacity_hint=capacity_hint)
+
+
+def simdbuild_traverse_bvh(position, spec: SpheresBVHSpecs, order: int = ND_ORDER_REFERENCE,
+                           mode: int = ND_PAIRS_ORDERED, ctx=None, capacity_hint=None):
+    """simdbuild_traverse_bvh (ext/NaiveSIMD.jl:706-710): the SIMD twin of
+    leafbuild_traverse_bvh -- the same tree and traversal (atomsperleaf must be
+    4), pairs kept when sqrt(d^2) < r (:529,589) rather than d^2 < r^2.  The
+    reference runs its query leaves on several threads; ND_PAIRS_ORDERED gives
+    its order on one thread.
+    """
+    ctx = ctx or default_context()
+    x = _positions(position)
+    cs = spec.c_spec()
+    fn = lambda h, *a: _lib.lib().nd_simd_leaf_pairs(h, ptr(x), ctypes.byref(cs), order, mode, *a)
     return _pairs(fn, ctx, capacity_hint=capacity_hint)
 
 

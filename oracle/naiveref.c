@@ -317,8 +317,27 @@ static inline int aabb_overlap(const ref_key* a, const ref_key* b) {
         ++count;                                               \
     } while (0)
 
+/* criterion 0: d^2 < r^2 (leafneighbor_traverse, BVHTraverse.jl:1048);
+ * criterion 1: sqrt(d^2) < r (simdonecluster_proximitytest! /
+ * simdtwocluster_proximitytest!, ext/NaiveSIMD.jl:529,589), with the same
+ * tree, traversal and emission order (simdneighbor_traverse, :610-704, on one
+ * thread). */
+static inline int pair_hit(float d2, float r, float r2, int32_t criterion) {
+    return criterion == 0 ? (d2 < r2) : (sqrtf(d2) < r);
+}
+
+int64_t ref_leaf_traverse_crit(const ref_key* keys, const int32_t* idx, const float* pos,
+                               int32_t nL, int32_t apl, float r, int32_t criterion, int32_t* pi,
+                               int32_t* pj, float* pd, int64_t cap);
+
 int64_t ref_leaf_traverse(const ref_key* keys, const int32_t* idx, const float* pos, int32_t nL,
                           int32_t apl, float r, int32_t* pi, int32_t* pj, float* pd, int64_t cap) {
+    return ref_leaf_traverse_crit(keys, idx, pos, nL, apl, r, 0, pi, pj, pd, cap);
+}
+
+int64_t ref_leaf_traverse_crit(const ref_key* keys, const int32_t* idx, const float* pos,
+                               int32_t nL, int32_t apl, float r, int32_t criterion, int32_t* pi,
+                               int32_t* pj, float* pd, int64_t cap) {
     const float r2 = r * r;
     int64_t count = 0;
     for (int32_t q = 1; q <= nL; ++q) {
@@ -328,7 +347,7 @@ int64_t ref_leaf_traverse(const ref_key* keys, const int32_t* idx, const float* 
         for (int32_t i = 0; i < apl - 1; ++i)
             for (int32_t j = i + 1; j < apl; ++j) {
                 float d2 = ref_dist2(&pos[3 * (A + i)], &pos[3 * (A + j)]);
-                if (d2 < r2) EMIT(idx[A + i], idx[A + j], sqrtf(d2));
+                if (pair_hit(d2, r, r2, criterion)) EMIT(idx[A + i], idx[A + j], sqrtf(d2));
             }
         int32_t t = ql->skip;
         while (t != 0) {
@@ -340,7 +359,7 @@ int64_t ref_leaf_traverse(const ref_key* keys, const int32_t* idx, const float* 
                     for (int32_t i = 0; i < apl; ++i)
                         for (int32_t j = 0; j < apl; ++j) {
                             float d2 = ref_dist2(&pos[3 * (A + i)], &pos[3 * (B + j)]);
-                            if (d2 < r2) EMIT(idx[A + i], idx[B + j], sqrtf(d2));
+                            if (pair_hit(d2, r, r2, criterion)) EMIT(idx[A + i], idx[B + j], sqrtf(d2));
                         }
                     t = node->skip;
                 } else {

@@ -83,6 +83,11 @@ int ref_tree(const float* xyz, int32_t n, float r, int32_t apl, int32_t order, i
 int64_t ref_leaf_traverse(const ref_key* keys, const int32_t* idx_sorted, const float* pos_sorted,
                           int32_t nL, int32_t apl, float r, int32_t* pi, int32_t* pj, float* pd,
                           int64_t cap);
+/* The same traversal with a pair criterion: 0 = d^2 < r^2 (leafneighbor_traverse),
+ * 1 = sqrt(d^2) < r (simdneighbor_traverse, ext/NaiveSIMD.jl:529,589). */
+int64_t ref_leaf_traverse_crit(const ref_key* keys, const int32_t* idx, const float* pos,
+                               int32_t nL, int32_t apl, float r, int32_t criterion, int32_t* pi,
+                               int32_t* pj, float* pd, int64_t cap);
 
 /* Same traversal, counting and hashing only, OpenMP over query leaves. */
 int64_t ref_leaf_traverse_hash(const ref_key* keys, const int32_t* idx_sorted,

@@ -89,6 +89,10 @@ def lib():
                 fn.argtypes = [ctypes.c_void_p, i32p, f32p, ctypes.c_int32, ctypes.c_int32,
                                ctypes.c_float, i32p, i32p, f32p, ctypes.c_int64]
                 fn.restype = ctypes.c_int64
+            L.ref_leaf_traverse_crit.argtypes = [ctypes.c_void_p, i32p, f32p, ctypes.c_int32,
+                                                 ctypes.c_int32, ctypes.c_float, ctypes.c_int32,
+                                                 i32p, i32p, f32p, ctypes.c_int64]
+            L.ref_leaf_traverse_crit.restype = ctypes.c_int64
             L.ref_leaf_traverse_hash.argtypes = [ctypes.c_void_p, i32p, f32p, ctypes.c_int32,
                                                  ctypes.c_int32, ctypes.c_float, u64p]
             L.ref_leaf_traverse_hash.restype = ctypes.c_int64
@@ -206,6 +210,15 @@ def leaf_traverse(t, r, apl):
     keys = np.ascontiguousarray(t["keys"])
     return _pairs_call(lib().ref_leaf_traverse, keys.ctypes.data, _p(t["index"], ctypes.c_int32),
                        _p(t["position"], ctypes.c_float), t["leaves"], apl, np.float32(r))
+
+
+def simd_leaf_traverse(t, r, apl):
+    """simdneighbor_traverse (ext/NaiveSIMD.jl:610-704) on one thread: the
+    leafneighbor_traverse order with the criterion sqrt(d^2) < r."""
+    keys = np.ascontiguousarray(t["keys"])
+    return _pairs_call(lib().ref_leaf_traverse_crit, keys.ctypes.data,
+                       _p(t["index"], ctypes.c_int32), _p(t["position"], ctypes.c_float),
+                       t["leaves"], apl, np.float32(r), 1)
 
 
 def leaf_traverse_hash(t, r, apl):

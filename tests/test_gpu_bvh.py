@@ -130,6 +130,30 @@ def test_degenerate_inputs(nd, oracle):
     assert len(nd.leafbuild_traverse_bvh(y, nd.SpheresBVHSpecs(0.0, 64, 4))) == 0
 
 
+def test_simdbuild_traverse_bvh(nd, oracle):
+    # simdbuild_traverse_bvh: the leafbuild tree and order with sqrt(d^2) < r,
+    # bit for bit against the oracle (radii whose sqrt threshold lies one ulp
+    # under fl(r * r) and one where they coincide), and on the boundary pair
+    from test_oracle import boundary_positions
+    x = uniform(92, 8192)
+    for r in (0.05, 0.1, 0.3, 0.0731):
+        spec = nd.SpheresBVHSpecs(r, len(x), 4)
+        p = nd.simdbuild_traverse_bvh(x, spec)
+        t = oracle.tree(x, r, 4)
+        ri, rj, rd = oracle.simd_leaf_traverse(t, r, 4)
+        assert np.array_equal(p["i"], ri) and np.array_equal(p["j"], rj)
+        assert np.array_equal(p["d"].view(np.int32), rd.view(np.int32))
+        pu = nd.simdbuild_traverse_bvh(x, spec, mode=nd.ND_PAIRS_UNORDERED)
+        assert np.array_equal(canon(pu["i"], pu["j"], pu["d"]), canon(ri, rj, rd))
+    xb = boundary_positions()
+    spec = nd.SpheresBVHSpecs(0.1, len(xb), 4)
+    s0 = {tuple(r) for r in canon(*(nd.leafbuild_traverse_bvh(xb, spec)[k] for k in "ijd"))}
+    s1 = {tuple(r) for r in canon(*(nd.simdbuild_traverse_bvh(xb, spec)[k] for k in "ijd"))}
+    assert len(s0 - s1) == 1 and not (s1 - s0)
+    with pytest.raises(nd.SpecError):
+        nd.simdbuild_traverse_bvh(x, nd.SpheresBVHSpecs(0.05, len(x), 2))
+
+
 def test_errors(nd):
     x = uniform(1, 64)
     spec = nd.SpheresBVHSpecs(0.1, 64, 4)

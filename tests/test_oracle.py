@@ -122,6 +122,38 @@ def test_sqrt_criterion_disagreement_is_boundary_only(oracle):
         assert abs(d - np.float32(0.1)) <= 4 * np.spacing(np.float32(0.1))
 
 
+# Two points whose Float32 squared distance is exactly 0.01f: inside r = 0.1
+# by d^2 < r^2 (fl(0.1f * 0.1f) = 0.010000001f) but not by sqrt(d^2) < r
+# (sqrtf(0.01f) rounds to 0.1f); the rest lie far from them.
+BOUNDARY_PAIR = np.array([[0.0, 0.0, 0.0], [0.060000002, 0.08, 0.0]], np.float32)
+
+
+def boundary_positions():
+    rest = np.random.default_rng(11).uniform(0.5, 1.0, (62, 3)).astype(np.float32)
+    return np.concatenate([BOUNDARY_PAIR, rest])
+
+
+def test_simd_traversal(oracle):
+    # simdneighbor_traverse: the leaf traversal with sqrt(d^2) < r -- its set
+    # equals brute force with that criterion; on the boundary pair it drops
+    # what leafneighbor_traverse keeps
+    x = uniform(91, 4096)
+    for r in (0.05, 0.1, 0.0731):
+        t = oracle.tree(x, r, 4)
+        assert np.array_equal(canon(*oracle.simd_leaf_traverse(t, r, 4)),
+                              canon(*oracle.brute_pairs(x, r, 1)))
+    xb = boundary_positions()
+    d2 = np.float32(np.float32(xb[1, 0] * xb[1, 0]) + np.float32(xb[1, 1] * xb[1, 1]))
+    assert d2 == np.float32(0.01) and d2 < np.float32(0.1) * np.float32(0.1)
+    assert not (np.sqrt(d2) < np.float32(0.1))
+    t = oracle.tree(xb, 0.1, 4)
+    s0 = {tuple(r) for r in canon(*oracle.leaf_traverse(t, 0.1, 4))}
+    s1 = {tuple(r) for r in canon(*oracle.simd_leaf_traverse(t, 0.1, 4))}
+    assert len(s0 - s1) == 1 and not (s1 - s0)
+    (i, j, _), = s0 - s1
+    assert {i, j} == {1, 2}
+
+
 def test_golden_vectors(oracle):
     for c in golden_cases():
         x = np.array(c["position"], np.float32)
