@@ -42,7 +42,8 @@ def _rel(a, b):
     return abs(a - b) / max(abs(b), 1e-30)
 
 
-@pytest.mark.parametrize("n,steps,charges", [(256, 100, False), (256, 100, True), (4096, 100, False)])
+@pytest.mark.parametrize("n,steps,charges", [(256, 100, False), (256, 100, True), (4096, 100, False),
+                                              (1000, 50, True)])
 def test_gradients_match_dual_oracle(nd, oracle, n, steps, charges):
     adj, c = _case(nd, oracle, n, steps, charges)
     rng = np.random.default_rng(11)

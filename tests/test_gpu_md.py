@@ -171,6 +171,25 @@ def test_md_union_searches_agree(nd, apl):
     assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
 
 
+@pytest.mark.parametrize("n,side", [(1500, 12.1), (78852, 45.6)])
+def test_md_partial_last_block(nd, oracle, n, side):
+    # atom counts that are not a multiple of the 256-atom block: the last
+    # block is partly empty (1,500: four threads per atom in the step kernel;
+    # 78,852: 309 blocks, one thread per atom) -- 30 steps against FP64
+    x0, v0, q = nd.synth.lj_system(0x4E440021, n, side, 0.8, charges=True)
+    eng = nd.MDEngine(_params(nd, side, coulomb=1.0, refit_check_every=3), x0, v0, q)
+    eng.run(30)
+    xg, vg, fg = eng.get()
+    d = eng.diagnostics()
+    eng.close()
+    assert d["skin_violations"] == 0
+    p = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(side,) * 3, dt=1e-3)
+    xr, vr, _ = oracle.md_run(p, x0, v0, q, steps=30)
+    assert np.abs(xg - xr).max() < 1e-5
+    f64, _, _ = oracle.forces(p, xg, q)
+    assert force_errors(fg, f64)[1] <= F_L2_TOL
+
+
 def test_md_neighbor_list_pair_set(nd, oracle):
     # The engine's list at a rebuild equals every pair with d^2 < r_list^2 on
     # the Float32 positions (full list: each pair twice).
