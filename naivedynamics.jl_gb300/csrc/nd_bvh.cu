@@ -817,13 +817,26 @@ __device__ __forceinline__ void warp_buf_flush(int2* bij, float* bd, int& nb,
     unsigned long long base = 0;
     if (lane == 0 && nb) base = atomicAdd(cursor, (unsigned long long)nb);
     base = __shfl_sync(0xffffffffu, base, 0);
-    for (int k = lane; k < nb; k += 32) {
-        const unsigned long long w = base + (unsigned long long)k;
-        if ((int64_t)w < cap) {
+    if ((int64_t)(base + (unsigned long long)nb) <= cap) {
+        // the whole run fits: 32-bit offsets from the run's first slot
+        int32_t* __restrict__ qi = pi + base;
+        int32_t* __restrict__ qj = pj + base;
+        float* __restrict__ qd = pd + base;
+        for (int k = lane; k < nb; k += 32) {
             const int2 ij = bij[k];
-            pi[w] = ij.x;
-            pj[w] = ij.y;
-            pd[w] = __fsqrt_rn(bd[k]);
+            qi[k] = ij.x;
+            qj[k] = ij.y;
+            qd[k] = __fsqrt_rn(bd[k]);
+        }
+    } else {
+        for (int k = lane; k < nb; k += 32) {
+            const unsigned long long w = base + (unsigned long long)k;
+            if ((int64_t)w < cap) {
+                const int2 ij = bij[k];
+                pi[w] = ij.x;
+                pj[w] = ij.y;
+                pd[w] = __fsqrt_rn(bd[k]);
+            }
         }
     }
     __syncwarp();
