@@ -260,6 +260,28 @@ nd_status nd_forces_pairs(nd_ctx* ctx, const nd_md_params* p, int32_t n, const d
                           float* force, double* energy);
 
 /*
+ * Bug-compatible force calls: what src/Forces.jl computes at HEAD, for scripts
+ * that depend on it (the calls above compute the intended physics).  pi, pj, pd:
+ * the pair list (1-based indices, Float32 distances) in the order the caller
+ * passes it -- the results depend on it; force: N x 3 Float32 out, zeroed
+ * first, the three components of an atom always equal.
+ *   force_lennardjones!(force, pairslist, position) (Forces.jl:6-45): for each
+ *     pair, force[i] .+= (24 eps / d) ((2 sigma / d)^12 - (sigma / d)^6) with
+ *     the hard-coded eps = -1f10 and sigma = 0.0001, nothing on force[j];
+ *   force_coulomb!(force, pairslist, charge) (Forces.jl:46-66): for each pair,
+ *     force[i] .+= q_i q_j / d^2, then force[j] .-= force[i] (the running
+ *     total), an order-dependent recurrence run on one GPU thread.
+ * Arithmetic follows Julia's promotion of the reference's types (Float32
+ * accumulators, distances and charges; Float64 sigma powers).
+ */
+nd_status nd_compat_force_lennardjones(nd_ctx* ctx, int32_t n, const int32_t* pi,
+                                       const int32_t* pj, const float* pd, int64_t npairs,
+                                       float* force);
+nd_status nd_compat_force_coulomb(nd_ctx* ctx, int32_t n, const int32_t* pi, const int32_t* pj,
+                                  const float* pd, int64_t npairs, const float* charge,
+                                  float* force);
+
+/*
  * Forces and energy of a configuration with the library's own neighbour search
  * (spatial-order leaf BVH at radius p->cutoff): the fused hot-path force kernel
  * run once.  Same physics and outputs as nd_forces_pairs.

@@ -22,7 +22,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libnaivegpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["nd_bvh.cu", "nd_md.cu", "nd_adjoint.cu", "nd_capi.cu", "nd_noalloc.cu"]
+SOURCES = ["nd_bvh.cu", "nd_md.cu", "nd_adjoint.cu", "nd_capi.cu", "nd_noalloc.cu", "nd_compat.cu"]
 
 
 def nvcc() -> str:

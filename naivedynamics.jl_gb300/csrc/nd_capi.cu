@@ -463,6 +463,24 @@ nd_status nd_forces_pairs(nd_ctx* h, const nd_md_params* p, int32_t n, const dou
     return nd::forces_pairs(c, p, n, x, q, pi, pj, npairs, force, energy);
 }
 
+nd_status nd_compat_force_lennardjones(nd_ctx* h, int32_t n, const int32_t* pi,
+                                       const int32_t* pj, const float* pd, int64_t npairs,
+                                       float* force) {
+    if (!h) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    return nd::compat_forces(&h->c, 0, n, pi, pj, pd, npairs, nullptr, force);
+}
+
+nd_status nd_compat_force_coulomb(nd_ctx* h, int32_t n, const int32_t* pi, const int32_t* pj,
+                                  const float* pd, int64_t npairs, const float* charge,
+                                  float* force) {
+    if (!h) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    return nd::compat_forces(&h->c, 1, n, pi, pj, pd, npairs, charge, force);
+}
+
 nd_status nd_forces(nd_ctx* h, const nd_md_params* p, int32_t n, const double* x,
                     const double* q, float* force, double* energy) {
     if (!h || !p || !x || n <= 0) return ND_ERR_ARG;

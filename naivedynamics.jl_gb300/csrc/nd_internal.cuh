@@ -229,6 +229,10 @@ nd_status forces_pairs(Ctx* c, const nd_md_params* p, int32_t n, const double* x
 // Two-phase ordered emission: count (computes per-query offsets, syncs) then write.
 // Squared-distance threshold of a pair criterion (ND_CRIT_*).
 float pair_threshold(float r, int32_t criterion);
+// Bug-compatible force_lennardjones! (kind 0) / force_coulomb! (kind 1) over a
+// host pair list in list order; force: host N x 3 Float32.
+nd_status compat_forces(Ctx* c, int kind, int32_t n, const int32_t* pi, const int32_t* pj,
+                        const float* pd, int64_t np, const float* q, float* force);
 nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int64_t* total);
 nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int32_t* pi, int32_t* pj,
                       float* pd);

@@ -136,6 +136,8 @@ SIGNATURES = {
                                _vp, ctypes.POINTER(_d)]),
     "nd_forces": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp,
                          ctypes.POINTER(_d)]),
+    "nd_compat_force_lennardjones": (_i32, [_vp, _i32, _vp, _vp, _vp, _i64, _vp]),
+    "nd_compat_force_coulomb": (_i32, [_vp, _i32, _vp, _vp, _vp, _i64, _vp, _vp]),
     "nd_md_create": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _pp]),
     "nd_md_create_dev": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _pp]),
     "nd_md_destroy": (_i32, [_vp]),

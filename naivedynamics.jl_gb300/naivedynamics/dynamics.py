@@ -25,6 +25,7 @@ from ._lib import (MDParams, ND_ORDER_SPATIAL, ND_UNION_BLOCKS, ND_UNION_TREE,
                    default_context, ptr)
 
 __all__ = ["ForceField", "md_params", "force_lennardjones_", "force_coulomb_", "sum_forces_",
+           "force_lennardjones_compat_", "force_coulomb_compat_",
            "forces", "SimSpec", "GenericObjectCollection", "GenericRandomCollector", "simulate_",
            "MDEngine", "Ensemble", "systems_table", "autotune"]
 
@@ -102,6 +103,48 @@ def force_coulomb_(force, pairslist, charge, position, k=1.0, cutoff=2.5, ctx=No
     reference signature it needs the positions for the direction."""
     p = md_params(sigma=1.0, epsilon=0.0, coulomb_k=k, cutoff=cutoff)
     return _pair_forces(force, pairslist, position, charge, p, ctx)[1]
+
+
+def _compat_pairs(pairslist):
+    if isinstance(pairslist, np.ndarray) and pairslist.dtype.names:
+        i, j, d = pairslist["i"], pairslist["j"], pairslist["d"]
+    elif isinstance(pairslist, dict):
+        i, j, d = pairslist["i"], pairslist["j"], pairslist["d"]
+    else:
+        i, j, d = pairslist
+    return (np.ascontiguousarray(i, np.int32), np.ascontiguousarray(j, np.int32),
+            np.ascontiguousarray(d, np.float32))
+
+
+def force_lennardjones_compat_(force, pairslist, position=None, ctx=None):
+    """force_lennardjones! as the reference computes it (Forces.jl:6-45):
+    force[i] .+= (24 eps / d) ((2 sigma / d)^12 - (sigma / d)^6) for every pair
+    in list order with its hard-coded eps = -1f10, sigma = 0.0001, the same
+    scalar on all three components and nothing on force[j].  force (N x 3
+    Float32) is overwritten; position is not used (as in the reference)."""
+    ctx = ctx or default_context()
+    i, j, d = _compat_pairs(pairslist)
+    out = np.zeros((np.asarray(force).shape[0], 3), np.float32)
+    ctx.check(_lib.lib().nd_compat_force_lennardjones(ctx.handle, out.shape[0], ptr(i), ptr(j),
+                                                      ptr(d), len(i), ptr(out)),
+              "nd_compat_force_lennardjones")
+    force[...] = out
+    return force
+
+
+def force_coulomb_compat_(force, pairslist, charge, ctx=None):
+    """force_coulomb! as the reference computes it (Forces.jl:46-66): for
+    every pair in list order force[i] .+= q_i q_j / d^2, then force[j] .-=
+    force[i] (its running total).  force (N x 3 Float32) is overwritten."""
+    ctx = ctx or default_context()
+    i, j, d = _compat_pairs(pairslist)
+    q = np.ascontiguousarray(charge, np.float32)
+    out = np.zeros((np.asarray(force).shape[0], 3), np.float32)
+    ctx.check(_lib.lib().nd_compat_force_coulomb(ctx.handle, out.shape[0], ptr(i), ptr(j),
+                                                 ptr(d), len(i), ptr(q), ptr(out)),
+              "nd_compat_force_coulomb")
+    force[...] = out
+    return force
 
 
 def sum_forces_(force, force1, force2):

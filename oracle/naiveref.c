@@ -494,6 +494,59 @@ int64_t ref_brute_pairs(const float* xyz, int32_t n, float r, int32_t criterion,
     return count;
 }
 
+/* ------------------------------------------------- bug-compatible force calls */
+
+/* Julia's Base.Math.pow_body(x::Float64, n::Integer), n >= 4: power by
+ * squaring carrying the low part of every product (two_mul), muladd fused. */
+static double jl_pow_int(double x, int n) {
+    double y = 1.0, xnlo = 0.0, ynlo = 0.0;
+    while (n > 1) {
+        if (n & 1) {
+            double err = fma(y, xnlo, x * ynlo);
+            double yy = x * y;
+            ynlo = fma(x, y, -yy) + err;
+            y = yy;
+        }
+        double err = x * 2.0 * xnlo;
+        double xx = x * x;
+        xnlo = fma(x, x, -xx) + err;
+        x = xx;
+        n >>= 1;
+    }
+    double err = fma(y, xnlo, x * ynlo);
+    return (isfinite(x) && isfinite(err)) ? fma(x, y, err) : x * y;
+}
+
+/* force_lennardjones! (Forces.jl:6-45) over the list in order. */
+void ref_compat_force_lj(int32_t n, const int32_t* pi, const int32_t* pj, const float* pd,
+                         int64_t np, float* force) {
+    const float eps = -1e10f;
+    const double sigma = 0.0001;
+    memset(force, 0, sizeof(float) * 3 * (size_t)n);
+    for (int64_t p = 0; p < np; ++p) {
+        const int32_t i = pi[p] - 1;
+        const float d = pd[p];
+        const float a = (24.0f * eps) / d;
+        const double b = jl_pow_int(2.0 * sigma / (double)d, 12);
+        const double c = jl_pow_int(sigma / (double)d, 6);
+        const double x = (double)a * (b - c);
+        for (int k = 0; k < 3; ++k) force[3 * i + k] = (float)((double)force[3 * i + k] + x);
+    }
+}
+
+/* force_coulomb! (Forces.jl:46-66) over the list in order. */
+void ref_compat_force_coulomb(int32_t n, const int32_t* pi, const int32_t* pj, const float* pd,
+                              int64_t np, const float* q, float* force) {
+    memset(force, 0, sizeof(float) * 3 * (size_t)n);
+    for (int64_t p = 0; p < np; ++p) {
+        const int32_t i = pi[p] - 1, j = pj[p] - 1;
+        const float d = pd[p];
+        const float add = (1.0f * q[i]) * q[j] / (d * d);
+        for (int k = 0; k < 3; ++k) force[3 * i + k] += add;
+        for (int k = 0; k < 3; ++k) force[3 * j + k] -= force[3 * i + k];
+    }
+}
+
 /* --------------------------------------------------------------- FP64 physics */
 
 static inline void pair_force(const ref_md_params* p, const double* xi, const double* xj,

@@ -105,6 +105,13 @@ int64_t ref_atom_traverse(const ref_key* keys, const int32_t* idx_sorted, const 
  * criterion 1: sqrt(d^2) < r (AllToAll.jl:86, ext/NaiveSIMD.jl:529,589).
  * Pairs (i, j) with i < j, 1-based, in lexicographic order.
  */
+/* Bug-compatible force_lennardjones! / force_coulomb! (Forces.jl:6-66): the
+ * list in order, Float32 accumulators, force N x 3 (zeroed first). */
+void ref_compat_force_lj(int32_t n, const int32_t* pi, const int32_t* pj, const float* pd,
+                         int64_t np, float* force);
+void ref_compat_force_coulomb(int32_t n, const int32_t* pi, const int32_t* pj, const float* pd,
+                              int64_t np, const float* q, float* force);
+
 int64_t ref_brute_pairs(const float* xyz, int32_t n, float r, int32_t criterion, int32_t* pi,
                         int32_t* pj, float* pd, int64_t cap);
 

@@ -96,6 +96,12 @@ def lib():
             L.ref_leaf_traverse_hash.argtypes = [ctypes.c_void_p, i32p, f32p, ctypes.c_int32,
                                                  ctypes.c_int32, ctypes.c_float, u64p]
             L.ref_leaf_traverse_hash.restype = ctypes.c_int64
+            L.ref_compat_force_lj.argtypes = [ctypes.c_int32, i32p, i32p, f32p, ctypes.c_int64,
+                                              f32p]
+            L.ref_compat_force_lj.restype = None
+            L.ref_compat_force_coulomb.argtypes = [ctypes.c_int32, i32p, i32p, f32p,
+                                                   ctypes.c_int64, f32p, f32p]
+            L.ref_compat_force_coulomb.restype = None
             L.ref_brute_pairs.argtypes = [f32p, ctypes.c_int32, ctypes.c_float, ctypes.c_int32,
                                           i32p, i32p, f32p, ctypes.c_int64]
             L.ref_brute_pairs.restype = ctypes.c_int64
@@ -210,6 +216,25 @@ def leaf_traverse(t, r, apl):
     keys = np.ascontiguousarray(t["keys"])
     return _pairs_call(lib().ref_leaf_traverse, keys.ctypes.data, _p(t["index"], ctypes.c_int32),
                        _p(t["position"], ctypes.c_float), t["leaves"], apl, np.float32(r))
+
+
+def compat_forces(kind, n, pairs, q=None):
+    """The reference's force_lennardjones! (kind 'lj') or force_coulomb!
+    (kind 'coulomb') as it computes them at HEAD (Forces.jl:6-66), over the
+    pair list (i, j, d) in order.  Returns N x 3 Float32."""
+    i = np.ascontiguousarray(pairs[0], np.int32)
+    j = np.ascontiguousarray(pairs[1], np.int32)
+    d = np.ascontiguousarray(pairs[2], np.float32)
+    out = np.zeros((n, 3), np.float32)
+    if kind == "lj":
+        lib().ref_compat_force_lj(n, _p(i, ctypes.c_int32), _p(j, ctypes.c_int32),
+                                  _p(d, ctypes.c_float), len(i), _p(out, ctypes.c_float))
+    else:
+        qq = np.ascontiguousarray(q, np.float32)
+        lib().ref_compat_force_coulomb(n, _p(i, ctypes.c_int32), _p(j, ctypes.c_int32),
+                                       _p(d, ctypes.c_float), len(i), _p(qq, ctypes.c_float),
+                                       _p(out, ctypes.c_float))
+    return out
 
 
 def simd_leaf_traverse(t, r, apl):

@@ -190,6 +190,30 @@ def test_md_partial_last_block(nd, oracle, n, side):
     assert force_errors(fg, f64)[1] <= F_L2_TOL
 
 
+def test_compat_force_calls(nd, oracle):
+    # force_lennardjones! / force_coulomb! as the reference computes them at
+    # HEAD, over the reference-order pair list of 4,096 points in the unit
+    # cube: bit for bit against the oracle's restatement (the Coulomb
+    # recurrence in list order, the LJ terms per atom in list order)
+    x = nd.synth.uniform_positions(0x4E440031, 4096, 1.0)
+    spec = nd.SpheresBVHSpecs(0.05, len(x), 4)
+    pairs = nd.leafbuild_traverse_bvh(x, spec)
+    q = np.where(np.arange(len(x)) % 2 == 0, 1.0, -1.0).astype(np.float32)
+    lst = (pairs["i"], pairs["j"], pairs["d"])
+    flj = nd.force_lennardjones_compat_(np.zeros((len(x), 3), np.float32), pairs, x)
+    fc = nd.force_coulomb_compat_(np.zeros((len(x), 3), np.float32), pairs, q)
+    assert np.array_equal(flj.view(np.int32), oracle.compat_forces("lj", len(x), lst).view(np.int32))
+    assert np.array_equal(fc.view(np.int32),
+                          oracle.compat_forces("coulomb", len(x), lst, q).view(np.int32))
+    assert np.abs(flj).max() > 0 and np.abs(fc).max() > 0
+    f = nd.sum_forces_(np.zeros_like(flj), flj, fc)
+    assert np.array_equal(f, flj + fc)
+    with pytest.raises(nd.NDError):
+        bad = (pairs["i"].copy(), pairs["j"], pairs["d"])
+        bad[0][0] = len(x) + 1
+        nd.force_coulomb_compat_(np.zeros((len(x), 3), np.float32), bad, q)
+
+
 def test_md_neighbor_list_pair_set(nd, oracle):
     # The engine's list at a rebuild equals every pair with d^2 < r_list^2 on
     # the Float32 positions (full list: each pair twice).

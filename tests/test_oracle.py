@@ -154,6 +154,37 @@ def test_simd_traversal(oracle):
     assert {i, j} == {1, 2}
 
 
+def test_compat_forces_oracle(oracle):
+    # force_coulomb! at HEAD: force[i] .+= q_i q_j / d^2, then force[j] .-=
+    # force[i] (the running total) -- by hand for a three-pair list
+    f32 = np.float32
+    i = np.array([1, 1, 2], np.int32)
+    j = np.array([2, 3, 3], np.int32)
+    d = np.array([0.5, 0.25, 0.75], np.float32)
+    q = np.array([1.0, -1.0, 2.0], np.float32)
+    F = np.zeros(3, np.float32)
+    for a, b, dd in zip(i - 1, j - 1, d):
+        F[a] = f32(F[a] + f32(f32(q[a] * q[b]) / f32(dd * dd)))
+        F[b] = f32(F[b] - F[a])
+    out = oracle.compat_forces("coulomb", 3, (i, j, d), q)
+    assert np.array_equal(out, np.repeat(F[:, None], 3, axis=1))
+    # force_lennardjones! at HEAD: only force[i] receives the pair term, the
+    # same on all three components, and it does not depend on the positions
+    lj = oracle.compat_forces("lj", 3, (i, j, d))
+    assert np.all(lj[2] == 0) and np.all(lj[:, 0] == lj[:, 1]) and np.all(lj[:, 1] == lj[:, 2])
+    # each atom's additions in list order: swapping pairs of different atoms
+    # changes nothing
+    lj2 = oracle.compat_forces("lj", 3, (i[[2, 0, 1]], j[[2, 0, 1]], d[[2, 0, 1]]))
+    assert np.array_equal(lj, lj2)
+    # magnitude check of one term against float64 math (the power by squaring
+    # is within an ulp of the exact power)
+    t = (np.float64(f32(f32(24.0) * f32(-1e10)) / f32(0.5))
+         * ((2e-4 / 0.5) ** 12 - (1e-4 / 0.5) ** 6))
+    one = oracle.compat_forces("lj", 2, (np.array([1], np.int32), np.array([2], np.int32),
+                                         np.array([0.5], np.float32)))
+    assert one[0, 0] == np.float32(t) and np.all(one[1] == 0)
+
+
 def test_golden_vectors(oracle):
     for c in golden_cases():
         x = np.array(c["position"], np.float32)
