@@ -282,6 +282,40 @@ nd_status nd_compat_force_coulomb(nd_ctx* ctx, int32_t n, const int32_t* pi, con
                                   float* force);
 
 /*
+ * simulate!(sys, spec, clct) as written (src/Simulator.jl:154-256) for a
+ * GenericObjectCollection{Float32}, a GenericRandomCollector{Float32} and a
+ * SimSpec{Int64, Float32} (integer stepwidth: every operation stays in
+ * Float32).  Each step, over the all-pairs list of unique_pairs
+ * (src/Neighbors/AllToAll.jl:65-80, distances from the previous step):
+ *   F    = force_lennardjones!(threshold_pairs(list, 0.01)) + force_coulomb!(list)
+ *   x   += v dt + (F/m) dt^2 / 2
+ *   v   += (F/m + Fnext/m) dt / 2        Fnext: the previous step's all-pairs forces
+ *   Fnext = force_lennardjones!(list) + force_coulomb!(list);  boundary_reflect!
+ *   update_pairslist!;  every 10th step rescale_velocity!;  log the positions
+ * with the compat force formulas above.  position, velocity, force: N x 3
+ * Float32, in/out (force in: the first step's Fnext).  mass, charge: N.
+ * poslog: NULL or (duration + 1) x N x 3 Float32 out: frame k the positions
+ * after step k, frame 0 the final positions (the reference's poslog[1] is
+ * sys.position itself).  1 <= n <= 65536 (the list holds n(n-1)/2 pairs).
+ * A negative rescale_velocity! radicand (Julia's DomainError) stops the run
+ * after that step's pair update with ND_ERR_ARG; the state is then the one
+ * the reference holds when it throws.
+ */
+typedef struct nd_compat_sim {
+    float min_dim[3];          /* GenericRandomCollector minDim */
+    float max_dim[3];          /* GenericRandomCollector maxDim */
+    float temperature;         /* GenericRandomCollector temperature (Tf) */
+    int64_t objectnumber;      /* GenericRandomCollector objectnumber */
+    int64_t stepwidth;         /* SimSpec stepwidth (Int64) */
+    int64_t duration;          /* SimSpec duration (steps) */
+    float velocity_dampening;  /* SimSpec velocityDampening (gamma) */
+} nd_compat_sim;
+
+nd_status nd_compat_simulate(nd_ctx* ctx, const nd_compat_sim* spec, int32_t n, float* position,
+                             float* velocity, float* force, const float* mass,
+                             const float* charge, float* poslog);
+
+/*
  * Forces and energy of a configuration with the library's own neighbour search
  * (spatial-order leaf BVH at radius p->cutoff): the fused hot-path force kernel
  * run once.  Same physics and outputs as nd_forces_pairs.

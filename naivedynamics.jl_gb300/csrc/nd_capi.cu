@@ -306,7 +306,7 @@ nd_status nd_ctx_destroy(nd_ctx* h) {
     nd::DevBuf* bufs[] = {&c->xyz, &c->codes, &c->codes_alt, &c->perm, &c->perm_alt, &c->pos4,
                           &c->idx, &c->keys, &c->store, &c->hist, &c->counts, &c->offsets,
                           &c->partial, &c->pairs_i, &c->pairs_j, &c->pairs_d, &c->misc, &c->hash,
-                          &c->leafpairs, &c->ranges, &c->tasks};
+                          &c->leafpairs, &c->ranges, &c->tasks, &c->compat};
     for (nd::DevBuf* b : bufs) nd::free_buf(*b);
     if (c->d_err) cudaFree(c->d_err);
     if (c->h_err) cudaFreeHost(c->h_err);
@@ -479,6 +479,15 @@ nd_status nd_compat_force_coulomb(nd_ctx* h, int32_t n, const int32_t* pi, const
     nd_status st = nd::set_device(&h->c);
     if (st) return st;
     return nd::compat_forces(&h->c, 1, n, pi, pj, pd, npairs, charge, force);
+}
+
+nd_status nd_compat_simulate(nd_ctx* h, const nd_compat_sim* spec, int32_t n, float* position,
+                             float* velocity, float* force, const float* mass,
+                             const float* charge, float* poslog) {
+    if (!h) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    return nd::compat_simulate(&h->c, spec, n, position, velocity, force, mass, charge, poslog);
 }
 
 nd_status nd_forces(nd_ctx* h, const nd_md_params* p, int32_t n, const double* x,

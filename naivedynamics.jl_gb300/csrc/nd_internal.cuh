@@ -136,7 +136,7 @@ struct Ctx {
     std::string last_error;
     // scratch buffers of the neighbour-search pipeline, grown on demand
     DevBuf xyz, codes, codes_alt, perm, perm_alt, pos4, idx, keys, store, hist, counts, offsets,
-        partial, pairs_i, pairs_j, pairs_d, misc, hash, leafpairs, ranges, tasks;
+        partial, pairs_i, pairs_j, pairs_d, misc, hash, leafpairs, ranges, tasks, compat;
     struct MDEngine* sim_cache = nullptr;  // engine re-used by nd_simulate
     bool no_alloc = false;                 // buffers are fixed slices: never grow them
 };
@@ -233,6 +233,9 @@ float pair_threshold(float r, int32_t criterion);
 // host pair list in list order; force: host N x 3 Float32.
 nd_status compat_forces(Ctx* c, int kind, int32_t n, const int32_t* pi, const int32_t* pj,
                         const float* pd, int64_t np, const float* q, float* force);
+// simulate! as written over the all-pairs list (host arrays in and out).
+nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x, float* v,
+                          float* force, const float* mass, const float* q, float* poslog);
 nd_status count_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int64_t* total);
 nd_status write_pairs(Ctx* c, const TreeBuffers& t, float r2, int kind, int32_t* pi, int32_t* pj,
                       float* pd);

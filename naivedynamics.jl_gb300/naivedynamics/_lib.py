@@ -75,6 +75,14 @@ class MDParams(ctypes.Structure):
                 ("union_search", ctypes.c_int32), ("refit_check_every", ctypes.c_int32)]
 
 
+class CompatSim(ctypes.Structure):
+    """nd_compat_sim: the collector and SimSpec fields simulate! reads."""
+    _fields_ = [("min_dim", ctypes.c_float * 3), ("max_dim", ctypes.c_float * 3),
+                ("temperature", ctypes.c_float), ("objectnumber", ctypes.c_int64),
+                ("stepwidth", ctypes.c_int64), ("duration", ctypes.c_int64),
+                ("velocity_dampening", ctypes.c_float)]
+
+
 class MDDiag(ctypes.Structure):
     """nd_md_diag."""
     _fields_ = [("skin_violations", ctypes.c_int64), ("max_neighbors", ctypes.c_int32),
@@ -138,6 +146,8 @@ SIGNATURES = {
                          ctypes.POINTER(_d)]),
     "nd_compat_force_lennardjones": (_i32, [_vp, _i32, _vp, _vp, _vp, _i64, _vp]),
     "nd_compat_force_coulomb": (_i32, [_vp, _i32, _vp, _vp, _vp, _i64, _vp, _vp]),
+    "nd_compat_simulate": (_i32, [_vp, ctypes.POINTER(CompatSim), _i32, _vp, _vp, _vp, _vp, _vp,
+                                  _vp]),
     "nd_md_create": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _pp]),
     "nd_md_create_dev": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _pp]),
     "nd_md_destroy": (_i32, [_vp]),

@@ -262,6 +262,46 @@ def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCo
     return sys
 
 
+def simulate_compat_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCollector,
+                     log: bool = True, ctx=None):
+    """simulate!(sys, spec, clct) as the reference computes it
+    (Simulator.jl:154-256): the all-pairs list of unique_pairs, the
+    bug-compatible force calls (force_lennardjones! on the pairs closer than
+    0.01, then on all pairs; force_coulomb! on all pairs), x += v dt +
+    a(t) dt^2 / 2, v += (a(t) + a(t - dt)) dt / 2, boundary_reflect!, and
+    rescale_velocity! every 10 steps towards clct.temperature with gamma =
+    spec.vDamp -- in Float32 with an integer spec.stepwidth, as the
+    reference's SimSpec{Int64, Float32} holds it.
+
+    Updates sys.position / sys.velocity / sys.force (Float64 arrays holding
+    Float32 values) and returns the poslog, (duration + 1) x N x 3 Float32:
+    element 0 is the final positions (the reference's poslog[1] is
+    sys.position itself), element k the positions after step k.  Raises
+    NDError where the reference raises DomainError (a negative
+    rescale_velocity! radicand); sys then holds the state at that point."""
+    ctx = ctx or default_context()
+    if int(spec.stepwidth) != spec.stepwidth:
+        raise ValueError("SimSpec{Int64, Float32} holds an integer stepwidth")
+    n = sys.position.shape[0]
+    x = np.ascontiguousarray(sys.position, np.float32).copy()
+    v = np.ascontiguousarray(sys.velocity, np.float32).copy()
+    f = np.ascontiguousarray(sys.force, np.float32).reshape(n, 3).copy()
+    m = np.ones(n, np.float32) if sys.mass is None else np.ascontiguousarray(sys.mass, np.float32)
+    q = (np.zeros(n, np.float32) if sys.charge is None
+         else np.ascontiguousarray(sys.charge, np.float32))
+    cs = _lib.CompatSim((ctypes.c_float * 3)(*clct.minDim), (ctypes.c_float * 3)(*clct.maxDim),
+                        clct.temperature, int(clct.objectnumber), int(spec.stepwidth),
+                        int(spec.duration), spec.vDamp)
+    poslog = np.zeros((int(spec.duration) + 1, n, 3), np.float32) if log else None
+    st = _lib.lib().nd_compat_simulate(ctx.handle, ctypes.byref(cs), n, ptr(x), ptr(v), ptr(f),
+                                       ptr(m), ptr(q), ptr(poslog))
+    sys.position[...] = x
+    sys.velocity[...] = v
+    sys.force = f
+    ctx.check(st, "nd_compat_simulate")
+    return poslog
+
+
 class MDEngine:
     """Device-resident simulation state (nd_md_*).
 

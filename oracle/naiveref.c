@@ -547,6 +547,117 @@ void ref_compat_force_coulomb(int32_t n, const int32_t* pi, const int32_t* pj, c
     }
 }
 
+/* update_pairslist! (AllToAll.jl:7-62): d = sqrt(sum((a[i] .- a[j]) .^ 2)). */
+static void compat_update_pairs(const float* x, const int32_t* pi, const int32_t* pj, float* pd,
+                                int64_t np) {
+    for (int64_t p = 0; p < np; ++p) {
+        const float* a = &x[3 * (pi[p] - 1)];
+        const float* b = &x[3 * (pj[p] - 1)];
+        const float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+        pd[p] = sqrtf(dx * dx + dy * dy + dz * dz);
+    }
+}
+
+/* rescale_velocity! (Simulator.jl:119-144); 1 on DomainError. */
+static int compat_rescale(float* v, float Tf, float gamma, const float* mass, int32_t n,
+                          int64_t objectcount) {
+    float Ti = 0.0f;
+    const float kb = 1.0f;
+    const float objects = (float)objectcount;
+    for (int32_t k = 0; k < n; ++k) {
+        const float* w = &v[3 * k];
+        /* (v1^2 + v2^2 + v3^2) ^ 0.5 promoted to Float64, stored as Float32 */
+        const float s = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+        const float vv = (float)sqrt((double)s);
+        Ti += (2.0f / (3.0f * objects * kb)) * vv * mass[k] / 2.0f;
+    }
+    const float r = 1.0f + gamma * (Tf / Ti - 1.0f);
+    if (r < 0.0f) return 1;
+    const double beta = sqrt((double)r);
+    for (int64_t e = 0; e < 3 * (int64_t)n; ++e) v[e] = (float)((double)v[e] * beta);
+    return 0;
+}
+
+int ref_compat_simulate(const ref_compat_sim* spec, int32_t n, float* x, float* v, float* force,
+                        const float* mass, const float* q, float* poslog) {
+    if (n < 1) return 0;
+    const size_t n3 = 3 * (size_t)n;
+    const int64_t np = (int64_t)n * (n - 1) / 2;
+    int32_t* pi = (int32_t*)malloc(sizeof(int32_t) * (size_t)(np + 1));
+    int32_t* pj = (int32_t*)malloc(sizeof(int32_t) * (size_t)(np + 1));
+    float* pd = (float*)malloc(sizeof(float) * (size_t)(np + 1));
+    int32_t* ti = (int32_t*)malloc(sizeof(int32_t) * (size_t)(np + 1));
+    int32_t* tj = (int32_t*)malloc(sizeof(int32_t) * (size_t)(np + 1));
+    float* td = (float*)malloc(sizeof(float) * (size_t)(np + 1));
+    float* fnext = (float*)malloc(sizeof(float) * n3);
+    float* flj = (float*)malloc(sizeof(float) * n3);
+    float* fc = (float*)malloc(sizeof(float) * n3);
+    float* at = (float*)malloc(sizeof(float) * n3);
+    float* atdt = (float*)malloc(sizeof(float) * n3);
+    int status = 0;
+    const float dt = (float)spec->stepwidth;
+    const float dt2 = (float)(int64_t)((uint64_t)spec->stepwidth * (uint64_t)spec->stepwidth);
+    memcpy(fnext, force, sizeof(float) * n3); /* force_nextstep = deepcopy(sys.force) */
+    /* pairslist = unique_pairs(sys.position) (AllToAll.jl:65-80) */
+    int64_t p = 0;
+    for (int32_t i = 1; i <= n - 1; ++i)
+        for (int32_t j = i + 1; j <= n; ++j) {
+            pi[p] = i;
+            pj[p] = j;
+            ++p;
+        }
+    compat_update_pairs(x, pi, pj, pd, np);
+    for (int64_t step = 1; step <= spec->duration; ++step) {
+        /* LJ_pairs = threshold_pairs(pairslist, 0.01) */
+        int64_t nt = 0;
+        for (int64_t k = 0; k < np; ++k)
+            if (pd[k] < 0.01f) {
+                ti[nt] = pi[k];
+                tj[nt] = pj[k];
+                td[nt] = pd[k];
+                ++nt;
+            }
+        ref_compat_force_lj(n, ti, tj, td, nt, flj);
+        ref_compat_force_coulomb(n, pi, pj, pd, np, q, fc);
+        for (size_t e = 0; e < n3; ++e) force[e] = flj[e] + fc[e]; /* sum_forces! */
+        for (size_t e = 0; e < n3; ++e) at[e] = force[e] / mass[e / 3];
+        for (size_t e = 0; e < n3; ++e) x[e] += v[e] * dt + ((at[e] * dt2) / 2.0f);
+        for (size_t e = 0; e < n3; ++e) atdt[e] = fnext[e] / mass[e / 3];
+        memcpy(fnext, force, sizeof(float) * n3);
+        ref_compat_force_lj(n, pi, pj, pd, np, flj);
+        ref_compat_force_coulomb(n, pi, pj, pd, np, q, fc);
+        for (size_t e = 0; e < n3; ++e) fnext[e] = flj[e] + fc[e];
+        for (size_t e = 0; e < n3; ++e) v[e] += ((at[e] + atdt[e]) * dt) / 2.0f;
+        /* boundary_reflect! (Simulator.jl:81-111) */
+        for (int32_t i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) {
+                float* xk = &x[3 * i + k];
+                float* vk = &v[3 * i + k];
+                if (spec->min_dim[k] > *xk) {
+                    *vk *= -1.0f;
+                    *xk = spec->min_dim[k];
+                }
+                if (spec->max_dim[k] < *xk) {
+                    *vk *= -1.0f;
+                    *xk = spec->max_dim[k];
+                }
+            }
+        memcpy(force, fnext, sizeof(float) * n3);
+        compat_update_pairs(x, pi, pj, pd, np);
+        if (step % 10 == 0 &&
+            compat_rescale(v, spec->temperature, spec->velocity_dampening, mass, n,
+                           spec->objectnumber)) {
+            status = 1;
+            break;
+        }
+        if (poslog) memcpy(poslog + step * (int64_t)n3, x, sizeof(float) * n3);
+    }
+    if (poslog && status == 0) memcpy(poslog, x, sizeof(float) * n3);
+    free(pi), free(pj), free(pd), free(ti), free(tj), free(td);
+    free(fnext), free(flj), free(fc), free(at), free(atdt);
+    return status;
+}
+
 /* --------------------------------------------------------------- FP64 physics */
 
 static inline void pair_force(const ref_md_params* p, const double* xi, const double* xj,

@@ -112,6 +112,22 @@ void ref_compat_force_lj(int32_t n, const int32_t* pi, const int32_t* pj, const 
 void ref_compat_force_coulomb(int32_t n, const int32_t* pi, const int32_t* pj, const float* pd,
                               int64_t np, const float* q, float* force);
 
+/* simulate! as written (Simulator.jl:154-256), Float32 state, Int64
+ * stepwidth; the layout of the spec matches the library's nd_compat_sim.
+ * poslog: NULL or (duration + 1) x n x 3.  Returns 0, or 1 when
+ * rescale_velocity! raises Julia's DomainError (state as at the throw). */
+typedef struct ref_compat_sim {
+    float min_dim[3];
+    float max_dim[3];
+    float temperature;
+    int64_t objectnumber;
+    int64_t stepwidth;
+    int64_t duration;
+    float velocity_dampening;
+} ref_compat_sim;
+int ref_compat_simulate(const ref_compat_sim* spec, int32_t n, float* x, float* v, float* force,
+                        const float* mass, const float* q, float* poslog);
+
 int64_t ref_brute_pairs(const float* xyz, int32_t n, float r, int32_t criterion, int32_t* pi,
                         int32_t* pj, float* pd, int64_t cap);
 

@@ -36,6 +36,13 @@ class RefAdjSpec(ctypes.Structure):
                 ("r_switch", ctypes.c_double)]
 
 
+class RefCompatSim(ctypes.Structure):
+    _fields_ = [("min_dim", ctypes.c_float * 3), ("max_dim", ctypes.c_float * 3),
+                ("temperature", ctypes.c_float), ("objectnumber", ctypes.c_int64),
+                ("stepwidth", ctypes.c_int64), ("duration", ctypes.c_int64),
+                ("velocity_dampening", ctypes.c_float)]
+
+
 class RefMDParams(ctypes.Structure):
     _fields_ = [("sigma", ctypes.c_double), ("epsilon", ctypes.c_double),
                 ("coulomb_k", ctypes.c_double), ("cutoff", ctypes.c_double),
@@ -102,6 +109,9 @@ def lib():
             L.ref_compat_force_coulomb.argtypes = [ctypes.c_int32, i32p, i32p, f32p,
                                                    ctypes.c_int64, f32p, f32p]
             L.ref_compat_force_coulomb.restype = None
+            L.ref_compat_simulate.argtypes = [ctypes.POINTER(RefCompatSim), ctypes.c_int32, f32p,
+                                              f32p, f32p, f32p, f32p, f32p]
+            L.ref_compat_simulate.restype = ctypes.c_int
             L.ref_brute_pairs.argtypes = [f32p, ctypes.c_int32, ctypes.c_float, ctypes.c_int32,
                                           i32p, i32p, f32p, ctypes.c_int64]
             L.ref_brute_pairs.restype = ctypes.c_int64
@@ -235,6 +245,27 @@ def compat_forces(kind, n, pairs, q=None):
                                        _p(d, ctypes.c_float), len(i), _p(qq, ctypes.c_float),
                                        _p(out, ctypes.c_float))
     return out
+
+
+def compat_simulate(x, v, force, mass, charge, min_dim, max_dim, temperature, objectnumber,
+                    stepwidth, duration, vdamp, log=True):
+    """simulate! as written (Simulator.jl:154-256) for Float32 state and an
+    Int64 stepwidth.  Returns (x, v, force, poslog or None, status): status 1
+    is rescale_velocity!'s DomainError."""
+    x = np.array(x, np.float32, order="C").reshape(-1, 3)
+    v = np.array(v, np.float32, order="C").reshape(-1, 3)
+    f = np.array(force, np.float32, order="C").reshape(-1, 3)
+    m = np.ascontiguousarray(mass, np.float32)
+    q = np.ascontiguousarray(charge, np.float32)
+    n = len(x)
+    spec = RefCompatSim((ctypes.c_float * 3)(*min_dim), (ctypes.c_float * 3)(*max_dim),
+                        temperature, objectnumber, stepwidth, duration, vdamp)
+    log_arr = np.zeros((duration + 1, n, 3), np.float32) if log else None
+    st = lib().ref_compat_simulate(ctypes.byref(spec), n, _p(x, ctypes.c_float),
+                                   _p(v, ctypes.c_float), _p(f, ctypes.c_float),
+                                   _p(m, ctypes.c_float), _p(q, ctypes.c_float),
+                                   _p(log_arr, ctypes.c_float) if log else None)
+    return x, v, f, log_arr, st
 
 
 def simd_leaf_traverse(t, r, apl):

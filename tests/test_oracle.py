@@ -185,6 +185,41 @@ def test_compat_forces_oracle(oracle):
     assert one[0, 0] == np.float32(t) and np.all(one[1] == 0)
 
 
+def test_compat_simulate_oracle(oracle):
+    # simulate! as written, checked against by-hand cases of its formulas
+    box = dict(min_dim=(0.0, 0.0, 0.0), max_dim=(1.0, 1.0, 1.0))
+    # two neutral atoms far apart (no LJ pair below 0.01, no charge): the
+    # all-pairs LJ term (added to force[i] only) is ~1e-11 at d = 0.7, so the
+    # motion is x += v to 1e-6; a wall crossing clamps x and flips v exactly
+    x = np.array([[0.2, 0.5, 0.5], [0.9, 0.5, 0.5]], np.float32)
+    v = np.array([[0.1, 0.0, 0.0], [0.05, 0.0, 0.0]], np.float32)
+    xs, vs, fs, log, st = oracle.compat_simulate(
+        x, v, np.zeros((2, 3)), np.ones(2), np.zeros(2), temperature=0.0, objectnumber=2,
+        stepwidth=1, duration=3, vdamp=0.0, **box)
+    assert st == 0
+    xe = np.array([[0.3, 0.5, 0.5], [0.95, 0.5, 0.5]], np.float32)
+    assert np.allclose(log[1], xe, atol=1e-6) and np.allclose(log[3][0], [0.5, 0.5, 0.5], atol=1e-6)
+    assert log[3][1][0] == 1.0 and vs[1][0] == np.float32(-0.05)
+    assert np.all(fs[1] == 0) and np.all(fs[0] > 0) and fs[0][0] == fs[0][1] == fs[0][2]
+    assert np.array_equal(log[0], xs)
+    # a negative rescale_velocity! radicand at step 10 is Julia's DomainError
+    rng = np.random.default_rng(3)
+    x = rng.uniform(0.1, 0.9, (8, 3)).astype(np.float32)
+    v = rng.uniform(-1e-3, 1e-3, (8, 3)).astype(np.float32)
+    *_, st = oracle.compat_simulate(x, v, np.zeros((8, 3)), np.ones(8), np.zeros(8),
+                                    temperature=1e-9, objectnumber=8, stepwidth=1,
+                                    duration=12, vdamp=3.0, log=False, **box)
+    assert st == 1
+    # gamma = 0 leaves beta = 1; gamma = 1 scales the velocities by
+    # sqrt(Tf / Ti), Ti = 2 / (3 N) sum |v_i| m_i / 2 (linear in |v|, as written)
+    run = lambda g: oracle.compat_simulate(x, v, np.zeros((8, 3)), np.ones(8), np.zeros(8),
+                                           temperature=0.5, objectnumber=8, stepwidth=1,
+                                           duration=10, vdamp=g, log=False, **box)[1]
+    v0, v1 = run(0.0), run(1.0)
+    Ti = np.sum(2 / (3 * 8) * np.linalg.norm(v0.astype(np.float64), axis=1) / 2)
+    assert np.allclose(v1, v0 * np.sqrt(0.5 / Ti), rtol=1e-6, atol=0)
+
+
 def test_golden_vectors(oracle):
     for c in golden_cases():
         x = np.array(c["position"], np.float32)
