@@ -269,6 +269,64 @@ def batched_leg(nd, ctx, ext, flush):
             "sharding": f"{ws} rank(s), greedy balance of the systems' atom counts"}
 
 
+COMPAT_N, COMPAT_STEPS = 4096, 20
+
+
+def compat_leg(nd, ctx, ext, flush, cpu=True):
+    """simulate! as written (nd_compat_simulate): 4,096 atoms from a collector
+    shaped like the reference scripts' (unit box, temperature 0.01, masses in
+    [1, 5), charges in +-1e-9), 20 steps of stepwidth 1 over the all-pairs
+    list, timed as one call with host buffers in and out (the reference's
+    poslog included); the oracle's literal restatement of the same loop on
+    the host cores is the CPU comparison."""
+    import numpy as np
+
+    import torch
+
+    rng = np.random.default_rng(SEED)
+    n = COMPAT_N
+    m = rng.uniform(1.0, 5.0, n).astype(np.float32)
+    q = rng.uniform(-1e-9, 1e-9, n).astype(np.float32)
+    x = rng.uniform(0.0, 1.0, (n, 3)).astype(np.float32)
+    v = np.repeat((np.float32(0.01) / np.float32(n) * np.float32(3 * n) / m)[:, None], 3, axis=1)
+    spec = nd.SimSpec(duration=COMPAT_STEPS, stepwidth=1, vDamp=1.0)
+    clct = nd.GenericRandomCollector(objectnumber=n, minDim=(0.0, 0.0, 0.0),
+                                     maxDim=(1.0, 1.0, 1.0), temperature=0.01)
+    walls, dev = [], []
+    for k in range(4):
+        sys_ = nd.GenericObjectCollection(x, v, mass=m, charge=q)
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record(ext)
+        log = nd.simulate_compat_(sys_, spec, clct, ctx=ctx)
+        b.record(ext)
+        b.synchronize()
+        if k > 0:
+            walls.append(time.perf_counter() - t0)
+            dev.append(a.elapsed_time(b) * 1e-3)
+    wall = float(np.median(walls))
+    out = {"workload": f"simulate! as written, {n} atoms, {COMPAT_STEPS} steps (all-pairs list)",
+           "metric": "atom-steps/s", "value": n * COMPAT_STEPS / wall,
+           "ms_per_md_step": wall * 1e3 / COMPAT_STEPS,
+           "device_span_ms_per_md_step": float(np.median(dev)) * 1e3 / COMPAT_STEPS,
+           "api": "nd_compat_simulate, host arrays and the poslog copied in the timed call",
+           "finite_fraction_final": float(np.isfinite(log[0]).mean())}
+    if cpu:
+        from oracle import naiveref as R
+        steps = 2
+        t0 = time.perf_counter()
+        R.compat_simulate(x, v, np.zeros((n, 3)), m, q, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), 0.01, n,
+                          1, steps, 1.0, log=False)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n * steps / dt, "unit": "atom-steps/s", "cores": 1,
+                               "kind": "port",
+                               "sample": f"{n} atoms x {steps} steps of the oracle's sequential "
+                                         f"restatement, {dt:.2f} s"}
+    return out
+
+
 def plain_leg(nd, ctx, ext, flush):
     """Plain LJ velocity Verlet at 4,096 atoms (cube side 17, min separation
     0.8, v ~ N(0,1), sigma = eps = 1, r_c 2.5, dt 1e-3, rebuild every 10):
@@ -607,6 +665,8 @@ def run_gb300(args):
                                       check_every=args.adjoint_check_every)
     if rank == 0 and not args.no_stress:
         line["ns_stress"] = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline)
+    if rank == 0 and not args.no_compat:
+        line["compat_simulate"] = compat_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(steps=10)
     if rank == 0:
@@ -674,6 +734,8 @@ def run_only(args):
     elif args.only == "adjoint":
         out = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps,
                           check_every=args.adjoint_check_every)
+    elif args.only == "compat":
+        out = compat_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline)
     else:
         out = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline,
                          points=args.stress_points)
@@ -706,7 +768,9 @@ def main():
                     help="union search of the fixed-settings engine of --only md")
     ap.add_argument("--check-every", type=int, default=3,
                     help="early-refit check interval of the fixed-settings engine of --only md")
-    ap.add_argument("--only", choices=["md", "plain", "batched", "adjoint", "stress"],
+    ap.add_argument("--no-compat", action="store_true",
+                    help="skip the simulate!-as-written measurement")
+    ap.add_argument("--only", choices=["md", "plain", "batched", "adjoint", "stress", "compat"],
                     help="run one secondary measurement alone and print its JSON object "
                          "(for profiling)")
     args = ap.parse_args()

@@ -316,6 +316,37 @@ nd_status nd_compat_simulate(nd_ctx* ctx, const nd_compat_sim* spec, int32_t n, 
                              const float* charge, float* poslog);
 
 /*
+ * collect_objects(clct::GenericRandomCollector) (src/MDInput.jl:305-369) on
+ * the device: masses, charges and positions uniform in the collector's
+ * ranges (generate_positions, :175-190), velocities T * veldist * 3N kb / m
+ * per component with veldist a Float32 uniform split normalised to sum 1
+ * (randomvelocity) or T / N * 3N kb / m, and unique_pairs_prune (:228-259) as
+ * written: atom i (1-based, i <= N - 2) with an atom j in i+1 .. N-1 closer
+ * than minimumdistance gets Inf coordinates (the reference's re-placement
+ * loop never runs: its condition tooClose < 0 is never true); *pruned (may
+ * be NULL) receives their number.  Draws come from a counter-based splitmix64
+ * stream of `seed` instead of Julia's global RNG, so values match the
+ * reference's distributions, not its draws.  position, velocity: N x 3
+ * Float32 out; mass, charge: N Float32 out; N = objectnumber <= 2^28.
+ */
+typedef struct nd_collector {
+    int64_t objectnumber;
+    float min_dim[3];
+    float max_dim[3];
+    float temperature;
+    int32_t randomvelocity;
+    float minmass;
+    float maxmass;
+    float minimumdistance;
+    float mincharge;
+    float maxcharge;
+} nd_collector;
+
+nd_status nd_collect_objects(nd_ctx* ctx, const nd_collector* collector, uint64_t seed,
+                             float* position, float* velocity, float* mass, float* charge,
+                             int64_t* pruned);
+
+/*
  * Forces and energy of a configuration with the library's own neighbour search
  * (spatial-order leaf BVH at radius p->cutoff): the fused hot-path force kernel
  * run once.  Same physics and outputs as nd_forces_pairs.

@@ -481,6 +481,15 @@ nd_status nd_compat_force_coulomb(nd_ctx* h, int32_t n, const int32_t* pi, const
     return nd::compat_forces(&h->c, 1, n, pi, pj, pd, npairs, charge, force);
 }
 
+nd_status nd_collect_objects(nd_ctx* h, const nd_collector* collector, uint64_t seed,
+                             float* position, float* velocity, float* mass, float* charge,
+                             int64_t* pruned) {
+    if (!h) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    return nd::collect_objects(&h->c, collector, seed, position, velocity, mass, charge, pruned);
+}
+
 nd_status nd_compat_simulate(nd_ctx* h, const nd_compat_sim* spec, int32_t n, float* position,
                              float* velocity, float* force, const float* mass,
                              const float* charge, float* poslog) {

@@ -125,62 +125,73 @@ __global__ void k_iota(int32_t* v, int64_t n) {
 
 // ------------------------------------------------ simulate! as written
 // The all-pairs list of unique_pairs (AllToAll.jl:65-80) holds (i, j) for
-// i < j in row-major order; only the distances are stored, row i (0-based)
-// from tri_row(i).
+// i < j, row by row (row i: j = i + 1 .. n - 1, 0-based).  Nothing of it is
+// stored in that order: the Lennard-Jones terms are stored by offset
+// k = j - i - 1 along the rows (entry (k, i) at koff(k) + i, so the threads
+// of consecutive atoms read consecutive entries), the Coulomb terms by level.
 
-__host__ __device__ inline int64_t tri_row(int32_t i, int32_t n) {
-    return (int64_t)i * (2 * (int64_t)n - i - 1) / 2;
+__host__ __device__ inline int64_t koff(int32_t k, int32_t n) {
+    return (int64_t)k * (n - 1) - (int64_t)k * (k - 1) / 2;
 }
 
 // update_pairslist! (AllToAll.jl:7-62): d = sqrt(sum((a[i] .- a[j]).^2)),
-// the sum left to right.  One block per row.
-__global__ void k_cs_pairs(const float* __restrict__ x, int32_t n, float* __restrict__ d) {
+// the sum left to right, and the pair's force_lennardjones! term
+// (lennardjones_interior depends on d alone) with whether d < thr
+// (threshold_pairs, AllToAll.jl:83-88).  One block per row.
+__global__ void k_cs_pairs(const float* __restrict__ x, int32_t n, float thr,
+                           double* __restrict__ ljt, unsigned char* __restrict__ near) {
     const int32_t i = blockIdx.x;
     const float xi = x[3 * (int64_t)i], yi = x[3 * (int64_t)i + 1], zi = x[3 * (int64_t)i + 2];
-    float* row = d + tri_row(i, n) - (i + 1);
     for (int32_t j = i + 1 + threadIdx.x; j < n; j += blockDim.x) {
         const float dx = __fsub_rn(xi, x[3 * (int64_t)j]);
         const float dy = __fsub_rn(yi, x[3 * (int64_t)j + 1]);
         const float dz = __fsub_rn(zi, x[3 * (int64_t)j + 2]);
-        row[j] = __fsqrt_rn(
+        const float dd = __fsqrt_rn(
             __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        const int64_t e = koff(j - i - 1, n) + i;
+        ljt[e] = lj_compat_term(dd);
+        near[e] = dd < thr;
     }
 }
 
-// force_lennardjones! over the whole list and over threshold_pairs(list, thr)
-// (AllToAll.jl:83-88: the pairs with d < thr, in list order) in one pass.
-// Atom i's terms are its row, in order; a warp per atom computes 32 terms at
-// a time and adds them one by one (the Float32 accumulator, each addition
-// rounded through Float64 as Julia's promotion does).
-__global__ void __launch_bounds__(256) k_cs_lj(const float* __restrict__ d, int32_t n, float thr,
-                                               float* __restrict__ ljthr,
-                                               float* __restrict__ ljall) {
-    const int32_t i = (int32_t)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
+// force_lennardjones! over the whole list and over threshold_pairs(list,
+// thr): atom i's terms are its row, added in order to Float32 accumulators,
+// each addition rounded through Float64 as Julia's promotion does.  One thread
+// per atom, one warp per block so that the atoms' serial Float64 additions
+// spread over the SMs' Float64 pipes; the loads run 16 terms ahead.
+__global__ void k_cs_lj(const double* __restrict__ ljt, const unsigned char* __restrict__ near,
+                        int32_t n, float* __restrict__ ljthr, float* __restrict__ ljall) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float* row = d + tri_row(i, n);
     const int32_t L = n - 1 - i;
     float fa = 0.0f, ft = 0.0f;
-    for (int32_t b = 0; b < L; b += 32) {
-        double t = 0.0;
-        bool use = false;
-        if (b + lane < L) {
-            const float dd = __ldg(&row[b + lane]);
-            t = lj_compat_term(dd);
-            use = dd < thr;
+    int64_t e = i;  // koff(0) + i
+    int32_t k = 0;
+    for (; k + 16 <= L; k += 16) {
+        double t[16];
+        unsigned char u[16];
+        int64_t ee = e;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            t[r] = __ldg(&ljt[ee]);
+            u[r] = __ldg(&near[ee]);
+            ee += n - 1 - (k + r);
         }
-        const unsigned used = __ballot_sync(0xffffffffu, use);
-        const int cnt = min(32, L - b);
-        for (int k = 0; k < cnt; ++k) {
-            const double tk = __shfl_sync(0xffffffffu, t, k);
-            fa = __double2float_rn(__dadd_rn((double)fa, tk));
-            if ((used >> k) & 1u) ft = __double2float_rn(__dadd_rn((double)ft, tk));
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            fa = __double2float_rn(__dadd_rn((double)fa, t[r]));
+            if (u[r]) ft = __double2float_rn(__dadd_rn((double)ft, t[r]));
         }
+        e = ee;
     }
-    if (lane == 0) {
-        ljthr[i] = ft;
-        ljall[i] = fa;
+    for (; k < L; ++k) {
+        const double t = __ldg(&ljt[e]);
+        fa = __double2float_rn(__dadd_rn((double)fa, t));
+        if (__ldg(&near[e])) ft = __double2float_rn(__dadd_rn((double)ft, t));
+        e += n - 1 - k;
     }
+    ljthr[i] = ft;
+    ljall[i] = fa;
 }
 
 // force_coulomb! over the all-pairs list.  Pair (i, j) depends on the pairs
@@ -188,46 +199,151 @@ __global__ void __launch_bounds__(256) k_cs_lj(const float* __restrict__ d, int3
 // (i - 1, i)) and (i - 1, j), so the pairs with i + j = s form one level
 // whose pairs touch distinct atoms, and level s follows level s - 1.  Running
 // the levels in order, each pair's two updates exactly as written, gives every
-// atom the same sequence of roundings as the sequential loop.  One block;
-// the accumulators (and charges) in shared memory when they fit.
-template <bool SMEM>
-__global__ void __launch_bounds__(1024, 1) k_cs_coulomb(const float* __restrict__ d,
-                                                        const float* __restrict__ q, int32_t n,
-                                                        float* __restrict__ F) {
-    extern __shared__ float sh[];
-    float* f = SMEM ? sh : F;
-    const float* qq = SMEM ? sh + n : q;
-    for (int32_t k = threadIdx.x; k < n; k += blockDim.x) {
-        f[k] = 0.0f;
-        if (SMEM) sh[n + k] = q[k];
+// atom the same sequence of roundings as the sequential loop.
+//
+// The pair terms k q_i q_j / d^2 do not depend on the recurrence: they are
+// computed in parallel beforehand and stored level by level (level s at
+// level_off(s), its pairs by increasing i), so each level is one contiguous,
+// coalesced segment.
+
+__host__ __device__ inline int32_t level_lo(int32_t s, int32_t n) { return max(0, s - (n - 1)); }
+__host__ __device__ inline int32_t level_count(int32_t s, int32_t n) {
+    return (s - 1) / 2 - level_lo(s, n) + 1;
+}
+// Pairs in the levels before s: level t <= n - 1 holds ceil(t / 2) pairs, so
+// floor(s^2 / 4) for s <= n; the map (i, j) -> (n-1-j, n-1-i) reverses the
+// levels, which gives P - floor((2n - 1 - s)^2 / 4) for s >= n - 1.
+__host__ __device__ inline int64_t level_off(int32_t s, int32_t n) {
+    if (s <= n) return (int64_t)s * s / 4;
+    const int64_t r = 2 * (int64_t)n - 1 - s;
+    return (int64_t)n * (n - 1) / 2 - r * r / 4;
+}
+
+// The pair terms of one level per block, from the positions with the same
+// operations as update_pairslist! (so the same d).
+// stride > 0: level s at s * stride (16-byte aligned segments); else packed.
+__global__ void k_cs_cterms(const float* __restrict__ x, const float* __restrict__ q, int32_t n,
+                            int32_t stride, float* __restrict__ cterm) {
+    const int32_t s = blockIdx.x + 1;
+    const int32_t ilo = level_lo(s, n), cnt = level_count(s, n);
+    float* out = cterm + (stride ? (int64_t)s * stride : level_off(s, n));
+    for (int32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+        const int32_t i = ilo + k, j = s - i;
+        const float dx = __fsub_rn(x[3 * (int64_t)i], x[3 * (int64_t)j]);
+        const float dy = __fsub_rn(x[3 * (int64_t)i + 1], x[3 * (int64_t)j + 1]);
+        const float dz = __fsub_rn(x[3 * (int64_t)i + 2], x[3 * (int64_t)j + 2]);
+        const float d = __fsqrt_rn(
+            __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        // k * charge[i] * charge[j] ./ (d .^ 2), k = 1
+        out[k] = __fdiv_rn(__fmul_rn(q[i], q[j]), __fmul_rn(d, d));
     }
+}
+
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(src) : "memory");
+}
+
+constexpr int kRingThreads = 256;
+constexpr int kLevelBatch = 8;  // pairs of a level per thread with their loads in flight
+
+// The recurrence, accumulators in shared memory, the pair terms of the next
+// RING - 1 levels copied ahead into a shared ring in 16-byte pieces (levels
+// at a fixed 16-byte-aligned stride).  One barrier per level: after a level's
+// updates each thread waits for its own copies of the next level, and the
+// barrier makes every thread's updates and copies visible to all.
+template <int RING>
+__global__ void __launch_bounds__(kRingThreads, 1) k_cs_coulomb_ring(const float* __restrict__ cterm,
+                                                                     int32_t n, int32_t stride,
+                                                                     float* __restrict__ F) {
+    extern __shared__ float4 sh4[];
+    float* ring = reinterpret_cast<float*>(sh4);  // RING x stride, 16-byte aligned
+    float* f = ring + (int64_t)RING * stride;
+    for (int32_t k = threadIdx.x; k < n; k += blockDim.x) f[k] = 0.0f;
+    const int32_t smax = 2 * n - 3;
+    auto issue = [&](int32_t s) {
+        if (s <= smax) {
+            const int32_t pieces = (level_count(s, n) + 3) >> 2;
+            const float* src = cterm + (int64_t)s * stride;
+            float* dst = ring + (s % RING) * (int64_t)stride;
+            for (int32_t k = threadIdx.x; k < pieces; k += blockDim.x)
+                cp_async16(dst + 4 * k, src + 4 * k);
+        }
+        cp_async_commit();  // one group per level, empty or not
+    };
+    for (int32_t s = 1; s < RING; ++s) issue(s);
+    cp_async_wait<RING - 2>();  // level 1
+    __syncthreads();
+    for (int32_t s = 1; s <= smax; ++s) {
+        const float* cc = ring + (s % RING) * (int64_t)stride;
+        const int32_t ilo = level_lo(s, n), ihi = (s - 1) / 2;
+        // the pairs of a level touch distinct atoms: all of this thread's
+        // loads go first, then the updates (kLevelBatch pairs at a time)
+        for (int32_t i0 = ilo + (int32_t)threadIdx.x; i0 <= ihi;
+             i0 += kLevelBatch * (int32_t)blockDim.x) {
+            float a[kLevelBatch], b[kLevelBatch], t[kLevelBatch];
+#pragma unroll
+            for (int m = 0; m < kLevelBatch; ++m) {
+                const int32_t i = i0 + m * (int32_t)blockDim.x;
+                if (i <= ihi) {
+                    a[m] = f[i];
+                    b[m] = f[s - i];
+                    t[m] = cc[i - ilo];
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < kLevelBatch; ++m) {
+                const int32_t i = i0 + m * (int32_t)blockDim.x;
+                if (i <= ihi) {
+                    const float fi = __fadd_rn(a[m], t[m]);
+                    f[i] = fi;
+                    f[s - i] = __fsub_rn(b[m], fi);
+                }
+            }
+        }
+        issue(s + RING - 1);
+        cp_async_wait<RING - 2>();  // this thread's pieces of level s + 1
+        __syncthreads();
+    }
+    cp_async_wait<0>();
+    for (int32_t k = threadIdx.x; k < n; k += blockDim.x) F[k] = f[k];
+}
+
+// The same recurrence with the accumulators in global memory (any n): the
+// block's own writes are visible to it after each barrier.  The first item of
+// the next level is loaded ahead.
+__global__ void __launch_bounds__(1024, 1) k_cs_coulomb_global(const float* __restrict__ cterm,
+                                                               int32_t n, float* F) {
+    for (int32_t k = threadIdx.x; k < n; k += blockDim.x) F[k] = 0.0f;
     __syncthreads();
     const int32_t smax = 2 * n - 3;
-    // the first pair of this thread in the next level, loaded ahead
     auto first = [&](int32_t s) -> float {
-        const int32_t i = max(0, s - (n - 1)) + (int32_t)threadIdx.x;
-        if (s > smax || i > (s - 1) / 2) return 0.0f;
-        return __ldg(&d[tri_row(i, n) + (s - 2 * i - 1)]);
+        if (s > smax || (int32_t)threadIdx.x >= level_count(s, n)) return 0.0f;
+        return __ldg(&cterm[level_off(s, n) + threadIdx.x]);
     };
-    float dn = first(1);
+    float cn = first(1);
     for (int32_t s = 1; s <= smax; ++s) {
-        const float dc = dn;
-        dn = first(s + 1);
-        const int32_t ilo = max(0, s - (n - 1)), ihi = (s - 1) / 2;
+        const float c0 = cn;
+        cn = first(s + 1);
+        const int32_t ilo = level_lo(s, n), ihi = (s - 1) / 2;
+        const float* cc = cterm + level_off(s, n);
         for (int32_t i = ilo + (int32_t)threadIdx.x; i <= ihi; i += blockDim.x) {
             const int32_t j = s - i;
-            const float dd = i == ilo + (int32_t)threadIdx.x ? dc
-                                                             : __ldg(&d[tri_row(i, n) + (j - i - 1)]);
-            // k * charge[i] * charge[j] ./ (d .^ 2), k = 1
-            const float c = __fdiv_rn(__fmul_rn(qq[i], qq[j]), __fmul_rn(dd, dd));
-            const float fi = __fadd_rn(f[i], c);
-            f[i] = fi;
-            f[j] = __fsub_rn(f[j], fi);
+            const float c = i == ilo + (int32_t)threadIdx.x ? c0 : __ldg(&cc[i - ilo]);
+            const float fi = __fadd_rn(F[i], c);
+            F[i] = fi;
+            F[j] = __fsub_rn(F[j], fi);
         }
         __syncthreads();
     }
-    if (SMEM)
-        for (int32_t k = threadIdx.x; k < n; k += blockDim.x) F[k] = sh[k];
 }
 
 // One step's per-atom part (Simulator.jl:183-228): sum_forces!, the position
@@ -323,10 +439,24 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
     const int64_t chunk =
         poslog ? std::max<int64_t>(1, std::min<int64_t>(spec->duration, chunk_frames)) : 0;
     nd_status st;
-    if ((st = ensure(c, c->pairs_d, sizeof(float) * (size_t)std::max<int64_t>(P, 1)))) return st;
+    // Coulomb terms: levels at a 16-byte-aligned stride when the recurrence
+    // runs in shared memory (the widest level is level n - 1), else packed
+    const int32_t maxc = n > 1 ? level_count(n - 1, n) : 1;
+    const int32_t stride = (maxc + 3) & ~3;
+    auto shmem = [&](int r) { return sizeof(float) * ((size_t)r * stride + (size_t)n); };
+    int ring = 0;
+    for (int r : {8, 4, 3})
+        if (!ring && !force_global && shmem(r) <= 200 * 1024) ring = r;
+    const int32_t nlev = std::max(2 * n - 3, 0);
+    const size_t ncterm = ring ? (size_t)(nlev + 1) * stride : (size_t)std::max<int64_t>(P, 1);
+    if ((st = ensure(c, c->leafpairs, sizeof(float) * ncterm))) return st;
+    if ((st = ensure(c, c->pairs_i, sizeof(double) * (size_t)std::max<int64_t>(P, 1)))) return st;
+    if ((st = ensure(c, c->pairs_j, (size_t)std::max<int64_t>(P, 1)))) return st;
     const size_t small = sizeof(float) * (4 * n3 + 6 * (size_t)n);
     if ((st = ensure(c, c->compat, small + (size_t)(chunk * frame_bytes)))) return st;
-    float* dd = (float*)c->pairs_d.p;
+    float* cterm = (float*)c->leafpairs.p;               // Coulomb pair terms, by level
+    double* ljt = (double*)c->pairs_i.p;                 // LJ pair terms, by row offset
+    unsigned char* near = (unsigned char*)c->pairs_j.p;  // d < 0.01, same layout
     float* dx = (float*)c->compat.p;
     float* dv = dx + n3;
     float* dF = dv + n3;
@@ -349,13 +479,35 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
     if (e == cudaSuccess) e = cudaMemcpyAsync(dq, q, n * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "compat simulate upload");
 
-    const bool smem = !force_global && 2 * (size_t)n * sizeof(float) <= 200 * 1024;
-    const size_t shb = smem ? 2 * (size_t)n * sizeof(float) : 0;
-    if (smem) {
-        e = cudaFuncSetAttribute(k_cs_coulomb<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)shb);
+    const size_t shb = ring ? shmem(ring) : 0;
+    if (ring) {
+        const void* fn = ring == 8   ? (const void*)k_cs_coulomb_ring<8>
+                         : ring == 4 ? (const void*)k_cs_coulomb_ring<4>
+                                     : (const void*)k_cs_coulomb_ring<3>;
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shb);
         if (e != cudaSuccess) return cuda_fail(c, e, "compat simulate smem");
     }
+    // force_coulomb! and force_lennardjones! over the current list
+    auto forces = [&]() {
+        if (ring == 8)
+            k_cs_coulomb_ring<8><<<1, kRingThreads, shb, s>>>(cterm, n, stride, cf);
+        else if (ring == 4)
+            k_cs_coulomb_ring<4><<<1, kRingThreads, shb, s>>>(cterm, n, stride, cf);
+        else if (ring == 3)
+            k_cs_coulomb_ring<3><<<1, kRingThreads, shb, s>>>(cterm, n, stride, cf);
+        else
+            k_cs_coulomb_global<<<1, 1024, 0, s>>>(cterm, n, cf);
+        k_cs_lj<<<(unsigned)cdiv(n, 32), 32, 0, s>>>(ljt, near, n, ljthr, ljall);
+        c->launches += 2;
+    };
+    // update_pairslist!: the list's LJ terms and Coulomb terms
+    auto pairs = [&]() {
+        if (n > 1) {
+            k_cs_pairs<<<n - 1, 256, 0, s>>>(dx, n, 0.01f, ljt, near);
+            k_cs_cterms<<<nlev, 256, 0, s>>>(dx, dq, n, ring ? stride : 0, cterm);
+            c->launches += 2;
+        }
+    };
     const float dt = (float)spec->stepwidth;
     const float dt2 = (float)(int64_t)((uint64_t)spec->stepwidth * (uint64_t)spec->stepwidth);
     const float3 lo = make_float3(spec->min_dim[0], spec->min_dim[1], spec->min_dim[2]);
@@ -363,12 +515,8 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
     // rescale_velocity!: 2 / (3 * objects * kb), objects = Float32(objectnumber), kb = 1
     const float cT = 2.0f / ((3.0f * (float)spec->objectnumber) * 1.0f);
     const unsigned ga = (unsigned)cdiv(n, 256);
-    const unsigned gw = (unsigned)cdiv((int64_t)n * 32, 256);
 
-    if (n > 1) {
-        k_cs_pairs<<<n - 1, 256, 0, s>>>(dx, n, dd);  // pairslist = unique_pairs(position)
-        c->launches++;
-    }
+    pairs();  // pairslist = unique_pairs(position)
     int64_t pending = 0;  // frames in the device chunk not yet copied out
     int64_t first = 1;    // step of the chunk's first frame
     auto flush = [&]() -> nd_status {
@@ -383,21 +531,15 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
         return ND_OK;
     };
     for (int64_t step = 1; step <= spec->duration; ++step) {
-        k_cs_lj<<<gw, 256, 0, s>>>(dd, n, 0.01f, ljthr, ljall);
         // force_coulomb! runs twice per step on the same list and charges: one
-        // evaluation gives both results
-        if (smem)
-            k_cs_coulomb<true><<<1, 1024, shb, s>>>(dd, dq, n, cf);
-        else
-            k_cs_coulomb<false><<<1, 1024, 0, s>>>(dd, dq, n, cf);
+        // evaluation gives both results; so does force_lennardjones!'s pass
+        // over the whole list and its threshold_pairs part
+        forces();
         float* frame = poslog ? dlog + pending * (int64_t)n3 : nullptr;
         k_cs_step<<<ga, 256, 0, s>>>(dx, dv, dF, dFn, dm, ljthr, ljall, cf, n, dt, dt2, lo, hi,
                                       frame);
-        c->launches += 3;
-        if (n > 1) {
-            k_cs_pairs<<<n - 1, 256, 0, s>>>(dx, n, dd);  // update_pairslist!
-            c->launches++;
-        }
+        c->launches += 2;
+        pairs();  // update_pairslist!
         if (step % 10 == 0) {
             k_cs_rescale<<<1, 1024, 0, s>>>(dv, dm, n, cT, spec->temperature,
                                              spec->velocity_dampening, term, c->d_err);
@@ -424,6 +566,184 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
         e = cudaMemcpyAsync(poslog, dx, n3 * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "compat simulate download");
     return sync_and_check(c, "compat simulate");
+}
+
+namespace {
+
+// ------------------------------------------------ collect_objects
+// collect_objects(::GenericRandomCollector) (MDInput.jl:305-369) with a
+// counter-based stream in place of Julia's global RNG: draw k of stream c is
+// mix64(seed ^ mix64(c << 56 ^ k)).  Uniform(a, b) as Distributions draws it:
+// a + (b - a) * u with u in [0, 1) (53 bits), stored as Float32; rand(Float32)
+// for the velocity split: 24 bits.
+
+__host__ __device__ inline uint64_t cobj_bits(uint64_t seed, uint64_t stream, uint64_t k) {
+    return mix64(seed ^ mix64((stream << 56) ^ k));
+}
+__host__ __device__ inline float cobj_uniform(uint64_t seed, uint64_t stream, uint64_t k, float a,
+                                              float b) {
+    const double u = (double)(cobj_bits(seed, stream, k) >> 11) * 0x1.0p-53;
+    return (float)((double)a + (double)(b - a) * u);
+}
+__host__ __device__ inline float cobj_rand32(uint64_t seed, uint64_t stream, uint64_t k) {
+    return (float)(cobj_bits(seed, stream, k) >> 40) * 0x1.0p-24f;
+}
+
+// mass, charge, position (generate_positions, MDInput.jl:175-190) and the
+// velocity split draws of every atom.
+__global__ void k_cobj_draw(nd_collector cl, uint64_t seed, int32_t n, float* __restrict__ x,
+                            float* __restrict__ m, float* __restrict__ q,
+                            float* __restrict__ vd) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    m[i] = cobj_uniform(seed, 0, i, cl.minmass, cl.maxmass);
+    q[i] = cobj_uniform(seed, 1, i, cl.mincharge, cl.maxcharge);
+    for (int d = 0; d < 3; ++d) {
+        x[3 * (int64_t)i + d] = cobj_uniform(seed, 2 + d, i, cl.min_dim[d], cl.max_dim[d]);
+        vd[(int64_t)d * n + i] = cobj_rand32(seed, 5 + d, i);
+    }
+}
+
+// sum(veldist) per dimension in a fixed order: 256-element chunks reduced as
+// a binary tree (stride 128, 64, .., 1), then the chunk sums in chunk order.
+__global__ void __launch_bounds__(256) k_cobj_chunks(const float* __restrict__ vd, int32_t n,
+                                                     int32_t nchunk, float* __restrict__ part) {
+    __shared__ float t[256];
+    const int d = blockIdx.y;
+    const int64_t k = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    t[threadIdx.x] = k < n ? vd[(int64_t)d * n + k] : 0.0f;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) t[threadIdx.x] = __fadd_rn(t[threadIdx.x], t[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(int64_t)d * nchunk + blockIdx.x] = t[0];
+}
+
+__global__ void k_cobj_total(const float* __restrict__ part, int32_t nchunk, float* sum) {
+    const int d = threadIdx.x;
+    if (d >= 3) return;
+    float s = 0.0f;
+    for (int32_t c = 0; c < nchunk; ++c) s = __fadd_rn(s, part[(int64_t)d * nchunk + c]);
+    sum[d] = s;
+}
+
+// velocity[i][d] = T * veldist[i] * 3 * N * kb / mass[i] with veldist ./=
+// sum(veldist), or T / N * 3 * N * kb / mass[i] (kb = 1), in Float32.
+__global__ void k_cobj_velocity(nd_collector cl, int32_t n, const float* __restrict__ m,
+                                const float* __restrict__ vd, const float* __restrict__ sum,
+                                float* __restrict__ v) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float N = (float)cl.objectnumber;
+    for (int d = 0; d < 3; ++d) {
+        float a;
+        if (cl.randomvelocity) {
+            const float vn = __fdiv_rn(vd[(int64_t)d * n + i], sum[d]);
+            a = __fmul_rn(__fmul_rn(__fmul_rn(cl.temperature, vn), 3.0f), N);
+        } else {
+            a = __fmul_rn(__fmul_rn(__fdiv_rn(cl.temperature, N), 3.0f), N);
+        }
+        v[3 * (int64_t)i + d] = __fdiv_rn(__fmul_rn(a, 1.0f), m[i]);
+    }
+}
+
+// unique_pairs_prune (MDInput.jl:228-259) as written: for i in 1:N-1, j in
+// i+1:N-1 (the last atom is never compared), sqrt(dx^2 + dy^2 + dz^2) <
+// minimumdistance fills a[i] with Inf.  A filled a[i] meets nothing after,
+// and every a[j] compared is still the drawn one, so atom i is filled exactly
+// when some j in (i, N-1) lies within the distance of it: one thread per i,
+// the candidates staged through shared memory.
+__global__ void __launch_bounds__(256) k_cobj_prune(const float* __restrict__ x, int32_t n,
+                                                    float dmin, unsigned char* __restrict__ hit) {
+    __shared__ float3 tile[256];
+    const int32_t i = blockIdx.x * 256 + threadIdx.x;
+    const int32_t jmax = n - 2;  // last compared atom, 0-based
+    float3 a = make_float3(0.f, 0.f, 0.f);
+    if (i < n) a = make_float3(x[3 * (int64_t)i], x[3 * (int64_t)i + 1], x[3 * (int64_t)i + 2]);
+    bool found = false;
+    for (int32_t j0 = blockIdx.x * 256; j0 <= jmax; j0 += 256) {
+        const int32_t jl = j0 + threadIdx.x;
+        if (jl <= jmax)
+            tile[threadIdx.x] =
+                make_float3(x[3 * (int64_t)jl], x[3 * (int64_t)jl + 1], x[3 * (int64_t)jl + 2]);
+        __syncthreads();
+        if (!found && i < jmax) {
+            const int32_t kend = min(256, jmax - j0 + 1);
+            for (int k = max(0, i + 1 - j0); k < kend; ++k) {
+                const float dx = __fsub_rn(a.x, tile[k].x), dy = __fsub_rn(a.y, tile[k].y),
+                            dz = __fsub_rn(a.z, tile[k].z);
+                const float d = __fsqrt_rn(
+                    __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+                if (d < dmin) {
+                    found = true;
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (i < n) hit[i] = found;
+}
+
+__global__ void k_cobj_fill(float* __restrict__ x, const unsigned char* __restrict__ hit, int32_t n,
+                            unsigned long long* count) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !hit[i]) return;
+    x[3 * (int64_t)i] = x[3 * (int64_t)i + 1] = x[3 * (int64_t)i + 2] = __int_as_float(0x7f800000);
+    atomicAdd(count, 1ull);
+}
+
+}  // namespace
+
+nd_status collect_objects(Ctx* c, const nd_collector* cl, uint64_t seed, float* x, float* v,
+                          float* m, float* q, int64_t* pruned) {
+    if (!cl || !x || !v || !m || !q) return ND_ERR_ARG;
+    if (cl->objectnumber < 1 || cl->objectnumber > (1 << 28)) {
+        c->last_error = "nd_collect_objects: 1 <= objectnumber <= 2^28";
+        return ND_ERR_ARG;
+    }
+    const int32_t n = (int32_t)cl->objectnumber;
+    const size_t n3 = 3 * (size_t)n;
+    const int32_t nchunk = (int32_t)cdiv(n, 256);
+    nd_status st;
+    // [count (16 B)] [x, v, m, q, veldist, chunk sums, sums (Float32)] [hit (bytes)]
+    const size_t nf = 2 * n3 + 2 * (size_t)n + n3 + 3 * (size_t)nchunk + 4;
+    if ((st = ensure(c, c->compat, 16 + sizeof(float) * nf + (size_t)n))) return st;
+    unsigned long long* cnt = (unsigned long long*)c->compat.p;
+    float* dx = (float*)((char*)c->compat.p + 16);
+    float* dv = dx + n3;
+    float* dm = dv + n3;
+    float* dq = dm + n;
+    float* vd = dq + n;
+    float* part = vd + n3;
+    float* sum = part + 3 * (size_t)nchunk;
+    unsigned char* hit = (unsigned char*)(sum + 4);
+    cudaStream_t s = c->stream;
+    const unsigned g = (unsigned)cdiv(n, 256);
+    cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s);
+    k_cobj_draw<<<g, 256, 0, s>>>(*cl, seed, n, dx, dm, dq, vd);
+    if (cl->randomvelocity) {
+        k_cobj_chunks<<<dim3((unsigned)nchunk, 3), 256, 0, s>>>(vd, n, nchunk, part);
+        k_cobj_total<<<1, 32, 0, s>>>(part, nchunk, sum);
+        c->launches += 2;
+    }
+    k_cobj_velocity<<<g, 256, 0, s>>>(*cl, n, dm, vd, sum, dv);
+    k_cobj_prune<<<g, 256, 0, s>>>(dx, n, cl->minimumdistance, hit);
+    k_cobj_fill<<<g, 256, 0, s>>>(dx, hit, n, cnt);
+    c->launches += 4;
+    if ((st = check_launch(c, "collect_objects"))) return st;
+    unsigned long long h_cnt = 0;
+    cudaError_t e = cudaMemcpyAsync(x, dx, n3 * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v, dv, n3 * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m, dm, n * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(q, dq, n * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "collect_objects download");
+    if ((st = sync_and_check(c, "collect_objects"))) return st;
+    if (pruned) *pruned = (int64_t)h_cnt;
+    return ND_OK;
 }
 
 nd_status compat_forces(Ctx* c, int kind, int32_t n, const int32_t* pi, const int32_t* pj,

@@ -233,6 +233,9 @@ float pair_threshold(float r, int32_t criterion);
 // host pair list in list order; force: host N x 3 Float32.
 nd_status compat_forces(Ctx* c, int kind, int32_t n, const int32_t* pi, const int32_t* pj,
                         const float* pd, int64_t np, const float* q, float* force);
+// collect_objects(::GenericRandomCollector) on the device (host arrays out).
+nd_status collect_objects(Ctx* c, const nd_collector* cl, uint64_t seed, float* x, float* v,
+                          float* m, float* q, int64_t* pruned);
 // simulate! as written over the all-pairs list (host arrays in and out).
 nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x, float* v,
                           float* force, const float* mass, const float* q, float* poslog);

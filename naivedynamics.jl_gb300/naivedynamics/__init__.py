@@ -15,8 +15,8 @@ from .bvh import (SpheresBVHSpecs, APointPrimitive, leafTreeData, TreeData,
 from .dynamics import (ForceField, md_params, force_lennardjones_, force_coulomb_, sum_forces_,
                        force_lennardjones_compat_, force_coulomb_compat_,
                        forces, SimSpec, GenericObjectCollection, GenericRandomCollector,
-                       simulate_, simulate_compat_, MDEngine, Ensemble, systems_table,
-                       autotune)
+                       simulate_, simulate_compat_, collect_objects, MDEngine, Ensemble,
+                       systems_table, autotune)
 from .adjoint import Adjoint, adj_spec, histogram_loss_function
 from . import synth
 

@@ -83,6 +83,15 @@ class CompatSim(ctypes.Structure):
                 ("velocity_dampening", ctypes.c_float)]
 
 
+class Collector(ctypes.Structure):
+    """nd_collector: the GenericRandomCollector fields collect_objects reads."""
+    _fields_ = [("objectnumber", ctypes.c_int64), ("min_dim", ctypes.c_float * 3),
+                ("max_dim", ctypes.c_float * 3), ("temperature", ctypes.c_float),
+                ("randomvelocity", ctypes.c_int32), ("minmass", ctypes.c_float),
+                ("maxmass", ctypes.c_float), ("minimumdistance", ctypes.c_float),
+                ("mincharge", ctypes.c_float), ("maxcharge", ctypes.c_float)]
+
+
 class MDDiag(ctypes.Structure):
     """nd_md_diag."""
     _fields_ = [("skin_violations", ctypes.c_int64), ("max_neighbors", ctypes.c_int32),
@@ -148,6 +157,8 @@ SIGNATURES = {
     "nd_compat_force_coulomb": (_i32, [_vp, _i32, _vp, _vp, _vp, _i64, _vp, _vp]),
     "nd_compat_simulate": (_i32, [_vp, ctypes.POINTER(CompatSim), _i32, _vp, _vp, _vp, _vp, _vp,
                                   _vp]),
+    "nd_collect_objects": (_i32, [_vp, ctypes.POINTER(Collector), ctypes.c_uint64, _vp, _vp, _vp,
+                                  _vp, _vp]),
     "nd_md_create": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _pp]),
     "nd_md_create_dev": (_i32, [_vp, ctypes.POINTER(MDParams), _i32, _vp, _vp, _vp, _vp, _pp]),
     "nd_md_destroy": (_i32, [_vp]),

@@ -183,12 +183,18 @@ class SimSpec:
 
 @dataclass
 class GenericRandomCollector:
-    """The fields of GenericRandomCollector (MDInput.jl:67-84) the step loop uses."""
+    """GenericRandomCollector (MDInput.jl:67-84): the box and temperature the
+    step loop uses, and the ranges collect_objects draws from."""
     objectnumber: int
     minDim: tuple
     maxDim: tuple
     temperature: float = 0.0
     minimumdistance: float = 0.0
+    randomvelocity: bool = False
+    minmass: float = 1.0
+    maxmass: float = 1.0
+    mincharge: float = 0.0
+    maxcharge: float = 0.0
 
 
 @dataclass
@@ -209,6 +215,33 @@ class GenericObjectCollection:
             self.force = np.zeros((n, 3), np.float32)
         if self.index is None:
             self.index = np.arange(1, n + 1, dtype=np.int64)
+
+
+def collect_objects(clct: GenericRandomCollector, seed: int = 0, ctx=None):
+    """collect_objects(clct) (MDInput.jl:305-369) on the GPU: masses, charges
+    and positions uniform in the collector's ranges, velocities from its
+    temperature (randomvelocity: a random split per component), and the
+    reference's pruning as written -- atoms closer than clct.minimumdistance to
+    a later atom (the last atom excepted) get Inf positions, their number in
+    the result's `pruned`.  The draws come from a counter-based stream of
+    `seed`, not Julia's RNG: same distributions, different values.  Returns a
+    GenericObjectCollection (Float32 values)."""
+    ctx = ctx or default_context()
+    n = int(clct.objectnumber)
+    cl = _lib.Collector(n, (ctypes.c_float * 3)(*clct.minDim), (ctypes.c_float * 3)(*clct.maxDim),
+                        clct.temperature, int(bool(clct.randomvelocity)), clct.minmass,
+                        clct.maxmass, clct.minimumdistance, clct.mincharge, clct.maxcharge)
+    x = np.empty((n, 3), np.float32)
+    v = np.empty((n, 3), np.float32)
+    m = np.empty(n, np.float32)
+    q = np.empty(n, np.float32)
+    pruned = ctypes.c_int64(0)
+    ctx.check(_lib.lib().nd_collect_objects(ctx.handle, ctypes.byref(cl), int(seed), ptr(x),
+                                            ptr(v), ptr(m), ptr(q), ctypes.byref(pruned)),
+              "nd_collect_objects")
+    sys = GenericObjectCollection(x, v, mass=m, charge=q)
+    sys.pruned = int(pruned.value)
+    return sys
 
 
 def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCollector,

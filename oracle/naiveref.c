@@ -658,6 +658,64 @@ int ref_compat_simulate(const ref_compat_sim* spec, int32_t n, float* x, float* 
     return status;
 }
 
+/* collect_objects (MDInput.jl:305-369).  Draw k of stream c is
+ * mix64(seed ^ mix64(c << 56 ^ k)); Uniform(a, b) = a + (b - a) u, u of 53
+ * bits, stored as Float32; rand(Float32) of 24 bits. */
+static uint64_t cobj_bits(uint64_t seed, uint64_t stream, uint64_t k) {
+    return mix64(seed ^ mix64((stream << 56) ^ k));
+}
+static float cobj_uniform(uint64_t seed, uint64_t stream, uint64_t k, float a, float b) {
+    const double u = (double)(cobj_bits(seed, stream, k) >> 11) * 0x1.0p-53;
+    return (float)((double)a + (double)(b - a) * u);
+}
+
+int64_t ref_collect_objects(const ref_collector* cl, uint64_t seed, float* x, float* v, float* m,
+                            float* q) {
+    const int64_t n = cl->objectnumber;
+    float* vd = (float*)malloc(sizeof(float) * 3 * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        m[i] = cobj_uniform(seed, 0, (uint64_t)i, cl->minmass, cl->maxmass);
+        q[i] = cobj_uniform(seed, 1, (uint64_t)i, cl->mincharge, cl->maxcharge);
+        for (int d = 0; d < 3; ++d) {
+            x[3 * i + d] = cobj_uniform(seed, 2 + d, (uint64_t)i, cl->min_dim[d], cl->max_dim[d]);
+            vd[d * n + i] = (float)(cobj_bits(seed, 5 + d, (uint64_t)i) >> 40) * 0x1.0p-24f;
+        }
+    }
+    /* sum(veldist): 256-element chunks as a binary tree, chunk sums in order */
+    float sum[3] = {0.0f, 0.0f, 0.0f};
+    for (int d = 0; d < 3; ++d)
+        for (int64_t c0 = 0; c0 < n; c0 += 256) {
+            float t[256];
+            for (int k = 0; k < 256; ++k) t[k] = c0 + k < n ? vd[d * n + c0 + k] : 0.0f;
+            for (int w = 128; w > 0; w >>= 1)
+                for (int k = 0; k < w; ++k) t[k] = t[k] + t[k + w];
+            sum[d] = sum[d] + t[0];
+        }
+    const float N = (float)n;
+    for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            const float a = cl->randomvelocity
+                                ? cl->temperature * (vd[d * n + i] / sum[d]) * 3.0f * N
+                                : cl->temperature / N * 3.0f * N;
+            v[3 * i + d] = a * 1.0f / m[i];
+        }
+    free(vd);
+    /* unique_pairs_prune (MDInput.jl:228-259) as written */
+    int64_t tooClose = 0;
+    for (int64_t i = 1; i <= n - 1; ++i)
+        for (int64_t j = i + 1; j <= n - 1; ++j) {
+            float* a = &x[3 * (i - 1)];
+            const float* b = &x[3 * (j - 1)];
+            const float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+            const float d2 = sqrtf(dx * dx + dy * dy + dz * dz);
+            if (d2 < cl->minimumdistance) {
+                a[0] = a[1] = a[2] = INFINITY;
+                tooClose += 1;
+            }
+        }
+    return tooClose;
+}
+
 /* --------------------------------------------------------------- FP64 physics */
 
 static inline void pair_force(const ref_md_params* p, const double* xi, const double* xj,

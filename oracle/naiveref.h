@@ -128,6 +128,24 @@ typedef struct ref_compat_sim {
 int ref_compat_simulate(const ref_compat_sim* spec, int32_t n, float* x, float* v, float* force,
                         const float* mass, const float* q, float* poslog);
 
+/* collect_objects (MDInput.jl:305-369) with the library's counter-based
+ * stream (layout matches nd_collector); unique_pairs_prune's loop run
+ * literally.  Returns the number of atoms filled with Inf. */
+typedef struct ref_collector {
+    int64_t objectnumber;
+    float min_dim[3];
+    float max_dim[3];
+    float temperature;
+    int32_t randomvelocity;
+    float minmass;
+    float maxmass;
+    float minimumdistance;
+    float mincharge;
+    float maxcharge;
+} ref_collector;
+int64_t ref_collect_objects(const ref_collector* cl, uint64_t seed, float* x, float* v, float* m,
+                            float* q);
+
 int64_t ref_brute_pairs(const float* xyz, int32_t n, float r, int32_t criterion, int32_t* pi,
                         int32_t* pj, float* pd, int64_t cap);
 

@@ -43,6 +43,14 @@ class RefCompatSim(ctypes.Structure):
                 ("velocity_dampening", ctypes.c_float)]
 
 
+class RefCollector(ctypes.Structure):
+    _fields_ = [("objectnumber", ctypes.c_int64), ("min_dim", ctypes.c_float * 3),
+                ("max_dim", ctypes.c_float * 3), ("temperature", ctypes.c_float),
+                ("randomvelocity", ctypes.c_int32), ("minmass", ctypes.c_float),
+                ("maxmass", ctypes.c_float), ("minimumdistance", ctypes.c_float),
+                ("mincharge", ctypes.c_float), ("maxcharge", ctypes.c_float)]
+
+
 class RefMDParams(ctypes.Structure):
     _fields_ = [("sigma", ctypes.c_double), ("epsilon", ctypes.c_double),
                 ("coulomb_k", ctypes.c_double), ("cutoff", ctypes.c_double),
@@ -112,6 +120,9 @@ def lib():
             L.ref_compat_simulate.argtypes = [ctypes.POINTER(RefCompatSim), ctypes.c_int32, f32p,
                                               f32p, f32p, f32p, f32p, f32p]
             L.ref_compat_simulate.restype = ctypes.c_int
+            L.ref_collect_objects.argtypes = [ctypes.POINTER(RefCollector), ctypes.c_uint64, f32p,
+                                              f32p, f32p, f32p]
+            L.ref_collect_objects.restype = ctypes.c_int64
             L.ref_brute_pairs.argtypes = [f32p, ctypes.c_int32, ctypes.c_float, ctypes.c_int32,
                                           i32p, i32p, f32p, ctypes.c_int64]
             L.ref_brute_pairs.restype = ctypes.c_int64
@@ -266,6 +277,24 @@ def compat_simulate(x, v, force, mass, charge, min_dim, max_dim, temperature, ob
                                    _p(m, ctypes.c_float), _p(q, ctypes.c_float),
                                    _p(log_arr, ctypes.c_float) if log else None)
     return x, v, f, log_arr, st
+
+
+def collect_objects(seed, objectnumber, min_dim, max_dim, temperature, randomvelocity, minmass,
+                    maxmass, minimumdistance, mincharge, maxcharge):
+    """collect_objects (MDInput.jl:305-369) with the library's seeded stream:
+    (x, v, mass, charge, number of atoms filled with Inf)."""
+    n = int(objectnumber)
+    cl = RefCollector(n, (ctypes.c_float * 3)(*min_dim), (ctypes.c_float * 3)(*max_dim),
+                      temperature, int(bool(randomvelocity)), minmass, maxmass, minimumdistance,
+                      mincharge, maxcharge)
+    x = np.zeros((n, 3), np.float32)
+    v = np.zeros((n, 3), np.float32)
+    m = np.zeros(n, np.float32)
+    q = np.zeros(n, np.float32)
+    cnt = lib().ref_collect_objects(ctypes.byref(cl), ctypes.c_uint64(seed), _p(x, ctypes.c_float),
+                                    _p(v, ctypes.c_float), _p(m, ctypes.c_float),
+                                    _p(q, ctypes.c_float))
+    return x, v, m, q, cnt
 
 
 def simd_leaf_traverse(t, r, apl):

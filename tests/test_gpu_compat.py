@@ -97,7 +97,7 @@ def test_compat_simulate_domain_error(nd, oracle):
 
 def test_compat_simulate_global_form_and_log_chunks(nd, oracle, monkeypatch):
     # the Coulomb levels with accumulators in global memory (the form for
-    # more than 25,600 atoms) and a device log flushed every 4 frames
+    # more than about 20,000 atoms) and a device log flushed every 4 frames
     monkeypatch.setenv("NAIVEGPU_COMPAT_GLOBAL", "1")
     monkeypatch.setenv("NAIVEGPU_COMPAT_LOG_CHUNK", "4")
     sys, log, err, (xo, vo, fo, logo, st) = _run_both(nd, oracle, 300, 31, 1, 14, 1.0, 0.01,
@@ -117,3 +117,46 @@ def test_compat_simulate_rejects(nd):
         nd.simulate_compat_(sys, nd.SimSpec(duration=3, stepwidth=0.5), clct)
     with pytest.raises(nd.NDError):
         nd.simulate_compat_(sys, nd.SimSpec(duration=-1, stepwidth=1), clct)
+
+
+COLLECT = [
+    # objectnumber, seed, temperature, random velocities, minimumdistance
+    (1, 41, 0.01, False, 0.0001),
+    (2, 42, 0.01, True, 0.0001),
+    (1000, 43, 0.01, False, 0.0001),   # the reference scripts' collector
+    (5000, 44, 0.05, True, 0.02),      # a few hundred atoms pruned
+    (20000, 45, 0.5, True, 0.005),     # 79 velocity chunks
+]
+
+
+@pytest.mark.parametrize("case", COLLECT, ids=lambda c: f"n{c[0]}")
+def test_collect_objects_bit_exact(nd, oracle, case):
+    n, seed, T, rv, dmin = case
+    clct = nd.GenericRandomCollector(objectnumber=n, minDim=(0.0, -1.0, 0.0),
+                                     maxDim=(1.0, 1.0, 2.0), temperature=T, minimumdistance=dmin,
+                                     randomvelocity=rv, minmass=1.0, maxmass=5.0,
+                                     mincharge=-1e-9, maxcharge=1e-9)
+    sys = nd.collect_objects(clct, seed=seed)
+    x, v, m, q, cnt = oracle.collect_objects(seed, n, (0.0, -1.0, 0.0), (1.0, 1.0, 2.0), T, rv,
+                                             1.0, 5.0, dmin, -1e-9, 1e-9)
+    assert np.array_equal(_bits(sys.position), _bits(x))
+    assert np.array_equal(_bits(sys.velocity), _bits(v))
+    assert np.array_equal(_bits(sys.mass), _bits(m))
+    assert np.array_equal(_bits(sys.charge), _bits(q))
+    assert sys.pruned == cnt
+    if n == 5000:
+        assert cnt > 100
+
+
+def test_collect_then_simulate_compat(nd, oracle):
+    # a legacy script end to end: collect_objects, then simulate! as written
+    clct = nd.GenericRandomCollector(objectnumber=400, minDim=(0.0, 0.0, 0.0),
+                                     maxDim=(1.0, 1.0, 1.0), temperature=0.01,
+                                     minimumdistance=0.0001, minmass=1.0, maxmass=5.0,
+                                     mincharge=-1e-9, maxcharge=1e-9)
+    sys = nd.collect_objects(clct, seed=7)
+    x0, v0 = sys.position.astype(np.float32), sys.velocity.astype(np.float32)
+    log = nd.simulate_compat_(sys, nd.SimSpec(duration=12, stepwidth=1, vDamp=1.0), clct)
+    ref = oracle.compat_simulate(x0, v0, np.zeros((400, 3)), sys.mass, sys.charge, BOX[0], BOX[1],
+                                 0.01, 400, 1, 12, 1.0)
+    assert np.array_equal(_bits(log), _bits(ref[3]))

@@ -220,6 +220,36 @@ def test_compat_simulate_oracle(oracle):
     assert np.allclose(v1, v0 * np.sqrt(0.5 / Ti), rtol=1e-6, atol=0)
 
 
+def test_collect_objects_oracle(oracle):
+    # ranges, the velocity formulas and unique_pairs_prune's rule, by hand
+    box = ((0.0, 0.0, 0.0), (1.0, 2.0, 3.0))
+    x, v, m, q, cnt = oracle.collect_objects(5, 3000, box[0], box[1], 0.01, False, 1.0, 5.0,
+                                             0.02, -1e-9, 1e-9)
+    fin = np.isfinite(x).all(axis=1)
+    assert cnt == int((~fin).sum()) > 0 and fin[-1] and fin[-2]
+    assert np.all((m >= 1) & (m < 5)) and np.all((q >= -1e-9) & (q < 1e-9))
+    assert np.all(x[fin] >= 0) and np.all(x[fin] < np.array([1, 2, 3], np.float32))
+    T, N = np.float32(0.01), np.float32(3000)
+    assert np.array_equal(v, np.repeat(((T / N * np.float32(3) * N) * np.float32(1) / m)[:, None],
+                                       3, axis=1))
+    # pruned exactly when a later atom other than the last lies within 0.02
+    _, _, _, _, c0 = oracle.collect_objects(5, 3000, box[0], box[1], 0.01, False, 1.0, 5.0, 0.0,
+                                            -1e-9, 1e-9)
+    x0 = oracle.collect_objects(5, 3000, box[0], box[1], 0.01, False, 1.0, 5.0, 0.0, -1e-9,
+                                1e-9)[0]
+    assert c0 == 0 and np.array_equal(x0[fin], x[fin])
+    d = x0[:, None, :] - x0[None, :, :]
+    dist = np.sqrt((d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2])
+    close = (dist < np.float32(0.02)) & np.triu(np.ones((3000, 3000), bool), 1)
+    close[:, -1] = False
+    assert np.array_equal(close.any(axis=1), ~fin)
+    # random split: each component's v m / (3 N T) sums to 1
+    _, vr, mr, _, _ = oracle.collect_objects(6, 1000, box[0], box[1], 0.5, True, 1.0, 5.0, 0.0,
+                                             0.0, 0.0)
+    share = (vr.astype(np.float64) * mr[:, None]) / (3 * 1000 * 0.5)
+    assert np.allclose(share.sum(axis=0), 1.0, atol=1e-5)
+
+
 def test_golden_vectors(oracle):
     for c in golden_cases():
         x = np.array(c["position"], np.float32)
