@@ -252,7 +252,7 @@ __device__ __forceinline__ void cp_async16(float* dst, const float* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(src) : "memory");
 }
 
-constexpr int kRingThreads = 256;
+constexpr int kRingThreads = 128;  // fewest warps paying the per-level overhead (measured: 128 of 32-1024)
 constexpr int kLevelBatch = 8;  // pairs of a level per thread with their loads in flight
 
 // The recurrence, accumulators in shared memory, the pair terms of the next
