@@ -487,8 +487,34 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
         e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shb);
         if (e != cudaSuccess) return cuda_fail(c, e, "compat simulate smem");
     }
-    // force_coulomb! and force_lennardjones! over the current list
-    auto forces = [&]() {
+    // Two chains per step, both from the list of the previous step's
+    // positions: force_coulomb! (update_pairslist!'s Coulomb terms, then the
+    // levels on one SM) on the context's stream, and force_lennardjones!
+    // (the LJ terms of update_pairslist!, then the row sums) on a side stream
+    // over the other SMs.  The step kernel waits for both; the side chain of
+    // the next step waits for the step kernel.
+    struct Side {
+        cudaStream_t s2 = nullptr;
+        cudaEvent_t moved = nullptr, lj = nullptr;
+        ~Side() {
+            if (s2) cudaStreamSynchronize(s2);
+            if (moved) cudaEventDestroy(moved);
+            if (lj) cudaEventDestroy(lj);
+            if (s2) cudaStreamDestroy(s2);
+        }
+    } side;
+    e = cudaStreamCreateWithFlags(&side.s2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&side.moved, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&side.lj, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(c, e, "compat simulate streams");
+    cudaStream_t s2 = side.s2;
+    auto coulomb_terms = [&]() {
+        if (n > 1) {
+            k_cs_cterms<<<nlev, 256, 0, s>>>(dx, dq, n, ring ? stride : 0, cterm);
+            c->launches++;
+        }
+    };
+    auto coulomb = [&]() {
         if (ring == 8)
             k_cs_coulomb_ring<8><<<1, kRingThreads, shb, s>>>(cterm, n, stride, cf);
         else if (ring == 4)
@@ -497,16 +523,17 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
             k_cs_coulomb_ring<3><<<1, kRingThreads, shb, s>>>(cterm, n, stride, cf);
         else
             k_cs_coulomb_global<<<1, 1024, 0, s>>>(cterm, n, cf);
-        k_cs_lj<<<(unsigned)cdiv(n, 32), 32, 0, s>>>(ljt, near, n, ljthr, ljall);
-        c->launches += 2;
+        c->launches++;
     };
-    // update_pairslist!: the list's LJ terms and Coulomb terms
-    auto pairs = [&]() {
-        if (n > 1) {
-            k_cs_pairs<<<n - 1, 256, 0, s>>>(dx, n, 0.01f, ljt, near);
-            k_cs_cterms<<<nlev, 256, 0, s>>>(dx, dq, n, ring ? stride : 0, cterm);
-            c->launches += 2;
-        }
+    // after the positions of stream `after` moved: the LJ terms and sums on s2
+    auto lj_chain = [&](cudaStream_t after) -> cudaError_t {
+        cudaError_t ee = cudaEventRecord(side.moved, after);
+        if (ee == cudaSuccess) ee = cudaStreamWaitEvent(s2, side.moved, 0);
+        if (ee != cudaSuccess) return ee;
+        if (n > 1) k_cs_pairs<<<n - 1, 256, 0, s2>>>(dx, n, 0.01f, ljt, near);
+        k_cs_lj<<<(unsigned)cdiv(n, 32), 32, 0, s2>>>(ljt, near, n, ljthr, ljall);
+        c->launches += n > 1 ? 2 : 1;
+        return cudaEventRecord(side.lj, s2);
     };
     const float dt = (float)spec->stepwidth;
     const float dt2 = (float)(int64_t)((uint64_t)spec->stepwidth * (uint64_t)spec->stepwidth);
@@ -516,7 +543,9 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
     const float cT = 2.0f / ((3.0f * (float)spec->objectnumber) * 1.0f);
     const unsigned ga = (unsigned)cdiv(n, 256);
 
-    pairs();  // pairslist = unique_pairs(position)
+    // pairslist = unique_pairs(position)
+    coulomb_terms();
+    if ((e = lj_chain(s)) != cudaSuccess) return cuda_fail(c, e, "compat simulate streams");
     int64_t pending = 0;  // frames in the device chunk not yet copied out
     int64_t first = 1;    // step of the chunk's first frame
     auto flush = [&]() -> nd_status {
@@ -534,12 +563,17 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
         // force_coulomb! runs twice per step on the same list and charges: one
         // evaluation gives both results; so does force_lennardjones!'s pass
         // over the whole list and its threshold_pairs part
-        forces();
+        coulomb();
         float* frame = poslog ? dlog + pending * (int64_t)n3 : nullptr;
+        e = cudaStreamWaitEvent(s, side.lj, 0);
+        if (e != cudaSuccess) return cuda_fail(c, e, "compat simulate streams");
         k_cs_step<<<ga, 256, 0, s>>>(dx, dv, dF, dFn, dm, ljthr, ljall, cf, n, dt, dt2, lo, hi,
                                       frame);
-        c->launches += 2;
-        pairs();  // update_pairslist!
+        c->launches++;
+        if (step < spec->duration) {  // update_pairslist! (unused after the last step)
+            coulomb_terms();
+            if ((e = lj_chain(s)) != cudaSuccess) return cuda_fail(c, e, "compat simulate streams");
+        }
         if (step % 10 == 0) {
             k_cs_rescale<<<1, 1024, 0, s>>>(dv, dm, n, cT, spec->temperature,
                                              spec->velocity_dampening, term, c->d_err);
