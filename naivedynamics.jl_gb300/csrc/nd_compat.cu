@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) k_cs_coulomb_ring(const float
 // The same recurrence with the accumulators in global memory (any n): the
 // block's own writes are visible to it after each barrier.  The first item of
 // the next level is loaded ahead.
-__global__ void __launch_bounds__(1024, 1) k_cs_coulomb_global(const float* __restrict__ cterm,
+__global__ void __launch_bounds__(kRingThreads, 1) k_cs_coulomb_global(const float* __restrict__ cterm,
                                                                int32_t n, float* F) {
     for (int32_t k = threadIdx.x; k < n; k += blockDim.x) F[k] = 0.0f;
     __syncthreads();
@@ -522,7 +522,7 @@ nd_status compat_simulate(Ctx* c, const nd_compat_sim* spec, int32_t n, float* x
         else if (ring == 3)
             k_cs_coulomb_ring<3><<<1, kRingThreads, shb, s>>>(cterm, n, stride, cf);
         else
-            k_cs_coulomb_global<<<1, 1024, 0, s>>>(cterm, n, cf);
+            k_cs_coulomb_global<<<1, kRingThreads, 0, s>>>(cterm, n, cf);
         c->launches++;
     };
     // after the positions of stream `after` moved: the LJ terms and sums on s2
