@@ -680,8 +680,9 @@ __device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const
 
 // Packed single precision (sm_100 and later): one instruction applies the
 // operation to both halves of a 64-bit register pair, so two list entries
-// share each instruction of the pair arithmetic.  Every half is rounded as
-// the scalar instruction would round it.
+// share each instruction of the pair arithmetic.  The forces are held to a
+// tolerance against FP64, not to the scalar form's bits: a packed sequence
+// can end an ulp away from the scalar one (measured on distance tests).
 __device__ __forceinline__ uint64_t pk2(float a, float b) {
     uint64_t r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
