@@ -327,7 +327,8 @@ nd_status nd_compat_simulate(nd_ctx* ctx, const nd_compat_sim* spec, int32_t n, 
  * be NULL) receives their number.  Draws come from a counter-based splitmix64
  * stream of `seed` instead of Julia's global RNG, so values match the
  * reference's distributions, not its draws.  position, velocity: N x 3
- * Float32 out; mass, charge: N Float32 out; N = objectnumber <= 2^28.
+ * Float32 out; mass, charge: N Float32 out; N = objectnumber <= 2^20 (the
+ * pruning compares all pairs, as the reference does).
  */
 typedef struct nd_collector {
     int64_t objectnumber;

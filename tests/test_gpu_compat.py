@@ -148,6 +148,13 @@ def test_collect_objects_bit_exact(nd, oracle, case):
         assert cnt > 100
 
 
+def test_collect_objects_rejects(nd):
+    for n in (0, (1 << 20) + 1):
+        clct = nd.GenericRandomCollector(objectnumber=n, minDim=BOX[0], maxDim=BOX[1])
+        with pytest.raises(nd.NDError):
+            nd.collect_objects(clct)
+
+
 def test_collect_then_simulate_compat(nd, oracle):
     # a legacy script end to end: collect_objects, then simulate! as written
     clct = nd.GenericRandomCollector(objectnumber=400, minDim=(0.0, 0.0, 0.0),
