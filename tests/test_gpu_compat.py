@@ -85,6 +85,26 @@ def test_compat_simulate_bit_exact(nd, oracle, case):
         assert np.any(sys.force != 0)
 
 
+def test_compat_simulate_offset_box(nd, oracle):
+    # walls at negative and unequal coordinates, stepwidth 3 (dt^2 = 9)
+    lo, hi = (-2.0, -0.5, 1.0), (-1.0, 0.75, 1.5)
+    rng = np.random.default_rng(77)
+    n = 333
+    x = (np.array(lo) + rng.random((n, 3)) * (np.array(hi) - np.array(lo))).astype(np.float32)
+    v = rng.uniform(-0.01, 0.01, (n, 3)).astype(np.float32)
+    m = rng.uniform(1.0, 5.0, n).astype(np.float32)
+    q = rng.uniform(-0.1, 0.1, n).astype(np.float32)
+    sys = nd.GenericObjectCollection(x, v, mass=m, charge=q)
+    clct = nd.GenericRandomCollector(objectnumber=n, minDim=lo, maxDim=hi, temperature=0.02)
+    log = nd.simulate_compat_(sys, nd.SimSpec(duration=13, stepwidth=3, vDamp=0.7), clct)
+    xo, vo, fo, logo, st = oracle.compat_simulate(x, v, np.zeros((n, 3)), m, q, lo, hi, 0.02, n,
+                                                  3, 13, 0.7)
+    assert st == 0
+    assert np.array_equal(_bits(log), _bits(logo))
+    assert np.array_equal(_bits(sys.velocity), _bits(vo))
+    assert np.array_equal(_bits(sys.force), _bits(fo))
+
+
 def test_compat_simulate_domain_error(nd, oracle):
     # gamma = 3 with Tf far below Ti: 1 + 3 (Tf / Ti - 1) < 0 at step 10
     sys, log, err, (xo, vo, fo, logo, st) = _run_both(nd, oracle, 64, 21, 1, 30, 3.0, 1e-9,
@@ -126,6 +146,8 @@ COLLECT = [
     (1000, 43, 0.01, False, 0.0001),   # the reference scripts' collector
     (5000, 44, 0.05, True, 0.02),      # a few hundred atoms pruned
     (20000, 45, 0.5, True, 0.005),     # 79 velocity chunks
+    (256, 46, 0.1, True, 0.05),        # one full velocity chunk
+    (257, 47, 0.1, True, 0.05),        # a second chunk of one atom
 ]
 
 
