@@ -871,14 +871,29 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         for (; s < cnt; ++s)
             accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), pk, fx, fy, fz, ue);
     } else {
-        // slice `part` of the list, the next index loaded ahead
-        int32_t li = part < cnt ? L[(int64_t)part * kBlock] : 0;
-        for (int32_t s = part; s < cnt; s += TPA) {
-            const int32_t sn = s + TPA;
-            const int32_t next = sn < cnt ? L[(int64_t)sn * kBlock] : 0;
-            accum_pair<COUL, MODE == 1>(ri, fetch(li), pk, fx, fy, fz, ue);
-            li = next;
+        // slice `part` of the list (entries part, part + TPA, ..., in that
+        // order): four indices loaded ahead while the previous four are computed
+        int32_t li[4] = {0, 0, 0, 0};
+        auto load4 = [&](int32_t s0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int32_t sk = s0 + k * TPA;
+                li[k] = sk < cnt ? L[(int64_t)sk * kBlock] : 0;
+            }
+        };
+        int32_t s = part;
+        if (s < cnt) load4(s);
+        for (; s + 3 * TPA < cnt; s += 4 * TPA) {
+            int4 rj[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
+            load4(s + 4 * TPA);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue);
         }
+        // at most three entries left, their indices already loaded
+        for (int k = 0; s < cnt && k < 4; s += TPA, ++k)
+            accum_pair<COUL, MODE == 1>(ri, fetch(li[k]), pk, fx, fy, fz, ue);
         __shared__ float spart[TPA > 1 ? TPA - 1 : 1][4][kBlock];
         if (part > 0) {
             spart[part - 1][0][tid] = fx;
