@@ -25,8 +25,9 @@
 // LJ: each atom's additions are independent of other atoms' -- the pairs are
 // sorted by i (stable, so each atom keeps its list order) and one thread per
 // atom adds its run.  Coulomb: every update reads the result of earlier ones
-// through force[i] and force[j]; the recurrence runs on one thread in list
-// order (no parallel form reproduces its roundings).
+// through force[i] and force[j]; for an arbitrary list the recurrence runs on
+// one thread in list order, for the all-pairs order of unique_pairs it splits
+// into levels of independent pairs (compat_simulate).
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -203,8 +204,8 @@ __global__ void k_cs_lj(const double* __restrict__ ljt, const unsigned char* __r
 //
 // The pair terms k q_i q_j / d^2 do not depend on the recurrence: they are
 // computed in parallel beforehand and stored level by level (level s at
-// level_off(s), its pairs by increasing i), so each level is one contiguous,
-// coalesced segment.
+// s * stride for the shared-memory form, at level_off(s) when packed; its
+// pairs by increasing i), so each level is one contiguous, coalesced segment.
 
 __host__ __device__ inline int32_t level_lo(int32_t s, int32_t n) { return max(0, s - (n - 1)); }
 __host__ __device__ inline int32_t level_count(int32_t s, int32_t n) {
