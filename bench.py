@@ -37,9 +37,26 @@ UNION_NAMES = {0: "blocks", 1: "tree"}
 SEED = 0x4E440002
 METRIC = "LJ+Coulomb atom-steps/s @262k (FP32 forces, FP64 x/v, rebuild every 10)"
 UNIT = "atom-steps/s"
-WORKLOAD = ("lj_coulomb_262144: N=262144 uniform cube side 68 (min separation 0.8), q=+/-1, "
-            "sigma=eps=1, k=1, r_c=2.5, skin >= 0.3 (autotuned), dt=1e-3, rebuild every 10, "
-            "100 MD steps per bench step")
+WORKLOAD = ("lj_coulomb_262144: N=262144, cube side 68, min separation 0.8, q=+/-1, "
+            "sigma=eps=1, k=1, r_c=2.5, dt=1e-3, rebuild every 10")
+# the workload as both arms report it (the arms' own settings are reported
+# beside it: "engine" for the GPU arm, "reference_path" for the CPU arm)
+CONFIG = {"workload": WORKLOAD, "n_atoms": N_ATOMS, "side": SIDE, "cutoff": 2.5, "dt": 1e-3,
+          "rebuild_every": REBUILD,
+          "l2": "GPU arm: 512 MB buffer written before every timed step (outside the events); "
+                "CPU arm: not applicable"}
+REF_SKIN = 0.3
+
+
+def _plain(o):
+    """JSON-ready copy: numpy scalars and arrays as Python numbers and lists."""
+    if isinstance(o, dict):
+        return {k: _plain(v) for k, v in o.items()}
+    if isinstance(o, (list, tuple)):
+        return [_plain(v) for v in o]
+    if hasattr(o, "tolist"):
+        return o.tolist()
+    return o
 
 
 def _md_params(nd, order=None):
@@ -128,49 +145,70 @@ def _ncu_traffic():
         return None
 
 
-def cpu_baseline_sample(steps=10):
-    """The reference path on the host cores: the oracle restatement of
-    leafbuild_traverse_bvh (reference Morton order) rebuilt every 10 steps at
-    r_c + skin, FP64 LJ+Coulomb forces over that list, KDK velocity Verlet."""
-    import naivedynamics as nd
-    from oracle import naiveref as R
-    x, v, q = nd.synth.lj_system(SEED, N_ATOMS, SIDE, 0.8, charges=True)
+def _ref_session(R):
+    """The reference path on the host cores, from the oracle library alone:
+    inputs from its own generators (the GPU arm's inputs bit for bit), then the
+    oracle restatement of leafbuild_traverse_bvh (reference Morton order) at
+    r_c + skin, FP64 LJ + Coulomb over that list and KDK velocity Verlet, as a
+    session whose first list and forces are built at creation."""
+    x, v, q = R.synth_lj_system(SEED, N_ATOMS, SIDE, 0.8, charges=True)
     p = R.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(SIDE,) * 3, dt=1e-3)
+    return R.MDSession(p, x, v, q, rebuild=REBUILD, skin=REF_SKIN, apl=4,
+                       order=R.REF_ORDER_REFERENCE)
+
+
+def cpu_baseline_sample(windows=2):
+    """Steady-state windows of the CPU reference path: each window is REBUILD
+    MD steps with one leaf-BVH build and REBUILD force evaluations."""
+    from oracle import naiveref as R
+    sess = _ref_session(R)
+    sess.steps(REBUILD)  # one untimed window
     t0 = time.perf_counter()
-    R.md_run_bvh(p, x, v, q, steps=steps, rebuild=REBUILD, skin=0.3, apl=4,
-                 order=R.REF_ORDER_REFERENCE)
+    sess.steps(REBUILD * windows)
     dt = time.perf_counter() - t0
-    return {"value": N_ATOMS * steps / dt, "unit": UNIT, "cores": R.num_threads(),
+    sess.close()
+    return {"value": N_ATOMS * REBUILD * windows / dt, "unit": UNIT, "cores": R.num_threads(),
             "kind": "port",
-            "sample": f"{N_ATOMS} atoms x {steps} MD steps (initial leaf-BVH build + 1 rebuild, "
-                      f"reference Morton order, OpenMP over {R.num_threads()} threads), {dt:.2f} s"}
+            "sample": f"{N_ATOMS} atoms x {windows} steady-state windows of {REBUILD} MD steps "
+                      f"(one leaf-BVH build in reference Morton order per window, FP64 forces, "
+                      f"OpenMP over {R.num_threads()} threads), {dt:.2f} s"}
 
 
 def run_reference(args):
+    """The CPU reference arm: the oracle port of the reference path (Julia is
+    not installed here or on the GPU machine) on all host threads, one
+    steady-state window of REBUILD MD steps per bench step.  Loads the oracle
+    library only."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    import naivedynamics as nd  # noqa: F401  (synthetic inputs only)
-    samples = []
+    from oracle import naiveref as R
+    sess = _ref_session(R)
+    times = []
     for k in range(args.warmup + args.steps):
-        s = cpu_baseline_sample(steps=10)
+        t0 = time.perf_counter()
+        sess.steps(REBUILD)
         if k >= args.warmup:
-            samples.append(s)
-    total_as = sum(N_ATOMS * 10 for _ in samples)
-    total_t = sum(N_ATOMS * 10 / s["value"] for s in samples)
-    value = total_as / total_t
+            times.append(time.perf_counter() - t0)
+    sess.close()
+    total_t = sum(times)
+    value = N_ATOMS * REBUILD * len(times) / total_t
+    sample = (f"{N_ATOMS} atoms, {len(times)} steady-state windows of {REBUILD} MD steps, each "
+              f"one leaf-BVH build (reference Morton order, r_c + skin {REF_SKIN}) and "
+              f"{REBUILD} FP64 force evaluations, OpenMP over {R.num_threads()} threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * total_t / len(samples), "higher_is_better": True,
+            "ms_per_step": 1e3 * total_t / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD.replace("100 MD steps", "10 MD steps"),
-                       "reference_path": "oracle port of leafbuild_traverse_bvh + FP64 forces "
-                                         "+ KDK (reference Julia not installable: no julia)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": samples[0]["cores"],
-                             "kind": "port", "sample": samples[0]["sample"]},
+            "config": CONFIG,
+            "reference_path": ("oracle port of leafbuild_traverse_bvh + FP64 forces + KDK; "
+                               f"{REBUILD} MD steps per bench step (reference Julia not "
+                               "installable: no julia)"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": R.num_threads(),
+                             "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(_plain(line)), flush=True)
 
 
 ENSEMBLE_STEPS = 200
@@ -213,6 +251,7 @@ def batched_leg(nd, ctx, ext, flush):
 
     bat = nd.Ensemble(tuned, table, e["x"], e["v"], ctx=ctx)
     _, _, f_bat = bat.get()
+    pe_bat0, _ = bat.energies()
     bat.run(REBUILD)  # the opening window (its own captured graph)
     bat.sync()
     l0 = ctx.launch_count()
@@ -220,7 +259,24 @@ def batched_leg(nd, ctx, ext, flush):
     t_bat = timed(lambda: bat.run(ENSEMBLE_STEPS))
     bat_diag = bat.diagnostics()
     bat_launches = ctx.launch_count() - l0 + bat_diag["body_kernels"] - d0["body_kernels"]
+    x_end, _, f_end = bat.get()
+    pe_end, _ = bat.energies()
     bat.close()
+    # every system's forces and potential energy against the FP64 oracle run
+    # on that system alone, at the input and after the timed steps
+    from oracle import naiveref as R
+    pa = l2 = er = 0.0
+    for k in range(len(e["n_atoms"])):
+        sl = slice(int(off[k]), int(off[k + 1]))
+        pk = R.md_params(sigma=float(e["sigma"][k]), epsilon=float(e["epsilon"][k]), cutoff=2.5,
+                         box_lo=tuple(e["box_lo"][k]), box_hi=tuple(e["box_hi"][k]), dt=1e-3)
+        for xx, ff, pe in ((e["x"][sl], f_bat[sl], pe_bat0[k]), (x_end[sl], f_end[sl], pe_end[k])):
+            g, u, _ = R.forces(pk, xx)
+            a_, b_ = _force_errors(ff, g)
+            pa, l2, er = max(pa, a_), max(l2, b_), max(er, abs(pe - u) / abs(u))
+    errors = {"force_err_per_atom": pa, "force_err_l2": l2, "energy_rel": er,
+              "over": f"{len(e['n_atoms'])} systems, input and after {ENSEMBLE_STEPS + REBUILD} "
+                      "steps", "bar": 1e-5}
 
     plain = []
     f_err = 0.0
@@ -248,7 +304,7 @@ def batched_leg(nd, ctx, ext, flush):
     v_bat = work / t_bat
     v_plain = work / t_plain
     n_all = int(e_all["n_atoms"].sum())
-    return {"metric": "ensemble atom-steps/s, batched vs plain", "unit": UNIT,
+    return {"metric": "ensemble atom-steps/s, batched vs plain", "unit": UNIT, "errors": errors,
             "workload": (f"ensemble_512: {len(e_all['n_atoms'])} LJ systems, {n_all} atoms "
                          f"(N_s {int(e_all['n_atoms'].min())}..{int(e_all['n_atoms'].max())}), "
                          "rho U[0.6,0.9], sigma U[0.9,1.1], eps U[0.8,1.2], r_c 2.5, "
@@ -356,8 +412,34 @@ def plain_leg(nd, ctx, ext, flush):
             times.append(a.elapsed_time(b))
     d = eng.diagnostics()
     eng.close()
+    # errors against FP64: forces at the input and after 100 steps, the
+    # 100-step energy drift of both (truncated LJ: energy jumps where pairs
+    # cross r_c, in both)
+    from oracle import naiveref as R
+    pr = R.md_params(cutoff=2.5, box_hi=(side,) * 3, dt=1e-3)
+    e = nd.MDEngine(p, x, v, ctx=ctx)
+    _, _, f0 = e.get()
+    pe0, ke0 = e.energy()
+    e.run(steps)
+    x1, v1, f1 = e.get()
+    pe1, ke1 = e.energy()
+    e.close()
+    g0, u0, _ = R.forces(pr, x)
+    xr, vr, _ = R.md_run(pr, x, v, steps=steps)
+    g1, u1, _ = R.forces(pr, x1)
+    ur, _, _ = R.forces(pr, xr)
+    kr = 0.5 * float((vr ** 2).sum())
+    ke_0 = 0.5 * float((v ** 2).sum())
+    pa = max(_force_errors(f0, g0)[0], _force_errors(f1, g1)[0])
+    l2 = max(_force_errors(f0, g0)[1], _force_errors(f1, g1)[1])
+    drift = abs((pe1 + ke1) - (pe0 + ke0)) / abs(pe0 + ke0)
+    drift64 = abs((ur + kr) - (u0 + ke_0)) / abs(u0 + ke_0)
+    errors = {"force_err_per_atom": pa, "force_err_l2": l2,
+              "energy_rel": max(abs(pe0 - u0) / abs(u0), abs(pe1 - u1) / abs(u1)),
+              "energy_drift_100_steps": drift, "energy_drift_100_steps_fp64": drift64,
+              "max_dx_vs_fp64_100_steps": float(np.abs(x1 - xr).max()), "bar": 1e-5}
     ms = float(np.median(times))
-    out = {"metric": "plain LJ atom-steps/s @4096", "unit": UNIT,
+    out = {"metric": "plain LJ atom-steps/s @4096", "unit": UNIT, "errors": errors,
            "workload": "plain_lj_4096: N=4096 uniform cube side 17 (min separation 0.8), "
                        "sigma=eps=1, r_c 2.5, skin >= 0.3 (autotuned), dt 1e-3, rebuild every "
                        "10, 100 steps",
@@ -367,8 +449,6 @@ def plain_leg(nd, ctx, ext, flush):
                      "union_search": UNION_NAMES[p.union_search],
                      "refit_check_every": max(p.refit_check_every, 1)},
            "early_refits": d["early_refits"], "skin_violations": d["skin_violations"]}
-    from oracle import naiveref as R
-    pr = R.md_params(cutoff=2.5, box_hi=(side,) * 3, dt=1e-3)
     t0 = time.perf_counter()
     R.md_run_bvh(pr, x, v, steps=steps, rebuild=REBUILD, skin=0.3, apl=4,
                  order=R.REF_ORDER_REFERENCE)
@@ -621,24 +701,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math, f64 state",
         "data": "synthetic (seeded splitmix64 generators)",
-        "config": {"workload": WORKLOAD, "n_atoms": N_ATOMS, "md_steps_per_step": MD_PER_STEP,
-                   "rebuild_every": REBUILD,
-                   "atom_order": f"3-D Hilbert, re-sorted every {params.resort_every}th rebuild, "
-                                 "refit between",
-                   "tuned": {"skin": params.skin, "atomsperleaf": params.atomsperleaf,
-                             "resort_every": params.resort_every,
-                             "stage_policy": params.stage_policy,
-                             "union_search": UNION_NAMES[params.union_search],
-                             "refit_check_every": max(params.refit_check_every, 1),
-                             "autotune_s": round(tune_s, 2)},
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
-                   "l2": "512 MB buffer written before every timed step (outside the events)",
-                   "neighbours_per_atom": round(nbr, 2),
-                   "skin_violations": diag["skin_violations"],
-                   "early_refits_timed": early,
-                   "resorts_timed": diag["resorts"] - diag0["resorts"],
-                   "refits_timed": diag["refits"] - diag0["refits"],
-                   "wall_s_timed_region": round(wall, 4)},
+        "config": CONFIG,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
@@ -649,17 +712,41 @@ def run_gb300(args):
                 "h2d_bytes_per_step": int(x.nbytes + v.nbytes + q.nbytes),
                 "d2h_bytes_per_step": int(x.nbytes + v.nbytes + fh.numel() * 4),
                 "api": "nd_simulate (simulate!) with pinned host buffers"},
+        "engine": {"md_steps_per_step": MD_PER_STEP,
+                   "atom_order": f"3-D Hilbert, re-sorted every {params.resort_every}th rebuild, "
+                                 "refit between",
+                   "tuned": {"skin": params.skin, "atomsperleaf": params.atomsperleaf,
+                             "resort_every": params.resort_every,
+                             "stage_policy": params.stage_policy,
+                             "union_search": UNION_NAMES[params.union_search],
+                             "refit_check_every": max(params.refit_check_every, 1),
+                             "autotune_s": round(tune_s, 2)},
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
+                   "neighbours_per_atom": round(nbr, 2),
+                   "skin_violations": diag["skin_violations"],
+                   "early_refits_timed": early,
+                   "resorts_timed": diag["resorts"] - diag0["resorts"],
+                   "refits_timed": diag["refits"] - diag0["refits"],
+                   "wall_s_timed_region": round(wall, 4)},
     }
     clocks = clk.summary()
     if clocks:
         line["clocks"] = clocks
+    if diag["skin_violations"] > 0:
+        print(f"warning: {diag['skin_violations']} atom-steps ran on lists an atom had left by "
+              "more than skin/2", file=sys.stderr)
+    errors = {}
+    if rank == 0:
+        errors["lj_coulomb_262144"] = headline_errors(nd, eng, x, q)
     eng.close()
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample()
+    b = None
     if not args.no_batched:
         b = batched_leg(nd, ctx, ext, flush)  # every rank runs its share of the systems
-        if rank == 0:
-            line["batched"] = b
     if rank == 0 and not args.no_plain:
         line["plain_lj_4096"] = plain_leg(nd, ctx, ext, flush)
+        errors["plain_lj_4096"] = line["plain_lj_4096"].pop("errors")
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_leg(nd, ctx, ext, flush, steps=args.adjoint_steps,
                                       check_every=args.adjoint_check_every)
@@ -667,13 +754,50 @@ def run_gb300(args):
         line["ns_stress"] = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_compat:
         line["compat_simulate"] = compat_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline)
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(steps=10)
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        # the per-result errors and the batched result last, compact, so that
+        # the end of the line carries them
+        if b is not None:
+            errors["ensemble_512"] = b.pop("errors")
+        line["errors_vs_fp64"] = errors
+        if b is not None:
+            line["batched"] = b
+        print(json.dumps(_plain(line)), flush=True)
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _force_errors(f32, f64):
+    """(max_i |dF_i| / max(|F64_i|, 1e-3 rms|F64|), |dF|_2 / |F64|_2)."""
+    import numpy as np
+    df = np.linalg.norm(np.asarray(f32, np.float64) - f64, axis=1)
+    nf = np.linalg.norm(f64, axis=1)
+    floor = 1e-3 * np.sqrt(np.mean(nf ** 2))
+    return (float(np.max(df / np.maximum(nf, floor))),
+            float(np.linalg.norm(df) / np.linalg.norm(f64)))
+
+
+def headline_errors(nd, eng, x0, q):
+    """Force and energy errors of the headline engine against the FP64 oracle:
+    at the bench's input (a fresh engine with the same settings) and at the
+    state the timed steps left."""
+    from oracle import naiveref as R
+    p = R.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(SIDE,) * 3, dt=1e-3)
+    x1, _, f1 = eng.get()
+    pe1, _ = eng.energy()
+    f64, u64, _ = R.forces(p, x1, q)
+    pa1, l21 = _force_errors(f1, f64)
+    import numpy as np
+    e = nd.MDEngine(eng.params, x0, np.zeros_like(x0), q, ctx=eng.ctx)
+    _, _, f0 = e.get()
+    pe0, _ = e.energy()
+    e.close()
+    g64, v64, _ = R.forces(p, x0, q)
+    pa0, l20 = _force_errors(f0, g64)
+    return {"force_err_per_atom": max(pa0, pa1), "force_err_l2": max(l20, l21),
+            "energy_rel": max(abs(pe0 - v64) / abs(v64), abs(pe1 - u64) / abs(u64)),
+            "at": "input and end of the timed steps", "bar": 1e-5}
 
 
 def md_eager_leg(nd, ctx, union_search="blocks", check_every=3):
@@ -739,7 +863,7 @@ def run_only(args):
     else:
         out = stress_leg(nd, ctx, ext, flush, cpu=not args.no_cpu_baseline,
                          points=args.stress_points)
-    print(json.dumps(out), flush=True)
+    print(json.dumps(_plain(out)), flush=True)
     ctx.close()
 
 

@@ -178,7 +178,11 @@ nd_status nd_tree(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, int32_
  * (i, j, d) -- every unordered pair with d^2 < r^2 once -- into pi/pj/pd.
  * *count receives the number of pairs; if it exceeds capacity nothing is written
  * and ND_NEED_REALLOC is returned (call again with capacity >= *count, or with
- * capacity 0 to only count).  mode: ND_PAIRS_ORDERED / ND_PAIRS_UNORDERED.
+ * capacity 0 to only count).  mode: ND_PAIRS_ORDERED (the order the reference
+ * emits on one thread) or ND_PAIRS_UNORDERED (the same pairs in the order the
+ * GPU produces them: the two-phase warp-cooperative emission, which needs
+ * atomsperleaf == 4; with any other leaf width an unordered request is served
+ * by the ordered emission).
  */
 nd_status nd_leaf_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, int32_t order,
                         int32_t mode, int32_t* pi, int32_t* pj, float* pd, int64_t capacity,
@@ -217,8 +221,34 @@ nd_status nd_atom_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, 
                         int32_t* pi, int32_t* pj, float* pd, int64_t capacity, int64_t* count);
 
 /*
- * The leaf pair-list pipeline of nd_leaf_pairs_dev (same kernels, same results,
- * bit for bit) for callers that cannot allocate device memory: code running
+ * gpubvh_neighborlist!(neighborlist, treedata, spec, backend) (ext/NaiveKA.jl:
+ * 597-636; declared at src/PkgExtensions.jl:67): the pair list of new
+ * positions from a kept tree.  index and morton_code are the kept treedata's
+ * mortonpositions (1-based original index and code of each sorted slot, as
+ * nd_tree returns them); xyz holds the new positions in the caller's order.
+ * The order and the sorted codes are reused, so the build reproduces the kept
+ * topology with the boxes of the new positions -- the refit that TreeData!
+ * (BVHTraverse.jl:601-655) intends between rebuilds -- and the pairs are
+ * leafneighbor_traverse's over that tree: the pair set equals a fresh build's
+ * (every box is exact), the ordered emission follows the kept tree.  keys
+ * (nkeys GridKeys, the leafTreeData layout, root box overwritten) and
+ * position (N x 3, kept order) receive the refreshed treedata (either may be
+ * NULL).  Same pair buffer protocol and modes as nd_leaf_pairs.  ND_ERR_ARG
+ * when index is not a permutation of 1..N or morton_code is not ascending.
+ * The reference's body reads an undefined `position` at HEAD; the new
+ * positions are this call's xyz.
+ */
+nd_status nd_leaf_pairs_refresh(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec,
+                                const int32_t* index, const int32_t* morton_code, int32_t mode,
+                                nd_gridkey* keys, int64_t nkeys, float* position, int32_t* pi,
+                                int32_t* pj, float* pd, int64_t capacity, int64_t* count);
+
+/*
+ * The leaf pair-list pipeline of nd_leaf_pairs_dev for callers that cannot
+ * allocate device memory (the same kernels: in ND_PAIRS_ORDERED mode the same
+ * list bit for bit; in ND_PAIRS_UNORDERED mode with atomsperleaf == 4 a
+ * one-pass emission that gives the same pairs with the same distance bits in
+ * another order): code running
  * under a host runtime that owns the device memory budget through its own pool,
  * or a time-critical loop in which cudaMalloc/cudaFree would stall the device.
  * No counterpart in the reference (it allocates freely).  Takes no context:
@@ -227,11 +257,15 @@ nd_status nd_atom_pairs(nd_ctx* ctx, const float* xyz, const nd_bvh_spec* spec, 
  * (a cudaStream_t, NULL = default stream) and the call synchronises it to read
  * the pair count.  Scratch is one file-scope device array of ~5.3 MB reserved
  * on every GPU that loads the library until the process exits; nothing is
- * allocated.  Limits: atom_count <= 65536 and atomsperleaf >= 2, otherwise
- * ND_ERR_ARG.  All calls share that array, so calls that overlap on the GPU
- * (other streams or host threads) race: serialise them.  The first call on a
- * device looks up the array's address (with that device current); make it
- * before any stream capture.  Errors are returned as status codes only.
+ * allocated.  Limits: atom_count <= 65536 and atomsperleaf >= 2 (in both
+ * modes; an unordered request with another leaf width than 4 is served by the
+ * ordered emission), otherwise ND_ERR_ARG.  All calls share that array, so
+ * calls that overlap on the GPU (other streams or host threads) race:
+ * serialise them.  The first call on a device looks up the array's address
+ * (with that device current) and keeps it for the life of the process; make
+ * that first call before any stream capture.  The kept address does not
+ * survive cudaDeviceReset: do not call this entry point after resetting the
+ * device in the same process.  Errors are returned as status codes only.
  */
 nd_status nd_leaf_pairs_noalloc_dev(const float* xyz, const nd_bvh_spec* spec, int32_t order,
                                     int32_t mode, int32_t* pi, int32_t* pj, float* pd,
@@ -410,6 +444,17 @@ typedef struct {
  * its list-build position in the next step (its displacement plus twice its
  * last move reaches 95% of skin/2) is followed by an early refit. */
 nd_status nd_md_diagnostics(nd_md* md, nd_md_diag* out);
+/* The engine's current neighbour lists as directed pairs (pi[k], pj[k]) of
+ * 1-based caller indices -- every list entry, so each unordered pair appears
+ * once from each side -- in no particular order, with near[k] = 1 for entries
+ * of the near segment (pairs closer than 1.2 sigma + 0.1 at the list build,
+ * whose forces are evaluated with exact r^2 residuals).  With capacity below
+ * the entry count, *count receives the count and ND_NEED_REALLOC is returned.
+ * Host arrays; synchronises.  No counterpart in the reference, whose pair
+ * lists are plain vectors (leafneighbor_traverse, src/Neighbors/
+ * BVHTraverse.jl:1236): the engine's lists are read back for verification. */
+nd_status nd_md_list_pairs(nd_md* md, int32_t* pi, int32_t* pj, uint8_t* near,
+                           int64_t capacity, int64_t* count);
 /* Advance `steps` steps without captured graphs, timing each step kernel with
  * its own pair of CUDA events on the context stream: ms[k] (host array of
  * `steps`) receives the k-th step kernel's duration.  Synchronises. */

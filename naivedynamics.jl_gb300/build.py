@@ -34,8 +34,11 @@ def nvcc() -> str:
 
 def _compile(src: str, verbose_ptxas: bool) -> tuple[str, str]:
     out = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
+    # host code: no FMA contraction, so the host-side generators give the same
+    # bits on x86 and on Arm hosts (device code is unaffected)
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-Wall", "-c", os.path.join(CSRC, src), "-o", out]
+           "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "-c",
+           os.path.join(CSRC, src), "-o", out]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -87,9 +87,9 @@ template <bool COUL>
 __device__ __forceinline__ void hvp_pair(const AdjArgs& a, const int4& ri, const float4& gi,
                                          const int4& rj, const float4& gj, float3& hv,
                                          float& eacc, float& sacc) {
-    const float dx = (float)(ri.x - rj.x) * a.invS;
-    const float dy = (float)(ri.y - rj.y) * a.invS;
-    const float dz = (float)(ri.z - rj.z) * a.invS;
+    const float dx = (float)idiff(ri.x, rj.x) * a.invS;
+    const float dy = (float)idiff(ri.y, rj.y) * a.invS;
+    const float dz = (float)idiff(ri.z, rj.z) * a.invS;
     const float r2 = dx * dx + dy * dy + dz * dz;
     if (!(r2 < a.rc2)) return;
     const float inv_r2 = 1.0f / r2;
@@ -187,14 +187,15 @@ __global__ void __launch_bounds__(kBlock * kAdjTPA) k_adj_reverse(AdjArgs a) {
     if (!valid) i = a.n - 1;
     const int4 ri = __ldg(&a.recs[i]);
     const float4 gi = a.g4_in[i];
-    const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
+    const int32_t cpk = valid ? __ldg(&a.ncount[i]) : 0;
+    const int32_t cnt = list_total(cpk);
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock;
     float3 hv = make_float3(0.f, 0.f, 0.f);
     float eacc = 0.f, sacc = 0.f;
-    int32_t li = part < cnt ? L[llist_at(part, al)] : 0;
+    int32_t li = part < cnt ? L[llist_at(list_slot(part, cpk, a.lcap), al)] : 0;
     for (int32_t s = part; s < cnt; s += kAdjTPA) {
         const int32_t sn = s + kAdjTPA;
-        const int32_t next = sn < cnt ? L[llist_at(sn, al)] : 0;
+        const int32_t next = sn < cnt ? L[llist_at(list_slot(sn, cpk, a.lcap), al)] : 0;
         int4 rj;
         float4 gj;
         if (li < a.smrec) {
@@ -262,19 +263,20 @@ __global__ void __launch_bounds__(kBlock) k_adj_hist(AdjArgs a) {
     if (i >= a.n) return;
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
     const int4 ri = __ldg(&a.recs[i]);
-    const int32_t cnt = __ldg(&a.ncount[i]);
+    const int32_t cpk = __ldg(&a.ncount[i]);
+    const int32_t cnt = list_total(cpk);
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock;
     for (int32_t b0 = 0; b0 < a.bins; b0 += kHistChunk) {
         float acc[kHistChunk];
 #pragma unroll
         for (int k = 0; k < kHistChunk; ++k) acc[k] = 0.0f;
         for (int32_t s = 0; s < cnt; ++s) {
-            const int64_t j = adj_atom(U, L[llist_at(s, tid)], a.apl);
+            const int64_t j = adj_atom(U, L[llist_at(list_slot(s, cpk, a.lcap), tid)], a.apl);
             if (j <= i) continue;
             const int4 rj = __ldg(&a.recs[j]);
-            const float dx = (float)(ri.x - rj.x) * a.invS;
-            const float dy = (float)(ri.y - rj.y) * a.invS;
-            const float dz = (float)(ri.z - rj.z) * a.invS;
+            const float dx = (float)idiff(ri.x, rj.x) * a.invS;
+            const float dy = (float)idiff(ri.y, rj.y) * a.invS;
+            const float dz = (float)idiff(ri.z, rj.z) * a.invS;
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (!(r2 < a.rmax2)) continue;
             const float r = sqrtf(r2);
@@ -333,15 +335,16 @@ __global__ void __launch_bounds__(kBlock) k_adj_terminal(AdjArgs a) {
     if (i >= a.n) return;
     const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
     const int4 ri = __ldg(&a.recs[i]);
-    const int32_t cnt = __ldg(&a.ncount[i]);
+    const int32_t cpk = __ldg(&a.ncount[i]);
+    const int32_t cnt = list_total(cpk);
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock;
     float gx = 0.f, gy = 0.f, gz = 0.f;
     for (int32_t s = 0; s < cnt; ++s) {
-        const int64_t j = adj_atom(U, L[llist_at(s, tid)], a.apl);
+        const int64_t j = adj_atom(U, L[llist_at(list_slot(s, cpk, a.lcap), tid)], a.apl);
         const int4 rj = __ldg(&a.recs[j]);
-        const float dx = (float)(ri.x - rj.x) * a.invS;
-        const float dy = (float)(ri.y - rj.y) * a.invS;
-        const float dz = (float)(ri.z - rj.z) * a.invS;
+        const float dx = (float)idiff(ri.x, rj.x) * a.invS;
+        const float dy = (float)idiff(ri.y, rj.y) * a.invS;
+        const float dz = (float)idiff(ri.z, rj.z) * a.invS;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (!(r2 < a.rmax2)) continue;
         const float r = sqrtf(r2);

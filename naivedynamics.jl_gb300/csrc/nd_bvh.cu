@@ -495,6 +495,63 @@ nd_status build_tree(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t a
     return check_launch(c, "tree");
 }
 
+// Sorted -> original permutation (0-based) from the 1-based original indices
+// of a kept order.
+__global__ void k_kept_perm(const int32_t* __restrict__ idx1, int32_t n, int32_t* __restrict__ perm) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) perm[i] = idx1[i] - 1;
+}
+
+// Tree of new positions in a kept order: the sorted codes and the order of an
+// earlier build are reused, so the Apetrei build (which depends on the sorted
+// codes only) reproduces that build's topology, and the leaf and internal
+// boxes are those of the new positions -- the refit that TreeData!
+// (src/Neighbors/BVHTraverse.jl:601-655) intends between rebuilds.  idx1 and
+// codes are device arrays (1-based original index and code, sorted order).
+nd_status build_tree_kept(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t apl,
+                          const int32_t* idx1, const int32_t* codes_sorted, int64_t nkeys,
+                          TreeBuffers* out) {
+    int32_t nL = n / apl;
+    nd_status st;
+    if ((st = ensure(c, c->perm, sizeof(int32_t) * (size_t)n))) return st;
+    if ((st = ensure(c, c->pos4, sizeof(float4) * (size_t)n))) return st;
+    if ((st = ensure(c, c->idx, sizeof(int32_t) * (size_t)n))) return st;
+    if ((st = ensure(c, c->keys, 32 * (size_t)nkeys))) return st;
+    if ((st = ensure(c, c->store, sizeof(int32_t) * (size_t)std::max(nL - 1, 1)))) return st;
+    if ((st = ensure(c, c->ranges, sizeof(int2) * (size_t)std::max(nL - 1, 1)))) return st;
+    int32_t* perm = (int32_t*)c->perm.p;
+    k_kept_perm<<<(unsigned)cdiv(n, 256), 256, 0, c->stream>>>(idx1, n, perm);
+    c->launches++;
+    float4* keys = (float4*)c->keys.p;
+    cudaError_t e = cudaMemsetAsync(keys, 0, 32 * (size_t)nkeys, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "keys reset");
+    k_leaf_boxes<<<(int)cdiv(nL, 128), 128, 0, c->stream>>>(xyz_dev, perm, nL, apl, r / 2.0f,
+                                                           (float4*)c->pos4.p,
+                                                           (int32_t*)c->idx.p, keys);
+    c->launches++;
+    if ((st = check_launch(c, "kept leaf boxes"))) return st;
+    int2* ranges = (int2*)c->ranges.p;
+    if ((st = build_internal_nodes(c, keys, (int32_t*)c->store.p, codes_sorted, nL, apl, ranges)))
+        return st;
+    out->n = n;
+    out->nL = nL;
+    out->apl = apl;
+    out->codes = codes_sorted;
+    out->perm = perm;
+    out->pos4 = (const float4*)c->pos4.p;
+    out->idx = (const int32_t*)c->idx.p;
+    out->keys = keys;
+    out->ranges = ranges;
+    out->nkeys = nkeys;
+    return check_launch(c, "kept tree");
+}
+
+// bounding_volume_hierarchy!'s root-box overwrite on a built tree.
+void root_overwrite(Ctx* c, float4* keys, int32_t nL) {
+    k_root_overwrite<<<1, 1, 0, c->stream>>>(keys, nL);
+    c->launches++;
+}
+
 // ==================================================================== scan
 
 constexpr int SC_THREADS = 1024;

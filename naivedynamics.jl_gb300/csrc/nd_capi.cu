@@ -151,6 +151,10 @@ static nd_status tree_from_host(Ctx* c, const float* xyz, const nd_bvh_spec* s, 
                       boxes, nkeys, overwrite_root, t);
 }
 
+static nd_status pairs_from_tree(Ctx* c, const TreeBuffers& t, const nd_bvh_spec* s,
+                                 int32_t mode, int kind, bool host, int32_t* pi, int32_t* pj,
+                                 float* pd, int64_t capacity, int64_t* count, int32_t criterion);
+
 nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode, int kind,
                        const float* xyz, bool host, int32_t* pi, int32_t* pj, float* pd,
                        int64_t capacity, int64_t* count, int32_t criterion) {
@@ -172,6 +176,15 @@ nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode
                         2LL * nL - 1, false, &t);
     }
     if (st) return st;
+    return pairs_from_tree(c, t, s, mode, kind, host, pi, pj, pd, capacity, count, criterion);
+}
+
+// Pair emission over a built tree (the second half of pairs_common).
+static nd_status pairs_from_tree(Ctx* c, const TreeBuffers& t, const nd_bvh_spec* s,
+                                 int32_t mode, int kind, bool host, int32_t* pi, int32_t* pj,
+                                 float* pd, int64_t capacity, int64_t* count,
+                                 int32_t criterion) {
+    nd_status st;
     const float r = s->neighbor_distance;
     const float r2 = pair_threshold(r, criterion);
     int64_t total = 0;
@@ -428,6 +441,77 @@ nd_status nd_leaf_pairs_dev(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, i
     return nd::pairs_common(&h->c, s, order, mode, 0, xyz, false, pi, pj, pd, capacity, count);
 }
 
+nd_status nd_leaf_pairs_refresh(nd_ctx* h, const float* xyz, const nd_bvh_spec* s,
+                                const int32_t* index, const int32_t* morton_code, int32_t mode,
+                                nd_gridkey* keys, int64_t nkeys, float* position, int32_t* pi,
+                                int32_t* pj, float* pd, int64_t capacity, int64_t* count) {
+    if (!h || !xyz || !index || !morton_code || !count || capacity < 0) return ND_ERR_ARG;
+    if (capacity > 0 && (!pi || !pj || !pd)) return ND_ERR_ARG;
+    if (keys && nkeys < 0) return ND_ERR_ARG;
+    Ctx* c = &h->c;
+    nd_status st = nd::spec_ok(s);
+    if (st) return st;
+    const int32_t n = s->atom_count, nL = s->leaves_count;
+    if (n - 1 < 2 * nL - 1) return ND_ERR_SPEC;  // leafTreeData needs atomsperleaf >= 2
+    if (mode != ND_PAIRS_ORDERED && mode != ND_PAIRS_UNORDERED) return ND_ERR_ARG;
+    // the kept order must be a permutation and its codes ascending
+    {
+        std::vector<uint8_t> seen((size_t)n, 0);
+        for (int32_t k = 0; k < n; ++k) {
+            const int32_t v = index[k];
+            if (v < 1 || v > n || seen[v - 1]) return ND_ERR_ARG;
+            seen[v - 1] = 1;
+            if (morton_code[k] < 0 || (k > 0 && morton_code[k] < morton_code[k - 1]))
+                return ND_ERR_ARG;
+        }
+    }
+    if ((st = nd::set_device(c))) return st;
+    if ((st = nd::ensure(c, c->xyz, 3 * sizeof(float) * (size_t)n))) return st;
+    if ((st = nd::ensure(c, c->perm_alt, sizeof(int32_t) * (size_t)n))) return st;
+    if ((st = nd::ensure(c, c->codes, sizeof(int32_t) * (size_t)n))) return st;
+    cudaError_t e = cudaMemcpyAsync(c->xyz.p, xyz, 3 * sizeof(float) * (size_t)n,
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->perm_alt.p, index, sizeof(int32_t) * (size_t)n,
+                            cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->codes.p, morton_code, sizeof(int32_t) * (size_t)n,
+                            cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return nd::cuda_fail(c, e, "refresh upload");
+    const int64_t need = std::max<int64_t>(2LL * nL - 1, n - 1);
+    nd::TreeBuffers t;
+    if ((st = nd::build_tree_kept(c, (const float*)c->xyz.p, n, s->neighbor_distance,
+                                  s->atomsperleaf, (const int32_t*)c->perm_alt.p,
+                                  (const int32_t*)c->codes.p, need, &t)))
+        return st;
+    const nd_status pst = pairs_from_tree(c, t, s, mode, 0, true, pi, pj, pd, capacity, count,
+                                          ND_CRIT_SQUARED);
+    if (pst != ND_OK && pst != ND_NEED_REALLOC) return pst;
+    // the kept tree with the new boxes (root box overwritten, as the reference
+    // returns it) and the positions in the kept order
+    nd::root_overwrite(c, t.keys, nL);
+    std::vector<float4> pos4;
+    if (keys && nkeys > 0) {
+        const int64_t k = std::min(nkeys, need);
+        e = cudaMemcpyAsync(keys, t.keys, 32 * (size_t)k, cudaMemcpyDeviceToHost, c->stream);
+        if (nkeys > k) memset(keys + k, 0, 32 * (size_t)(nkeys - k));
+    }
+    if (e == cudaSuccess && position) {
+        pos4.resize((size_t)n);
+        e = cudaMemcpyAsync(pos4.data(), t.pos4, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost,
+                            c->stream);
+    }
+    if (e != cudaSuccess) return nd::cuda_fail(c, e, "refresh download");
+    if ((st = nd::sync_and_check(c, "refresh"))) return st;
+    if (position)
+        for (int32_t i = 0; i < n; ++i) {
+            position[3 * (size_t)i] = pos4[i].x;
+            position[3 * (size_t)i + 1] = pos4[i].y;
+            position[3 * (size_t)i + 2] = pos4[i].z;
+        }
+    return pst;
+}
+
 nd_status nd_simd_leaf_pairs(nd_ctx* h, const float* xyz, const nd_bvh_spec* s, int32_t order,
                              int32_t mode, int32_t* pi, int32_t* pj, float* pd,
                              int64_t capacity, int64_t* count) {
@@ -641,6 +725,13 @@ nd_status nd_md_stats(nd_md* md, int64_t* steps, int64_t* rebuilds, int64_t* lis
 nd_status nd_md_diagnostics(nd_md* md, nd_md_diag* out) {
     if (!md_live(md) || !out) return ND_ERR_ARG;
     return md_wrap(md, nd::md_diagnostics(md->e, out));
+}
+
+nd_status nd_md_list_pairs(nd_md* md, int32_t* pi, int32_t* pj, uint8_t* near,
+                           int64_t capacity, int64_t* count) {
+    if (!md_live(md) || capacity < 0) return ND_ERR_ARG;
+    nd::set_device(&md->ctx->c);
+    return md_wrap(md, nd::md_list_pairs(md->e, pi, pj, near, capacity, count));
 }
 
 nd_status nd_md_step_times(nd_md* md, int32_t steps, float* ms) {

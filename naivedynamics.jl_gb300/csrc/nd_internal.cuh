@@ -172,6 +172,13 @@ nd_status radix_sort_pairs(Ctx* c, uint32_t* keys, int32_t* vals, int32_t n, int
 nd_status build_tree(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t apl,
                      int32_t order, int32_t boxes, int64_t nkeys, bool overwrite_root,
                      TreeBuffers* out);
+// Tree of new positions in the order (1-based original indices idx1) and with
+// the sorted codes of an earlier build: same topology, new boxes (device
+// arrays); the leaf-box half-width is r/2 (leafTreeData).
+nd_status build_tree_kept(Ctx* c, const float* xyz_dev, int32_t n, float r, int32_t apl,
+                          const int32_t* idx1, const int32_t* codes_sorted, int64_t nkeys,
+                          TreeBuffers* out);
+void root_overwrite(Ctx* c, float4* keys, int32_t nL);
 // Exclusive int64 scan on the context stream; total written to *total_dev.
 nd_status scan_exclusive(Ctx* c, const int64_t* in, int64_t* out, int64_t n, int64_t* total_dev);
 
@@ -218,6 +225,8 @@ nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list
                    int32_t* capacity);
 int64_t md_launches_per_run(MDEngine* m, int64_t steps);
 nd_status md_diagnostics(MDEngine* m, nd_md_diag* out);
+nd_status md_list_pairs(MDEngine* m, int32_t* pi, int32_t* pj, uint8_t* near, int64_t cap,
+                        int64_t* count);
 nd_status md_set_thermostat(MDEngine* m, double temperature, double gamma, int32_t every);
 nd_status md_set_log(MDEngine* m, int32_t every, int32_t frames);
 nd_status md_log_count(MDEngine* m, int64_t* count);

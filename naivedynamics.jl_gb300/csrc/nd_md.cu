@@ -34,6 +34,47 @@ constexpr int kSmallTPA = 4;         // threads per atom of the step kernel for 
 constexpr int kSizingFcap = 8192;    // BFS frontier entries per buffer in the sizing build
 constexpr int kSizingUcap = 8192;    // union capacity of the sizing build
 
+// Scale of the wrap-around fixed-point grid: a listed pair is within
+// r_c + skin at the build and its atoms move at most skin/2 each before the
+// next refit, so its per-axis separation stays below r_c + 2 skin; a quarter
+// of head-room on top.  At r_c = 2.5 and skin 0.4 the grid step is 2^-28.
+static double md_scale(const nd_md_params& p) {
+    const double span = 1.25 * (p.cutoff + 2.0 * std::max(p.skin, 0.0));
+    return std::ldexp(1.0, (int)std::floor(std::log2(2147483648.0 / span)));
+}
+
+// Near-pair constants of a system with LJ sigma, epsilon and Coulomb constant
+// kc at grid scale S.  The split
+// keeps hi = x_fp with its low k bits cleared below 2^(k+10) in magnitude for
+// separations up to 1.25 rnb, so the sum of the three squared hi parts is an
+// exact float.
+static NearK md_near(double sigma, double eps, double kc, double S) {
+    NearK k{};
+    const double rn = 1.3 * sigma, rnb = rn + 0.1;
+    k.rn2u = (float)(rn * rn * S * S);
+    const double sig2 = sigma * sigma * S * S;
+    k.sig2lo = (float)(sig2 - (double)(float)sig2);
+    const double e24 = 24.0 * eps * S, kcu = kc * S * S;
+    k.e24lo = (float)(e24 - (double)(float)e24);
+    k.kclo = (float)(kcu - (double)(float)kcu);
+    k.rnb2 = (float)(rnb * rnb);
+    int b = (int)std::ceil(std::log2(1.25 * rnb * S)) - 10;
+    b = std::min(std::max(b, 0), 23);
+    k.hmask = (int32_t)(~((1u << b) - 1u));
+    return k;
+}
+
+// Range bound of |x_fp| (before the wrap) for a frame at scale S whose walls
+// span ext: sc is the coarsest power-of-two scale at which the frame (the
+// walls and 1/16 of the extent on each side) fits int32, and a coordinate is
+// in range while (x - o) sc does.
+static double md_frame_lim(double ext, double S) {
+    const double range = ext * 1.125;
+    const double sc = std::ldexp(1.0, (int)std::floor(std::log2(2147480000.0 / range)));
+    return 2147480000.0 * (S / sc);
+}
+
+
 
 // ------------------------------------------------------------- small kernels
 
@@ -80,7 +121,8 @@ __global__ void k_md_pos32(const double* __restrict__ x0, const double* __restri
 __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict__ perm,
                              const float* __restrict__ xyz32, int32_t n, Frame fr,
                              const SysRow* __restrict__ sys, float4* __restrict__ pos32,
-                             int4* __restrict__ rec, int4* __restrict__ recb, int32_t* err) {
+                             int4* __restrict__ rec, uint2* __restrict__ recf,
+                             int4* __restrict__ recb, int32_t* err) {
     int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int32_t o = perm[k];
@@ -91,13 +133,16 @@ __global__ void k_md_reorder(SetPtrs src, SetPtrs dst, const int32_t* __restrict
         r = sys + sv;
     }
     int32_t f[3];
+    uint32_t g[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double xv = src.x[d][o];
         dst.x[d][k] = xv;
         dst.w[d][k] = src.w[d][o];
-        f[d] = to_fixed(xv, r ? r->o[d] : fr.o[d], r ? r->s : fr.s, err, k);
+        f[d] = to_fixed(xv, r ? r->o[d] : fr.o[d], r ? r->s : fr.s, r ? r->lim : fr.lim, err, k,
+                        g[d]);
     }
+    recf[k] = pack_fine(g[0], g[1], g[2]);
     double qv = src.q[o];
     dst.q[k] = qv;
     dst.im[k] = src.im[o];
@@ -517,21 +562,37 @@ __global__ void __launch_bounds__(kBlock)
     }
 }
 
-// Exact per-atom lists inside the block's union: the union's Float32
-// positions are staged in shared memory (up to smpos entries; the rest are read
-// from L2), then the APL lanes of a leaf walk that leaf's candidate list
-// together, each testing its own atom against the candidate leaf's atoms with
-// the reference distance (Float32, d^2 < r_list^2) and storing union indices
-// as uint16.  pos.w holds the atom's sorted index (excludes the atom itself).
+// Exact per-atom lists inside the block's union.  The union's Float32
+// positions are staged in shared memory (up to smpos entries; the rest are
+// read from L2).  Each thread builds its own atom's list in two passes over
+// its leaf's candidate leaves (the union leaves whose atom boxes lie within
+// r_list of the leaf's, k_md_block_union):
+//  1. a point-to-box test of the atom against every candidate leaf's atom box
+//     (the key box shrunk by the half-width h, less a rounding margin),
+//     recorded as one bit per candidate in shared memory;
+//  2. the reference distance test (Float32, d^2 < r_list^2) against the atoms
+//     of the candidate leaves whose bit is set, in candidate order.
+// About a quarter of the candidate leaves pass the box test at r_list = 2.9,
+// so the second pass does about a quarter of the distance tests of a walk over
+// all candidates, and since a box test never drops an atom within r_list the
+// list is the same, entry for entry.  Union indices are stored as uint16:
+// entries closer than the near bound (rnb2, or the atom's system's) from slot
+// 0 upwards, the others from slot lcap - 1 downwards.  pos.w holds the atom's
+// sorted index (excludes the atom itself).
 template <int APL>
 __global__ void __launch_bounds__(kBlock)
-    k_md_block_lists(const float4* __restrict__ pos, int32_t n, float rl2, int32_t ucap,
+    k_md_block_lists(const float4* __restrict__ pos, const float4* __restrict__ keys,
+                     int32_t n, float rl2, float h, float margin, float rnb2,
+                     const int32_t* __restrict__ sid, const SysRow* __restrict__ sys,
+                     int32_t ucap,
                      int32_t smpos, const int32_t* __restrict__ ulist,
                      const int32_t* __restrict__ ucount, const uint16_t* __restrict__ llist_leaf,
                      const int32_t* __restrict__ lcount_leaf, int32_t lcap_leaf, int32_t lcap,
                      uint16_t* __restrict__ llist, int32_t* __restrict__ ncount, int32_t* err,
                      int32_t* diag, int32_t sizing, unsigned* pressure) {
     extern __shared__ float4 spos[];
+    // candidate bits after the staged positions: word w of thread t at w * kBlock + t
+    uint32_t* sbits = reinterpret_cast<uint32_t*>(spos + smpos);
     const int tid = threadIdx.x;
     const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
     {
@@ -565,22 +626,51 @@ __global__ void __launch_bounds__(kBlock)
     const int64_t own = (valid ? i : (int64_t)blockIdx.x * kBlock) / APL;
     const float4 p = __ldg(&pos[valid ? i : (int64_t)blockIdx.x * kBlock]);
     const int32_t nc = valid ? min(__ldg(&lcount_leaf[own]), lcap_leaf) : 0;
-    // candidate entries eight at a time (a leaf's list starts on a 16-byte
-    // boundary: lcap_leaf is a multiple of 8), the next eight loaded while the
-    // current ones are tested
     const uint4* __restrict__ C = reinterpret_cast<const uint4*>(llist_leaf + own * lcap_leaf);
+    const uint16_t* __restrict__ C16 = llist_leaf + own * lcap_leaf;
+    // pass 1: one bit per candidate leaf whose atom box the atom can reach
+    {
+        uint32_t word = 0;
+        uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
+        for (int32_t k0 = 0; k0 < nc; k0 += 8) {
+            const uint4 cur = nxt;
+            if (k0 + 8 < nc) nxt = __ldg(&C[(k0 >> 3) + 1]);
+            const uint32_t cw[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+            for (int hh = 0; hh < 8; ++hh) {
+                const int32_t k = k0 + hh;
+                if (k < nc) {
+                    const int32_t u = (int32_t)((cw[hh >> 1] >> (16 * (hh & 1))) & 0xffffu);
+                    const int64_t leaf = __ldg(&U[u]);
+                    const float4 a = __ldg(&keys[2 * leaf]), b = __ldg(&keys[2 * leaf + 1]);
+                    // per-axis gap between the atom and the leaf's atom box
+                    // (key box less h on every side), less the margin
+                    const float gx = fmaxf(fmaxf((a.x + h) - p.x, p.x - (a.w - h)) - margin, 0.0f);
+                    const float gy = fmaxf(fmaxf((a.y + h) - p.y, p.y - (b.x - h)) - margin, 0.0f);
+                    const float gz = fmaxf(fmaxf((a.z + h) - p.z, p.z - (b.y - h)) - margin, 0.0f);
+                    if (gx * gx + gy * gy + gz * gz < rl2) word |= 1u << (k & 31);
+                }
+                if ((k & 31) == 31) {
+                    sbits[(k >> 5) * kBlock + tid] = word;
+                    word = 0;
+                }
+            }
+        }
+        if (nc & 31) sbits[(nc >> 5) * kBlock + tid] = word;
+    }
+    // pass 2: the distance tests against the atoms of the marked leaves
     uint16_t* __restrict__ L = llist + (int64_t)blockIdx.x * lcap * kBlock + tid;
     const int32_t self = (int32_t)i;
-    int32_t cnt = 0;
-    uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
-    for (int32_t k0 = 0; k0 < nc; k0 += 8) {
-        const uint4 cur = nxt;
-        if (k0 + 8 < nc) nxt = __ldg(&C[(k0 >> 3) + 1]);
-        const uint32_t cw[4] = {cur.x, cur.y, cur.z, cur.w};
-#pragma unroll
-        for (int h = 0; h < 8; ++h) {
-            if (k0 + h >= nc) break;
-            const int32_t u = (int32_t)((cw[h >> 1] >> (16 * (h & 1))) & 0xffffu);
+    const float nb2 = sid ? __ldg(&sys[__ldg(&sid[valid ? i : (int64_t)blockIdx.x * kBlock])].nk.rnb2)
+                          : rnb2;
+    int32_t cnt = 0, nn = 0, nf = 0;  // all hits; near and other entries stored
+    const int32_t nw = (nc + 31) >> 5;
+    for (int32_t w = 0; w < nw; ++w) {
+        uint32_t bits = sbits[w * kBlock + tid];
+        while (bits) {
+            const int32_t k = (w << 5) + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            const int32_t u = __ldg(&C16[k]);
             float4 q[APL];
             if ((u + 1) * APL <= smpos) {
 #pragma unroll
@@ -592,17 +682,22 @@ __global__ void __launch_bounds__(kBlock)
             }
 #pragma unroll
             for (int e = 0; e < APL; ++e) {
-                const bool hit = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z) < rl2 &&
-                                 __float_as_int(q[e].w) != self;
+                const float d2 = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z);
+                const bool hit = d2 < rl2 && __float_as_int(q[e].w) != self;
                 if (hit) {
-                    if (cnt < lcap) L[cnt * kBlock] = (uint16_t)(u * APL + e);
+                    if (cnt < lcap) {
+                        const bool near = d2 < nb2;
+                        L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)(u * APL + e);
+                        nn += near ? 1 : 0;
+                        nf += near ? 0 : 1;
+                    }
                     ++cnt;
                 }
             }
         }
     }
     if (!valid) return;
-    ncount[i] = min(cnt, lcap);
+    ncount[i] = nn | (nf << 16);
     if (cnt > lcap && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)i);
     atomicMax(&diag[1], cnt);
     if (pressure && 10 * cnt > 9 * lcap) atomicOr(pressure, 1u);
@@ -613,19 +708,23 @@ __global__ void __launch_bounds__(kBlock)
 // state in its current order.
 __global__ void k_md_refit_pos(SetPtrs st, int32_t n, Frame fr, const SysRow* __restrict__ sys,
                                float4* __restrict__ pos32, int4* __restrict__ rec,
-                               int4* __restrict__ recb, int32_t* err, unsigned* counter) {
+                               uint2* __restrict__ recf, int4* __restrict__ recb, int32_t* err,
+                               unsigned* counter) {
     int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (counter && k == 0) atomicAdd(counter, 1u);
     if (k >= n) return;
     const SysRow* r = st.sid ? sys + st.sid[k] : nullptr;
     int32_t f[3];
+    uint32_t g[3];
     float xf[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double xv = st.x[d][k];
         xf[d] = (float)(r ? xv + r->off[d] : xv);
-        f[d] = to_fixed(xv, r ? r->o[d] : fr.o[d], r ? r->s : fr.s, err, k);
+        f[d] = to_fixed(xv, r ? r->o[d] : fr.o[d], r ? r->s : fr.s, r ? r->lim : fr.lim, err, k,
+                        g[d]);
     }
+    recf[k] = pack_fine(g[0], g[1], g[2]);
     pos32[k] = make_float4(xf[0], xf[1], xf[2], __int_as_float(k));
     const int4 rv = make_int4(f[0], f[1], f[2], __float_as_int((float)st.q[k]));
     rec[k] = rv;
@@ -638,19 +737,145 @@ __global__ void k_md_refit_pos(SetPtrs st, int32_t n, Frame fr, const SysRow* __
 // Pair constants of one system in fixed-point units.
 struct PairK {
     float rc2u, sig2u, eps24u, eps4, kcu, kceu;
+    float rn2u, sig2lo, e24lo, kclo;
+    int32_t hmask;
 };
+
+// Low part of a separation split: the value in [0, 2^23) as a float, exact,
+// by placing it in the mantissa of 2^23.
+__device__ __forceinline__ float lo_part(int32_t v) {
+    return __fsub_rn(__int_as_float(0x4B000000 | v), 8388608.0f);
+}
+
+// A force as three two-float sums (hi + lo per component).
+struct DF3 {
+    float xh, xl, yh, yl, zh, zl;
+};
+
+// (h, l) += (t, tl): TwoSum of the high parts (Knuth), low parts added.
+__device__ __forceinline__ void df_acc(float& h, float& l, float t, float tl) {
+    const float s = __fadd_rn(h, t);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(t, bb));
+    h = s;
+    l = __fadd_rn(l, __fadd_rn(e, tl));
+}
+
+// Fine-grid difference of one coordinate (16-bit fields), in coarse units.
+__device__ __forceinline__ float fine_diff(uint32_t a, uint32_t b, int sh) {
+    const int32_t d = (int32_t)((a >> sh) & 0xffffu) - (int32_t)((b >> sh) & 0xffffu);
+    return __fmul_rn(__int2float_rn(d), 1.52587890625e-05f);  // 2^-16, exact
+}
+
+// Near pair (i, j), separation below 1.3 sigma: the pair term in two-float
+// arithmetic (each quantity a float pair hi + lo carrying about 44 bits), so
+// that an atom whose large near terms cancel keeps its small net force to
+// FP64-like accuracy.  The steep part of the potential amplifies a relative
+// error in r^2 about 30-fold near its minimum (where 2 s6 - 1 cancels) and
+// the terms reach hundreds at r < sigma, so every step carries its residual:
+//  * separation: the coarse integer difference splits exactly into hi (low k
+//    bits cleared, at most 11 significant bits) + lo (< 2^k); the fine-grid
+//    difference (16 more bits) is added; sum hi^2 is an exact float, the rest
+//    of r^2 and the rounding of the sum are kept in r2lo (Fast2Sum);
+//  * 1/r^2 = ir2 (1 + eta): eta from the exact residual 1 - r2 ir2 (FMA) and
+//    r2lo, so the approximate reciprocal square root needs no Newton step;
+//  * every product with its FMA residual (Dekker), 2 s6 - 1 by TwoSum;
+//  * the term's three components added to two-float sums (df_acc).
+// Explicitly rounded operations (__f*_rn) keep the compiler from contracting
+// a product whose residual is taken separately.
+template <bool COUL, bool ENERGY>
+__device__ __forceinline__ void accum_near(const int4& ri, const int4& rj, const uint2& fi,
+                                           const uint2& fj, const PairK& a, DF3& acc, float& ue) {
+    const int32_t ix = idiff(ri.x, rj.x), iy = idiff(ri.y, rj.y), iz = idiff(ri.z, rj.z);
+    const float hx = __int2float_rn(ix & a.hmask), lx = lo_part(ix & ~a.hmask);
+    const float hy = __int2float_rn(iy & a.hmask), ly = lo_part(iy & ~a.hmask);
+    const float hz = __int2float_rn(iz & a.hmask), lz = lo_part(iz & ~a.hmask);
+    const float fx = fine_diff(fi.x, fj.x, 0), fy = fine_diff(fi.x, fj.x, 16),
+                fz = fine_diff(fi.y, fj.y, 0);
+    // separation as two floats per axis: d = dh + dl
+    const float dxh = __fadd_rn(hx, lx), dyh = __fadd_rn(hy, ly), dzh = __fadd_rn(hz, lz);
+    const float dxl = __fadd_rn(__fsub_rn(lx, __fsub_rn(dxh, hx)), fx);
+    const float dyl = __fadd_rn(__fsub_rn(ly, __fsub_rn(dyh, hy)), fy);
+    const float dzl = __fadd_rn(__fsub_rn(lz, __fsub_rn(dzh, hz)), fz);
+    const float P = __fmaf_rn(hz, hz, __fmaf_rn(hy, hy, __fmul_rn(hx, hx)));  // exact
+    const float t = __fmaf_rn(hx, lx, __fmaf_rn(hy, ly, __fmul_rn(hz, lz)));
+    const float l2 = __fmaf_rn(lx, lx, __fmaf_rn(ly, ly, __fmul_rn(lz, lz)));
+    const float u = __fmaf_rn(dxh, fx, __fmaf_rn(dyh, fy, __fmul_rn(dzh, fz)));
+    const float cl = __fmaf_rn(2.0f, u, __fmaf_rn(2.0f, t, l2));
+    const float r2 = __fadd_rn(P, cl);
+    if (!(r2 < a.rc2u)) return;
+    const float r2lo = __fsub_rn(cl, __fsub_rn(r2, P));
+    const float ir = rsqrtf(r2);
+    const float ir2 = __fmul_rn(ir, ir);
+    const float eta = __fmaf_rn(-r2lo, ir2, __fmaf_rn(-r2, ir2, 1.0f));
+    const float ir2l = __fmul_rn(ir2, eta);
+    // s2 = sigma^2 / r^2, s4, s6 as two floats
+    const float s2 = __fmul_rn(a.sig2u, ir2);
+    const float s2l = __fmaf_rn(a.sig2lo, ir2, __fmaf_rn(a.sig2u, ir2l, __fmaf_rn(a.sig2u, ir2, -s2)));
+    const float s4 = __fmul_rn(s2, s2);
+    const float s4l = __fmaf_rn(__fmul_rn(2.0f, s2), s2l, __fmaf_rn(s2, s2, -s4));
+    const float s6 = __fmul_rn(s4, s2);
+    const float s6l = __fmaf_rn(s4, s2l, __fmaf_rn(s4l, s2, __fmaf_rn(s4, s2, -s6)));
+    // w = 2 s6 - 1
+    const float a2 = __fmul_rn(2.0f, s6);
+    const float wh = __fsub_rn(a2, 1.0f);
+    const float wb = __fsub_rn(wh, a2);
+    const float we = __fadd_rn(__fsub_rn(a2, __fsub_rn(wh, wb)), __fsub_rn(-1.0f, wb));
+    const float wl = __fmaf_rn(2.0f, s6l, we);
+    // LJ magnitude 24 eps / r^2 s6 (2 s6 - 1)
+    const float p1 = __fmul_rn(ir2, s6);
+    const float p1l = __fmaf_rn(ir2l, s6, __fmaf_rn(ir2, s6l, __fmaf_rn(ir2, s6, -p1)));
+    const float p2 = __fmul_rn(p1, wh);
+    const float p2l = __fmaf_rn(p1l, wh, __fmaf_rn(p1, wl, __fmaf_rn(p1, wh, -p2)));
+    float fh = __fmul_rn(a.eps24u, p2);
+    float fl = __fmaf_rn(a.e24lo, p2, __fmaf_rn(a.eps24u, p2l, __fmaf_rn(a.eps24u, p2, -fh)));
+    float uu = 0.f;
+    if (ENERGY) uu = a.eps4 * s6 * (s6 - 1.0f);
+    if (COUL) {
+        const float qi = __int_as_float(ri.w), qj = __int_as_float(rj.w);
+        const float qh = __fmul_rn(qi, qj), ql = __fmaf_rn(qi, qj, -qh);
+        const float kh = __fmul_rn(a.kcu, qh);
+        const float kl = __fmaf_rn(a.kclo, qh, __fmaf_rn(a.kcu, ql, __fmaf_rn(a.kcu, qh, -kh)));
+        // 1/r = ir + irl: the residual of ir^2 against ir2 and eta
+        const float eir = __fmaf_rn(ir, ir, -ir2);
+        const float irl = __fmul_rn(__fmul_rn(0.5f, ir), __fmaf_rn(-eir, r2, eta));
+        const float i3 = __fmul_rn(ir, ir2);
+        const float i3l = __fmaf_rn(irl, ir2, __fmaf_rn(ir, ir2l, __fmaf_rn(ir, ir2, -i3)));
+        const float ch = __fmul_rn(kh, i3);
+        const float cl2 = __fmaf_rn(kl, i3, __fmaf_rn(kh, i3l, __fmaf_rn(kh, i3, -ch)));
+        const float sh = __fadd_rn(fh, ch);
+        const float sb = __fsub_rn(sh, fh);
+        const float se = __fadd_rn(__fsub_rn(fh, __fsub_rn(sh, sb)), __fsub_rn(ch, sb));
+        fh = sh;
+        fl = __fadd_rn(fl, __fadd_rn(cl2, se));
+        if (ENERGY) uu += a.kceu * qh * ir;
+    }
+    // components fmag * d, into the two-float sums
+    {
+        const float tx = __fmul_rn(fh, dxh);
+        df_acc(acc.xh, acc.xl, tx, __fmaf_rn(fl, dxh, __fmaf_rn(fh, dxl, __fmaf_rn(fh, dxh, -tx))));
+        const float ty = __fmul_rn(fh, dyh);
+        df_acc(acc.yh, acc.yl, ty, __fmaf_rn(fl, dyh, __fmaf_rn(fh, dyl, __fmaf_rn(fh, dyh, -ty))));
+        const float tz = __fmul_rn(fh, dzh);
+        df_acc(acc.zh, acc.zl, tz, __fmaf_rn(fl, dzh, __fmaf_rn(fh, dzl, __fmaf_rn(fh, dzh, -tz))));
+    }
+    if (ENERGY) ue += uu;
+}
 
 // Pair (i, j) from fixed-point records: the integer difference is exact, its
 // conversion to float rounds once, so r_ij keeps full single precision at any
 // box size inside the frame.  Constants are pre-scaled, so the force comes out
-// in physical units per fixed-point unit of displacement.
+// in physical units per fixed-point unit of displacement.  Returns true,
+// adding nothing, for a pair closer than 1.3 sigma (one that came near after
+// the list build): the caller evaluates it with accum_near.
 template <bool COUL, bool ENERGY>
-__device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const PairK& a,
+__device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const PairK& a,
                                           float& fx, float& fy, float& fz, float& ue) {
-    const float dx = (float)(ri.x - rj.x);
-    const float dy = (float)(ri.y - rj.y);
-    const float dz = (float)(ri.z - rj.z);
+    const float dx = (float)idiff(ri.x, rj.x);
+    const float dy = (float)idiff(ri.y, rj.y);
+    const float dz = (float)idiff(ri.z, rj.z);
     const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < a.rn2u) return true;
     if (r2 < a.rc2u) {
         float inv_r2, inv_r = 0.f;
         if (COUL) {
@@ -676,6 +901,7 @@ __device__ __forceinline__ void accum_pair(const int4& ri, const int4& rj, const
         fz += fmag * dz;
         if (ENERGY) ue += u;
     }
+    return false;
 }
 
 // Packed single precision (sm_100 and later): one instruction applies the
@@ -714,19 +940,29 @@ struct PairK2 {
 // Forces of the pairs (i, a) and (i, b) together (no energies): the same
 // terms as accum_pair, the pair outside the cutoff contributing zero.  The
 // accumulators hold the running sums of the a-entries and the b-entries
-// separately; the caller adds the halves at the end.
+// separately; the caller adds the halves at the end.  When a pair is closer
+// than 1.3 sigma (rare: one that came near after the list build) the other
+// takes the scalar form into (sx, sy, sz) and the near one is left to the
+// caller: the return value has bit 0 set for a, bit 1 for b.
 template <bool COUL>
-__device__ __forceinline__ void accum_pair2(const int4& ri, const int4& ra, const int4& rb,
-                                           const PairK& k1, const PairK2& k, uint64_t& fx,
-                                           uint64_t& fy, uint64_t& fz) {
-    const uint64_t dx = pk2((float)(ri.x - ra.x), (float)(ri.x - rb.x));
-    const uint64_t dy = pk2((float)(ri.y - ra.y), (float)(ri.y - rb.y));
-    const uint64_t dz = pk2((float)(ri.z - ra.z), (float)(ri.z - rb.z));
+__device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, const int4& rb,
+                                               const PairK& k1, const PairK2& k, uint64_t& fx,
+                                               uint64_t& fy, uint64_t& fz, float& sx, float& sy,
+                                               float& sz) {
+    const uint64_t dx = pk2((float)idiff(ri.x, ra.x), (float)idiff(ri.x, rb.x));
+    const uint64_t dy = pk2((float)idiff(ri.y, ra.y), (float)idiff(ri.y, rb.y));
+    const uint64_t dz = pk2((float)idiff(ri.z, ra.z), (float)idiff(ri.z, rb.z));
     const uint64_t r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
     float r2a, r2b;
     upk2(r2, r2a, r2b);
+    if ((r2a < k1.rn2u) | (r2b < k1.rn2u)) {
+        float ue = 0.f;
+        unsigned m = accum_pair<COUL, false>(ri, ra, k1, sx, sy, sz, ue) ? 1u : 0u;
+        m |= accum_pair<COUL, false>(ri, rb, k1, sx, sy, sz, ue) ? 2u : 0u;
+        return m;
+    }
     const bool ina = r2a < k1.rc2u, inb = r2b < k1.rc2u;
-    if (!(ina | inb)) return;
+    if (!(ina | inb)) return 0u;
     uint64_t inv_r = 0, inv_r2;
     if (COUL) {
         inv_r = pk2(rsqrtf(r2a), rsqrtf(r2b));
@@ -753,6 +989,7 @@ __device__ __forceinline__ void accum_pair2(const int4& ri, const int4& ra, cons
     fx = fma2(fmag, dx, fx);
     fy = fma2(fmag, dy, fy);
     fz = fma2(fmag, dz, fz);
+    return 0u;
 }
 
 // One block per 256 atoms.  MODE 0: step (force, pending half kick, kick,
@@ -808,7 +1045,8 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     // join the warp reductions (measure) and the block vote (step)
     if (!valid) i = a.n - 1;
     const int4 ri = __ldg(&a.rec_in[i]);
-    PairK pk{a.rc2u, a.sig2u, a.eps24u, a.eps4, a.kcu, a.kceu};
+    PairK pk{a.rc2u, a.sig2u, a.eps24u, a.eps4, a.kcu, a.kceu,
+             a.nk.rn2u, a.nk.sig2lo, a.nk.e24lo, a.nk.kclo, a.nk.hmask};
     int32_t sv = 0;
     const SysRow* __restrict__ row = nullptr;
     double S = a.fr.s;
@@ -822,18 +1060,49 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         pk.rc2u = __ldg(&row->rc2u);
         pk.kcu = __ldg(&row->kcu);
         pk.kceu = __ldg(&row->kceu);
+        pk.rn2u = __ldg(&row->nk.rn2u);
+        pk.sig2lo = __ldg(&row->nk.sig2lo);
+        pk.e24lo = __ldg(&row->nk.e24lo);
+        pk.kclo = __ldg(&row->nk.kclo);
+        pk.hmask = __ldg(&row->nk.hmask);
         S = __ldg(&row->s);
         hs2u = __ldg(&row->hs2u);
         hsu = __ldg(&row->hsu);
     }
-    const int32_t cnt = valid ? __ldg(&a.ncount[i]) : 0;
+    // near entries (slots 0, 1, ...) and the others (slots lcap - 1, lcap - 2, ...)
+    const int32_t cpk = valid ? __ldg(&a.ncount[i]) : 0;
+    const int32_t nn = list_near(cpk), nf = cpk >> 16;
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
+    const uint16_t* __restrict__ LF = L + (int64_t)(a.lcap - 1) * kBlock;
+    const int32_t lsh = __ffs(a.apl) - 1, emask = a.apl - 1;
     auto fetch = [&](int32_t li) -> int4 {
         if (li < a.smrec) return srec[li];
-        const int32_t u = li / a.apl, e = li - u * a.apl;
-        return __ldg(&a.rec_in[(int64_t)__ldg(&U[u]) * a.apl + e]);
+        return __ldg(&a.rec_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
     };
+    // fine bits of a union entry's record (near pairs only)
+    auto fine = [&](int32_t li) -> uint2 {
+        return __ldg(&a.recf_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
+    };
+    const uint2 fi = __ldg(&a.recf_in[i]);
+    // near terms in two-float sums, the others in single precision
+    DF3 nacc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float fx = 0.f, fy = 0.f, fz = 0.f, ue = 0.f;
+    {
+        // near entries of this thread's slice, the next index loaded ahead
+        int32_t s = part;
+        int32_t li = s < nn ? L[(int64_t)s * kBlock] : 0;
+        for (; s < nn; s += TPA) {
+            const int32_t sn = s + TPA;
+            const int32_t next = sn < nn ? L[(int64_t)sn * kBlock] : 0;
+            accum_near<COUL, MODE == 1>(ri, fetch(li), fi, fine(li), pk, nacc, ue);
+            li = next;
+        }
+    }
+    // an entry of the other segment that came closer than 1.3 sigma
+    auto far_near = [&](int32_t s) {
+        const int32_t li = LF[-(int64_t)s * kBlock];
+        accum_near<COUL, MODE == 1>(ri, fetch(li), fi, fine(li), pk, nacc, ue);
+    };
     if constexpr (TPA == 1) {
         // groups of four neighbours; the next group's indices are loaded
         // while the current group is computed
@@ -841,76 +1110,100 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         uint64_t fx2 = 0, fy2 = 0, fz2 = 0;  // packed (0.0f, 0.0f)
         int32_t s = 0;
         int32_t li[4];
-        if (cnt >= 4) {
+        if (nf >= 4) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)k * kBlock];
+            for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)k * kBlock];
         }
-        for (; s + 4 <= cnt; s += 4) {
+        for (; s + 4 <= nf; s += 4) {
             int4 rj[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
-            if (s + 8 <= cnt) {
+            if (s + 8 <= nf) {
 #pragma unroll
-                for (int k = 0; k < 4; ++k) li[k] = L[(int64_t)(s + 4 + k) * kBlock];
+                for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)(s + 4 + k) * kBlock];
             }
             if constexpr (MODE == 1) {
 #pragma unroll
-                for (int k = 0; k < 4; ++k) accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue);
+                for (int k = 0; k < 4; ++k)
+                    if (accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue)) far_near(s + k);
             } else {
                 // two entries per packed instruction
-                accum_pair2<COUL>(ri, rj[0], rj[1], pk, pk2c, fx2, fy2, fz2);
-                accum_pair2<COUL>(ri, rj[2], rj[3], pk, pk2c, fx2, fy2, fz2);
+                const unsigned m0 = accum_pair2<COUL>(ri, rj[0], rj[1], pk, pk2c, fx2, fy2, fz2, fx, fy, fz);
+                const unsigned m1 = accum_pair2<COUL>(ri, rj[2], rj[3], pk, pk2c, fx2, fy2, fz2, fx, fy, fz);
+                if (m0 | m1) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (((k < 2 ? m0 : m1) >> (k & 1)) & 1u) far_near(s + k);
+                }
             }
         }
         if constexpr (MODE != 1) {
             float a, b;
-            upk2(fx2, a, b); fx = a + b;
-            upk2(fy2, a, b); fy = a + b;
-            upk2(fz2, a, b); fz = a + b;
+            upk2(fx2, a, b); fx += a + b;
+            upk2(fy2, a, b); fy += a + b;
+            upk2(fz2, a, b); fz += a + b;
         }
-        for (; s < cnt; ++s)
-            accum_pair<COUL, MODE == 1>(ri, fetch(L[(int64_t)s * kBlock]), pk, fx, fy, fz, ue);
+        for (; s < nf; ++s)
+            if (accum_pair<COUL, MODE == 1>(ri, fetch(LF[-(int64_t)s * kBlock]), pk, fx, fy, fz, ue))
+                far_near(s);
+        // the force: two-float near sums with the single-precision sums added
+        // to their low parts, rounded once
+        fx = __fadd_rn(nacc.xh, __fadd_rn(nacc.xl, fx));
+        fy = __fadd_rn(nacc.yh, __fadd_rn(nacc.yl, fy));
+        fz = __fadd_rn(nacc.zh, __fadd_rn(nacc.zl, fz));
     } else {
-        // slice `part` of the list (entries part, part + TPA, ..., in that
+        // slice `part` of the far entries (part, part + TPA, ..., in that
         // order): four indices loaded ahead while the previous four are computed
         int32_t li[4] = {0, 0, 0, 0};
         auto load4 = [&](int32_t s0) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int32_t sk = s0 + k * TPA;
-                li[k] = sk < cnt ? L[(int64_t)sk * kBlock] : 0;
+                li[k] = sk < nf ? LF[-(int64_t)sk * kBlock] : 0;
             }
         };
         int32_t s = part;
-        if (s < cnt) load4(s);
-        for (; s + 3 * TPA < cnt; s += 4 * TPA) {
+        if (s < nf) load4(s);
+        for (; s + 3 * TPA < nf; s += 4 * TPA) {
             int4 rj[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
             load4(s + 4 * TPA);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue);
+            for (int k = 0; k < 4; ++k)
+                if (accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue)) far_near(s + k * TPA);
         }
         // at most three entries left, their indices already loaded
-        for (int k = 0; s < cnt && k < 4; s += TPA, ++k)
-            accum_pair<COUL, MODE == 1>(ri, fetch(li[k]), pk, fx, fy, fz, ue);
-        __shared__ float spart[TPA > 1 ? TPA - 1 : 1][4][kBlock];
+        for (int k = 0; s < nf && k < 4; s += TPA, ++k)
+            if (accum_pair<COUL, MODE == 1>(ri, fetch(li[k]), pk, fx, fy, fz, ue)) far_near(s);
+        // each slice as a two-float value (its single-precision sum in the low
+        // part); the slices added in a fixed order
+        nacc.xl = __fadd_rn(nacc.xl, fx);
+        nacc.yl = __fadd_rn(nacc.yl, fy);
+        nacc.zl = __fadd_rn(nacc.zl, fz);
+        __shared__ float spart[TPA > 1 ? TPA - 1 : 1][7][kBlock];
         if (part > 0) {
-            spart[part - 1][0][tid] = fx;
-            spart[part - 1][1][tid] = fy;
-            spart[part - 1][2][tid] = fz;
-            spart[part - 1][3][tid] = ue;
+            spart[part - 1][0][tid] = nacc.xh;
+            spart[part - 1][1][tid] = nacc.xl;
+            spart[part - 1][2][tid] = nacc.yh;
+            spart[part - 1][3][tid] = nacc.yl;
+            spart[part - 1][4][tid] = nacc.zh;
+            spart[part - 1][5][tid] = nacc.zl;
+            spart[part - 1][6][tid] = ue;
         }
         __syncthreads();
         if (own) {
 #pragma unroll
             for (int p = 0; p < TPA - 1; ++p) {
-                fx += spart[p][0][tid];
-                fy += spart[p][1][tid];
-                fz += spart[p][2][tid];
-                ue += spart[p][3][tid];
+                df_acc(nacc.xh, nacc.xl, spart[p][0][tid], spart[p][1][tid]);
+                df_acc(nacc.yh, nacc.yl, spart[p][2][tid], spart[p][3][tid]);
+                df_acc(nacc.zh, nacc.zl, spart[p][4][tid], spart[p][5][tid]);
+                ue += spart[p][6][tid];
             }
         }
+        fx = __fadd_rn(nacc.xh, nacc.xl);
+        fy = __fadd_rn(nacc.yh, nacc.yl);
+        fz = __fadd_rn(nacc.zh, nacc.zl);
     }
     if (valid && own) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
     const double imv = MASS ? a.im[i] : 1.0;
@@ -950,6 +1243,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         // half kick in one add), x += dt v, walls, next record.
         const float kdt = FIRST ? a.hdt : 2.0f * a.hdt;
         int32_t xi[3];
+        uint32_t xf[3];
         bool trig = false;
         if (valid && own) {
 #pragma unroll
@@ -957,30 +1251,32 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
             double v = a.w[d][i] + (double)(kdt * fv[d]) * imv;
             double x = fma(a.dt, v, a.x[d][i]);
             const double os = BATCH ? __ldg(&row->os[d]) : a.os[d];
-            int32_t q = __double2int_rn(fma(x, S, -os));
-            // integer pre-check; the exact FP64 test of boundary_reflect! runs
-            // only for atoms within a grid step of a wall
-            const int32_t lfp = BATCH ? __ldg(&row->lo_fp[d]) : a.lo_fp[d];
-            const int32_t hfp = BATCH ? __ldg(&row->hi_fp[d]) : a.hi_fp[d];
+            long long q = __double2ll_rn(fma(x, S * kFine, -os));
+            // integer pre-check (before the wrap); the exact FP64 test of
+            // boundary_reflect! runs only for atoms within a grid step of a wall
+            const int64_t lfp = BATCH ? __ldg(&row->lo_fp[d]) : a.lo_fp[d];
+            const int64_t hfp = BATCH ? __ldg(&row->hi_fp[d]) : a.hi_fp[d];
             if (q <= lfp + 1 || q >= hfp - 1) {
                 const double lo = BATCH ? __ldg(&row->lo[d]) : a.lo[d];
                 const double hi = BATCH ? __ldg(&row->hi[d]) : a.hi[d];
                 if (lo > x) { v = -v; x = lo; }
                 if (hi < x) { v = -v; x = hi; }
-                q = __double2int_rn(fma(x, S, -os));
+                q = __double2ll_rn(fma(x, S * kFine, -os));
                 if (!(x == x)) set_error(a.err, ND_ERR_NONFINITE, (int32_t)i);
             }
             a.x[d][i] = x;
             a.w[d][i] = v;
-            xi[d] = q;
+            xi[d] = (int32_t)(uint32_t)(unsigned long long)(q >> 16);
+            xf[d] = (uint32_t)q & 0xffffu;
         }
         a.rec_out[i] = make_int4(xi[0], xi[1], xi[2], ri.w);
+        a.recf_out[i] = pack_fine(xf[0], xf[1], xf[2]);
         // A list built at r_c + skin stays valid while no atom moved more than
         // skin/2 since the build; count the atom-steps that broke that bound
         // where the next step keeps the list without a check.
         const int4 rb = __ldg(&a.rec_build[i]);
-        const float ex = (float)(xi[0] - rb.x), ey = (float)(xi[1] - rb.y),
-                    ez = (float)(xi[2] - rb.z);
+        const float ex = (float)idiff(xi[0], rb.x), ey = (float)idiff(xi[1], rb.y),
+                    ez = (float)idiff(xi[2], rb.z);
         const float e2 = ex * ex + ey * ey + ez * ez;
         if (a.unchecked && e2 > hs2u) atomicAdd(a.diag, 1ull);
         // Ask for a refit before the next step when this atom could pass the
@@ -989,8 +1285,8 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         // it more than twice as far as this one; with a check after every
         // step, trig_k = 2 still covers one step more).
         if (a.vote) {
-            const float sx = (float)(xi[0] - ri.x), sy = (float)(xi[1] - ri.y),
-                        sz = (float)(xi[2] - ri.z);
+            const float sx = (float)idiff(xi[0], ri.x), sy = (float)idiff(xi[1], ri.y),
+                        sz = (float)idiff(xi[2], ri.z);
             trig = sqrtf(e2) + a.trig_k * sqrtf(sx * sx + sy * sy + sz * sz) > 0.95f * hsu;
         }
         }
@@ -1091,6 +1387,7 @@ static nd_status md_alloc(MDEngine* m) {
         m->set[s].orig = (int32_t*)(b + 8 * n);
         m->set[s].sid = m->nsys > 0 ? m->set[s].orig + n : nullptr;
         if ((st = ensure(c, m->rec_buf[s], n * sizeof(int4)))) return st;
+        if ((st = ensure(c, m->recf_buf[s], n * sizeof(uint2)))) return st;
     }
     if ((st = ensure(c, m->recb, n * sizeof(int4)))) return st;
     if ((st = ensure(c, m->lcount_leaf, sizeof(int32_t) * (size_t)m->nL))) return st;
@@ -1157,7 +1454,14 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
         return st;
     m->union_smem = sizeof(int32_t) * (2 * (size_t)fcap + p2);
     m->step_smem = sizeof(int4) * (size_t)m->ucap_sm * m->apl;
-    m->lists_smem = sizeof(float4) * (size_t)m->ucap_sm * m->apl;
+    // the list kernel stages positions and one candidate bit per thread and
+    // candidate leaf; fewer staged positions when both do not fit
+    {
+        const size_t bits = sizeof(uint32_t) * kBlock * (size_t)((lcap_leaf + 31) / 32);
+        const int64_t room = ((int64_t)maxsm - 1024 - (int64_t)bits) / (int64_t)sizeof(float4);
+        m->lists_smpos = (int32_t)std::max<int64_t>(0, std::min<int64_t>((int64_t)m->ucap_sm * m->apl, room));
+        m->lists_smem = sizeof(float4) * (size_t)m->lists_smpos + bits;
+    }
     // threads per atom of the step kernel: more than one for grids under two
     // waves of one block per SM, when the slice partials fit beside the
     // staged union
@@ -1229,6 +1533,8 @@ StepArgs md_step_args(MDEngine* m, int rec_in) {
     a.ncount = (const int32_t*)m->ncount.p;
     a.rec_in = (const int4*)m->rec_buf[rec_in].p;
     a.rec_out = (int4*)m->rec_buf[rec_in ^ 1].p;
+    a.recf_in = (const uint2*)m->recf_buf[rec_in].p;
+    a.recf_out = (uint2*)m->recf_buf[rec_in ^ 1].p;
     for (int d = 0; d < 3; ++d) {
         a.x[d] = m->set[m->cur].x[d];
         a.w[d] = m->set[m->cur].w[d];
@@ -1261,10 +1567,11 @@ StepArgs md_step_args(MDEngine* m, int rec_in) {
     a.trig_k = 2.0f * (float)std::max(m->check_every - 1, 1);
     a.unchecked = 0;
     for (int d = 0; d < 3; ++d) {
-        a.os[d] = m->fr.o[d] * S;
-        a.lo_fp[d] = (int32_t)std::floor((p.box_lo[d] - m->fr.o[d]) * S);
-        a.hi_fp[d] = (int32_t)std::ceil((p.box_hi[d] - m->fr.o[d]) * S);
+        a.os[d] = m->fr.o[d] * S * kFine;
+        a.lo_fp[d] = (int64_t)std::floor((p.box_lo[d] - m->fr.o[d]) * S * kFine);
+        a.hi_fp[d] = (int64_t)std::ceil((p.box_hi[d] - m->fr.o[d]) * S * kFine);
     }
+    a.nk = md_near(p.sigma, p.epsilon, p.coulomb_k, S);
     a.rc2u = (float)(p.cutoff * p.cutoff * S * S);
     a.sig2u = (float)(p.sigma * p.sigma * S * S);
     a.eps24u = (float)(24.0 * p.epsilon * S);
@@ -1366,7 +1673,7 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
     if (kind == RB_REFIT) {
         k_md_refit_pos<<<g, 256, 0, c->stream>>>(
             live, n, m->fr, sys, (float4*)m->pos32.p, (int4*)m->rec_buf[rec >= 0 ? rec : 0].p,
-            (int4*)m->recb.p, c->d_err, counter);
+            (uint2*)m->recf_buf[rec >= 0 ? rec : 0].p, (int4*)m->recb.p, c->d_err, counter);
         c->launches++;
     } else {
         SetPtrs& tmp = m->set[1];
@@ -1381,7 +1688,8 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
         if ((st = radix_sort_pairs(c, (uint32_t*)codes, perm, n, 30))) return st;
         k_md_reorder<<<g, 256, 0, c->stream>>>(live, tmp, perm, (const float*)m->xyz32.p, n,
                                                m->fr, sys, (float4*)m->pos32.p,
-                                               (int4*)m->rec_buf[0].p, (int4*)m->recb.p, c->d_err);
+                                               (int4*)m->rec_buf[0].p, (uint2*)m->recf_buf[0].p,
+                                               (int4*)m->recb.p, c->d_err);
         k_md_copy_set<<<g, 256, 0, c->stream>>>(tmp, live, n);
         c->launches += 2;
     }
@@ -1403,6 +1711,18 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
     // query boxes slightly above r_list/2 so the box tests never drop a pair;
     // the distance test alone decides membership
     const float hq = (rl / 2.0f) * 1.0001f + 1e-6f;
+    // rounding margin of the lists' point-to-box test: a few ulps of the
+    // largest coordinate (the boxes are atom positions -/+ r_list/2, rounded)
+    float box_margin;
+    {
+        double cmax = 0.0;
+        if (m->nsys > 0) cmax = m->tree_frame[3];
+        else
+            for (int d = 0; d < 3; ++d)
+                cmax = std::max({cmax, std::fabs(m->p.box_lo[d]), std::fabs(m->p.box_hi[d])});
+        cmax += 2.0 * (double)rl;
+        box_margin = (float)(std::ldexp(1.0, std::ilogb(std::max(cmax, 1.0)) - 20) + 1e-6);
+    }
     k_md_block_union<<<(unsigned)m->nblocks, kBlock, m->union_smem, c->stream>>>(
         keys, (const float4*)m->bbox.p, m->nblocks, tree ? 1 : 0, (const float4*)m->pos32.p,
         live.sid, n, m->nL, m->apl, hq, rl, m->fcap, m->ucap,
@@ -1411,7 +1731,9 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
         sizing ? 1 : 0, pressure);
 #define ND_LISTS(A)                                                                             \
     k_md_block_lists<A><<<(unsigned)m->nblocks, kBlock, m->lists_smem, c->stream>>>(            \
-        (const float4*)m->pos32.p, n, rl * rl, m->ucap, m->ucap_sm * m->apl,                    \
+        (const float4*)m->pos32.p, keys, n, rl * rl, rl / 2.0f, box_margin,                     \
+        md_near(m->p.sigma, m->p.epsilon, m->p.coulomb_k, m->fr.s).rnb2,                        \
+        m->nsys > 0 ? live.sid : nullptr, sys, m->ucap, m->lists_smpos,                         \
         (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p,                                \
         (const uint16_t*)m->llist_leaf.p, (const int32_t*)m->lcount_leaf.p, m->lcap_leaf,       \
         m->lcap, (uint16_t*)m->llist.p, (int32_t*)m->ncount.p, c->d_err,                        \
@@ -1847,17 +2169,16 @@ bool md_compatible(MDEngine* m, const nd_md_params* p, int32_t n, bool has_q, bo
            memcmp(&m->p, p, sizeof(nd_md_params)) == 0;
 }
 
-// Fixed-point frame from the walls: a margin of 1/16 of the largest extent on
-// every side, scale = the largest power of two that keeps the frame in int32.
+// Fixed-point frame from the walls: origin 1/16 of the largest extent below
+// the lower walls, scale from md_scale.
 static nd_status md_frame(MDEngine* m) {
     double ext = 0.0;
     for (int d = 0; d < 3; ++d) ext = std::max(ext, m->p.box_hi[d] - m->p.box_lo[d]);
     if (!(ext > 0.0) || !std::isfinite(ext)) return ND_ERR_ARG;
     const double margin = ext / 16.0;
     for (int d = 0; d < 3; ++d) m->fr.o[d] = m->p.box_lo[d] - margin;
-    const double range = ext + 2.0 * margin;
-    int k = (int)std::floor(std::log2(2147480000.0 / range));
-    m->fr.s = std::ldexp(1.0, k);
+    m->fr.s = md_scale(m->p);
+    m->fr.lim = md_frame_lim(ext, m->fr.s);
     return ND_OK;
 }
 
@@ -1897,17 +2218,19 @@ static nd_status md_frame_batch(MDEngine* m, const nd_system* sys) {
         const int32_t cell[3] = {k % G, (k / G) % G, k / (G * G)};
         double ext = 0.0;
         for (int d = 0; d < 3; ++d) ext = std::max(ext, y.box_hi[d] - y.box_lo[d]);
-        const double S = std::ldexp(1.0, (int)std::floor(std::log2(2147480000.0 / (ext * 1.125))));
+        const double S = md_scale(m->p);
         r.s = S;
+        r.lim = md_frame_lim(ext, S);
         for (int d = 0; d < 3; ++d) {
             r.o[d] = y.box_lo[d] - ext / 16.0;
-            r.os[d] = r.o[d] * S;
+            r.os[d] = r.o[d] * S * kFine;
             r.off[d] = cell[d] * slot + 0.5 * gap - y.box_lo[d];
             r.lo[d] = y.box_lo[d];
             r.hi[d] = y.box_hi[d];
-            r.lo_fp[d] = (int32_t)std::floor((y.box_lo[d] - r.o[d]) * S);
-            r.hi_fp[d] = (int32_t)std::ceil((y.box_hi[d] - r.o[d]) * S);
+            r.lo_fp[d] = (int64_t)std::floor((y.box_lo[d] - r.o[d]) * S * kFine);
+            r.hi_fp[d] = (int64_t)std::ceil((y.box_hi[d] - r.o[d]) * S * kFine);
         }
+        r.nk = md_near(y.sigma, y.epsilon, m->p.coulomb_k, S);
         r.sig2u = (float)(y.sigma * y.sigma * S * S);
         r.eps24u = (float)(24.0 * y.epsilon * S);
         r.eps4 = (float)(4.0 * y.epsilon);
@@ -2131,7 +2454,8 @@ nd_status md_destroy(MDEngine* m) {
     if (!m) return ND_OK;
     if (m->graph_main) cudaGraphExecDestroy(m->graph_main);
     if (m->graph_first) cudaGraphExecDestroy(m->graph_first);
-    DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->rec_buf[0], &m->rec_buf[1], &m->recb,
+    DevBuf* bufs[] = {&m->set_buf[0], &m->set_buf[1], &m->rec_buf[0], &m->rec_buf[1],
+                      &m->recf_buf[0], &m->recf_buf[1], &m->recb,
                       &m->xyz32, &m->pos32, &m->keys, &m->store, &m->bbox, &m->ulist, &m->ucount,
                       &m->llist_leaf, &m->lcount_leaf, &m->llist,
                       &m->ncount, &m->f, &m->vtmp, &m->acc, &m->aos, &m->diag, &m->sysrow,
@@ -2327,10 +2651,77 @@ nd_status md_stats(MDEngine* m, int64_t* steps, int64_t* rebuilds, int64_t* list
         e = cudaStreamSynchronize(m->sub.stream);
         if (e != cudaSuccess) return cuda_fail(&m->sub, e, "md stats");
         int64_t s = 0;
-        for (int32_t v : h) s += v;
+        for (int32_t v : h) s += (v & 0xffff) + (v >> 16);
         *list_pairs = s;
     }
     return ND_OK;
+}
+
+// Entries of the current lists as directed pairs of 1-based caller indices
+// (each unordered pair once from each side), with the near-segment flag, in
+// no particular order.
+__global__ void k_md_list_pairs(const int32_t* __restrict__ ncount,
+                                const uint16_t* __restrict__ llist,
+                                const int32_t* __restrict__ ulist, const int32_t* __restrict__ orig,
+                                int32_t n, int32_t apl, int32_t ucap, int32_t lcap,
+                                int32_t* __restrict__ pi, int32_t* __restrict__ pj,
+                                uint8_t* __restrict__ near, int64_t cap,
+                                unsigned long long* cursor) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t b = i / kBlock, t = i - b * kBlock;
+    const int32_t c = ncount[i];
+    const uint16_t* L = llist + (int64_t)b * lcap * kBlock;
+    const int32_t* U = ulist + (int64_t)b * ucap;
+    const int32_t tot = list_total(c), nn = list_near(c);
+    for (int32_t s = 0; s < tot; ++s) {
+        const int32_t li = L[llist_at(list_slot(s, c, lcap), t)];
+        const int32_t j = U[li / apl] * apl + li % apl;
+        const unsigned long long k = atomicAdd(cursor, 1ull);
+        if ((int64_t)k < cap) {
+            pi[k] = orig[i] + 1;
+            pj[k] = orig[j] + 1;
+            near[k] = s < nn ? 1 : 0;
+        }
+    }
+}
+
+nd_status md_list_pairs(MDEngine* m, int32_t* pi, int32_t* pj, uint8_t* near, int64_t cap,
+                        int64_t* count) {
+    Ctx* c = &m->sub;
+    nd_status st = sync_and_check(c, "md list pairs");
+    if (st) return st;
+    int32_t *dpi = nullptr, *dpj = nullptr;
+    uint8_t* dn = nullptr;
+    unsigned long long* cur = nullptr;
+    const size_t k = (size_t)std::max<int64_t>(cap, 1);
+    cudaError_t e = cudaMalloc(&dpi, k * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&dpj, k * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&dn, k);
+    if (e == cudaSuccess) e = cudaMalloc(&cur, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemsetAsync(cur, 0, sizeof(unsigned long long), c->stream);
+    unsigned long long total = 0;
+    if (e == cudaSuccess) {
+        k_md_list_pairs<<<(unsigned)cdiv(m->n, 256), 256, 0, c->stream>>>(
+            (const int32_t*)m->ncount.p, (const uint16_t*)m->llist.p, (const int32_t*)m->ulist.p,
+            m->set[m->cur].orig, m->n, m->apl, m->ucap, m->lcap, dpi, dpj, dn, cap, cur);
+        c->launches++;
+        e = cudaMemcpyAsync(&total, cur, sizeof(total), cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    const int64_t got = std::min<int64_t>((int64_t)total, cap);
+    if (e == cudaSuccess && got > 0 && pi) e = cudaMemcpy(pi, dpi, got * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && got > 0 && pj) e = cudaMemcpy(pj, dpj, got * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && got > 0 && near) e = cudaMemcpy(near, dn, got, cudaMemcpyDeviceToHost);
+    cudaFree(dpi);
+    cudaFree(dpj);
+    cudaFree(dn);
+    cudaFree(cur);
+    if (e != cudaSuccess) return cuda_fail(c, e, "md list pairs");
+    m->parent->launches += c->launches;
+    c->launches = 0;
+    if (count) *count = (int64_t)total;
+    return (int64_t)total > cap ? ND_NEED_REALLOC : ND_OK;
 }
 
 nd_status md_diagnostics(MDEngine* m, nd_md_diag* out) {

@@ -9,10 +9,16 @@ namespace nd {
 
 constexpr int kBlock = 256;          // atoms per block in the list and step kernels
 
-// Fixed-point frame of the pair records: x_fp = rint((x - origin) * scale).
+// Fixed-point frame of the pair records: x_fp = rint((x - origin) * scale)
+// modulo 2^32.  The scale is the largest power of two at which every listed
+// pair's per-axis separation stays below 2^31 grid units, so the wrapped
+// int32 difference of two records is the exact separation even where the
+// records themselves wrap.  lim bounds |x_fp| before the wrap: positions
+// beyond the walls by more than the frame's margin are range errors.
 struct Frame {
     double o[3];
     double s;
+    double lim;
 };
 
 struct SetPtrs {
@@ -24,6 +30,29 @@ struct SetPtrs {
     int32_t* sid;  // batched ensembles: system of each atom (nullptr for one system)
 };
 
+// Near pairs (separation below 1.3 sigma when evaluated) carry most of the
+// rounding error of single-precision pair terms: the force of a pair near the
+// potential minimum is a difference of two nearly equal terms, so a relative
+// error in r^2 reaches the force amplified about 30-fold.  Their terms are
+// evaluated in two-float arithmetic (see accum_near in nd_md.cu).  The list
+// build puts pairs closer than rnb (1.3 sigma + 0.1) in a separate segment of
+// each atom's list; a pair of the other segment that comes closer than 1.3
+// sigma during the window is caught by the rn2u test.
+struct NearK {
+    float rn2u;     // (1.3 sigma S)^2: evaluate accurately below this
+    float sig2lo;   // sigma^2 S^2 - sig2u (rounding of the LJ constant)
+    float e24lo;    // 24 eps S - eps24u
+    float kclo;     // k S^2 - kcu
+    float rnb2;     // (1.3 sigma + 0.1)^2 in physical units: list segment bound
+    int32_t hmask;  // clears the low k bits of a separation: the exact split
+};
+
+// Pair records hold the position on the grid of scale S (coarse, int32 modulo
+// 2^32); a second record per atom holds the next 16 bits of each coordinate
+// (the fine grid, scale S * 2^16), which only the near-pair terms read:
+// coarse = floor(X / 2^16) and fine = X mod 2^16 for X = rint((x - o) S 2^16).
+constexpr double kFine = 65536.0;
+
 // Per-system constants of a batched ensemble.  Each system keeps its own
 // fixed-point frame (origin o, scale s) and is placed in its own slot of the
 // tree frame (Float32 positions = x + off), slots far enough apart that no
@@ -31,22 +60,37 @@ struct SetPtrs {
 // fixed-point units.
 struct SysRow {
     double o[3];                 // fixed-point frame origin
-    double os[3];                // o * s
+    double os[3];                // o * s * 2^16
     double off[3];               // tree-frame offset
     double lo[3], hi[3];         // walls
-    double s;                    // fixed-point scale
-    int32_t lo_fp[3], hi_fp[3];  // walls in fixed point
+    double s;                    // fixed-point scale (coarse grid)
+    double lim;                  // range bound of x_fp before the wrap (coarse units)
+    int64_t lo_fp[3], hi_fp[3];  // walls on the fine grid (before the wrap)
     float sig2u, eps24u, eps4, rc2u, kcu, kceu, hs2u, hsu;
+    NearK nk;                    // near-pair constants
 };
 
-__device__ __forceinline__ int32_t to_fixed(double x, double o, double s, int32_t* err,
-                                            int32_t who) {
-    double t = fma(x, s, -(o * s));
-    if (!(t > -2147483000.0 && t < 2147483000.0)) {
+// Records keep x_fp modulo 2^32; the difference of two records, taken modulo
+// 2^32, is the exact separation of any listed pair.
+__device__ __forceinline__ int32_t idiff(int32_t a, int32_t b) {
+    return (int32_t)((uint32_t)a - (uint32_t)b);
+}
+
+// Coarse record coordinate (modulo 2^32) and its fine bits of position x.
+__device__ __forceinline__ int32_t to_fixed(double x, double o, double s, double lim,
+                                            int32_t* err, int32_t who, uint32_t& fine) {
+    const double sf = s * kFine;
+    double t = fma(x, sf, -(o * sf));
+    if (!(t > -lim * kFine && t < lim * kFine)) {
         set_error(err, isfinite(x) ? ND_ERR_RANGE : ND_ERR_NONFINITE, who);
         t = 0.0;
     }
-    return __double2int_rn(t);
+    const long long X = __double2ll_rn(t);
+    fine = (uint32_t)X & 0xffffu;
+    return (int32_t)(uint32_t)(unsigned long long)(X >> 16);
+}
+__device__ __forceinline__ uint2 pack_fine(uint32_t fx, uint32_t fy, uint32_t fz) {
+    return make_uint2(fx | (fy << 16), fz);
 }
 
 struct StepArgs {
@@ -58,6 +102,8 @@ struct StepArgs {
     const int32_t* __restrict__ ncount;
     const int4* __restrict__ rec_in;
     int4* __restrict__ rec_out;
+    const uint2* __restrict__ recf_in;  // fine bits of the records
+    uint2* __restrict__ recf_out;
     double* x[3];
     double* w[3];
     const double* __restrict__ im;
@@ -68,8 +114,9 @@ struct StepArgs {
     unsigned long long* __restrict__ diag;  // [0] atom-steps moved > skin/2 since the build
     int32_t* err;
     float half_skin2u;  // (skin/2)^2 in fixed-point units
-    double os[3];       // origin * scale (fixed-point offset)
-    int32_t lo_fp[3], hi_fp[3];  // walls in fixed point (filter for the exact FP64 test)
+    double os[3];       // origin * scale * 2^16 (fixed-point offset, fine grid)
+    int64_t lo_fp[3], hi_fp[3];  // walls on the fine grid (filter for the exact FP64 test)
+    NearK nk;           // near-pair constants (one system)
     // pair constants in fixed-point units (S = frame scale)
     float rc2u;    // (r_c S)^2
     float sig2u;   // (sigma S)^2
@@ -113,7 +160,7 @@ struct MDEngine {
     bool rebuild_due = false;
     int64_t steps = 0, rebuilds = 0;
     Frame fr{};
-    DevBuf set_buf[2], rec_buf[2], recb, xyz32, pos32, keys, store, bbox, ulist, ucount, llist_leaf,
+    DevBuf set_buf[2], rec_buf[2], recf_buf[2], recb, xyz32, pos32, keys, store, bbox, ulist, ucount, llist_leaf,
         lcount_leaf, llist, ncount, f, vtmp, acc, aos, diag, sysrow, sid_in;
     // batched ensemble (nsys > 0): per-system rows and the Hilbert grid whose
     // level-log2(G) cells are the systems' slots
@@ -136,6 +183,7 @@ struct MDEngine {
     int64_t resort_kernels = 0;       // kernels of one re-sort rebuild
     int64_t eager_bodies = 0;         // kernels of rebuild bodies run eagerly (counted by the host)
     size_t step_smem = 0, union_smem = 0, lists_smem = 0;
+    int32_t lists_smpos = 0;  // positions the list kernel stages in shared memory
     int32_t tpa = 1;  // threads per atom of the step kernel
     // observers of the step loop: thermostat (rescale_velocity!) and position log
     double thermo_T = 0.0, thermo_gamma = 0.0;
@@ -148,11 +196,20 @@ struct MDEngine {
 enum { RB_RESORT = 0, RB_REFIT = 1 };
 
 // Per-atom neighbour lists (uint16 indices into the block's union), per block
-// of kBlock atoms, slot-major: entry s of the block's thread t is element
+// of kBlock atoms, slot-major: slot s of the block's thread t is element
 // s * kBlock + t, so a warp reading its atoms' s-th entries reads 64
-// contiguous bytes.
+// contiguous bytes.  Each list has two segments: the near entries from slot
+// 0 upwards and the others from slot lcap - 1 downwards; ncount packs the
+// two counts (near in the low 16 bits).
 __device__ __forceinline__ int64_t llist_at(int32_t s, int32_t t) {
     return (int64_t)s * kBlock + t;
+}
+__device__ __forceinline__ int32_t list_near(int32_t c) { return c & 0xffff; }
+__device__ __forceinline__ int32_t list_total(int32_t c) { return (c & 0xffff) + (c >> 16); }
+// slot of logical entry s (near entries first, then the others in build order)
+__device__ __forceinline__ int32_t list_slot(int32_t s, int32_t c, int32_t lcap) {
+    const int32_t nn = c & 0xffff;
+    return s < nn ? s : lcap - 1 - (s - nn);
 }
 
 // Rebuild of the neighbour lists (re-sort or refit; see nd_md.cu).

@@ -11,16 +11,20 @@
 // buffers; the library never grows anything.
 //
 // Limits and sharing rules (also stated in include/naivegpu.h):
-//   * at most kNoAllocMaxAtoms atoms, atomsperleaf >= 2; larger requests are
-//     rejected with ND_ERR_ARG before any work is enqueued;
+//   * at most kNoAllocMaxAtoms atoms, atomsperleaf >= 2 in both modes (an
+//     unordered request with a leaf width other than 4 is served by the
+//     ordered emission); larger requests are rejected with ND_ERR_ARG before
+//     any work is enqueued;
 //   * the array (kNoAllocBytes, ~5.3 MB) is reserved on every GPU that loads
 //     the library and stays there until the process exits;
 //   * all calls share the one array, so calls whose work overlaps on the GPU
 //     (different streams, or different host threads) race and corrupt each
 //     other -- serialise them;
 //   * the first call on a device looks the array's device address up
-//     (cudaGetSymbolAddress, with that device current); make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress, with that device current) and keeps it for the
+//     life of the process; make that first call before any stream capture.
+//     The kept address does not survive cudaDeviceReset (the module, and with
+//     it the array, is loaded again afterwards): no call after a reset.
 #include <mutex>
 
 #include "nd_internal.cuh"

@@ -11,7 +11,8 @@ from ._lib import (Context, NDError, SpecError, InexactError, default_context,
                    GRIDKEY_DTYPE, PAIR_DTYPE)
 from .bvh import (SpheresBVHSpecs, APointPrimitive, leafTreeData, TreeData,
                   leafbuild_traverse_bvh, simdbuild_traverse_bvh, build_traverse_bvh,
-                  gpubvh_neighborlist, neighbor_pairs_dev, pair_hash_dev)
+                  gpubvh_neighborlist, gpubvh_neighborlist_, neighbor_pairs_dev,
+                  pair_hash_dev)
 from .dynamics import (ForceField, md_params, force_lennardjones_, force_coulomb_, sum_forces_,
                        force_lennardjones_compat_, force_coulomb_compat_,
                        forces, SimSpec, GenericObjectCollection, GenericRandomCollector,

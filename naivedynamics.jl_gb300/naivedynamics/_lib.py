@@ -140,6 +140,8 @@ SIGNATURES = {
                        _vp]),
     "nd_leaf_pairs": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _i32, _i32, _vp, _vp, _vp, _i64,
                              ctypes.POINTER(_i64)]),
+    "nd_leaf_pairs_refresh": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _vp, _vp, _i32, _vp, _i64,
+                                     _vp, _vp, _vp, _vp, _i64, ctypes.POINTER(_i64)]),
     "nd_leaf_pairs_dev": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _i32, _i32, _vp, _vp, _vp,
                                  _i64, ctypes.POINTER(_i64)]),
     "nd_simd_leaf_pairs": (_i32, [_vp, _vp, ctypes.POINTER(BVHSpec), _i32, _i32, _vp, _vp, _vp,
@@ -180,6 +182,7 @@ SIGNATURES = {
                               _vp, _vp, _vp, _vp, _i32, ctypes.POINTER(MDParams),
                               ctypes.POINTER(_d)]),
     "nd_md_diagnostics": (_i32, [_vp, ctypes.POINTER(MDDiag)]),
+    "nd_md_list_pairs": (_i32, [_vp, _vp, _vp, _vp, _i64, ctypes.POINTER(_i64)]),
     "nd_md_set_thermostat": (_i32, [_vp, _d, _d, _i32]),
     "nd_md_set_log": (_i32, [_vp, _i32, _i32]),
     "nd_md_log_count": (_i32, [_vp, ctypes.POINTER(_i64)]),

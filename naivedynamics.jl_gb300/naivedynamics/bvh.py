@@ -6,6 +6,7 @@ Names, argument meaning and results follow the reference:
   leafbuild_traverse_bvh   BVHTraverse.jl:1423-1428
   build_traverse_bvh       BVHTraverse.jl:1416-1421
   gpubvh_neighborlist      ext/NaiveKA.jl:470-558
+  gpubvh_neighborlist!     ext/NaiveKA.jl:597-636 (gpubvh_neighborlist_)
 Pair lists are structured arrays of (i, j, d) = Tuple{Int32,Int32,Float32}
 with 1-based original indices, every unordered pair once.
 """
@@ -24,7 +25,7 @@ from ._lib import (GRIDKEY_DTYPE, ND_BOX_ATOM, ND_BOX_LEAF, ND_NEED_REALLOC, ND_
 
 __all__ = ["SpheresBVHSpecs", "APointPrimitive", "leafTreeData", "TreeData",
            "leafbuild_traverse_bvh", "simdbuild_traverse_bvh", "build_traverse_bvh",
-           "gpubvh_neighborlist", "neighbor_pairs_dev", "pair_hash_dev", "GRIDKEY_DTYPE",
+           "gpubvh_neighborlist", "gpubvh_neighborlist_", "neighbor_pairs_dev", "pair_hash_dev", "GRIDKEY_DTYPE",
            "PAIR_DTYPE", "ND_ORDER_REFERENCE", "ND_ORDER_SPATIAL", "ND_PAIRS_ORDERED",
            "ND_PAIRS_UNORDERED"]
 
@@ -191,6 +192,65 @@ def gpubvh_neighborlist(backend, position, spec: SpheresBVHSpecs, order: int = N
     keys, pos, perm, store = leafTreeData(position, spec, order=order, ctx=ctx)
     pairs = leafbuild_traverse_bvh(position, spec, order=order, ctx=ctx)
     return GPUNeighborList(pairs, (keys, pos, perm, store))
+
+
+def gpubvh_neighborlist_(neighborlist, treedata, spec: SpheresBVHSpecs, backend, position=None,
+                         mode: int = ND_PAIRS_ORDERED):
+    """gpubvh_neighborlist!(neighborlist, treedata, spec, backend)
+    (ext/NaiveKA.jl:597-636): the pair list of new positions from a kept tree.
+
+    treedata is what gpubvh_neighborlist (or leafTreeData) returned: (tree,
+    mortonpositions, mortsort, store).  The new positions are `position`
+    (caller order), or, when it is None, the ones the caller wrote into
+    treedata's mortonpositions.position (kept order, rows labelled by
+    mortonpositions.index).  The kept order and sorted codes are reused -- the
+    same topology, boxes of the new positions -- and treedata's tree and
+    positions are updated in place; neighborlist (a PAIR_DTYPE array that owns
+    its memory) is resized and filled in place.  Returns (pairlist, treedata)
+    like gpubvh_neighborlist.  The reference's body reads an undefined
+    `position` at HEAD; here the new positions come as described.
+    """
+    if backend is None or isinstance(backend, int):
+        ctx = default_context(backend or 0)
+    else:
+        ctx = backend
+    keys, mpos, perm, store = treedata
+    n = spec.atom_count
+    index = np.ascontiguousarray(mpos.index, np.int32)
+    code = np.ascontiguousarray(mpos.morton_code, np.int32)
+    if position is None:
+        x = np.empty((n, 3), np.float32)
+        x[index - 1] = mpos.position
+    else:
+        x = _positions(position)
+    if x.shape[0] != n or index.shape[0] != n:
+        raise ValueError("position length differs from spec.atom_count")
+    cs = spec.c_spec()
+    newpos = np.empty((n, 3), np.float32)
+    count = ctypes.c_int64()
+    cap = 0
+    while True:
+        pi = np.empty(max(cap, 1), np.int32)
+        pj = np.empty(max(cap, 1), np.int32)
+        pd = np.empty(max(cap, 1), np.float32)
+        st = _lib.lib().nd_leaf_pairs_refresh(ctx.handle, ptr(x), ctypes.byref(cs), ptr(index),
+                                              ptr(code), mode, ptr(keys), int(keys.shape[0]),
+                                              ptr(newpos), ptr(pi), ptr(pj), ptr(pd), cap,
+                                              ctypes.byref(count))
+        if st == ND_NEED_REALLOC:
+            cap = int(count.value)
+            continue
+        ctx.check(st, "gpubvh_neighborlist!")
+        break
+    k = int(count.value)
+    mpos.position[...] = newpos
+    out = neighborlist
+    if out is None or out.dtype != PAIR_DTYPE:
+        out = np.empty(k, PAIR_DTYPE)
+    else:
+        out.resize(k, refcheck=False)
+    out["i"], out["j"], out["d"] = pi[:k], pj[:k], pd[:k]
+    return GPUNeighborList(out, (keys, mpos, perm, store))
 
 
 def neighbor_pairs_dev(xyz_dev, spec: SpheresBVHSpecs, pi_dev, pj_dev, pd_dev, capacity: int,

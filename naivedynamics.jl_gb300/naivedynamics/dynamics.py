@@ -432,6 +432,22 @@ class MDEngine:
                        "nd_md_diagnostics")
         return {name: getattr(d, name) for name, _ in d._fields_ if name != "reserved"}
 
+    def list_pairs(self):
+        """The engine's current neighbour lists: (i, j, near) arrays of directed
+        entries (1-based caller indices; each unordered pair once from each
+        side), near = 1 for the near segment."""
+        n = ctypes.c_int64()
+        st = _lib.lib().nd_md_list_pairs(self.handle, None, None, None, 0, ctypes.byref(n))
+        if st not in (0, 1):
+            self.ctx.check(st, "nd_md_list_pairs")
+        cap = n.value
+        pi = np.empty(cap, np.int32)
+        pj = np.empty(cap, np.int32)
+        near = np.empty(cap, np.uint8)
+        self.ctx.check(_lib.lib().nd_md_list_pairs(self.handle, ptr(pi), ptr(pj), ptr(near), cap,
+                                                   ctypes.byref(n)), "nd_md_list_pairs")
+        return pi, pj, near
+
     def step_times(self, steps: int):
         """Advance `steps` steps eagerly, timing each step kernel with CUDA
         events on the context stream; returns the durations in ms."""

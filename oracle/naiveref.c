@@ -246,6 +246,11 @@ static void bvh_interior(ref_key* keys, int32_t* store, int32_t i, int32_t nL,
     }
 }
 
+static int tree_in_order(const float* xyz, int32_t n, float r, int32_t apl, int32_t boxes,
+                         int32_t overwrite_root, ref_key* keys, int64_t nkeys,
+                         const int32_t* idx_sorted, const int32_t* code_sorted, float* pos_sorted,
+                         int32_t* store);
+
 int ref_tree(const float* xyz, int32_t n, float r, int32_t apl, int32_t order, int32_t boxes,
              int32_t overwrite_root, ref_key* keys, int64_t nkeys, int32_t* idx_sorted,
              int32_t* code_sorted, float* pos_sorted, int32_t* perm) {
@@ -268,10 +273,28 @@ int ref_tree(const float* xyz, int32_t n, float r, int32_t apl, int32_t order, i
         int32_t o = perm[k];
         idx_sorted[k] = o + 1;
         code_sorted[k] = codes[o];
-        for (int d = 0; d < 3; ++d) pos_sorted[3 * k + d] = xyz[3 * o + d];
     }
     free(codes);
+    st = tree_in_order(xyz, n, r, apl, boxes, overwrite_root, keys, nkeys, idx_sorted,
+                       code_sorted, pos_sorted, store);
+    free(store);
+    return st;
+}
 
+/* The tree of positions xyz in a given sorted order (1-based original index
+ * per sorted slot) with given sorted codes: leaf boxes, then the Apetrei
+ * build, which depends on the sorted codes only.  With the order and codes of
+ * an earlier build this is that build's topology with the boxes of the new
+ * positions (the refit TreeData!, BVHTraverse.jl:601-655, intends). */
+static int tree_in_order(const float* xyz, int32_t n, float r, int32_t apl, int32_t boxes,
+                         int32_t overwrite_root, ref_key* keys, int64_t nkeys,
+                         const int32_t* idx_sorted, const int32_t* code_sorted, float* pos_sorted,
+                         int32_t* store) {
+    int32_t nL = n / apl;
+    for (int32_t k = 0; k < n; ++k) {
+        int32_t o = idx_sorted[k] - 1;
+        for (int d = 0; d < 3; ++d) pos_sorted[3 * k + d] = xyz[3 * o + d];
+    }
     memset(keys, 0, sizeof(ref_key) * (size_t)nkeys);
     /* leafcluster_primitives (:376-410) uses r/2, cluster_primitives (:341-375) r. */
     float h = (boxes == REF_BOX_LEAF) ? r / 2.0f : r;
@@ -298,8 +321,22 @@ int ref_tree(const float* xyz, int32_t n, float r, int32_t apl, int32_t order, i
     if (overwrite_root) {
         for (int d = 0; d < 3; ++d) { KEY(nL + 1).min[d] = 0.0f; KEY(nL + 1).max[d] = 1.0f; }
     }
-    free(store);
     return REF_OK;
+}
+
+int ref_tree_kept(const float* xyz, int32_t n, float r, int32_t apl, int32_t overwrite_root,
+                  ref_key* keys, int64_t nkeys, const int32_t* idx_sorted,
+                  const int32_t* code_sorted, float* pos_sorted) {
+    int32_t nL = 0, nB = 0;
+    int st = ref_spec(n, apl, &nL, &nB);
+    if (st != REF_OK) return st;
+    if ((int64_t)n - 1 < 2LL * nL - 1 || nkeys < 2LL * nL - 1) return REF_ERR_SPEC;
+    int32_t* store = (int32_t*)calloc((size_t)nB, sizeof(int32_t));
+    if (!store) return REF_ERR_NOMEM;
+    st = tree_in_order(xyz, n, r, apl, REF_BOX_LEAF, overwrite_root, keys, nkeys, idx_sorted,
+                       code_sorted, pos_sorted, store);
+    free(store);
+    return st;
 }
 
 /* ------------------------------------------------------------------ traversal */
@@ -1041,4 +1078,197 @@ int64_t ref_md_run_bvh(const ref_md_params* p, int32_t n, double* x, double* v, 
     int64_t np = L.n;
     free(L.i); free(L.j); free(fth);
     return st < 0 ? st : np;
+}
+
+/* ---------------------------------------------- steady-state CPU baseline */
+
+/* The loop of ref_md_run_bvh as a session: creation copies the state, builds
+ * the first list and evaluates the forces (the set-up a run pays once);
+ * ref_md_bvh_steps then advances with the rebuild after every `rebuild`-th
+ * step since creation, so a window of `rebuild` steps holds exactly one
+ * leaf-BVH build and `rebuild` force evaluations. */
+struct ref_md_bvh {
+    ref_md_params p;
+    int32_t n, rebuild, apl, order, nt;
+    float rl;
+    int64_t done;
+    double *x, *v, *f, *q, *im, *fth;
+    pairbuf L;
+};
+
+ref_md_bvh* ref_md_bvh_create(const ref_md_params* p, int32_t n, const double* x,
+                              const double* v, const double* q, const double* m,
+                              int32_t rebuild, double skin, int32_t apl, int32_t order) {
+    ref_md_bvh* s = (ref_md_bvh*)calloc(1, sizeof(ref_md_bvh));
+    if (!s) return NULL;
+    s->p = *p;
+    s->n = n;
+    s->rebuild = rebuild;
+    s->apl = apl;
+    s->order = order;
+    s->nt = ref_num_threads();
+    s->rl = (float)(p->cutoff + skin);
+    const size_t b = sizeof(double) * 3 * (size_t)n;
+    s->x = (double*)malloc(b);
+    s->v = (double*)malloc(b);
+    s->f = (double*)malloc(b);
+    s->q = q ? (double*)malloc(sizeof(double) * (size_t)n) : NULL;
+    s->im = (double*)malloc(sizeof(double) * (size_t)n);
+    s->fth = (double*)malloc(b * (size_t)s->nt);
+    if (!s->x || !s->v || !s->f || (q && !s->q) || !s->im || !s->fth) {
+        ref_md_bvh_destroy(s);
+        return NULL;
+    }
+    memcpy(s->x, x, b);
+    memcpy(s->v, v, b);
+    if (q) memcpy(s->q, q, sizeof(double) * (size_t)n);
+    for (int32_t i = 0; i < n; ++i) s->im[i] = m ? 1.0 / m[i] : 1.0;
+    if (build_half_list(s->x, n, s->rl, apl, order, &s->L) < 0) {
+        ref_md_bvh_destroy(s);
+        return NULL;
+    }
+    forces_from_list(&s->p, n, s->x, s->q, &s->L, s->f, s->fth, s->nt);
+    return s;
+}
+
+int64_t ref_md_bvh_steps(ref_md_bvh* s, int64_t steps) {
+    const int32_t n = s->n;
+    const double h = 0.5 * s->p.dt;
+    for (int64_t k = 0; k < steps; ++k) {
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; ++i)
+            for (int d = 0; d < 3; ++d) {
+                s->v[3 * i + d] += h * s->f[3 * i + d] * s->im[i];
+                s->x[3 * i + d] += s->p.dt * s->v[3 * i + d];
+            }
+        reflect(&s->p, n, s->x, s->v);
+        ++s->done;
+        if (s->rebuild > 0 && s->done % s->rebuild == 0) {
+            int64_t st = build_half_list(s->x, n, s->rl, s->apl, s->order, &s->L);
+            if (st < 0) return st;
+        }
+        forces_from_list(&s->p, n, s->x, s->q, &s->L, s->f, s->fth, s->nt);
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; ++i)
+            for (int d = 0; d < 3; ++d) s->v[3 * i + d] += h * s->f[3 * i + d] * s->im[i];
+    }
+    return s->L.n;
+}
+
+void ref_md_bvh_get(const ref_md_bvh* s, double* x, double* v, double* f) {
+    const size_t b = sizeof(double) * 3 * (size_t)s->n;
+    if (x) memcpy(x, s->x, b);
+    if (v) memcpy(v, s->v, b);
+    if (f) memcpy(f, s->f, b);
+}
+
+void ref_md_bvh_destroy(ref_md_bvh* s) {
+    if (!s) return;
+    free(s->x); free(s->v); free(s->f); free(s->q); free(s->im); free(s->fth);
+    free(s->L.i); free(s->L.j);
+    free(s);
+}
+
+/* ------------------------------------------------------ synthetic inputs */
+
+/* The benchmark workloads' seeded inputs, generated here so that the CPU
+ * baseline needs nothing but this library: a splitmix64 stream (Steele, Lea
+ * and Flood 2014), uniforms from its top 53 bits, normals by Box-Muller (one
+ * value per pair of uniforms), positions by random sequential addition with a
+ * minimum separation over a cell grid, charges +1 / -1 half each shuffled by
+ * Fisher-Yates.  They match the GPU library's host generators bit for bit
+ * (checked by the test suite). */
+typedef struct { uint64_t s; } sm64;
+
+static uint64_t sm64_next(sm64* g) {
+    uint64_t z = (g->s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static double sm64_uniform(sm64* g) { return (double)(sm64_next(g) >> 11) * 0x1.0p-53; }
+
+static double sm64_normal(sm64* g) {
+    double u1 = sm64_uniform(g);
+    double u2 = sm64_uniform(g);
+    if (u1 < 1e-300) u1 = 1e-300;
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+int ref_synth_uniform(uint64_t seed, int32_t n, double lo, double side, float* xyz) {
+    if (!xyz || n < 0) return REF_ERR_ARG;
+    sm64 g = {seed};
+    for (int64_t k = 0; k < 3LL * n; ++k) xyz[k] = (float)(lo + side * sm64_uniform(&g));
+    return 0;
+}
+
+int ref_synth_uniform_mindist(uint64_t seed, int32_t n, double side, double dmin, double* xyz) {
+    if (!xyz || n < 0 || !(side > 0) || !(dmin >= 0)) return REF_ERR_ARG;
+    sm64 g = {seed};
+    int nc = dmin > 0 ? (int)floor(side / dmin) : 1;
+    if (nc < 1) nc = 1;
+    if (nc > 1024) nc = 1024;
+    const double cs = side / nc;
+    const size_t ncell = (size_t)nc * nc * nc;
+    int32_t* head = (int32_t*)malloc(sizeof(int32_t) * ncell);
+    int32_t* next = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    if (!head || !next) { free(head); free(next); return REF_ERR_NOMEM; }
+    for (size_t c = 0; c < ncell; ++c) head[c] = -1;
+    const double d2 = dmin * dmin;
+    int status = 0;
+    for (int32_t i = 0; i < n && status == 0; ++i) {
+        int placed = 0;
+        for (int attempt = 0; attempt < 100000 && !placed; ++attempt) {
+            double p[3];
+            int ci[3];
+            for (int d = 0; d < 3; ++d) {
+                p[d] = side * sm64_uniform(&g);
+                int c = (int)(p[d] / cs);
+                ci[d] = c < nc - 1 ? c : nc - 1;
+            }
+            int ok = 1;
+            for (int oz = -1; oz <= 1 && ok; ++oz)
+                for (int oy = -1; oy <= 1 && ok; ++oy)
+                    for (int ox = -1; ox <= 1 && ok; ++ox) {
+                        int X = ci[0] + ox, Y = ci[1] + oy, Z = ci[2] + oz;
+                        if (X < 0 || Y < 0 || Z < 0 || X >= nc || Y >= nc || Z >= nc) continue;
+                        for (int32_t j = head[((size_t)Z * nc + Y) * nc + X]; j >= 0; j = next[j]) {
+                            double dx = p[0] - xyz[3 * (size_t)j], dy = p[1] - xyz[3 * (size_t)j + 1],
+                                   dz = p[2] - xyz[3 * (size_t)j + 2];
+                            if (dx * dx + dy * dy + dz * dz < d2) { ok = 0; break; }
+                        }
+                    }
+            if (!ok) continue;
+            for (int d = 0; d < 3; ++d) xyz[3 * (size_t)i + d] = p[d];
+            size_t cell = ((size_t)ci[2] * nc + ci[1]) * nc + ci[0];
+            next[i] = head[cell];
+            head[cell] = i;
+            placed = 1;
+        }
+        if (!placed) status = REF_ERR_ARG;
+    }
+    free(head);
+    free(next);
+    return status;
+}
+
+int ref_synth_normal(uint64_t seed, int64_t count, double s, double* out) {
+    if (!out || count < 0) return REF_ERR_ARG;
+    sm64 g = {seed};
+    for (int64_t k = 0; k < count; ++k) out[k] = s * sm64_normal(&g);
+    return 0;
+}
+
+int ref_synth_charges(uint64_t seed, int32_t n, double* q) {
+    if (!q || n < 0 || (n & 1)) return REF_ERR_ARG;
+    sm64 g = {seed};
+    for (int32_t i = 0; i < n; ++i) q[i] = i < n / 2 ? 1.0 : -1.0;
+    for (int32_t i = n - 1; i > 0; --i) {
+        int32_t j = (int32_t)(sm64_next(&g) % (uint64_t)(i + 1));
+        double t = q[i];
+        q[i] = q[j];
+        q[j] = t;
+    }
+    return 0;
 }

@@ -75,6 +75,13 @@ int ref_tree(const float* xyz, int32_t n, float r, int32_t apl, int32_t order, i
              int32_t overwrite_root, ref_key* keys, int64_t nkeys, int32_t* idx_sorted,
              int32_t* code_sorted, float* pos_sorted, int32_t* perm);
 
+/* The leafTreeData tree (leaf boxes p -/+ r/2) of positions xyz in a kept
+ * order: idx_sorted (1-based original index per sorted slot) and code_sorted
+ * from an earlier ref_tree; the same topology with the new boxes. */
+int ref_tree_kept(const float* xyz, int32_t n, float r, int32_t apl, int32_t overwrite_root,
+                  ref_key* keys, int64_t nkeys, const int32_t* idx_sorted,
+                  const int32_t* code_sorted, float* pos_sorted);
+
 /*
  * leafneighbor_traverse (BVHTraverse.jl:1236-1323) run with one thread: emits
  * pairs in the reference's serial order.  Returns the number of pairs; writes
@@ -212,6 +219,33 @@ int64_t ref_md_run_bvh(const ref_md_params* p, int32_t n, double* x, double* v, 
                        double skin, int32_t apl, int32_t order);
 
 int ref_num_threads(void);
+
+/*
+ * The same loop as a session, for timing steady-state windows: create copies
+ * x, v (N x 3), q, m (either may be NULL), builds the first list and evaluates
+ * the forces; steps advances, rebuilding after every `rebuild`-th step since
+ * creation (so `rebuild` steps hold one build), and returns the pairs of the
+ * current list or a negative status.  NULL from create: bad input or no memory.
+ */
+typedef struct ref_md_bvh ref_md_bvh;
+ref_md_bvh* ref_md_bvh_create(const ref_md_params* p, int32_t n, const double* x,
+                              const double* v, const double* q, const double* m,
+                              int32_t rebuild, double skin, int32_t apl, int32_t order);
+int64_t ref_md_bvh_steps(ref_md_bvh* s, int64_t steps);
+void ref_md_bvh_get(const ref_md_bvh* s, double* x, double* v, double* f);
+void ref_md_bvh_destroy(ref_md_bvh* s);
+
+/*
+ * Seeded synthetic inputs of the benchmark workloads (splitmix64 stream):
+ * uniform Float32 positions in [lo, lo + side)^3; FP64 positions in
+ * [0, side)^3 with no two closer than dmin (random sequential addition);
+ * N(0, s^2) values; charges +1 / -1, half each, shuffled.  Status 0 or
+ * negative.
+ */
+int ref_synth_uniform(uint64_t seed, int32_t n, double lo, double side, float* xyz);
+int ref_synth_uniform_mindist(uint64_t seed, int32_t n, double side, double dmin, double* xyz);
+int ref_synth_normal(uint64_t seed, int64_t count, double s, double* out);
+int ref_synth_charges(uint64_t seed, int32_t n, double* q);
 
 /* ------------------------------------------------ differentiable trajectory */
 

@@ -99,6 +99,10 @@ def lib():
                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
                                    ctypes.c_int64, i32p, i32p, f32p, i32p]
             L.ref_tree.restype = ctypes.c_int
+            L.ref_tree_kept.argtypes = [f32p, ctypes.c_int32, ctypes.c_float, ctypes.c_int32,
+                                        ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, i32p, i32p,
+                                        f32p]
+            L.ref_tree_kept.restype = ctypes.c_int
             for name in ("ref_leaf_traverse", "ref_atom_traverse"):
                 fn = getattr(L, name)
                 fn.argtypes = [ctypes.c_void_p, i32p, f32p, ctypes.c_int32, ctypes.c_int32,
@@ -149,6 +153,26 @@ def lib():
             L.ref_adj_dual.restype = ctypes.c_int
             L.ref_num_threads.argtypes = []
             L.ref_num_threads.restype = ctypes.c_int
+            L.ref_md_bvh_create.argtypes = [ctypes.POINTER(RefMDParams), ctypes.c_int32, f64p,
+                                            f64p, f64p, f64p, ctypes.c_int32, ctypes.c_double,
+                                            ctypes.c_int32, ctypes.c_int32]
+            L.ref_md_bvh_create.restype = ctypes.c_void_p
+            L.ref_md_bvh_steps.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+            L.ref_md_bvh_steps.restype = ctypes.c_int64
+            L.ref_md_bvh_get.argtypes = [ctypes.c_void_p, f64p, f64p, f64p]
+            L.ref_md_bvh_get.restype = None
+            L.ref_md_bvh_destroy.argtypes = [ctypes.c_void_p]
+            L.ref_md_bvh_destroy.restype = None
+            L.ref_synth_uniform.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_double,
+                                            ctypes.c_double, f32p]
+            L.ref_synth_uniform.restype = ctypes.c_int
+            L.ref_synth_uniform_mindist.argtypes = [ctypes.c_uint64, ctypes.c_int32,
+                                                    ctypes.c_double, ctypes.c_double, f64p]
+            L.ref_synth_uniform_mindist.restype = ctypes.c_int
+            L.ref_synth_normal.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_double, f64p]
+            L.ref_synth_normal.restype = ctypes.c_int
+            L.ref_synth_charges.argtypes = [ctypes.c_uint64, ctypes.c_int32, f64p]
+            L.ref_synth_charges.restype = ctypes.c_int
             _lib = L
     return _lib
 
@@ -216,6 +240,26 @@ def tree(xyz, r, apl, order=REF_ORDER_REFERENCE, boxes=REF_BOX_LEAF, overwrite_r
     if boxes == REF_BOX_LEAF:
         keys = keys[: n - 1]
     return dict(keys=keys, index=idx, code=code, position=pos, perm=perm, leaves=nl)
+
+
+def tree_kept(xyz, r, apl, index, code, overwrite_root=True):
+    """leafTreeData of new positions in a kept order (index: 1-based original
+    index per sorted slot, code: the sorted codes of an earlier tree()): the
+    same topology with the new boxes.  Returns the dict of tree()."""
+    a = _xyz(xyz)
+    n = a.shape[0]
+    nl, _ = spec(n, apl)
+    nkeys = max(n - 1, 2 * nl - 1)
+    keys = np.zeros(nkeys, KEY_DTYPE)
+    idx = np.ascontiguousarray(index, np.int32)
+    cd = np.ascontiguousarray(code, np.int32)
+    pos = np.empty((n, 3), np.float32)
+    _check(lib().ref_tree_kept(_p(a, ctypes.c_float), n, np.float32(r), apl,
+                               1 if overwrite_root else 0, keys.ctypes.data, nkeys,
+                               _p(idx, ctypes.c_int32), _p(cd, ctypes.c_int32),
+                               _p(pos, ctypes.c_float)))
+    return dict(keys=keys[: n - 1], index=idx.copy(), code=cd.copy(), position=pos,
+                perm=idx - 1, leaves=nl)
 
 
 def _pairs_call(fn, *args, cap_hint=1024):
@@ -455,3 +499,76 @@ def adj_dual(p, s, x0, v0, q=None, m=None, dx0=None, dv0=None, target=None):
                               _p(xo, f64), _p(vo, f64), _p(ev, ctypes.c_uint64)))
     return dict(loss=loss.value, dloss=dl, hist=hist, x=xo, v=vo,
                 events=(int(ev[0]), int(ev[1])))
+
+
+class MDSession:
+    """ref_md_bvh_*: the CPU-baseline loop as a session (first list and forces
+    at creation, then steady-state steps with a rebuild every `rebuild`)."""
+
+    def __init__(self, p, x, v, q=None, m=None, rebuild=10, skin=0.3, apl=4,
+                 order=REF_ORDER_REFERENCE):
+        x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+        v = np.ascontiguousarray(v, np.float64).reshape(-1, 3)
+        qq = None if q is None else np.ascontiguousarray(q, np.float64)
+        mm = None if m is None else np.ascontiguousarray(m, np.float64)
+        self.n = x.shape[0]
+        self.h = lib().ref_md_bvh_create(ctypes.byref(p), self.n, _p(x, ctypes.c_double),
+                                         _p(v, ctypes.c_double), _p(qq, ctypes.c_double),
+                                         _p(mm, ctypes.c_double), rebuild, skin, apl, order)
+        if not self.h:
+            raise OracleError("ref_md_bvh_create failed")
+
+    def steps(self, k):
+        st = lib().ref_md_bvh_steps(self.h, int(k))
+        if st < 0:
+            raise OracleError(f"oracle status {st}")
+        return int(st)
+
+    def get(self):
+        x = np.empty((self.n, 3))
+        v = np.empty((self.n, 3))
+        f = np.empty((self.n, 3))
+        lib().ref_md_bvh_get(self.h, _p(x, ctypes.c_double), _p(v, ctypes.c_double),
+                             _p(f, ctypes.c_double))
+        return x, v, f
+
+    def close(self):
+        if self.h:
+            lib().ref_md_bvh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def synth_uniform(seed, n, side, lo=0.0):
+    out = np.empty((n, 3), np.float32)
+    _check(lib().ref_synth_uniform(seed, n, lo, side, _p(out, ctypes.c_float)))
+    return out
+
+
+def synth_uniform_mindist(seed, n, side, dmin):
+    out = np.empty((n, 3), np.float64)
+    _check(lib().ref_synth_uniform_mindist(seed, n, side, dmin, _p(out, ctypes.c_double)))
+    return out
+
+
+def synth_normal(seed, shape, s=1.0):
+    out = np.empty(shape, np.float64)
+    _check(lib().ref_synth_normal(seed, out.size, s, _p(out, ctypes.c_double)))
+    return out
+
+
+def synth_charges(seed, n):
+    out = np.empty(n, np.float64)
+    _check(lib().ref_synth_charges(seed, n, _p(out, ctypes.c_double)))
+    return out
+
+
+def synth_lj_system(seed, n, side, dmin=0.8, charges=False):
+    """The benchmark's LJ box inputs (x, v, q) from the oracle's own generators:
+    the same seeds and streams as the GPU library's nd_synth_* generators."""
+    x = synth_uniform_mindist(seed, n, side, dmin)
+    v = synth_normal(seed ^ 0x5EED0001, (n, 3), 1.0)
+    q = synth_charges(seed ^ 0x5EED0002, n) if charges else None
+    return x, v, q

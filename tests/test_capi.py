@@ -139,3 +139,31 @@ def test_pair_array_conversion(nd):
     assert list(i) == [1, 2, 3] and list(j) == [4, 5, 6]
     i, j = _pair_arrays([(1, 2, 0.5), (3, 4, 0.25)])
     assert list(i) == [1, 3] and list(j) == [2, 4]
+
+
+def test_oracle_generators_match_library(nd, oracle):
+    # The CPU baseline draws its inputs from the oracle's own generators (it
+    # never loads the GPU library); they must be the GPU arm's inputs bit for
+    # bit: the 262,144-atom workload's stream at a smaller size, and the plain
+    # LJ box.
+    for seed, n, side, ch in [(0x4E440002, 20000, 28.8, True), (0x4E440001, 4096, 17.0, False)]:
+        a = oracle.synth_lj_system(seed, n, side, 0.8, ch)
+        b = nd.synth.lj_system(seed, n, side, 0.8, ch)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        assert (a[2] is None and b[2] is None) or np.array_equal(a[2], b[2])
+    assert np.array_equal(oracle.synth_uniform(7, 1000, 3.0), nd.synth.uniform_positions(7, 1000, 3.0))
+
+
+def test_oracle_session_equals_run(oracle):
+    # The steady-state session (create, then steps) follows the same
+    # trajectory as the one-call CPU baseline loop.
+    x, v, q = oracle.synth_lj_system(0x4E440002, 2048, 13.6, 0.8, True)
+    p = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(13.6,) * 3, dt=1e-3)
+    xa, va, fa, na = oracle.md_run_bvh(p, x, v, q, steps=25, rebuild=10, skin=0.3, apl=4)
+    s = oracle.MDSession(p, x, v, q, rebuild=10, skin=0.3, apl=4)
+    s.steps(10)
+    nb = s.steps(15)
+    xb, vb, fb = s.get()
+    s.close()
+    assert na == nb
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)

@@ -102,6 +102,12 @@ def test_family_positions(nd, oracle, n):
 
 
 def test_position8_fixture(nd, oracle):
+    # test/BVHTraverse.jl:165-220: TreeData of the eight hand-placed points at
+    # r = 10, one atom per leaf; the skip ropes, the root box, every atom
+    # paired, and (:205-209) the per-atom traversal's list sorted by (i, j)
+    # equal to threshold_pairs(unique_pairs(position8), 10) -- indices and the
+    # Float32 distances sqrt(sum((a - b).^2)) of AllToAll.jl -- on the GPU
+    # and on the oracle.
     x = np.array([[0.1, 0.1, 0.1], [0.2, 0.2, 0.2], [0.346, 0.98, 0.12], [0.01, 0.76, 0.99],
                   [0.1111, 0.4, 0.31], [0.234, 0.29, 0.2], [0.11346, 0.918, 0.1276],
                   [0.061, 0.76, 0.989]], np.float32)
@@ -109,10 +115,62 @@ def test_position8_fixture(nd, oracle):
     keys, pos, perm, _ = nd.TreeData(x, spec)
     assert keys[7]["skip"] == 0 and all(keys[k]["skip"] != 0 for k in range(7))
     assert np.all(keys[8]["min"] < x) and np.all(x < keys[8]["max"])
-    pairs = nd.build_traverse_bvh(x, spec)
-    assert len(pairs) == 28
+    naive = oracle.brute_pairs(x, 10.0, criterion=1)  # unique_pairs + threshold_pairs (d < 10)
+    assert len(naive[0]) == 28
+    t = oracle.tree(x, 10.0, 1, boxes=oracle.REF_BOX_ATOM)
+    for lst in (_pairs_arr(nd.build_traverse_bvh(x, spec)), oracle.atom_traverse(t, 10.0, 1)):
+        i, j, d = (np.asarray(a) for a in lst)
+        paired = np.zeros(9, bool)
+        paired[i] = True
+        paired[j] = True
+        assert paired[1:].all()
+        a, b = np.minimum(i, j), np.maximum(i, j)
+        o = np.lexsort((b, a))  # sort!(list, by=x->x[2]); sort!(list, by=x->x[1])
+        assert np.array_equal(a[o], naive[0]) and np.array_equal(b[o], naive[1])
+        assert np.array_equal(d[o].view(np.int32), naive[2].view(np.int32))
     res = nd.gpubvh_neighborlist(None, x, nd.SpheresBVHSpecs(10.0, 8, 2))
     assert len(res.pairlist) == 28
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_gpubvh_neighborlist_refresh(nd, oracle, order):
+    # gpubvh_neighborlist!(neighborlist, treedata, spec, backend): the list of
+    # moved positions from the kept tree (same order and codes, new boxes);
+    # ordered emission bit-exact against the oracle's leaf traversal over the
+    # kept-order tree, the tree and positions written back into treedata, and
+    # the pair set equal to a fresh build's.
+    x = uniform(0x4E440051, 4096, 1.0)
+    spec = nd.SpheresBVHSpecs(0.05, len(x), 4)
+    res = nd.gpubvh_neighborlist(None, x, spec, order=order)
+    keys, mpos, perm, _ = res.treedata
+    code0 = mpos.morton_code.copy()
+    rng = np.random.default_rng(7)
+    y = (x + rng.normal(0.0, 0.004, x.shape)).astype(np.float32)
+    lst = res.pairlist
+    out = nd.gpubvh_neighborlist_(lst, res.treedata, spec, None, position=y)
+    assert out.pairlist is lst  # filled in place
+    t = oracle.tree_kept(y, 0.05, 4, mpos.index, code0)
+    _exact(out.pairlist, oracle.leaf_traverse(t, 0.05, 4))
+    n = len(keys)
+    assert np.array_equal(out.treedata[0].view(np.int32).reshape(n, 8),
+                          t["keys"][:n].view(np.int32).reshape(n, 8))
+    assert np.array_equal(out.treedata[1].position, t["position"])
+    fresh = oracle.leafbuild_traverse_bvh(y, 0.05, 4)
+    assert np.array_equal(canon(*_pairs_arr(out.pairlist)), canon(*fresh))
+    # positions written into treedata by the caller (the in-place form)
+    z = (y + rng.normal(0.0, 0.004, y.shape)).astype(np.float32)
+    out.treedata[1].position[...] = z[out.treedata[1].index - 1]
+    again = nd.gpubvh_neighborlist_(None, out.treedata, spec, None)
+    t2 = oracle.tree_kept(z, 0.05, 4, mpos.index, code0)
+    _exact(again.pairlist, oracle.leaf_traverse(t2, 0.05, 4))
+    un = nd.gpubvh_neighborlist_(None, again.treedata, spec, None, position=z,
+                                 mode=nd.ND_PAIRS_UNORDERED)
+    assert np.array_equal(canon(*_pairs_arr(un.pairlist)), canon(*oracle.leaf_traverse(t2, 0.05, 4)))
+    # a kept order that is not a permutation is refused
+    bad = (keys, nd.APointPrimitive(mpos.index.copy(), code0, mpos.position), perm, None)
+    bad[1].index[0] = bad[1].index[1]
+    with pytest.raises(nd.NDError):
+        nd.gpubvh_neighborlist_(None, bad, spec, None, position=z)
 
 
 def test_degenerate_inputs(nd, oracle):

@@ -2,9 +2,9 @@
 
 Tolerances (stated per result, as the contract requires):
   * forces: relative L2 error |F32 - F64|_2 / |F64|_2 <= 1e-5, and the per-atom
-    error max_i |dF_i| / max(|F64_i|, 1e-3 rms|F64|) <= 2e-3 (the floor term is
-    dominated by FP32 rounding of individual pair terms for atoms whose net
-    force nearly cancels);
+    error max_i |dF_i| / max(|F64_i|, 1e-3 rms|F64|) <= 1e-5 (pairs closer than
+    1.3 sigma are evaluated in two-float arithmetic, the rest in plain single
+    precision);
   * energies: relative error <= 1e-6;
   * dynamics over 100 steps (dt = 1e-3, rebuild every 10): positions within
     1e-5 (absolute, box side 17) of the FP64 trajectory -- an FP32 force error
@@ -20,7 +20,7 @@ from helpers import force_errors
 pytestmark = pytest.mark.gpu
 
 F_L2_TOL = 1e-5
-F_ATOM_TOL = 2e-3
+F_ATOM_TOL = 1e-5
 
 
 def _config1(nd, charges=False, n=4096, side=17.0, seed=0x4E440001):
@@ -93,7 +93,9 @@ def test_md_trajectory_vs_fp64(nd, oracle):
     # forces at the GPU's final positions vs FP64 forces there
     f64, u64, _ = oracle.forces(p, x)
     per_atom, l2 = force_errors(f, f64)
+    print(f"forces after 100 steps: per-atom {per_atom:.3e}  L2 {l2:.3e}")
     assert l2 <= F_L2_TOL
+    assert per_atom <= F_ATOM_TOL
     e0, e1 = pe0 + ke0, pe1 + ke1
     print(f"energy: {e0:.6f} -> {e1:.6f} (rel drift {abs(e1-e0)/abs(e0):.2e})")
     u0 = oracle.forces(p, x0)[1]
@@ -214,22 +216,65 @@ def test_compat_force_calls(nd, oracle):
         nd.force_coulomb_compat_(np.zeros((len(x), 3), np.float32), bad, q)
 
 
+def _dist2_ref(xf, i, j):
+    """Float32 sum((a - b).^2), left to right, as the list build computes it."""
+    d = xf[i] - xf[j]
+    return (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+
+
+def _check_engine_lists(eng, oracle, x, r_list, sigma=1.0):
+    """The engine's lists at its last build, as a set, against every pair with
+    d^2 < r_list^2 on the same Float32 positions, and the near segment against
+    d^2 < (1.3 sigma + 0.1)^2.  Up to 20,000 atoms the oracle is brute force
+    (AllToAll); above, the directed lists must be symmetric and their half
+    (i < j) must match the oracle's leaf-BVH traversal in count and 128-bit
+    order-free hash of (i, j, bits(d))."""
+    xf = np.asarray(x, np.float64).astype(np.float32)
+    n = len(xf)
+    pi, pj, near = eng.list_pairs()
+    d2 = _dist2_ref(xf, pi - 1, pj - 1)
+    rnb2 = np.float32((1.3 * sigma + 0.1) ** 2)
+    assert np.array_equal(near.astype(bool), d2 < rnb2)
+    got = np.sort(pi.astype(np.int64) * (n + 1) + pj)
+    if n <= 20000:
+        bi, bj, _ = oracle.brute_pairs(xf, np.float32(r_list), 0)
+        exp = np.sort(np.concatenate([bi.astype(np.int64) * (n + 1) + bj,
+                                      bj.astype(np.int64) * (n + 1) + bi]))
+        assert got.shape == exp.shape, (got.shape, exp.shape)
+        assert np.array_equal(got, exp)
+        npairs = len(bi)
+    else:
+        assert np.array_equal(got, np.sort(pj.astype(np.int64) * (n + 1) + pi))
+        h = pi < pj
+        d = np.sqrt(d2[h])
+        t = oracle.tree(xf, np.float32(r_list), 4, order=oracle.REF_ORDER_SPATIAL)
+        cnt, hash_ref = oracle.leaf_traverse_hash(t, np.float32(r_list), 4)
+        assert int(h.sum()) == cnt
+        assert oracle.pair_hash(pi[h], pj[h], d) == hash_ref
+        npairs = cnt
+    return npairs, int(near.sum()) // 2
+
+
 def test_md_neighbor_list_pair_set(nd, oracle):
-    # The engine's list at a rebuild equals every pair with d^2 < r_list^2 on
-    # the Float32 positions (full list: each pair twice).
+    # The engine's own lists (the ones the dynamics use), at the first build
+    # and at the rebuild after one window, equal as sets every pair with
+    # d^2 < r_list^2 on the Float32 positions of that build (each pair in both
+    # atoms' lists), near segments included; plain 4,096-atom LJ.
     x0, v0, _ = _config1(nd)
     eng = nd.MDEngine(_params(nd, 17.0), x0, v0)
-    eng.run(10)   # window 0 done, next run rebuilds
-    eng.run(1)    # rebuild at step 10 + one step
-    x10 = None
+    npairs, nnear = _check_engine_lists(eng, oracle, x0, np.float32(2.5 + 0.3))
+    assert eng.stats()["list_pairs"] == 2 * npairs
+    eng.run(10)
+    eng.run(1)    # the rebuild at step 10, then one step
     eng2 = nd.MDEngine(_params(nd, 17.0), x0, v0)
     eng2.run(10)
     x10, _, _ = eng2.get()
+    assert eng.diagnostics()["early_refits"] == 0
+    npairs10, _ = _check_engine_lists(eng, oracle, x10, np.float32(2.5 + 0.3))
+    print(f"engine lists: {npairs} pairs ({nnear} near) at step 0, {npairs10} at step 10")
+    # reference-order pair list on the same Float32 positions, bit-exact
     xf = x10.astype(np.float32)
     b = oracle.brute_pairs(xf, np.float32(2.8), 0)
-    lst = eng.stats()["list_pairs"]
-    assert lst == 2 * len(b[0])
-    # reference-order pair list on the same Float32 positions, bit-exact
     spec = nd.SpheresBVHSpecs(2.8, len(xf), 4)
     p = nd.leafbuild_traverse_bvh(xf, spec)
     t = oracle.tree(xf, 2.8, 4)
@@ -237,6 +282,39 @@ def test_md_neighbor_list_pair_set(nd, oracle):
     assert np.array_equal(p["i"], ri) and np.array_equal(p["j"], rj)
     assert np.array_equal(p["d"].view(np.int32), rd.view(np.int32))
     assert np.array_equal(canon(p["i"], p["j"], p["d"]), canon(*b))
+
+
+def test_config2_engine_vs_fp64(nd, oracle):
+    # The benchmarked system: 262,144 atoms, side 68, charges +/-1, LJ +
+    # Coulomb, r_c = 2.5, with the bench's engine settings (skin 0.4, eight
+    # atoms per leaf).  Forces and energy at step 0 and after two rebuild
+    # windows against FP64, the 20-step trajectory against the FP64
+    # integrator, and the lists at the first build as a set.
+    n, side = 262144, 68.0
+    x0, v0, q = nd.synth.lj_system(0x4E440002, n, side, 0.8, charges=True)
+    eng = nd.MDEngine(_params(nd, side, coulomb=1.0, skin=0.4, atomsperleaf=8), x0, v0, q)
+    p = oracle.md_params(coulomb_k=1.0, cutoff=2.5, box_hi=(side,) * 3, dt=1e-3)
+    npairs, nnear = _check_engine_lists(eng, oracle, x0, np.float32(2.5 + 0.4))
+    print(f"262k lists: {npairs} pairs, {nnear} near")
+    _, _, f0 = eng.get()
+    pe0, _ = eng.energy()
+    f64, u64, _ = oracle.forces(p, x0, q)
+    per_atom, l2 = force_errors(f0, f64)
+    print(f"262k step 0: per-atom {per_atom:.3e}  L2 {l2:.3e}  energy {abs(pe0-u64)/abs(u64):.2e}")
+    assert per_atom <= F_ATOM_TOL and l2 <= F_L2_TOL
+    assert abs(pe0 - u64) <= 1e-6 * abs(u64)
+    eng.run(20)
+    xg, vg, fg = eng.get()
+    pe1, _ = eng.energy()
+    xr, vr, _ = oracle.md_run(p, x0, v0, q, steps=20)
+    dx = np.abs(xg - xr).max()
+    f64b, u64b, _ = oracle.forces(p, xg, q)
+    per_atom_b, l2_b = force_errors(fg, f64b)
+    print(f"262k step 20: max|dx| {dx:.2e}  per-atom {per_atom_b:.3e}  L2 {l2_b:.3e}")
+    assert dx < 1e-5
+    assert per_atom_b <= F_ATOM_TOL and l2_b <= F_L2_TOL
+    assert abs(pe1 - u64b) <= 1e-6 * abs(u64b)
+    assert eng.diagnostics()["skin_violations"] == 0
 
 
 def test_md_graph_equals_eager_and_deterministic(nd):

@@ -395,3 +395,17 @@ def test_cpu_baseline_matches_fp64_step(oracle):
     xb, vb, fb, _ = oracle.md_run_bvh(p, x, v, steps=20, rebuild=10, skin=0.3, apl=4)
     assert np.abs(xa - xb).max() < 1e-11
     assert np.abs(va - vb).max() < 1e-9
+
+
+def test_tree_kept_order(oracle):
+    # The kept-order tree (gpubvh_neighborlist!'s refit): on the same
+    # positions it is the full build; on moved positions its leaf traversal
+    # gives the brute-force pair set.
+    x = uniform(0x4E440052, 2000, 1.0)
+    t = oracle.tree(x, 0.08, 4)
+    k = oracle.tree_kept(x, 0.08, 4, t["index"], t["code"])
+    assert np.array_equal(k["keys"].view(np.int32), t["keys"].view(np.int32))
+    y = (x + np.random.default_rng(3).normal(0.0, 0.01, x.shape)).astype(np.float32)
+    k = oracle.tree_kept(y, 0.08, 4, t["index"], t["code"])
+    assert np.array_equal(canon(*oracle.leaf_traverse(k, 0.08, 4)),
+                          canon(*oracle.brute_pairs(y, 0.08, 0)))
