@@ -59,6 +59,17 @@ def _plain(o):
     return o
 
 
+def _plain(o):
+    """JSON-ready copy: numpy scalars and arrays as Python numbers and lists."""
+    if isinstance(o, dict):
+        return {k: _plain(v) for k, v in o.items()}
+    if isinstance(o, (list, tuple)):
+        return [_plain(v) for v in o]
+    if hasattr(o, "tolist"):
+        return o.tolist()
+    return o
+
+
 def _md_params(nd, order=None):
     return nd.md_params(sigma=1.0, epsilon=1.0, coulomb_k=1.0, cutoff=2.5, skin=0.3, dt=1e-3,
                         box_lo=(0, 0, 0), box_hi=(SIDE, SIDE, SIDE), atomsperleaf=4,

@@ -835,6 +835,7 @@ nd_status adj_set_target(AdjEngine* A, const double* target) {
 }
 
 nd_status adj_forward(AdjEngine* A, double* hist, double* loss) {
+    NvtxRange nv("nd adjoint forward");
     MDEngine* m = A->m;
     Ctx* c = &m->sub;
     nd_status st;
@@ -872,6 +873,7 @@ nd_status adj_forward(AdjEngine* A, double* hist, double* loss) {
 }
 
 nd_status adj_backward(AdjEngine* A, double* dx0, double* dv0, double* dsigma, double* deps) {
+    NvtxRange nv("nd adjoint backward");
     MDEngine* m = A->m;
     Ctx* c = &m->sub;
     nd_status st;

@@ -158,6 +158,7 @@ static nd_status pairs_from_tree(Ctx* c, const TreeBuffers& t, const nd_bvh_spec
 nd_status pairs_common(Ctx* c, const nd_bvh_spec* s, int32_t order, int32_t mode, int kind,
                        const float* xyz, bool host, int32_t* pi, int32_t* pj, float* pd,
                        int64_t capacity, int64_t* count, int32_t criterion) {
+    NvtxRange nv("nd leaf pairs");
     nd_status st = spec_ok(s);
     if (st) return st;
     if (criterion != ND_CRIT_SQUARED && criterion != ND_CRIT_SQRT) return ND_ERR_ARG;
@@ -769,6 +770,7 @@ int64_t nd_md_launches_per_run(nd_md* md, int64_t steps) {
 
 nd_status nd_simulate(nd_ctx* h, const nd_md_params* p, int32_t n, double* x, double* v,
                       float* f, const double* q, const double* m, int64_t steps) {
+    nd::NvtxRange nv("nd simulate");
     if (!h || !p || !x || !v || steps < 0) return ND_ERR_ARG;
     Ctx* c = &h->c;
     nd_status st = nd::set_device(c);

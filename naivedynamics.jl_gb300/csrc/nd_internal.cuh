@@ -9,6 +9,7 @@
 #include <string>
 
 #include "../../include/naivegpu.h"
+#include <nvtx3/nvToolsExt.h>
 
 namespace nd {
 
@@ -118,6 +119,15 @@ __host__ __device__ inline void pair_hash_one(int32_t i, int32_t j, float d, uin
     h0 += x;
     h1 += y;
 }
+
+// NVTX range for the host-side phases (build, lists, steps, windows), so that
+// profilers can attribute launches; header-only NVTX3, a no-op without a tool.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ---------------------------------------------------------------- buffers
 

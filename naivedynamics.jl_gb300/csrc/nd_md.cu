@@ -649,14 +649,14 @@ __global__ void __launch_bounds__(kBlock)
                     const float gy = fmaxf(fmaxf((a.y + h) - p.y, p.y - (b.x - h)) - margin, 0.0f);
                     const float gz = fmaxf(fmaxf((a.z + h) - p.z, p.z - (b.y - h)) - margin, 0.0f);
                     if (gx * gx + gy * gy + gz * gz < rl2) word |= 1u << (k & 31);
-                }
-                if ((k & 31) == 31) {
-                    sbits[(k >> 5) * kBlock + tid] = word;
-                    word = 0;
+                    // a word is complete at every 32nd candidate and at the last
+                    if ((k & 31) == 31 || k == nc - 1) {
+                        sbits[(k >> 5) * kBlock + tid] = word;
+                        word = 0;
+                    }
                 }
             }
         }
-        if (nc & 31) sbits[(nc >> 5) * kBlock + tid] = word;
     }
     // pass 2: the distance tests against the atoms of the marked leaves
     uint16_t* __restrict__ L = llist + (int64_t)blockIdx.x * lcap * kBlock + tid;
@@ -1468,7 +1468,7 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     {
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
-        const size_t part_sm = sizeof(float) * 4 * kBlock * (kSmallTPA - 1);
+        const size_t part_sm = sizeof(float) * 7 * kBlock * (kSmallTPA - 1);
         m->tpa = (m->nsys == 0 && m->nblocks < 2 * nsm &&
                   (int)(m->step_smem + part_sm) + 1024 <= maxsm) ? kSmallTPA : 1;
     }
@@ -1659,6 +1659,7 @@ static unsigned* ctl_word(MDEngine* m, int k) { return (unsigned*)m->ctl.p + k; 
 // and the step parity restarts.  counter: device count of this kind of
 // rebuild (nullptr: not counted).  sizing: capacity-sizing pass.
 nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool sizing) {
+    NvtxRange nv(kind == RB_REFIT ? "nd md rebuild (refit)" : "nd md rebuild (re-sort)");
     Ctx* c = &m->sub;
     const int32_t n = m->n;
     const unsigned g = (unsigned)cdiv(n, 256);
@@ -1756,6 +1757,7 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
 // decides on the device: inside a capture an IF/ELSE node, otherwise after
 // reading the decision back.
 static nd_status md_window_begin(MDEngine* m, bool capture) {
+    NvtxRange nv("nd md window begin");
     Ctx* c = &m->sub;
     nd_status st;
     cudaGraphConditionalHandle h = 0;
@@ -1954,6 +1956,7 @@ static nd_status md_observe(MDEngine* m, int32_t p, bool capture, int64_t g) {
 // of events per step recorded around the step kernel.
 static nd_status md_steps(MDEngine* m, int32_t k, int32_t pos0, bool capture = false,
                           cudaEvent_t* ev = nullptr) {
+    NvtxRange nv(capture ? "nd md capture steps" : "nd md steps");
     Ctx* c = &m->sub;
     const int32_t R = m->p.rebuild_every;
     nd_status st;
@@ -2322,6 +2325,7 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
 nd_status md_create(Ctx* parent, const nd_md_params* p, int32_t n, const double* x,
                     const double* v, const double* q, const double* mass, bool host,
                     bool capture, MDEngine** out) {
+    NvtxRange nv("nd md create");
     return md_create_common(parent, p, n, x, v, q, mass, host, capture, out);
 }
 
@@ -2473,6 +2477,7 @@ nd_status md_destroy(MDEngine* m) {
 // Advance `steps` steps: whole windows replay the captured graph of the
 // current state set (rebuild + R steps); partial windows are enqueued eagerly.
 nd_status md_run(MDEngine* m, int64_t steps) {
+    NvtxRange nv("nd md run");
     Ctx* c = &m->sub;
     const int32_t R = m->p.rebuild_every;
     nd_status st;
@@ -2522,6 +2527,7 @@ nd_status md_run(MDEngine* m, int64_t steps) {
 // every step kernel with its own pair of events on the stream: ms[k] is the
 // k-th step kernel's duration.
 nd_status md_step_times(MDEngine* m, int32_t steps, float* ms) {
+    NvtxRange nv("nd md step times");
     Ctx* c = &m->sub;
     if (steps <= 0 || !ms) return ND_ERR_ARG;
     const int32_t R = m->p.rebuild_every;
