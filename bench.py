@@ -407,7 +407,14 @@ def plain_leg(nd, ctx, ext, flush):
     x, v, _ = nd.synth.lj_system(nd.synth.SEED_PLAIN_LJ, n, side, 0.8)
     p0 = nd.md_params(cutoff=2.5, skin=0.3, dt=1e-3, box_hi=(side,) * 3, atomsperleaf=4,
                       rebuild_every=REBUILD)
+    t0 = time.perf_counter()
     p, _ = nd.autotune(p0, x, v, trial_steps=50, ctx=ctx)
+    tune_s, tune_cached = time.perf_counter() - t0, nd.autotune.last_cached
+    # the same call again: served from the tuned-settings cache
+    t0 = time.perf_counter()
+    p_again, _ = nd.autotune(p0, x, v, trial_steps=50, ctx=ctx)
+    again_s, again_cached = time.perf_counter() - t0, nd.autotune.last_cached
+    assert all(getattr(p_again, k) == getattr(p, k) for k in nd.TUNED_FIELDS)
     eng = nd.MDEngine(p, x, v, ctx=ctx)
     times = []
     for k in range(6):
@@ -458,7 +465,11 @@ def plain_leg(nd, ctx, ext, flush):
            "tuned": {"skin": p.skin, "atomsperleaf": p.atomsperleaf,
                      "resort_every": p.resort_every, "stage_policy": p.stage_policy,
                      "union_search": UNION_NAMES[p.union_search],
-                     "refit_check_every": max(p.refit_check_every, 1)},
+                     "refit_check_every": max(p.refit_check_every, 1),
+                     "threads_per_atom": p.threads_per_atom,
+                     "autotune_s": round(tune_s, 3), "autotune_from_cache": tune_cached,
+                     "second_call_s": round(again_s, 4),
+                     "second_call_from_cache": again_cached},
            "early_refits": d["early_refits"], "skin_violations": d["skin_violations"]}
     t0 = time.perf_counter()
     R.md_run_bvh(pr, x, v, steps=steps, rebuild=REBUILD, skin=0.3, apl=4,
@@ -620,7 +631,7 @@ def run_gb300(args):
     # library's autotuner on this state, outside the timed region
     t0 = time.perf_counter()
     params, _ = nd.autotune(_md_params(nd), x, v, q, trial_steps=50, ctx=ctx)
-    tune_s = time.perf_counter() - t0
+    tune_s, tune_cached = time.perf_counter() - t0, nd.autotune.last_cached
     eng = nd.MDEngine(params, xd, vd, qd, device=True, ctx=ctx)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -731,7 +742,9 @@ def run_gb300(args):
                              "stage_policy": params.stage_policy,
                              "union_search": UNION_NAMES[params.union_search],
                              "refit_check_every": max(params.refit_check_every, 1),
-                             "autotune_s": round(tune_s, 2)},
+                             "threads_per_atom": params.threads_per_atom,
+                             "autotune_s": round(tune_s, 2),
+                             "autotune_from_cache": tune_cached},
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "neighbours_per_atom": round(nbr, 2),
                    "skin_violations": diag["skin_violations"],

@@ -110,6 +110,10 @@ typedef struct {
                               skin/2 from its list-build position within the next k steps
                               (assuming no step moves an atom more than twice as far as the
                               step before the check) */
+    int32_t threads_per_atom; /* threads sharing one atom's neighbour list in the step
+                              kernel: 1, 2 or 4; 0 = 4 for a single system whose blocks of
+                              256 atoms are fewer than two per SM, else 1 (ensembles: 1) */
+    int32_t reserved;      /* 0 */
 } nd_md_params;
 
 #define ND_UNION_BLOCKS 0
@@ -137,6 +141,10 @@ const char* nd_status_string(nd_status st);
 /* The context's cudaStream_t, for callers that enqueue their own work. */
 void* nd_ctx_stream(nd_ctx* ctx);
 nd_status nd_ctx_synchronize(nd_ctx* ctx);
+/* The context's device as "<name> sm_<major><minor> x<SMs>" (NUL-terminated,
+ * at most len bytes): a key for tuned settings.  No counterpart in the
+ * reference. */
+nd_status nd_ctx_device_name(const nd_ctx* ctx, char* buf, int32_t len);
 /* Number of kernels this library has launched on the context (diagnostics). */
 int64_t nd_ctx_launch_count(const nd_ctx* ctx);
 
@@ -530,6 +538,14 @@ nd_status nd_md_autotune(nd_ctx* ctx, const nd_md_params* p, int32_t n, int32_t 
  */
 nd_status nd_simulate(nd_ctx* ctx, const nd_md_params* p, int32_t n, double* x, double* v,
                       float* f, const double* q, const double* m, int64_t steps);
+
+/* Diagnostics (nd_md_diag) of the engine that the context's last nd_simulate
+ * call ran: a caller checks skin_violations > 0 -- atom-steps computed on a
+ * list that an atom had left by more than skin/2, so that pairs may have been
+ * missed -- and raises the skin or the check frequency.  ND_ERR_ARG when no
+ * call has run.  No counterpart in the reference (it rebuilds its all-pairs
+ * list every step and has no skin). */
+nd_status nd_simulate_diagnostics(nd_ctx* ctx, nd_md_diag* out);
 
 /* ------------------------------------------------------------------ adjoint */
 

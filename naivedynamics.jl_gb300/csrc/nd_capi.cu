@@ -335,6 +335,19 @@ const char* nd_status_string(nd_status st) { return nd::status_text(st); }
 
 void* nd_ctx_stream(nd_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
 
+nd_status nd_ctx_device_name(const nd_ctx* h, char* buf, int32_t len) {
+    if (!h || !buf || len <= 0) return ND_ERR_ARG;
+    cudaDeviceProp prop{};
+    cudaError_t e = cudaGetDeviceProperties(&prop, h->c.device);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return ND_ERR_CUDA;
+    }
+    snprintf(buf, (size_t)len, "%s sm_%d%d x%d", prop.name, prop.major, prop.minor,
+             prop.multiProcessorCount);
+    return ND_OK;
+}
+
 nd_status nd_ctx_synchronize(nd_ctx* h) {
     if (!h) return ND_ERR_ARG;
     return nd::sync_and_check(&h->c, "synchronize");
@@ -798,6 +811,13 @@ nd_status nd_simulate(nd_ctx* h, const nd_md_params* p, int32_t n, double* x, do
         c->sim_cache = nullptr;
     }
     return st;
+}
+
+nd_status nd_simulate_diagnostics(nd_ctx* h, nd_md_diag* out) {
+    if (!h || !out || !h->c.sim_cache) return ND_ERR_ARG;
+    nd_status st = nd::set_device(&h->c);
+    if (st) return st;
+    return nd::md_diagnostics(h->c.sim_cache, out);
 }
 
 // ------------------------------------------------------------------ adjoint

@@ -1468,9 +1468,14 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     {
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
-        const size_t part_sm = sizeof(float) * 7 * kBlock * (kSmallTPA - 1);
-        m->tpa = (m->nsys == 0 && m->nblocks < 2 * nsm &&
-                  (int)(m->step_smem + part_sm) + 1024 <= maxsm) ? kSmallTPA : 1;
+        auto fits = [&](int t) {
+            const size_t part_sm = sizeof(float) * 7 * kBlock * (size_t)(t - 1);
+            return (int)(m->step_smem + part_sm) + 1024 <= maxsm;
+        };
+        const int req = m->p.threads_per_atom;
+        if (m->nsys > 0) m->tpa = 1;
+        else if (req > 0) m->tpa = fits(req) ? req : 1;
+        else m->tpa = (m->nblocks < 2 * nsm && fits(kSmallTPA)) ? kSmallTPA : 1;
     }
     if ((int)m->union_smem + 1024 > maxsm || (lcap > 0 && (int)m->step_smem + 1024 > maxsm)) {
         c->last_error = "neighbour union too large for shared memory";
@@ -1504,7 +1509,8 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     ND_SMEM(false, false, false, 2)
 #undef ND_SMEM
 #define ND_SMEM(C, M, F, MODE) \
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false, kSmallTPA>, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false, kSmallTPA>, maxsm); \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false, 2>, maxsm);
     ND_SMEM(true, true, true, 0) ND_SMEM(true, true, false, 0) ND_SMEM(true, false, true, 0)
     ND_SMEM(true, false, false, 0) ND_SMEM(false, true, true, 0) ND_SMEM(false, true, false, 0)
     ND_SMEM(false, false, true, 0) ND_SMEM(false, false, false, 0)
@@ -1607,9 +1613,22 @@ static void launch_step_impl(MDEngine* m, const StepArgs& a, bool first) {
         c->launches++;
         return;
     }
-    if (m->tpa > 1) {
+    if (m->tpa == kSmallTPA) {
 #define ND_STEP(C, M, F) \
     k_md_step<C, M, F, MODE, false, kSmallTPA><<<grid, kBlock * kSmallTPA, sm, c->stream>>>(a)
+        if (coul) {
+            if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
+            else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
+        } else {
+            if (mass) { if (first) ND_STEP(false, true, true); else ND_STEP(false, true, false); }
+            else { if (first) ND_STEP(false, false, true); else ND_STEP(false, false, false); }
+        }
+#undef ND_STEP
+        c->launches++;
+        return;
+    }
+    if (m->tpa == 2) {
+#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE, false, 2><<<grid, kBlock * 2, sm, c->stream>>>(a)
         if (coul) {
             if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
             else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
@@ -2269,7 +2288,9 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
     if (p->rebuild_every <= 0 || !(p->cutoff > 0) || !(p->skin >= 0) || !(p->dt > 0) ||
         p->resort_every < 0 || p->stage_policy < 0 || p->stage_policy > 1 ||
         (p->union_search != ND_UNION_BLOCKS && p->union_search != ND_UNION_TREE) ||
-        p->refit_check_every < 0)
+        p->refit_check_every < 0 ||
+        (p->threads_per_atom != 0 && p->threads_per_atom != 1 && p->threads_per_atom != 2 &&
+         p->threads_per_atom != kSmallTPA))
         return ND_ERR_ARG;
     if (nsys < 0 || (nsys > 0 && !sys)) return ND_ERR_ARG;
     if (nsys > 0) {
@@ -2442,6 +2463,16 @@ nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsy
             c = s5;
             c.refit_check_every = ce;
             if ((result = consider(c))) goto done;
+        }
+        // threads sharing an atom's list in the step kernel (single systems)
+        if (nsys == 0) {
+            const nd_md_params s6 = win;
+            for (int32_t t : {1, 2, kSmallTPA}) {
+                if (t == s6.threads_per_atom) continue;
+                c = s6;
+                c.threads_per_atom = t;
+                if ((result = consider(c))) goto done;
+            }
         }
     }
 done:

@@ -17,7 +17,7 @@ from .dynamics import (ForceField, md_params, force_lennardjones_, force_coulomb
                        force_lennardjones_compat_, force_coulomb_compat_,
                        forces, SimSpec, GenericObjectCollection, GenericRandomCollector,
                        simulate_, simulate_compat_, collect_objects, MDEngine, Ensemble,
-                       systems_table, autotune)
+                       systems_table, autotune, autotune_cache_path, TUNED_FIELDS)
 from .adjoint import Adjoint, adj_spec, histogram_loss_function
 from . import synth
 

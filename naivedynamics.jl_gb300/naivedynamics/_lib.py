@@ -72,7 +72,8 @@ class MDParams(ctypes.Structure):
                 ("atomsperleaf", ctypes.c_int32), ("rebuild_every", ctypes.c_int32),
                 ("order", ctypes.c_int32), ("max_neighbors", ctypes.c_int32),
                 ("resort_every", ctypes.c_int32), ("stage_policy", ctypes.c_int32),
-                ("union_search", ctypes.c_int32), ("refit_check_every", ctypes.c_int32)]
+                ("union_search", ctypes.c_int32), ("refit_check_every", ctypes.c_int32),
+                ("threads_per_atom", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class CompatSim(ctypes.Structure):
@@ -131,6 +132,7 @@ SIGNATURES = {
     "nd_last_error": (ctypes.c_char_p, [_vp]),
     "nd_status_string": (ctypes.c_char_p, [_i32]),
     "nd_ctx_stream": (_vp, [_vp]),
+    "nd_ctx_device_name": (_i32, [_vp, ctypes.c_char_p, _i32]),
     "nd_ctx_synchronize": (_i32, [_vp]),
     "nd_ctx_launch_count": (_i64, [_vp]),
     "nd_bvh_spec_init": (_i32, [ctypes.POINTER(BVHSpec), _f, _i32, _i32]),
@@ -182,6 +184,7 @@ SIGNATURES = {
                               _vp, _vp, _vp, _vp, _i32, ctypes.POINTER(MDParams),
                               ctypes.POINTER(_d)]),
     "nd_md_diagnostics": (_i32, [_vp, ctypes.POINTER(MDDiag)]),
+    "nd_simulate_diagnostics": (_i32, [_vp, ctypes.POINTER(MDDiag)]),
     "nd_md_list_pairs": (_i32, [_vp, _vp, _vp, _vp, _i64, ctypes.POINTER(_i64)]),
     "nd_md_set_thermostat": (_i32, [_vp, _d, _d, _i32]),
     "nd_md_set_log": (_i32, [_vp, _i32, _i32]),
@@ -292,6 +295,11 @@ class Context:
 
     def launch_count(self) -> int:
         return int(lib().nd_ctx_launch_count(self.handle))
+
+    def device_name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        raise_for(lib().nd_ctx_device_name(self.handle, buf, 256), self.handle, "device name")
+        return buf.value.decode()
 
     def check(self, st: int, what: str = ""):
         raise_for(st, self.handle, what)

@@ -16,6 +16,10 @@ instead of the constants hard-coded at Forces.jl:17-19,57.
 from __future__ import annotations
 
 import ctypes
+import os
+import json
+import hashlib
+import warnings
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -41,7 +45,8 @@ class ForceField:
 def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e-3,
               box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), atomsperleaf=4, rebuild_every=10,
               order=ND_ORDER_SPATIAL, max_neighbors=0, resort_every=0,
-              stage_policy=0, union_search=ND_UNION_BLOCKS, refit_check_every=1) -> MDParams:
+              stage_policy=0, union_search=ND_UNION_BLOCKS, refit_check_every=1,
+              threads_per_atom=0) -> MDParams:
     p = MDParams()
     p.sigma, p.epsilon, p.coulomb_k, p.cutoff, p.skin, p.dt = (float(sigma), float(epsilon),
                                                                float(coulomb_k), float(cutoff),
@@ -54,6 +59,7 @@ def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e
                                                                  int(max_neighbors))
     p.resort_every, p.stage_policy = int(resort_every), int(stage_policy)
     p.union_search, p.refit_check_every = int(union_search), int(refit_check_every)
+    p.threads_per_atom = int(threads_per_atom)
     return p
 
 
@@ -244,9 +250,18 @@ def collect_objects(clct: GenericRandomCollector, seed: int = 0, ctx=None):
     return sys
 
 
+def _warn_skin(violations: int):
+    if violations > 0:
+        warnings.warn(f"{violations} atom-steps ran on neighbour lists that an atom had left by "
+                      "more than skin/2 (pairs may have been missed): raise the skin or check "
+                      "for early refits after every step (refit_check_every=1)",
+                      RuntimeWarning, stacklevel=3)
+
+
 def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCollector,
               ff: ForceField | None = None, skin=0.3, atomsperleaf=4, rebuild_every=10,
-              order=ND_ORDER_SPATIAL, log_every: int | None = None, ctx=None):
+              order=ND_ORDER_SPATIAL, log_every: int | None = None, refit_check_every=1,
+              ctx=None):
     """simulate!(sys, spec, clct) (Simulator.jl:154-256) on the GPU.
 
     Advances sys.position / sys.velocity in place by spec.duration steps of
@@ -256,7 +271,9 @@ def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCo
     towards clct.temperature every 10 steps (Simulator.jl:241-243).  With
     log_every, the positions after every log_every-th step are logged on the
     device and returned, the initial positions first -- the poslog that
-    simulate! returns (log_every = 1); otherwise sys is returned."""
+    simulate! returns (log_every = 1); otherwise sys is returned.  A
+    RuntimeWarning reports atom-steps that ran on a list an atom had left by
+    more than skin/2 (possible with refit_check_every > 1 on fast atoms)."""
     ff = ff or ForceField()
     ctx = ctx or default_context()
     n = sys.position.shape[0]
@@ -265,7 +282,8 @@ def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCo
     p = md_params(sigma=ff.sigma, epsilon=ff.epsilon,
                   coulomb_k=ff.coulomb_k if q is not None else 0.0, cutoff=ff.cutoff, skin=skin,
                   dt=spec.stepwidth, box_lo=clct.minDim, box_hi=clct.maxDim,
-                  atomsperleaf=atomsperleaf, rebuild_every=rebuild_every, order=order)
+                  atomsperleaf=atomsperleaf, rebuild_every=rebuild_every, order=order,
+                  refit_check_every=refit_check_every)
     if not log_every and not spec.vDamp:
         f = np.empty((n, 3), np.float32)
         st = _lib.lib().nd_simulate(ctx.handle, ctypes.byref(p), n, ptr(sys.position),
@@ -273,6 +291,10 @@ def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCo
                                     int(spec.duration))
         ctx.check(st, "nd_simulate")
         sys.force = f
+        d = _lib.MDDiag()
+        ctx.check(_lib.lib().nd_simulate_diagnostics(ctx.handle, ctypes.byref(d)),
+                  "nd_simulate_diagnostics")
+        _warn_skin(d.skin_violations)
         return sys
     x0 = sys.position.copy()
     eng = MDEngine(p, sys.position, sys.velocity, q, m, ctx=ctx)
@@ -285,6 +307,7 @@ def simulate_(sys: GenericObjectCollection, spec: SimSpec, clct: GenericRandomCo
         eng.run(int(spec.duration))
         x, v, f = eng.get()
         poslog = eng.log_read(0, frames) if frames else None
+        _warn_skin(eng.diagnostics()["skin_violations"])
     finally:
         eng.close()
     sys.position[...] = x
@@ -517,15 +540,67 @@ class Ensemble(MDEngine):
         return pe, ke
 
 
-def autotune(params: MDParams, x, v, q=None, m=None, systems=None, trial_steps=20, ctx=None):
+TUNED_FIELDS = ("skin", "atomsperleaf", "resort_every", "stage_policy", "union_search",
+                "refit_check_every", "threads_per_atom")
+
+
+def autotune_cache_path() -> str:
+    """The tuned-settings cache: $ND_AUTOTUNE_CACHE, else
+    ~/.cache/naivedynamics/autotune.json."""
+    return os.environ.get("ND_AUTOTUNE_CACHE") or os.path.join(
+        os.path.expanduser("~"), ".cache", "naivedynamics", "autotune.json")
+
+
+def _tune_key(ctx, params: MDParams, n: int, systems, has_q: bool, has_m: bool) -> str:
+    """Cache key: the device, the atom count, the density (1e-3 relative) and
+    everything of params the tuner does not change (cutoff, walls, dt, ...);
+    for an ensemble the systems' sizes, sigmas, epsilons and walls."""
+    fixed = {name: (list(getattr(params, name)) if name in ("box_lo", "box_hi")
+                    else getattr(params, name))
+             for name, _ in params._fields_ if name not in TUNED_FIELDS and name != "reserved"}
+    if systems is None:
+        vol = float(np.prod(np.asarray(params.box_hi) - np.asarray(params.box_lo)))
+        shape = {"n": n, "density": float(f"{n / vol:.4g}")}
+    else:
+        h = hashlib.sha256()
+        for r in systems:
+            h.update(np.array([r.n_atoms, r.sigma, r.epsilon, *r.box_lo, *r.box_hi],
+                              np.float64).tobytes())
+        shape = {"n": n, "systems": len(systems), "table": h.hexdigest()[:16]}
+    return json.dumps({"device": ctx.device_name(), "shape": shape, "fixed": fixed,
+                       "q": has_q, "m": has_m}, sort_keys=True)
+
+
+def autotune(params: MDParams, x, v, q=None, m=None, systems=None, trial_steps=20, ctx=None,
+             use_cache=True):
     """nd_md_autotune: the fastest (skin, atomsperleaf, resort_every,
-    stage_policy, union_search, refit_check_every) for this state, as a new MDParams, and its time per MD step in seconds.
-    systems=None tunes a plain engine."""
+    stage_policy, union_search, refit_check_every, threads_per_atom) for this
+    state, as a new MDParams, and its time per MD step in seconds.
+    systems=None tunes a plain engine.  With use_cache, the result is kept in
+    a JSON file (autotune_cache_path()) keyed by device, atom count, density
+    and the untuned parameters, and a later call with the same key returns it
+    without timing anything; autotune.last_cached tells which happened."""
     ctx = ctx or default_context()
     x = _f64(x, (-1, 3))
     v = _f64(v, (-1, 3))
     qq = None if q is None else _f64(q)
     mm = None if m is None else _f64(m)
+    key = path = None
+    if use_cache:
+        key = _tune_key(ctx, params, x.shape[0], systems, q is not None, m is not None)
+        path = autotune_cache_path()
+        try:
+            with open(path) as f:
+                hit = json.load(f).get(key)
+        except (OSError, ValueError):
+            hit = None
+        if hit:
+            best = MDParams()
+            ctypes.memmove(ctypes.byref(best), ctypes.byref(params), ctypes.sizeof(MDParams))
+            for name in TUNED_FIELDS:
+                setattr(best, name, hit["params"][name])
+            autotune.last_cached = True
+            return best, float(hit["seconds_per_step"])
     best = MDParams()
     sps = ctypes.c_double()
     ns = 0 if systems is None else len(systems)
@@ -533,4 +608,24 @@ def autotune(params: MDParams, x, v, q=None, m=None, systems=None, trial_steps=2
                                    ptr(x), ptr(v), ptr(qq), ptr(mm), int(trial_steps),
                                    ctypes.byref(best), ctypes.byref(sps))
     ctx.check(st, "nd_md_autotune")
+    autotune.last_cached = False
+    if use_cache:
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            try:
+                with open(path) as f:
+                    table = json.load(f)
+            except (OSError, ValueError):
+                table = {}
+            table[key] = {"params": {name: getattr(best, name) for name in TUNED_FIELDS},
+                          "seconds_per_step": sps.value}
+            tmp = f"{path}.{os.getpid()}.tmp"
+            with open(tmp, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+            os.replace(tmp, path)
+        except OSError:
+            pass  # a read-only home: tuned, not cached
     return best, sps.value
+
+
+autotune.last_cached = False

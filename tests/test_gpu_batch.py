@@ -227,10 +227,22 @@ def test_batch_errors(nd):
         nd.Ensemble(_params(nd), t, e["x"], e["v"])
 
 
-def test_autotune_plain_and_batch(nd):
+def test_autotune_plain_and_batch(nd, tmp_path, monkeypatch):
+    monkeypatch.setenv("ND_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
     x0, v0, _ = nd.synth.lj_system(0x4E440001, 4096, 17.0, 0.8)
     p = _params(nd, box_lo=(0, 0, 0), box_hi=(17, 17, 17))
     best, sps = nd.autotune(p, x0, v0, trial_steps=20)
+    assert not nd.autotune.last_cached
+    assert best.threads_per_atom in (1, 2, 4)
+    # the second call reads the cache: same settings, nothing timed
+    again, sps2 = nd.autotune(p, x0, v0, trial_steps=20)
+    assert nd.autotune.last_cached and sps2 == sps
+    assert all(getattr(again, k) == getattr(best, k) for k in nd.TUNED_FIELDS)
+    assert again.cutoff == p.cutoff and list(again.box_hi) == list(p.box_hi)
+    # another density is another key
+    x1, v1, _ = nd.synth.lj_system(0x4E440001, 4096, 18.0, 0.8)
+    nd.autotune(_params(nd, box_lo=(0, 0, 0), box_hi=(18, 18, 18)), x1, v1, trial_steps=20)
+    assert not nd.autotune.last_cached
     assert best.atomsperleaf in (2, 4, 8) and best.resort_every in (1, 5, 10)
     assert best.stage_policy in (0, 1) and best.union_search in (0, 1) and sps > 0
     assert abs(best.skin - p.skin) < 0.25 and best.skin >= p.skin

@@ -378,6 +378,18 @@ def test_md_skin_violations_counted(nd):
         eng.close()
     assert d[1]["skin_violations"] == 0 and d[1]["early_refits"] > 0
     assert d[3]["skin_violations"] > 0
+    # simulate! reports them to its caller (nd_simulate_diagnostics), and
+    # stays silent with a check after every step
+    import warnings
+    for ce, expect in ((3, True), (1, False)):
+        sys_ = nd.GenericObjectCollection(position=x0.copy(), velocity=v0 * 50.0)
+        clct = nd.GenericRandomCollector(512, (0, 0, 0), (8.5, 8.5, 8.5))
+        with warnings.catch_warnings(record=True) as w:
+            warnings.simplefilter("always")
+            nd.simulate_(sys_, nd.SimSpec(duration=10, stepwidth=1e-3), clct,
+                         nd.ForceField(1.0, 1.0, 0.0, 2.5), refit_check_every=ce)
+        hits = [x for x in w if issubclass(x.category, RuntimeWarning) and "skin/2" in str(x.message)]
+        assert bool(hits) == expect, (ce, [str(x.message) for x in w])
 
 
 def test_simulate_drop_in(nd, oracle):
