@@ -785,7 +785,7 @@ __device__ __forceinline__ float fine_diff(uint32_t a, uint32_t b, int sh) {
 // a product whose residual is taken separately.
 template <bool COUL, bool ENERGY>
 __device__ __forceinline__ void accum_near(const int4& ri, const int4& rj, const uint2& fi,
-                                           const uint2& fj, const PairK& a, DF3& acc, float& ue) {
+                                           const uint2& fj, const PairK& a, DF3& acc, double& ue) {
     const int32_t ix = idiff(ri.x, rj.x), iy = idiff(ri.y, rj.y), iz = idiff(ri.z, rj.z);
     const float hx = __int2float_rn(ix & a.hmask), lx = lo_part(ix & ~a.hmask);
     const float hy = __int2float_rn(iy & a.hmask), ly = lo_part(iy & ~a.hmask);
@@ -829,8 +829,12 @@ __device__ __forceinline__ void accum_near(const int4& ri, const int4& rj, const
     const float p2l = __fmaf_rn(p1l, wh, __fmaf_rn(p1, wl, __fmaf_rn(p1, wh, -p2)));
     float fh = __fmul_rn(a.eps24u, p2);
     float fl = __fmaf_rn(a.e24lo, p2, __fmaf_rn(a.eps24u, p2l, __fmaf_rn(a.eps24u, p2, -fh)));
-    float uu = 0.f;
-    if (ENERGY) uu = a.eps4 * s6 * (s6 - 1.0f);
+    // energy (measure pass only): from the two-float s6 in double precision
+    double uu = 0.0;
+    if (ENERGY) {
+        const double s6d = (double)s6 + (double)s6l;
+        uu = (double)a.eps4 * s6d * (s6d - 1.0);
+    }
     if (COUL) {
         const float qi = __int_as_float(ri.w), qj = __int_as_float(rj.w);
         const float qh = __fmul_rn(qi, qj), ql = __fmaf_rn(qi, qj, -qh);
@@ -848,7 +852,7 @@ __device__ __forceinline__ void accum_near(const int4& ri, const int4& rj, const
         const float se = __fadd_rn(__fsub_rn(fh, __fsub_rn(sh, sb)), __fsub_rn(ch, sb));
         fh = sh;
         fl = __fadd_rn(fl, __fadd_rn(cl2, se));
-        if (ENERGY) uu += a.kceu * qh * ir;
+        if (ENERGY) uu += (double)a.kceu * ((double)qi * (double)qj) * ((double)ir + (double)irl);
     }
     // components fmag * d, into the two-float sums
     {
@@ -870,7 +874,7 @@ __device__ __forceinline__ void accum_near(const int4& ri, const int4& rj, const
 // the list build): the caller evaluates it with accum_near.
 template <bool COUL, bool ENERGY>
 __device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const PairK& a,
-                                          float& fx, float& fy, float& fz, float& ue) {
+                                          float& fx, float& fy, float& fz, double& ue) {
     const float dx = (float)idiff(ri.x, rj.x);
     const float dy = (float)idiff(ri.y, rj.y);
     const float dz = (float)idiff(ri.z, rj.z);
@@ -899,7 +903,7 @@ __device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const
         fx += fmag * dx;
         fy += fmag * dy;
         fz += fmag * dz;
-        if (ENERGY) ue += u;
+        if (ENERGY) ue += (double)u;
     }
     return false;
 }
@@ -956,7 +960,7 @@ __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, 
     float r2a, r2b;
     upk2(r2, r2a, r2b);
     if ((r2a < k1.rn2u) | (r2b < k1.rn2u)) {
-        float ue = 0.f;
+        double ue = 0.0;
         unsigned m = accum_pair<COUL, false>(ri, ra, k1, sx, sy, sz, ue) ? 1u : 0u;
         m |= accum_pair<COUL, false>(ri, rb, k1, sx, sy, sz, ue) ? 2u : 0u;
         return m;
@@ -1086,7 +1090,8 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     const uint2 fi = __ldg(&a.recf_in[i]);
     // near terms in two-float sums, the others in single precision
     DF3 nacc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    float fx = 0.f, fy = 0.f, fz = 0.f, ue = 0.f;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    double ue = 0.0;  // potential energy (measure pass only)
     {
         // near entries of this thread's slice, the next index loaded ahead
         int32_t s = part;
@@ -1181,7 +1186,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         nacc.xl = __fadd_rn(nacc.xl, fx);
         nacc.yl = __fadd_rn(nacc.yl, fy);
         nacc.zl = __fadd_rn(nacc.zl, fz);
-        __shared__ float spart[TPA > 1 ? TPA - 1 : 1][7][kBlock];
+        __shared__ float spart[TPA > 1 ? TPA - 1 : 1][8][kBlock];
         if (part > 0) {
             spart[part - 1][0][tid] = nacc.xh;
             spart[part - 1][1][tid] = nacc.xl;
@@ -1189,7 +1194,9 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
             spart[part - 1][3][tid] = nacc.yl;
             spart[part - 1][4][tid] = nacc.zh;
             spart[part - 1][5][tid] = nacc.zl;
-            spart[part - 1][6][tid] = ue;
+            const float uh = (float)ue;
+            spart[part - 1][6][tid] = uh;
+            spart[part - 1][7][tid] = (float)(ue - (double)uh);
         }
         __syncthreads();
         if (own) {
@@ -1198,7 +1205,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
                 df_acc(nacc.xh, nacc.xl, spart[p][0][tid], spart[p][1][tid]);
                 df_acc(nacc.yh, nacc.yl, spart[p][2][tid], spart[p][3][tid]);
                 df_acc(nacc.zh, nacc.zl, spart[p][4][tid], spart[p][5][tid]);
-                ue += spart[p][6][tid];
+                ue += (double)spart[p][6][tid] + (double)spart[p][7][tid];
             }
         }
         fx = __fadd_rn(nacc.xh, nacc.xl);
@@ -1469,7 +1476,7 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
         auto fits = [&](int t) {
-            const size_t part_sm = sizeof(float) * 7 * kBlock * (size_t)(t - 1);
+            const size_t part_sm = sizeof(float) * 8 * kBlock * (size_t)(t - 1);
             return (int)(m->step_smem + part_sm) + 1024 <= maxsm;
         };
         const int req = m->p.threads_per_atom;
