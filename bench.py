@@ -445,7 +445,7 @@ def plain_leg(nd, ctx, ext, flush):
     g0, u0, _ = R.forces(pr, x)
     xr, vr, _ = R.md_run(pr, x, v, steps=steps)
     g1, u1, _ = R.forces(pr, x1)
-    ur, _, _ = R.forces(pr, xr)
+    _, ur, _ = R.forces(pr, xr)
     kr = 0.5 * float((vr ** 2).sum())
     ke_0 = 0.5 * float((v ** 2).sum())
     pa = max(_force_errors(f0, g0)[0], _force_errors(f1, g1)[0])

@@ -48,7 +48,7 @@ static double md_scale(const nd_md_params& p) {
 // keeps hi = x_fp with its low k bits cleared below 2^(k+10) in magnitude for
 // separations up to 1.25 rnb, so the sum of the three squared hi parts is an
 // exact float.
-static NearK md_near(double sigma, double eps, double kc, double S) {
+static NearK md_near(double sigma, double eps, double kc, double rc, double S) {
     NearK k{};
     const double rn = 1.3 * sigma, rnb = rn + 0.1;
     k.rn2u = (float)(rn * rn * S * S);
@@ -57,6 +57,8 @@ static NearK md_near(double sigma, double eps, double kc, double S) {
     const double e24 = 24.0 * eps * S, kcu = kc * S * S;
     k.e24lo = (float)(e24 - (double)(float)e24);
     k.kclo = (float)(kcu - (double)(float)kcu);
+    const double rc2 = rc * rc * S * S;
+    k.rc2lo = (float)(rc2 - (double)(float)rc2);
     k.rnb2 = (float)(rnb * rnb);
     int b = (int)std::ceil(std::log2(1.25 * rnb * S)) - 10;
     b = std::min(std::max(b, 0), 23);
@@ -737,8 +739,11 @@ __global__ void k_md_refit_pos(SetPtrs st, int32_t n, Frame fr, const SysRow* __
 // Pair constants of one system in fixed-point units.
 struct PairK {
     float rc2u, sig2u, eps24u, eps4, kcu, kceu;
-    float rn2u, sig2lo, e24lo, kclo;
+    float rn2u, sig2lo, e24lo, kclo, rc2lo;
     int32_t hmask;
+    // half-width of the band around rc2u inside which a single-precision r^2
+    // (a few ulps off) cannot decide the cutoff: 2^-19 rc2u
+    __device__ __forceinline__ float band() const { return rc2u * 1.9073486328125e-06f; }
 };
 
 // Low part of a separation split: the value in [0, 2^23) as a float, exact,
@@ -803,8 +808,10 @@ __device__ __forceinline__ void accum_near(const int4& ri, const int4& rj, const
     const float u = __fmaf_rn(dxh, fx, __fmaf_rn(dyh, fy, __fmul_rn(dzh, fz)));
     const float cl = __fmaf_rn(2.0f, u, __fmaf_rn(2.0f, t, l2));
     const float r2 = __fadd_rn(P, cl);
-    if (!(r2 < a.rc2u)) return;
     const float r2lo = __fsub_rn(cl, __fsub_rn(r2, P));
+    // the cutoff on the two-float r^2 against the two-float r_c^2 (exact where
+    // they are close: Sterbenz), so a pair at r_c is in or out as in FP64
+    if (!(__fadd_rn(__fsub_rn(r2, a.rc2u), __fsub_rn(r2lo, a.rc2lo)) < 0.0f)) return;
     const float ir = rsqrtf(r2);
     const float ir2 = __fmul_rn(ir, ir);
     const float eta = __fmaf_rn(-r2lo, ir2, __fmaf_rn(-r2, ir2, 1.0f));
@@ -871,7 +878,8 @@ __device__ __forceinline__ void accum_near(const int4& ri, const int4& rj, const
 // box size inside the frame.  Constants are pre-scaled, so the force comes out
 // in physical units per fixed-point unit of displacement.  Returns true,
 // adding nothing, for a pair closer than 1.3 sigma (one that came near after
-// the list build): the caller evaluates it with accum_near.
+// the list build) or within a few ulps of the cutoff (where single precision
+// cannot decide it): the caller evaluates it with accum_near.
 template <bool COUL, bool ENERGY>
 __device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const PairK& a,
                                           float& fx, float& fy, float& fz, double& ue) {
@@ -879,7 +887,7 @@ __device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const
     const float dy = (float)idiff(ri.y, rj.y);
     const float dz = (float)idiff(ri.z, rj.z);
     const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < a.rn2u) return true;
+    if ((r2 < a.rn2u) | (fabsf(r2 - a.rc2u) <= a.band())) return true;
     if (r2 < a.rc2u) {
         float inv_r2, inv_r = 0.f;
         if (COUL) {
@@ -945,9 +953,10 @@ struct PairK2 {
 // terms as accum_pair, the pair outside the cutoff contributing zero.  The
 // accumulators hold the running sums of the a-entries and the b-entries
 // separately; the caller adds the halves at the end.  When a pair is closer
-// than 1.3 sigma (rare: one that came near after the list build) the other
-// takes the scalar form into (sx, sy, sz) and the near one is left to the
-// caller: the return value has bit 0 set for a, bit 1 for b.
+// than 1.3 sigma (rare: one that came near after the list build) or lies
+// within a few ulps of the cutoff, the other takes the scalar form into (sx,
+// sy, sz) and that one is left to the caller: the return value has bit 0 set
+// for a, bit 1 for b.
 template <bool COUL>
 __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, const int4& rb,
                                                const PairK& k1, const PairK2& k, uint64_t& fx,
@@ -959,7 +968,9 @@ __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, 
     const uint64_t r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
     float r2a, r2b;
     upk2(r2, r2a, r2b);
-    if ((r2a < k1.rn2u) | (r2b < k1.rn2u)) {
+    const float band = k1.band();
+    if ((r2a < k1.rn2u) | (r2b < k1.rn2u) | (fabsf(r2a - k1.rc2u) <= band) |
+        (fabsf(r2b - k1.rc2u) <= band)) {
         double ue = 0.0;
         unsigned m = accum_pair<COUL, false>(ri, ra, k1, sx, sy, sz, ue) ? 1u : 0u;
         m |= accum_pair<COUL, false>(ri, rb, k1, sx, sy, sz, ue) ? 2u : 0u;
@@ -1050,7 +1061,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     if (!valid) i = a.n - 1;
     const int4 ri = __ldg(&a.rec_in[i]);
     PairK pk{a.rc2u, a.sig2u, a.eps24u, a.eps4, a.kcu, a.kceu,
-             a.nk.rn2u, a.nk.sig2lo, a.nk.e24lo, a.nk.kclo, a.nk.hmask};
+             a.nk.rn2u, a.nk.sig2lo, a.nk.e24lo, a.nk.kclo, a.nk.rc2lo, a.nk.hmask};
     int32_t sv = 0;
     const SysRow* __restrict__ row = nullptr;
     double S = a.fr.s;
@@ -1068,6 +1079,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         pk.sig2lo = __ldg(&row->nk.sig2lo);
         pk.e24lo = __ldg(&row->nk.e24lo);
         pk.kclo = __ldg(&row->nk.kclo);
+        pk.rc2lo = __ldg(&row->nk.rc2lo);
         pk.hmask = __ldg(&row->nk.hmask);
         S = __ldg(&row->s);
         hs2u = __ldg(&row->hs2u);
@@ -1584,7 +1596,7 @@ StepArgs md_step_args(MDEngine* m, int rec_in) {
         a.lo_fp[d] = (int64_t)std::floor((p.box_lo[d] - m->fr.o[d]) * S * kFine);
         a.hi_fp[d] = (int64_t)std::ceil((p.box_hi[d] - m->fr.o[d]) * S * kFine);
     }
-    a.nk = md_near(p.sigma, p.epsilon, p.coulomb_k, S);
+    a.nk = md_near(p.sigma, p.epsilon, p.coulomb_k, p.cutoff, S);
     a.rc2u = (float)(p.cutoff * p.cutoff * S * S);
     a.sig2u = (float)(p.sigma * p.sigma * S * S);
     a.eps24u = (float)(24.0 * p.epsilon * S);
@@ -1759,7 +1771,7 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
 #define ND_LISTS(A)                                                                             \
     k_md_block_lists<A><<<(unsigned)m->nblocks, kBlock, m->lists_smem, c->stream>>>(            \
         (const float4*)m->pos32.p, keys, n, rl * rl, rl / 2.0f, box_margin,                     \
-        md_near(m->p.sigma, m->p.epsilon, m->p.coulomb_k, m->fr.s).rnb2,                        \
+        md_near(m->p.sigma, m->p.epsilon, m->p.coulomb_k, m->p.cutoff, m->fr.s).rnb2,                        \
         m->nsys > 0 ? live.sid : nullptr, sys, m->ucap, m->lists_smpos,                         \
         (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p,                                \
         (const uint16_t*)m->llist_leaf.p, (const int32_t*)m->lcount_leaf.p, m->lcap_leaf,       \
@@ -2259,7 +2271,7 @@ static nd_status md_frame_batch(MDEngine* m, const nd_system* sys) {
             r.lo_fp[d] = (int64_t)std::floor((y.box_lo[d] - r.o[d]) * S * kFine);
             r.hi_fp[d] = (int64_t)std::ceil((y.box_hi[d] - r.o[d]) * S * kFine);
         }
-        r.nk = md_near(y.sigma, y.epsilon, m->p.coulomb_k, S);
+        r.nk = md_near(y.sigma, y.epsilon, m->p.coulomb_k, m->p.cutoff, S);
         r.sig2u = (float)(y.sigma * y.sigma * S * S);
         r.eps24u = (float)(24.0 * y.epsilon * S);
         r.eps4 = (float)(4.0 * y.epsilon);

@@ -43,6 +43,7 @@ struct NearK {
     float sig2lo;   // sigma^2 S^2 - sig2u (rounding of the LJ constant)
     float e24lo;    // 24 eps S - eps24u
     float kclo;     // k S^2 - kcu
+    float rc2lo;    // (r_c S)^2 - rc2u: the cutoff as a two-float value
     float rnb2;     // (1.3 sigma + 0.1)^2 in physical units: list segment bound
     int32_t hmask;  // clears the low k bits of a separation: the exact split
 };
