@@ -949,6 +949,137 @@ struct PairK2 {
           mone(pk2(-1.0f, -1.0f)), half_neg(pk2(-0.5f, -0.5f)), three_half(pk2(1.5f, 1.5f)) {}
 };
 
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// both halves negated (sign bits flipped)
+__device__ __forceinline__ uint64_t neg2(uint64_t a) { return a ^ 0x8000000080000000ull; }
+__device__ __forceinline__ uint64_t sp2(float a) { return pk2(a, a); }
+
+// (h, l) += the two halves of (H, L), a half at a time
+__device__ __forceinline__ void df_fold2(float& h, float& l, uint64_t H, uint64_t L) {
+    float ha, hb, la, lb;
+    upk2(H, ha, hb);
+    upk2(L, la, lb);
+    df_acc(h, l, ha, la);
+    df_acc(h, l, hb, lb);
+}
+
+// Separation parts of one near entry: hi (exact float of the masked coarse
+// difference), lo (exact), fine (exact), per axis.
+__device__ __forceinline__ void near_parts(const int4& ri, const int4& rj, const uint2& fi,
+                                           const uint2& fj, int32_t hmask, float h[3], float l[3],
+                                           float f[3]) {
+    const int32_t ix = idiff(ri.x, rj.x), iy = idiff(ri.y, rj.y), iz = idiff(ri.z, rj.z);
+    h[0] = __int2float_rn(ix & hmask); l[0] = lo_part(ix & ~hmask);
+    h[1] = __int2float_rn(iy & hmask); l[1] = lo_part(iy & ~hmask);
+    h[2] = __int2float_rn(iz & hmask); l[2] = lo_part(iz & ~hmask);
+    f[0] = fine_diff(fi.x, fj.x, 0);
+    f[1] = fine_diff(fi.x, fj.x, 16);
+    f[2] = fine_diff(fi.y, fj.y, 0);
+}
+
+// accum_near for two near entries (i, a) and (i, b) at once (no energies):
+// the same operations in the same order on both halves of packed registers
+// (add/sub/mul/fma.rn.f32x2 round each half as the scalar form does), so each
+// entry's term has the scalar form's bits; the two terms are then added to
+// the two-float sums one after the other, as the scalar form adds them.
+template <bool COUL>
+__device__ __forceinline__ void accum_near2(const int4& ri, const int4& ra, const int4& rb,
+                                            const uint2& fi, const uint2& fa, const uint2& fb,
+                                            const PairK& a, DF3& acc) {
+    float ha[3], la[3], fa3[3], hb[3], lb[3], fb3[3];
+    near_parts(ri, ra, fi, fa, a.hmask, ha, la, fa3);
+    near_parts(ri, rb, fi, fb, a.hmask, hb, lb, fb3);
+    uint64_t H[3], Lo[3], F[3], DH[3], DL[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        H[d] = pk2(ha[d], hb[d]);
+        Lo[d] = pk2(la[d], lb[d]);
+        F[d] = pk2(fa3[d], fb3[d]);
+        DH[d] = add2(H[d], Lo[d]);
+        DL[d] = add2(sub2(Lo[d], sub2(DH[d], H[d])), F[d]);
+    }
+    const uint64_t two = sp2(2.0f), one = sp2(1.0f);
+    const uint64_t P = fma2(H[2], H[2], fma2(H[1], H[1], mul2(H[0], H[0])));  // exact
+    const uint64_t t = fma2(H[0], Lo[0], fma2(H[1], Lo[1], mul2(H[2], Lo[2])));
+    const uint64_t l2 = fma2(Lo[0], Lo[0], fma2(Lo[1], Lo[1], mul2(Lo[2], Lo[2])));
+    const uint64_t u = fma2(DH[0], F[0], fma2(DH[1], F[1], mul2(DH[2], F[2])));
+    const uint64_t cl = fma2(two, u, fma2(two, t, l2));
+    const uint64_t r2 = add2(P, cl);
+    const uint64_t r2lo = sub2(cl, sub2(r2, P));
+    float da, db;
+    upk2(add2(sub2(r2, sp2(a.rc2u)), sub2(r2lo, sp2(a.rc2lo))), da, db);
+    const bool ina = da < 0.0f, inb = db < 0.0f;
+    if (!(ina | inb)) return;
+    float r2a, r2b;
+    upk2(r2, r2a, r2b);
+    const uint64_t ir = pk2(rsqrtf(r2a), rsqrtf(r2b));
+    const uint64_t ir2 = mul2(ir, ir);
+    const uint64_t eta = fma2(neg2(r2lo), ir2, fma2(neg2(r2), ir2, one));
+    const uint64_t ir2l = mul2(ir2, eta);
+    const uint64_t sg = sp2(a.sig2u);
+    const uint64_t s2 = mul2(sg, ir2);
+    const uint64_t s2l = fma2(sp2(a.sig2lo), ir2, fma2(sg, ir2l, fma2(sg, ir2, neg2(s2))));
+    const uint64_t s4 = mul2(s2, s2);
+    const uint64_t s4l = fma2(mul2(two, s2), s2l, fma2(s2, s2, neg2(s4)));
+    const uint64_t s6 = mul2(s4, s2);
+    const uint64_t s6l = fma2(s4, s2l, fma2(s4l, s2, fma2(s4, s2, neg2(s6))));
+    const uint64_t a2 = mul2(two, s6);
+    const uint64_t wh = sub2(a2, one);
+    const uint64_t wb = sub2(wh, a2);
+    const uint64_t we = add2(sub2(a2, sub2(wh, wb)), sub2(neg2(one), wb));
+    const uint64_t wl = fma2(two, s6l, we);
+    const uint64_t p1 = mul2(ir2, s6);
+    const uint64_t p1l = fma2(ir2l, s6, fma2(ir2, s6l, fma2(ir2, s6, neg2(p1))));
+    const uint64_t p2 = mul2(p1, wh);
+    const uint64_t p2l = fma2(p1l, wh, fma2(p1, wl, fma2(p1, wh, neg2(p2))));
+    const uint64_t e24 = sp2(a.eps24u);
+    uint64_t fh = mul2(e24, p2);
+    uint64_t fl = fma2(sp2(a.e24lo), p2, fma2(e24, p2l, fma2(e24, p2, neg2(fh))));
+    if (COUL) {
+        const float qi = __int_as_float(ri.w), qa = __int_as_float(ra.w), qb = __int_as_float(rb.w);
+        const float qha = __fmul_rn(qi, qa), qhb = __fmul_rn(qi, qb);
+        const uint64_t qh = pk2(qha, qhb);
+        const uint64_t ql = pk2(__fmaf_rn(qi, qa, -qha), __fmaf_rn(qi, qb, -qhb));
+        const uint64_t kc = sp2(a.kcu);
+        const uint64_t kh = mul2(kc, qh);
+        const uint64_t kl = fma2(sp2(a.kclo), qh, fma2(kc, ql, fma2(kc, qh, neg2(kh))));
+        const uint64_t eir = fma2(ir, ir, neg2(ir2));
+        const uint64_t irl = mul2(mul2(sp2(0.5f), ir), fma2(neg2(eir), r2, eta));
+        const uint64_t i3 = mul2(ir, ir2);
+        const uint64_t i3l = fma2(irl, ir2, fma2(ir, ir2l, fma2(ir, ir2, neg2(i3))));
+        const uint64_t ch = mul2(kh, i3);
+        const uint64_t cl2 = fma2(kl, i3, fma2(kh, i3l, fma2(kh, i3, neg2(ch))));
+        const uint64_t sh = add2(fh, ch);
+        const uint64_t sb = sub2(sh, fh);
+        const uint64_t se = add2(sub2(fh, sub2(sh, sb)), sub2(ch, sb));
+        fh = sh;
+        fl = add2(fl, add2(cl2, se));
+    }
+    if (!(ina & inb)) {
+        // one entry beyond the cutoff: its half contributes zero
+        float x0, x1, y0, y1;
+        upk2(fh, x0, x1);
+        upk2(fl, y0, y1);
+        fh = pk2(ina ? x0 : 0.0f, inb ? x1 : 0.0f);
+        fl = pk2(ina ? y0 : 0.0f, inb ? y1 : 0.0f);
+    }
+    const uint64_t tx = mul2(fh, DH[0]);
+    df_fold2(acc.xh, acc.xl, tx, fma2(fl, DH[0], fma2(fh, DL[0], fma2(fh, DH[0], neg2(tx)))));
+    const uint64_t ty = mul2(fh, DH[1]);
+    df_fold2(acc.yh, acc.yl, ty, fma2(fl, DH[1], fma2(fh, DL[1], fma2(fh, DH[1], neg2(ty)))));
+    const uint64_t tz = mul2(fh, DH[2]);
+    df_fold2(acc.zh, acc.zl, tz, fma2(fl, DH[2], fma2(fh, DL[2], fma2(fh, DH[2], neg2(tz)))));
+}
+
 // Forces of the pairs (i, a) and (i, b) together (no energies): the same
 // terms as accum_pair, the pair outside the cutoff contributing zero.  The
 // accumulators hold the running sums of the a-entries and the b-entries
@@ -1104,8 +1235,10 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     DF3 nacc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float fx = 0.f, fy = 0.f, fz = 0.f;
     double ue = 0.0;  // potential energy (measure pass only)
-    {
+    if constexpr (MODE == 1 || BATCH) {
         // near entries of this thread's slice, the next index loaded ahead
+        // (the measure pass, and ensembles, whose per-system constants leave
+        // no registers for the packed form)
         int32_t s = part;
         int32_t li = s < nn ? L[(int64_t)s * kBlock] : 0;
         for (; s < nn; s += TPA) {
@@ -1114,6 +1247,21 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
             accum_near<COUL, MODE == 1>(ri, fetch(li), fi, fine(li), pk, nacc, ue);
             li = next;
         }
+    } else {
+        // near entries of this thread's slice two at a time (packed), the
+        // next two indices loaded ahead; an odd last one alone
+        int32_t s = part;
+        int32_t la = s < nn ? L[(int64_t)s * kBlock] : 0;
+        int32_t lb = s + TPA < nn ? L[(int64_t)(s + TPA) * kBlock] : 0;
+        for (; s + TPA < nn; s += 2 * TPA) {
+            const int32_t s2 = s + 2 * TPA;
+            const int4 ra = fetch(la), rb = fetch(lb);
+            const uint2 fa = fine(la), fb = fine(lb);
+            la = s2 < nn ? L[(int64_t)s2 * kBlock] : 0;
+            lb = s2 + TPA < nn ? L[(int64_t)(s2 + TPA) * kBlock] : 0;
+            accum_near2<COUL>(ri, ra, rb, fi, fa, fb, pk, nacc);
+        }
+        if (s < nn) accum_near<COUL, false>(ri, fetch(la), fi, fine(la), pk, nacc, ue);
     }
     // an entry of the other segment that came closer than 1.3 sigma
     auto far_near = [&](int32_t s) {
@@ -2483,15 +2631,19 @@ nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsy
             c.refit_check_every = ce;
             if ((result = consider(c))) goto done;
         }
-        // threads sharing an atom's list in the step kernel (single systems)
+        // threads sharing an atom's list in the step kernel (single systems):
+        // the fastest explicit value, so the result names the one it runs
         if (nsys == 0) {
             const nd_md_params s6 = win;
+            double tbest = -1.0;
             for (int32_t t : {1, 2, kSmallTPA}) {
-                if (t == s6.threads_per_atom) continue;
                 c = s6;
                 c.threads_per_atom = t;
-                if ((result = consider(c))) goto done;
+                double tt = -1.0;
+                if ((result = trial(c, &tt))) goto done;
+                if (tt > 0.0 && (tbest < 0.0 || tt < tbest)) { tbest = tt; win = c; }
             }
+            if (tbest > 0.0) best_t = tbest;
         }
     }
 done:
