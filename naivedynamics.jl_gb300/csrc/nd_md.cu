@@ -901,17 +901,28 @@ __device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const
         const float s2 = a.sig2u * inv_r2;
         const float s6 = s2 * s2 * s2;
         float fmag = a.eps24u * inv_r2 * s6 * (2.0f * s6 - 1.0f);
-        float u = 0.f;
-        if (ENERGY) u = a.eps4 * s6 * (s6 - 1.0f);
         if (COUL) {
             const float qq = __int_as_float(ri.w) * __int_as_float(rj.w);
             fmag += a.kcu * qq * inv_r * inv_r2;
-            if (ENERGY) u += a.kceu * qq * inv_r;
         }
         fx += fmag * dx;
         fy += fmag * dy;
         fz += fmag * dz;
-        if (ENERGY) ue += (double)u;
+        if (ENERGY) {
+            // the measure pass: the energy in double precision from the exact
+            // integer separation (single-precision terms carry a systematic
+            // bias of a fraction of an ulp, which ten million pairs add up)
+            const double xd = (double)idiff(ri.x, rj.x), yd = (double)idiff(ri.y, rj.y),
+                         zd = (double)idiff(ri.z, rj.z);
+            const double r2d = xd * xd + yd * yd + zd * zd;
+            const double s2d = ((double)a.sig2u + (double)a.sig2lo) / r2d;
+            const double s6d = s2d * s2d * s2d;
+            double ud = (double)a.eps4 * s6d * (s6d - 1.0);
+            if (COUL)
+                ud += (double)a.kceu * ((double)__int_as_float(ri.w) * (double)__int_as_float(rj.w)) /
+                      sqrt(r2d);
+            ue += ud;
+        }
     }
     return false;
 }
