@@ -78,6 +78,44 @@ static double md_frame_lim(double ext, double S) {
 
 
 
+// Packed single precision (sm_100 and later): one instruction applies the
+// operation to both halves of a 64-bit register pair, so two list entries
+// share each instruction of the pair arithmetic.  The forces are held to a
+// tolerance against FP64, not to the scalar form's bits: a packed sequence
+// can end an ulp away from the scalar one (measured on distance tests).
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// both halves negated (sign bits flipped)
+__device__ __forceinline__ uint64_t neg2(uint64_t a) { return a ^ 0x8000000080000000ull; }
+__device__ __forceinline__ uint64_t sp2(float a) { return pk2(a, a); }
+
 // ------------------------------------------------------------- small kernels
 
 __global__ void k_md_split_aos(const double* __restrict__ aos, int32_t n, double* x0, double* x1,
@@ -564,27 +602,20 @@ __global__ void __launch_bounds__(kBlock)
     }
 }
 
-// Exact per-atom lists inside the block's union.  The union's Float32
-// positions are staged in shared memory (up to smpos entries; the rest are
-// read from L2).  Each thread builds its own atom's list in two passes over
-// its leaf's candidate leaves (the union leaves whose atom boxes lie within
-// r_list of the leaf's, k_md_block_union):
-//  1. a point-to-box test of the atom against every candidate leaf's atom box
-//     (the key box shrunk by the half-width h, less a rounding margin),
-//     recorded as one bit per candidate in shared memory;
-//  2. the reference distance test (Float32, d^2 < r_list^2) against the atoms
-//     of the candidate leaves whose bit is set, in candidate order.
-// About a quarter of the candidate leaves pass the box test at r_list = 2.9,
-// so the second pass does about a quarter of the distance tests of a walk over
-// all candidates, and since a box test never drops an atom within r_list the
-// list is the same, entry for entry.  Union indices are stored as uint16:
-// entries closer than the near bound (rnb2, or the atom's system's) from slot
-// 0 upwards, the others from slot lcap - 1 downwards.  pos.w holds the atom's
-// sorted index (excludes the atom itself).
+// Exact per-atom lists inside the block's union: the union's Float32
+// positions are staged in shared memory as three coordinate arrays (up to
+// smpos atoms; the rest are read from L2), then the APL lanes of a leaf walk
+// that leaf's candidate list together, each testing its own atom against the
+// candidate leaf's atoms with the reference distance (Float32
+// sum((a - b).^2) < r_list^2, left to right), two atoms per packed
+// instruction (sub/mul/add.rn.f32x2 round each half exactly as the scalar
+// operations do, so the distances are the reference's bits).  Union indices
+// are stored as uint16: entries closer than the near bound (rnb2, or the
+// atom's system's) from slot 0 upwards, the others from slot lcap - 1
+// downwards.  The atom itself is excluded by its position in the union.
 template <int APL>
 __global__ void __launch_bounds__(kBlock)
-    k_md_block_lists(const float4* __restrict__ pos, const float4* __restrict__ keys,
-                     int32_t n, float rl2, float h, float margin, float rnb2,
+    k_md_block_lists(const float4* __restrict__ pos, int32_t n, float rl2, float rnb2,
                      const int32_t* __restrict__ sid, const SysRow* __restrict__ sys,
                      int32_t ucap,
                      int32_t smpos, const int32_t* __restrict__ ulist,
@@ -592,15 +623,16 @@ __global__ void __launch_bounds__(kBlock)
                      const int32_t* __restrict__ lcount_leaf, int32_t lcap_leaf, int32_t lcap,
                      uint16_t* __restrict__ llist, int32_t* __restrict__ ncount, int32_t* err,
                      int32_t* diag, int32_t sizing, unsigned* pressure) {
-    extern __shared__ float4 spos[];
-    // candidate bits after the staged positions: word w of thread t at w * kBlock + t
-    uint32_t* sbits = reinterpret_cast<uint32_t*>(spos + smpos);
+    extern __shared__ float4 spos_raw[];
+    float* sx = reinterpret_cast<float*>(spos_raw);
+    float* sy = sx + smpos;
+    float* sz = sy + smpos;
     const int tid = threadIdx.x;
     const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
+    const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
     {
         // four positions per thread in flight: their leaf indices, then the
         // positions
-        const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
         const int32_t m = min(nu * APL, smpos);
         for (int32_t k = tid; k < m; k += 4 * kBlock) {
             int32_t lf[4];
@@ -618,7 +650,7 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int32_t kk = k + j * kBlock;
-                if (kk < m) spos[kk] = r[j];
+                if (kk < m) { sx[kk] = r[j].x; sy[kk] = r[j].y; sz[kk] = r[j].z; }
             }
         }
     }
@@ -628,72 +660,66 @@ __global__ void __launch_bounds__(kBlock)
     const int64_t own = (valid ? i : (int64_t)blockIdx.x * kBlock) / APL;
     const float4 p = __ldg(&pos[valid ? i : (int64_t)blockIdx.x * kBlock]);
     const int32_t nc = valid ? min(__ldg(&lcount_leaf[own]), lcap_leaf) : 0;
-    const uint4* __restrict__ C = reinterpret_cast<const uint4*>(llist_leaf + own * lcap_leaf);
-    const uint16_t* __restrict__ C16 = llist_leaf + own * lcap_leaf;
-    // pass 1: one bit per candidate leaf whose atom box the atom can reach
+    // the atom's own slot in the union (the union is sorted by leaf index)
+    int32_t self = -1;
     {
-        uint32_t word = 0;
-        uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
-        for (int32_t k0 = 0; k0 < nc; k0 += 8) {
-            const uint4 cur = nxt;
-            if (k0 + 8 < nc) nxt = __ldg(&C[(k0 >> 3) + 1]);
-            const uint32_t cw[4] = {cur.x, cur.y, cur.z, cur.w};
-#pragma unroll
-            for (int hh = 0; hh < 8; ++hh) {
-                const int32_t k = k0 + hh;
-                if (k < nc) {
-                    const int32_t u = (int32_t)((cw[hh >> 1] >> (16 * (hh & 1))) & 0xffffu);
-                    const int64_t leaf = __ldg(&U[u]);
-                    const float4 a = __ldg(&keys[2 * leaf]), b = __ldg(&keys[2 * leaf + 1]);
-                    // per-axis gap between the atom and the leaf's atom box
-                    // (key box less h on every side), less the margin
-                    const float gx = fmaxf(fmaxf((a.x + h) - p.x, p.x - (a.w - h)) - margin, 0.0f);
-                    const float gy = fmaxf(fmaxf((a.y + h) - p.y, p.y - (b.x - h)) - margin, 0.0f);
-                    const float gz = fmaxf(fmaxf((a.z + h) - p.z, p.z - (b.y - h)) - margin, 0.0f);
-                    if (gx * gx + gy * gy + gz * gz < rl2) word |= 1u << (k & 31);
-                    // a word is complete at every 32nd candidate and at the last
-                    if ((k & 31) == 31 || k == nc - 1) {
-                        sbits[(k >> 5) * kBlock + tid] = word;
-                        word = 0;
-                    }
-                }
-            }
+        int32_t lo = 0, hi = nu;
+        while (lo < hi) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (__ldg(&U[mid]) < own) lo = mid + 1; else hi = mid;
         }
+        if (lo < nu && __ldg(&U[lo]) == own) self = lo * APL + (int32_t)(i - own * APL);
     }
-    // pass 2: the distance tests against the atoms of the marked leaves
+    // candidate entries eight at a time (a leaf's list starts on a 16-byte
+    // boundary: lcap_leaf is a multiple of 8), the next eight loaded while the
+    // current ones are tested
+    const uint4* __restrict__ C = reinterpret_cast<const uint4*>(llist_leaf + own * lcap_leaf);
     uint16_t* __restrict__ L = llist + (int64_t)blockIdx.x * lcap * kBlock + tid;
-    const int32_t self = (int32_t)i;
     const float nb2 = sid ? __ldg(&sys[__ldg(&sid[valid ? i : (int64_t)blockIdx.x * kBlock])].nk.rnb2)
                           : rnb2;
     int32_t cnt = 0, nn = 0, nf = 0;  // all hits; near and other entries stored
-    const int32_t nw = (nc + 31) >> 5;
-    for (int32_t w = 0; w < nw; ++w) {
-        uint32_t bits = sbits[w * kBlock + tid];
-        while (bits) {
-            const int32_t k = (w << 5) + __ffs(bits) - 1;
-            bits &= bits - 1u;
-            const int32_t u = __ldg(&C16[k]);
-            float4 q[APL];
-            if ((u + 1) * APL <= smpos) {
+    auto emit = [&](int32_t slot, float d2) {
+        if (d2 < rl2 && slot != self) {
+            if (cnt < lcap) {
+                const bool near = d2 < nb2;
+                L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)slot;
+                nn += near ? 1 : 0;
+                nf += near ? 0 : 1;
+            }
+            ++cnt;
+        }
+    };
+    const uint64_t px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z);
+    uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
+    for (int32_t k0 = 0; k0 < nc; k0 += 8) {
+        const uint4 cur = nxt;
+        if (k0 + 8 < nc) nxt = __ldg(&C[(k0 >> 3) + 1]);
+        const uint32_t cw[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
-                for (int e = 0; e < APL; ++e) q[e] = spos[u * APL + e];
+        for (int h = 0; h < 8; ++h) {
+            if (k0 + h >= nc) break;
+            const int32_t u = (int32_t)((cw[h >> 1] >> (16 * (h & 1))) & 0xffffu);
+            const int32_t b = u * APL;
+            if (APL >= 2 && b + APL <= smpos) {
+#pragma unroll
+                for (int e = 0; e < APL; e += 2) {
+                    const uint64_t qx = *reinterpret_cast<const uint64_t*>(sx + b + e);
+                    const uint64_t qy = *reinterpret_cast<const uint64_t*>(sy + b + e);
+                    const uint64_t qz = *reinterpret_cast<const uint64_t*>(sz + b + e);
+                    const uint64_t dx = sub2(px, qx), dy = sub2(py, qy), dz = sub2(pz, qz);
+                    const uint64_t d2 = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+                    float d2a, d2b;
+                    upk2(d2, d2a, d2b);
+                    emit(b + e, d2a);
+                    emit(b + e + 1, d2b);
+                }
             } else {
                 const int64_t base = (int64_t)__ldg(&U[u]) * APL;
 #pragma unroll
-                for (int e = 0; e < APL; ++e) q[e] = __ldg(&pos[base + e]);
-            }
-#pragma unroll
-            for (int e = 0; e < APL; ++e) {
-                const float d2 = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z);
-                const bool hit = d2 < rl2 && __float_as_int(q[e].w) != self;
-                if (hit) {
-                    if (cnt < lcap) {
-                        const bool near = d2 < nb2;
-                        L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)(u * APL + e);
-                        nn += near ? 1 : 0;
-                        nf += near ? 0 : 1;
-                    }
-                    ++cnt;
+                for (int e = 0; e < APL; ++e) {
+                    const float4 q = (b + e < smpos) ? make_float4(sx[b + e], sy[b + e], sz[b + e], 0.f)
+                                                     : __ldg(&pos[base + e]);
+                    emit(b + e, dist2_ref(p.x, p.y, p.z, q.x, q.y, q.z));
                 }
             }
         }
@@ -927,30 +953,6 @@ __device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const
     return false;
 }
 
-// Packed single precision (sm_100 and later): one instruction applies the
-// operation to both halves of a 64-bit register pair, so two list entries
-// share each instruction of the pair arithmetic.  The forces are held to a
-// tolerance against FP64, not to the scalar form's bits: a packed sequence
-// can end an ulp away from the scalar one (measured on distance tests).
-__device__ __forceinline__ uint64_t pk2(float a, float b) {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void upk2(uint64_t v, float& a, float& b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
-    uint64_t d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-
 // Pair constants of PairK, each in both halves.
 struct PairK2 {
     uint64_t rc2u, sig2u, eps24u, kcu, two, mone, half_neg, three_half;
@@ -960,19 +962,6 @@ struct PairK2 {
           mone(pk2(-1.0f, -1.0f)), half_neg(pk2(-0.5f, -0.5f)), three_half(pk2(1.5f, 1.5f)) {}
 };
 
-__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
-    uint64_t d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
-    uint64_t d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-// both halves negated (sign bits flipped)
-__device__ __forceinline__ uint64_t neg2(uint64_t a) { return a ^ 0x8000000080000000ull; }
-__device__ __forceinline__ uint64_t sp2(float a) { return pk2(a, a); }
 
 // (h, l) += the two halves of (H, L), a half at a time
 __device__ __forceinline__ void df_fold2(float& h, float& l, uint64_t H, uint64_t L) {
@@ -1632,13 +1621,13 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
         return st;
     m->union_smem = sizeof(int32_t) * (2 * (size_t)fcap + p2);
     m->step_smem = sizeof(int4) * (size_t)m->ucap_sm * m->apl;
-    // the list kernel stages positions and one candidate bit per thread and
-    // candidate leaf; fewer staged positions when both do not fit
+    // the list kernel stages three coordinates per union atom (an even count,
+    // so coordinate pairs stay 8-byte aligned)
     {
-        const size_t bits = sizeof(uint32_t) * kBlock * (size_t)((lcap_leaf + 31) / 32);
-        const int64_t room = ((int64_t)maxsm - 1024 - (int64_t)bits) / (int64_t)sizeof(float4);
-        m->lists_smpos = (int32_t)std::max<int64_t>(0, std::min<int64_t>((int64_t)m->ucap_sm * m->apl, room));
-        m->lists_smem = sizeof(float4) * (size_t)m->lists_smpos + bits;
+        const int64_t room = ((int64_t)maxsm - 1024) / (int64_t)(3 * sizeof(float));
+        m->lists_smpos = (int32_t)(std::max<int64_t>(
+            0, std::min<int64_t>((int64_t)m->ucap_sm * m->apl, room)) & ~(int64_t)1);
+        m->lists_smem = 3 * sizeof(float) * (size_t)m->lists_smpos;
     }
     // threads per atom of the step kernel: more than one for grids under two
     // waves of one block per SM, when the slice partials fit beside the
@@ -1909,18 +1898,6 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
     // query boxes slightly above r_list/2 so the box tests never drop a pair;
     // the distance test alone decides membership
     const float hq = (rl / 2.0f) * 1.0001f + 1e-6f;
-    // rounding margin of the lists' point-to-box test: a few ulps of the
-    // largest coordinate (the boxes are atom positions -/+ r_list/2, rounded)
-    float box_margin;
-    {
-        double cmax = 0.0;
-        if (m->nsys > 0) cmax = m->tree_frame[3];
-        else
-            for (int d = 0; d < 3; ++d)
-                cmax = std::max({cmax, std::fabs(m->p.box_lo[d]), std::fabs(m->p.box_hi[d])});
-        cmax += 2.0 * (double)rl;
-        box_margin = (float)(std::ldexp(1.0, std::ilogb(std::max(cmax, 1.0)) - 20) + 1e-6);
-    }
     k_md_block_union<<<(unsigned)m->nblocks, kBlock, m->union_smem, c->stream>>>(
         keys, (const float4*)m->bbox.p, m->nblocks, tree ? 1 : 0, (const float4*)m->pos32.p,
         live.sid, n, m->nL, m->apl, hq, rl, m->fcap, m->ucap,
@@ -1929,7 +1906,7 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
         sizing ? 1 : 0, pressure);
 #define ND_LISTS(A)                                                                             \
     k_md_block_lists<A><<<(unsigned)m->nblocks, kBlock, m->lists_smem, c->stream>>>(            \
-        (const float4*)m->pos32.p, keys, n, rl * rl, rl / 2.0f, box_margin,                     \
+        (const float4*)m->pos32.p, n, rl * rl,                                                  \
         md_near(m->p.sigma, m->p.epsilon, m->p.coulomb_k, m->p.cutoff, m->fr.s).rnb2,                        \
         m->nsys > 0 ? live.sid : nullptr, sys, m->ucap, m->lists_smpos,                         \
         (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p,                                \
