@@ -603,16 +603,16 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // Exact per-atom lists inside the block's union: the union's Float32
-// positions are staged in shared memory as three coordinate arrays (up to
-// smpos atoms; the rest are read from L2), then the APL lanes of a leaf walk
-// that leaf's candidate list together, each testing its own atom against the
-// candidate leaf's atoms with the reference distance (Float32
-// sum((a - b).^2) < r_list^2, left to right), two atoms per packed
-// instruction (sub/mul/add.rn.f32x2 round each half exactly as the scalar
-// operations do, so the distances are the reference's bits).  Union indices
-// are stored as uint16: entries closer than the near bound (rnb2, or the
-// atom's system's) from slot 0 upwards, the others from slot lcap - 1
-// downwards.  The atom itself is excluded by its position in the union.
+// positions are staged in shared memory (up to smpos entries; the rest are read
+// from L2), then the APL lanes of a leaf walk that leaf's candidate list
+// together, each testing its own atom against the candidate leaf's atoms with
+// the reference distance (Float32, d^2 < r_list^2) and storing union indices
+// as uint16: entries closer than the near bound (rnb2, or the atom's system's)
+// from slot 0 upwards, the others from slot lcap - 1 downwards.  pos.w holds
+// the atom's sorted index (excludes the atom itself).  (Two atoms per packed
+// f32x2 instruction measured slower here, and its sums are not always the
+// scalar operations' bits: one pair of the 512-system ensemble came out 1 ulp
+// above r_list^2.)
 template <int APL>
 __global__ void __launch_bounds__(kBlock)
     k_md_block_lists(const float4* __restrict__ pos, int32_t n, float rl2, float rnb2,
@@ -623,16 +623,13 @@ __global__ void __launch_bounds__(kBlock)
                      const int32_t* __restrict__ lcount_leaf, int32_t lcap_leaf, int32_t lcap,
                      uint16_t* __restrict__ llist, int32_t* __restrict__ ncount, int32_t* err,
                      int32_t* diag, int32_t sizing, unsigned* pressure) {
-    extern __shared__ float4 spos_raw[];
-    float* sx = reinterpret_cast<float*>(spos_raw);
-    float* sy = sx + smpos;
-    float* sz = sy + smpos;
+    extern __shared__ float4 spos[];
     const int tid = threadIdx.x;
     const int32_t* __restrict__ U = ulist + (int64_t)blockIdx.x * ucap;
-    const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
     {
         // four positions per thread in flight: their leaf indices, then the
         // positions
+        const int32_t nu = min(__ldg(&ucount[blockIdx.x]), ucap);
         const int32_t m = min(nu * APL, smpos);
         for (int32_t k = tid; k < m; k += 4 * kBlock) {
             int32_t lf[4];
@@ -650,7 +647,7 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int32_t kk = k + j * kBlock;
-                if (kk < m) { sx[kk] = r[j].x; sy[kk] = r[j].y; sz[kk] = r[j].z; }
+                if (kk < m) spos[kk] = r[j];
             }
         }
     }
@@ -660,36 +657,15 @@ __global__ void __launch_bounds__(kBlock)
     const int64_t own = (valid ? i : (int64_t)blockIdx.x * kBlock) / APL;
     const float4 p = __ldg(&pos[valid ? i : (int64_t)blockIdx.x * kBlock]);
     const int32_t nc = valid ? min(__ldg(&lcount_leaf[own]), lcap_leaf) : 0;
-    // the atom's own slot in the union (the union is sorted by leaf index)
-    int32_t self = -1;
-    {
-        int32_t lo = 0, hi = nu;
-        while (lo < hi) {
-            const int32_t mid = (lo + hi) >> 1;
-            if (__ldg(&U[mid]) < own) lo = mid + 1; else hi = mid;
-        }
-        if (lo < nu && __ldg(&U[lo]) == own) self = lo * APL + (int32_t)(i - own * APL);
-    }
     // candidate entries eight at a time (a leaf's list starts on a 16-byte
     // boundary: lcap_leaf is a multiple of 8), the next eight loaded while the
     // current ones are tested
     const uint4* __restrict__ C = reinterpret_cast<const uint4*>(llist_leaf + own * lcap_leaf);
     uint16_t* __restrict__ L = llist + (int64_t)blockIdx.x * lcap * kBlock + tid;
+    const int32_t self = (int32_t)i;
     const float nb2 = sid ? __ldg(&sys[__ldg(&sid[valid ? i : (int64_t)blockIdx.x * kBlock])].nk.rnb2)
                           : rnb2;
     int32_t cnt = 0, nn = 0, nf = 0;  // all hits; near and other entries stored
-    auto emit = [&](int32_t slot, float d2) {
-        if (d2 < rl2 && slot != self) {
-            if (cnt < lcap) {
-                const bool near = d2 < nb2;
-                L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)slot;
-                nn += near ? 1 : 0;
-                nf += near ? 0 : 1;
-            }
-            ++cnt;
-        }
-    };
-    const uint64_t px = pk2(p.x, p.x), py = pk2(p.y, p.y), pz = pk2(p.z, p.z);
     uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
     for (int32_t k0 = 0; k0 < nc; k0 += 8) {
         const uint4 cur = nxt;
@@ -699,27 +675,27 @@ __global__ void __launch_bounds__(kBlock)
         for (int h = 0; h < 8; ++h) {
             if (k0 + h >= nc) break;
             const int32_t u = (int32_t)((cw[h >> 1] >> (16 * (h & 1))) & 0xffffu);
-            const int32_t b = u * APL;
-            if (APL >= 2 && b + APL <= smpos) {
+            float4 q[APL];
+            if ((u + 1) * APL <= smpos) {
 #pragma unroll
-                for (int e = 0; e < APL; e += 2) {
-                    const uint64_t qx = *reinterpret_cast<const uint64_t*>(sx + b + e);
-                    const uint64_t qy = *reinterpret_cast<const uint64_t*>(sy + b + e);
-                    const uint64_t qz = *reinterpret_cast<const uint64_t*>(sz + b + e);
-                    const uint64_t dx = sub2(px, qx), dy = sub2(py, qy), dz = sub2(pz, qz);
-                    const uint64_t d2 = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
-                    float d2a, d2b;
-                    upk2(d2, d2a, d2b);
-                    emit(b + e, d2a);
-                    emit(b + e + 1, d2b);
-                }
+                for (int e = 0; e < APL; ++e) q[e] = spos[u * APL + e];
             } else {
                 const int64_t base = (int64_t)__ldg(&U[u]) * APL;
 #pragma unroll
-                for (int e = 0; e < APL; ++e) {
-                    const float4 q = (b + e < smpos) ? make_float4(sx[b + e], sy[b + e], sz[b + e], 0.f)
-                                                     : __ldg(&pos[base + e]);
-                    emit(b + e, dist2_ref(p.x, p.y, p.z, q.x, q.y, q.z));
+                for (int e = 0; e < APL; ++e) q[e] = __ldg(&pos[base + e]);
+            }
+#pragma unroll
+            for (int e = 0; e < APL; ++e) {
+                const float d2 = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z);
+                const bool hit = d2 < rl2 && __float_as_int(q[e].w) != self;
+                if (hit) {
+                    if (cnt < lcap) {
+                        const bool near = d2 < nb2;
+                        L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)(u * APL + e);
+                        nn += near ? 1 : 0;
+                        nf += near ? 0 : 1;
+                    }
+                    ++cnt;
                 }
             }
         }
@@ -1621,14 +1597,8 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
         return st;
     m->union_smem = sizeof(int32_t) * (2 * (size_t)fcap + p2);
     m->step_smem = sizeof(int4) * (size_t)m->ucap_sm * m->apl;
-    // the list kernel stages three coordinates per union atom (an even count,
-    // so coordinate pairs stay 8-byte aligned)
-    {
-        const int64_t room = ((int64_t)maxsm - 1024) / (int64_t)(3 * sizeof(float));
-        m->lists_smpos = (int32_t)(std::max<int64_t>(
-            0, std::min<int64_t>((int64_t)m->ucap_sm * m->apl, room)) & ~(int64_t)1);
-        m->lists_smem = 3 * sizeof(float) * (size_t)m->lists_smpos;
-    }
+    m->lists_smpos = m->ucap_sm * m->apl;
+    m->lists_smem = sizeof(float4) * (size_t)m->lists_smpos;
     // threads per atom of the step kernel: more than one for grids under two
     // waves of one block per SM, when the slice partials fit beside the
     // staged union
@@ -1907,7 +1877,7 @@ nd_status md_rebuild(MDEngine* m, int kind, int rec, unsigned* counter, bool siz
 #define ND_LISTS(A)                                                                             \
     k_md_block_lists<A><<<(unsigned)m->nblocks, kBlock, m->lists_smem, c->stream>>>(            \
         (const float4*)m->pos32.p, n, rl * rl,                                                  \
-        md_near(m->p.sigma, m->p.epsilon, m->p.coulomb_k, m->p.cutoff, m->fr.s).rnb2,                        \
+        md_near(m->p.sigma, m->p.epsilon, m->p.coulomb_k, m->p.cutoff, m->fr.s).rnb2,           \
         m->nsys > 0 ? live.sid : nullptr, sys, m->ucap, m->lists_smpos,                         \
         (const int32_t*)m->ulist.p, (const int32_t*)m->ucount.p,                                \
         (const uint16_t*)m->llist_leaf.p, (const int32_t*)m->lcount_leaf.p, m->lcap_leaf,       \
