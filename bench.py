@@ -459,7 +459,7 @@ def plain_leg(nd, ctx, ext, flush):
     ms = float(np.median(times))
     out = {"metric": "plain LJ atom-steps/s @4096", "unit": UNIT, "errors": errors,
            "workload": "plain_lj_4096: N=4096 uniform cube side 17 (min separation 0.8), "
-                       "sigma=eps=1, r_c 2.5, skin >= 0.3 (autotuned), dt 1e-3, rebuild every "
+                       "sigma=eps=1, r_c 2.5, skin 0.1-0.5 (autotuned), dt 1e-3, rebuild every "
                        "10, 100 steps",
            "value": n * steps / (ms * 1e-3), "ms_per_100_steps": ms,
            "tuned": {"skin": p.skin, "atomsperleaf": p.atomsperleaf,

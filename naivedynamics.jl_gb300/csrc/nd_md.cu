@@ -33,6 +33,7 @@ namespace nd {
 constexpr int kSmallTPA = 4;         // threads per atom of the step kernel for small systems
 constexpr int kSizingFcap = 8192;    // BFS frontier entries per buffer in the sizing build
 constexpr int kSizingUcap = 8192;    // union capacity of the sizing build
+constexpr double kMinTunedSkin = 0.1;  // smallest skin the autotuner tries
 
 // Scale of the wrap-around fixed-point grid: a listed pair is within
 // r_c + skin at the build and its atoms move at most skin/2 each before the
@@ -1249,6 +1250,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         // while the current group is computed
         const PairK2 pk2c(pk);
         uint64_t fx2 = 0, fy2 = 0, fz2 = 0;  // packed (0.0f, 0.0f)
+        float gx = 0.f, gy = 0.f, gz = 0.f;  // measure pass: the odd entries
         int32_t s = 0;
         int32_t li[4];
         if (nf >= 4) {
@@ -1264,9 +1266,14 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
                 for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)(s + 4 + k) * kBlock];
             }
             if constexpr (MODE == 1) {
+                // even entries into (fx, fy, fz), odd ones into (gx, gy, gz),
+                // as the two halves of the packed form
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue)) far_near(s + k);
+                for (int k = 0; k < 4; ++k) {
+                    const bool nr = (k & 1) ? accum_pair<COUL, true>(ri, rj[k], pk, gx, gy, gz, ue)
+                                            : accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue);
+                    if (nr) far_near(s + k);
+                }
             } else {
                 // two entries per packed instruction
                 const unsigned m0 = accum_pair2<COUL>(ri, rj[0], rj[1], pk, pk2c, fx2, fy2, fz2, fx, fy, fz);
@@ -1283,6 +1290,10 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
             upk2(fx2, a, b); fx += a + b;
             upk2(fy2, a, b); fy += a + b;
             upk2(fz2, a, b); fz += a + b;
+        } else {
+            fx += gx;
+            fy += gy;
+            fz += gz;
         }
         for (; s < nf; ++s)
             if (accum_pair<COUL, MODE == 1>(ri, fetch(LF[-(int64_t)s * kBlock]), pk, fx, fy, fz, ue))
@@ -2488,8 +2499,8 @@ nd_status md_create_batch(Ctx* parent, const nd_md_params* p, int32_t nsys, cons
 // Autotuner.  Each candidate setting runs on a fresh engine from the same
 // host state -- one untimed window, then trial_steps timed with events on the
 // stream, early refits included -- and the settings are tuned one at a time
-// (coordinate descent): skin (the given one and +0.1, +0.2: a longer list
-// against fewer early refits), atoms per leaf (the leaf and traversal width),
+// (coordinate descent): skin (the given one and -0.2 .. +0.2 in steps of
+// 0.1, not below kMinTunedSkin: a longer list against fewer early refits), atoms per leaf (the leaf and traversal width),
 // re-sort interval, shared-memory staging policy, union search, early-refit
 // check interval.  Candidates that do not fit
 // (shared memory, leaf size not dividing every system) are skipped.
@@ -2555,9 +2566,10 @@ nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsy
         }
         if (best_t < 0.0) { result = ND_ERR_SPEC; parent->last_error = "no autotune candidate fits"; goto done; }
         const nd_md_params start = win;
-        for (double ds : {0.1, 0.2}) {
+        for (double ds : {-0.2, -0.1, 0.1, 0.2}) {
             nd_md_params c = start;
             c.skin = p->skin + ds;
+            if (c.skin < kMinTunedSkin - 1e-9) continue;
             if ((result = consider(c))) goto done;
         }
         const nd_md_params s1 = win;

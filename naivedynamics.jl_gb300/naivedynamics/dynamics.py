@@ -551,10 +551,15 @@ def autotune_cache_path() -> str:
         os.path.expanduser("~"), ".cache", "naivedynamics", "autotune.json")
 
 
+# the tuner's candidate set: a cached result from another set is not reused
+TUNER_VERSION = 2
+
+
 def _tune_key(ctx, params: MDParams, n: int, systems, has_q: bool, has_m: bool) -> str:
-    """Cache key: the device, the atom count, the density (1e-3 relative) and
-    everything of params the tuner does not change (cutoff, walls, dt, ...);
-    for an ensemble the systems' sizes, sigmas, epsilons and walls."""
+    """Cache key: the device, the atom count, the density (1e-3 relative),
+    everything of params the tuner does not change (cutoff, walls, dt, ...)
+    and the tuner's version; for an ensemble the systems' sizes, sigmas,
+    epsilons and walls."""
     fixed = {name: (list(getattr(params, name)) if name in ("box_lo", "box_hi")
                     else getattr(params, name))
              for name, _ in params._fields_ if name not in TUNED_FIELDS and name != "reserved"}
@@ -568,7 +573,7 @@ def _tune_key(ctx, params: MDParams, n: int, systems, has_q: bool, has_m: bool) 
                               np.float64).tobytes())
         shape = {"n": n, "systems": len(systems), "table": h.hexdigest()[:16]}
     return json.dumps({"device": ctx.device_name(), "shape": shape, "fixed": fixed,
-                       "q": has_q, "m": has_m}, sort_keys=True)
+                       "q": has_q, "m": has_m, "tuner": TUNER_VERSION}, sort_keys=True)
 
 
 def autotune(params: MDParams, x, v, q=None, m=None, systems=None, trial_steps=20, ctx=None,
