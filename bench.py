@@ -824,20 +824,20 @@ def headline_errors(nd, eng, x0, q):
             "at": "input and end of the timed steps", "bar": 1e-5}
 
 
-def md_eager_leg(nd, ctx, union_search="blocks", check_every=3):
+def md_eager_leg(nd, ctx, union_search="blocks", check_every=3, skin=0.4, apl=4):
     """The headline workload with the settings the autotuner picks for it
-    (skin 0.4, 8 atoms per leaf, re-sort every 10th window; the given union
-    search and early-refit check interval), created and run for ten windows
-    eagerly (nd_md_step_times), so that every kernel is a plain launch in a
-    known order for profiling: engine creation (three builds), then per window
-    a rebuild and ten steps."""
+    (by default skin 0.4, 4 atoms per leaf, re-sort every 10th window; the
+    given union search and early-refit check interval), created and run for
+    ten windows eagerly (nd_md_step_times), so that every kernel is a plain
+    launch in a known order for profiling: engine creation (three builds),
+    then per window a rebuild and ten steps."""
     import numpy as np
 
     import torch
 
     x, v, q = nd.synth.lj_system(SEED, N_ATOMS, SIDE, 0.8, charges=True)
     p = _md_params(nd)
-    p.skin, p.atomsperleaf, p.resort_every = 0.4, 8, 10
+    p.skin, p.atomsperleaf, p.resort_every = skin, apl, 10
     p.union_search = {v_: k for k, v_ in UNION_NAMES.items()}[union_search]
     p.refit_check_every = check_every
     eng = nd.MDEngine(p, x, v, q, ctx=ctx)
@@ -855,9 +855,12 @@ def md_eager_leg(nd, ctx, union_search="blocks", check_every=3):
         if k > 0:
             graph_ms.append(a.elapsed_time(b))
     d = eng.diagnostics()
+    nbr = eng.stats()["list_pairs"] / N_ATOMS
     eng.close()
-    return {"workload": WORKLOAD + f" (fixed settings, union search {union_search}, "
-                                   f"early-refit checks every {check_every} steps)",
+    return {"workload": WORKLOAD + f" (fixed settings: skin {skin}, {apl} atoms per leaf, "
+                                   f"union search {union_search}, early-refit checks every "
+                                   f"{check_every} steps)",
+            "neighbours_per_atom": round(nbr, 2),
             "early_refits": d["early_refits"], "skin_violations": d["skin_violations"],
             "step_kernel_ms_mean": float(np.mean(ms)),
             "graph_ms_per_100_steps": float(np.median(graph_ms)),
@@ -874,7 +877,7 @@ def run_only(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.only == "md":
         out = md_eager_leg(nd, ctx, union_search=args.union_search,
-                           check_every=args.check_every)
+                           check_every=args.check_every, skin=args.skin, apl=args.apl)
     elif args.only == "plain":
         out = plain_leg(nd, ctx, ext, flush)
     elif args.only == "batched":
@@ -919,6 +922,10 @@ def main():
                     help="union search of the fixed-settings engine of --only md")
     ap.add_argument("--check-every", type=int, default=3,
                     help="early-refit check interval of the fixed-settings engine of --only md")
+    ap.add_argument("--skin", type=float, default=0.4,
+                    help="skin of the fixed-settings engine of --only md")
+    ap.add_argument("--apl", type=int, default=4,
+                    help="atoms per leaf of the fixed-settings engine of --only md")
     ap.add_argument("--no-compat", action="store_true",
                     help="skip the simulate!-as-written measurement")
     ap.add_argument("--only", choices=["md", "plain", "batched", "adjoint", "stress", "compat"],
