@@ -448,14 +448,16 @@ typedef struct {
 
 /* Rebuilds are decided on the device: a window re-sorts every resort_every-th
  * time or when a list has passed 90% of its capacity since the last re-sort,
- * and refits otherwise; a step after which some atom could pass skin/2 from
- * its list-build position in the next step (its displacement plus twice its
- * last move reaches 95% of skin/2) is followed by an early refit. */
+ * and refits otherwise; a checked step (every refit_check_every-th = k-th step
+ * of a window) after which some atom could pass skin/2 from its list-build
+ * position before the next check (its displacement plus 2 (k - 1) times its
+ * last move, twice it for k = 1, reaches 95% of skin/2) is followed by an
+ * early refit. */
 nd_status nd_md_diagnostics(nd_md* md, nd_md_diag* out);
 /* The engine's current neighbour lists as directed pairs (pi[k], pj[k]) of
  * 1-based caller indices -- every list entry, so each unordered pair appears
  * once from each side -- in no particular order, with near[k] = 1 for entries
- * of the near segment (pairs closer than 1.2 sigma + 0.1 at the list build,
+ * of the near segment (pairs closer than 1.3 sigma + 0.1 at the list build,
  * whose forces are evaluated with exact r^2 residuals).  With capacity below
  * the entry count, *count receives the count and ND_NEED_REALLOC is returned.
  * Host arrays; synchronises.  No counterpart in the reference, whose pair
@@ -517,10 +519,11 @@ nd_status nd_batch_energies(nd_md* md, double* potential, double* kinetic);
 /*
  * Autotuner: times short runs of candidate engine settings on copies of the
  * given state (host arrays; the state is not advanced) and writes the fastest
- * into *best (skin -- p->skin, +0.1 or +0.2 --, atomsperleaf -- the
- * leaf/traversal width --, resort_every, stage_policy, union_search and
- * refit_check_every -- 1, 2 or 3; every other field copied from *p), tuning one
- * setting at a time.  nsys == 0 tunes a plain engine (sys ignored).  Candidates
+ * into *best (skin -- p->skin - 0.2 to p->skin + 0.2 in steps of 0.1, not below
+ * 0.1 --, atomsperleaf -- the leaf/traversal width --, resort_every,
+ * stage_policy, union_search, refit_check_every -- 1, 2 or 3 -- and, for a
+ * plain engine, threads_per_atom -- 1, 2 or 4; every other field copied from
+ * *p), tuning one setting at a time.  nsys == 0 tunes a plain engine (sys ignored).  Candidates
  * change only the summation order of the forces and the steps at which early
  * refits may run, not which pairs interact.  trial_steps: timed steps per candidate
  * (rounded up to whole rebuild windows).  seconds_per_step (may be NULL)
