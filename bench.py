@@ -824,7 +824,8 @@ def headline_errors(nd, eng, x0, q):
             "at": "input and end of the timed steps", "bar": 1e-5}
 
 
-def md_eager_leg(nd, ctx, union_search="blocks", check_every=3, skin=0.4, apl=4):
+def md_eager_leg(nd, ctx, union_search="blocks", check_every=3, skin=0.4, apl=4,
+                 stage_policy=0):
     """The headline workload with the settings the autotuner picks for it
     (by default skin 0.4, 4 atoms per leaf, re-sort every 10th window; the
     given union search and early-refit check interval), created and run for
@@ -838,6 +839,7 @@ def md_eager_leg(nd, ctx, union_search="blocks", check_every=3, skin=0.4, apl=4)
     x, v, q = nd.synth.lj_system(SEED, N_ATOMS, SIDE, 0.8, charges=True)
     p = _md_params(nd)
     p.skin, p.atomsperleaf, p.resort_every = skin, apl, 10
+    p.stage_policy = stage_policy
     p.union_search = {v_: k for k, v_ in UNION_NAMES.items()}[union_search]
     p.refit_check_every = check_every
     eng = nd.MDEngine(p, x, v, q, ctx=ctx)
@@ -877,7 +879,8 @@ def run_only(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.only == "md":
         out = md_eager_leg(nd, ctx, union_search=args.union_search,
-                           check_every=args.check_every, skin=args.skin, apl=args.apl)
+                           check_every=args.check_every, skin=args.skin, apl=args.apl,
+                           stage_policy=args.stage_policy)
     elif args.only == "plain":
         out = plain_leg(nd, ctx, ext, flush)
     elif args.only == "batched":
@@ -926,6 +929,9 @@ def main():
                     help="skin of the fixed-settings engine of --only md")
     ap.add_argument("--apl", type=int, default=4,
                     help="atoms per leaf of the fixed-settings engine of --only md")
+    ap.add_argument("--stage-policy", type=int, default=0, choices=[0, 1],
+                    help="union staging of the fixed-settings engine of --only md "
+                         "(0: near the mean union, 1: every union record)")
     ap.add_argument("--no-compat", action="store_true",
                     help="skip the simulate!-as-written measurement")
     ap.add_argument("--only", choices=["md", "plain", "batched", "adjoint", "stress", "compat"],

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "nd_md_engine.cuh"
@@ -1199,19 +1200,25 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
     const uint16_t* __restrict__ LF = L + (int64_t)(a.lcap - 1) * kBlock;
     const int32_t lsh = __ffs(a.apl) - 1, emask = a.apl - 1;
+    const uint2 fi = __ldg(&a.recf_in[i]);
+    // near terms in two-float sums, the others in single precision
+    DF3 nacc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    double ue = 0.0;  // potential energy (measure pass only)
+    __shared__ float spart[TPA > 1 ? TPA - 1 : 1][8][kBlock];
+    // The pair loops, compiled twice: for a block whose whole union is staged
+    // (the usual case; a block-uniform choice) a record is read from shared
+    // memory with no test, otherwise records past the staged part come from L2.
+    auto pairs = [&](auto staged) {
+    constexpr bool ALL = decltype(staged)::value;
     auto fetch = [&](int32_t li) -> int4 {
-        if (li < a.smrec) return srec[li];
+        if (ALL || li < a.smrec) return srec[li];
         return __ldg(&a.rec_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
     };
     // fine bits of a union entry's record (near pairs only)
     auto fine = [&](int32_t li) -> uint2 {
         return __ldg(&a.recf_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
     };
-    const uint2 fi = __ldg(&a.recf_in[i]);
-    // near terms in two-float sums, the others in single precision
-    DF3 nacc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    double ue = 0.0;  // potential energy (measure pass only)
     if constexpr (MODE == 1 || BATCH) {
         // near entries of this thread's slice, the next index loaded ahead
         // (the measure pass, and ensembles, whose per-system constants leave
@@ -1333,7 +1340,6 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         nacc.xl = __fadd_rn(nacc.xl, fx);
         nacc.yl = __fadd_rn(nacc.yl, fy);
         nacc.zl = __fadd_rn(nacc.zl, fz);
-        __shared__ float spart[TPA > 1 ? TPA - 1 : 1][8][kBlock];
         if (part > 0) {
             spart[part - 1][0][tid] = nacc.xh;
             spart[part - 1][1][tid] = nacc.xl;
@@ -1359,6 +1365,11 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         fy = __fadd_rn(nacc.yh, nacc.yl);
         fz = __fadd_rn(nacc.zh, nacc.zl);
     }
+    };
+    if (min(__ldg(&a.ucount[blockIdx.x]), a.ucap) * a.apl <= a.smrec)
+        pairs(std::true_type{});
+    else
+        pairs(std::false_type{});
     if (valid && own) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
     const double imv = MASS ? a.im[i] : 1.0;
     const float fv[3] = {fx, fy, fz};
