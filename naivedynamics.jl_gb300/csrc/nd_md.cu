@@ -668,40 +668,49 @@ __global__ void __launch_bounds__(kBlock)
     const float nb2 = sid ? __ldg(&sys[__ldg(&sid[valid ? i : (int64_t)blockIdx.x * kBlock])].nk.rnb2)
                           : rnb2;
     int32_t cnt = 0, nn = 0, nf = 0;  // all hits; near and other entries stored
-    uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
-    for (int32_t k0 = 0; k0 < nc; k0 += 8) {
-        const uint4 cur = nxt;
-        if (k0 + 8 < nc) nxt = __ldg(&C[(k0 >> 3) + 1]);
-        const uint32_t cw[4] = {cur.x, cur.y, cur.z, cur.w};
+    // compiled twice: for a block whose whole union is staged (block-uniform)
+    // the positions come from shared memory with no test
+    auto walk = [&](auto staged) {
+        constexpr bool ALL = decltype(staged)::value;
+        uint4 nxt = nc > 0 ? __ldg(&C[0]) : make_uint4(0u, 0u, 0u, 0u);
+        for (int32_t k0 = 0; k0 < nc; k0 += 8) {
+            const uint4 cur = nxt;
+            if (k0 + 8 < nc) nxt = __ldg(&C[(k0 >> 3) + 1]);
+            const uint32_t cw[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
-        for (int h = 0; h < 8; ++h) {
-            if (k0 + h >= nc) break;
-            const int32_t u = (int32_t)((cw[h >> 1] >> (16 * (h & 1))) & 0xffffu);
-            float4 q[APL];
-            if ((u + 1) * APL <= smpos) {
+            for (int h = 0; h < 8; ++h) {
+                if (k0 + h >= nc) break;
+                const int32_t u = (int32_t)((cw[h >> 1] >> (16 * (h & 1))) & 0xffffu);
+                float4 q[APL];
+                if (ALL || (u + 1) * APL <= smpos) {
 #pragma unroll
-                for (int e = 0; e < APL; ++e) q[e] = spos[u * APL + e];
-            } else {
-                const int64_t base = (int64_t)__ldg(&U[u]) * APL;
+                    for (int e = 0; e < APL; ++e) q[e] = spos[u * APL + e];
+                } else {
+                    const int64_t base = (int64_t)__ldg(&U[u]) * APL;
 #pragma unroll
-                for (int e = 0; e < APL; ++e) q[e] = __ldg(&pos[base + e]);
-            }
+                    for (int e = 0; e < APL; ++e) q[e] = __ldg(&pos[base + e]);
+                }
 #pragma unroll
-            for (int e = 0; e < APL; ++e) {
-                const float d2 = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z);
-                const bool hit = d2 < rl2 && __float_as_int(q[e].w) != self;
-                if (hit) {
-                    if (cnt < lcap) {
-                        const bool near = d2 < nb2;
-                        L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)(u * APL + e);
-                        nn += near ? 1 : 0;
-                        nf += near ? 0 : 1;
+                for (int e = 0; e < APL; ++e) {
+                    const float d2 = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z);
+                    const bool hit = d2 < rl2 && __float_as_int(q[e].w) != self;
+                    if (hit) {
+                        if (cnt < lcap) {
+                            const bool near = d2 < nb2;
+                            L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)(u * APL + e);
+                            nn += near ? 1 : 0;
+                            nf += near ? 0 : 1;
+                        }
+                        ++cnt;
                     }
-                    ++cnt;
                 }
             }
         }
-    }
+    };
+    if (min(__ldg(&ucount[blockIdx.x]), ucap) * APL <= smpos)
+        walk(std::true_type{});
+    else
+        walk(std::false_type{});
     if (!valid) return;
     ncount[i] = nn | (nf << 16);
     if (cnt > lcap && !sizing) set_error(err, ND_ERR_OVERFLOW, (int32_t)i);
@@ -1210,161 +1219,165 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     // (the usual case; a block-uniform choice) a record is read from shared
     // memory with no test, otherwise records past the staged part come from L2.
     auto pairs = [&](auto staged) {
-    constexpr bool ALL = decltype(staged)::value;
-    auto fetch = [&](int32_t li) -> int4 {
-        if (ALL || li < a.smrec) return srec[li];
-        return __ldg(&a.rec_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
-    };
-    // fine bits of a union entry's record (near pairs only)
-    auto fine = [&](int32_t li) -> uint2 {
-        return __ldg(&a.recf_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
-    };
-    if constexpr (MODE == 1 || BATCH) {
-        // near entries of this thread's slice, the next index loaded ahead
-        // (the measure pass, and ensembles, whose per-system constants leave
-        // no registers for the packed form)
-        int32_t s = part;
-        int32_t li = s < nn ? L[(int64_t)s * kBlock] : 0;
-        for (; s < nn; s += TPA) {
-            const int32_t sn = s + TPA;
-            const int32_t next = sn < nn ? L[(int64_t)sn * kBlock] : 0;
-            accum_near<COUL, MODE == 1>(ri, fetch(li), fi, fine(li), pk, nacc, ue);
-            li = next;
-        }
-    } else {
-        // near entries of this thread's slice two at a time (packed), the
-        // next two indices loaded ahead; an odd last one alone
-        int32_t s = part;
-        int32_t la = s < nn ? L[(int64_t)s * kBlock] : 0;
-        int32_t lb = s + TPA < nn ? L[(int64_t)(s + TPA) * kBlock] : 0;
-        for (; s + TPA < nn; s += 2 * TPA) {
-            const int32_t s2 = s + 2 * TPA;
-            const int4 ra = fetch(la), rb = fetch(lb);
-            const uint2 fa = fine(la), fb = fine(lb);
-            la = s2 < nn ? L[(int64_t)s2 * kBlock] : 0;
-            lb = s2 + TPA < nn ? L[(int64_t)(s2 + TPA) * kBlock] : 0;
-            accum_near2<COUL>(ri, ra, rb, fi, fa, fb, pk, nacc);
-        }
-        if (s < nn) accum_near<COUL, false>(ri, fetch(la), fi, fine(la), pk, nacc, ue);
-    }
-    // an entry of the other segment that came closer than 1.3 sigma
-    auto far_near = [&](int32_t s) {
-        const int32_t li = LF[-(int64_t)s * kBlock];
-        accum_near<COUL, MODE == 1>(ri, fetch(li), fi, fine(li), pk, nacc, ue);
-    };
-    if constexpr (TPA == 1) {
-        // groups of four neighbours; the next group's indices are loaded
-        // while the current group is computed
-        const PairK2 pk2c(pk);
-        uint64_t fx2 = 0, fy2 = 0, fz2 = 0;  // packed (0.0f, 0.0f)
-        float gx = 0.f, gy = 0.f, gz = 0.f;  // measure pass: the odd entries
-        int32_t s = 0;
-        int32_t li[4];
-        if (nf >= 4) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)k * kBlock];
-        }
-        for (; s + 4 <= nf; s += 4) {
-            int4 rj[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
-            if (s + 8 <= nf) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)(s + 4 + k) * kBlock];
+        constexpr bool ALL = decltype(staged)::value;
+        auto fetch = [&](int32_t li) -> int4 {
+            if (ALL || li < a.smrec) return srec[li];
+            return __ldg(&a.rec_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
+        };
+        // fine bits of a union entry's record (near pairs only)
+        auto fine = [&](int32_t li) -> uint2 {
+            return __ldg(&a.recf_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
+        };
+        if constexpr (MODE == 1 || BATCH) {
+            // near entries of this thread's slice, the next index loaded ahead
+            // (the measure pass, and ensembles, whose per-system constants leave
+            // no registers for the packed form)
+            int32_t s = part;
+            int32_t li = s < nn ? L[(int64_t)s * kBlock] : 0;
+            for (; s < nn; s += TPA) {
+                const int32_t sn = s + TPA;
+                const int32_t next = sn < nn ? L[(int64_t)sn * kBlock] : 0;
+                accum_near<COUL, MODE == 1>(ri, fetch(li), fi, fine(li), pk, nacc, ue);
+                li = next;
             }
-            if constexpr (MODE == 1) {
-                // even entries into (fx, fy, fz), odd ones into (gx, gy, gz),
-                // as the two halves of the packed form
+        } else {
+            // near entries of this thread's slice two at a time (packed), the
+            // next two indices loaded ahead; an odd last one alone
+            int32_t s = part;
+            int32_t la = s < nn ? L[(int64_t)s * kBlock] : 0;
+            int32_t lb = s + TPA < nn ? L[(int64_t)(s + TPA) * kBlock] : 0;
+            for (; s + TPA < nn; s += 2 * TPA) {
+                const int32_t s2 = s + 2 * TPA;
+                const int4 ra = fetch(la), rb = fetch(lb);
+                const uint2 fa = fine(la), fb = fine(lb);
+                la = s2 < nn ? L[(int64_t)s2 * kBlock] : 0;
+                lb = s2 + TPA < nn ? L[(int64_t)(s2 + TPA) * kBlock] : 0;
+                accum_near2<COUL>(ri, ra, rb, fi, fa, fb, pk, nacc);
+            }
+            if (s < nn) accum_near<COUL, false>(ri, fetch(la), fi, fine(la), pk, nacc, ue);
+        }
+        // an entry of the other segment that came closer than 1.3 sigma
+        auto far_near = [&](int32_t s) {
+            const int32_t li = LF[-(int64_t)s * kBlock];
+            accum_near<COUL, MODE == 1>(ri, fetch(li), fi, fine(li), pk, nacc, ue);
+        };
+        if constexpr (TPA == 1) {
+            // groups of four neighbours; the next group's indices are loaded
+            // while the current group is computed
+            const PairK2 pk2c(pk);
+            uint64_t fx2 = 0, fy2 = 0, fz2 = 0;  // packed (0.0f, 0.0f)
+            float gx = 0.f, gy = 0.f, gz = 0.f;  // measure pass: the odd entries
+            int32_t s = 0;
+            int32_t li[4];
+            if (nf >= 4) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)k * kBlock];
+            }
+            for (; s + 4 <= nf; s += 4) {
+                int4 rj[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
+                if (s + 8 <= nf) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)(s + 4 + k) * kBlock];
+                }
+                if constexpr (MODE == 1) {
+                    // even entries into (fx, fy, fz), odd ones into (gx, gy, gz),
+                    // as the two halves of the packed form
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const bool nr = (k & 1) ? accum_pair<COUL, true>(ri, rj[k], pk, gx, gy, gz, ue)
+                                                : accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue);
+                        if (nr) far_near(s + k);
+                    }
+                } else {
+                    // two entries per packed instruction
+                    const unsigned m0 = accum_pair2<COUL>(ri, rj[0], rj[1], pk, pk2c, fx2, fy2,
+                                                          fz2, fx, fy, fz);
+                    const unsigned m1 = accum_pair2<COUL>(ri, rj[2], rj[3], pk, pk2c, fx2, fy2,
+                                                          fz2, fx, fy, fz);
+                    if (m0 | m1) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (((k < 2 ? m0 : m1) >> (k & 1)) & 1u) far_near(s + k);
+                    }
+                }
+            }
+            if constexpr (MODE != 1) {
+                float a, b;
+                upk2(fx2, a, b); fx += a + b;
+                upk2(fy2, a, b); fy += a + b;
+                upk2(fz2, a, b); fz += a + b;
+            } else {
+                fx += gx;
+                fy += gy;
+                fz += gz;
+            }
+            for (; s < nf; ++s)
+                if (accum_pair<COUL, MODE == 1>(ri, fetch(LF[-(int64_t)s * kBlock]), pk, fx, fy,
+                                                fz, ue))
+                    far_near(s);
+            // the force: two-float near sums with the single-precision sums added
+            // to their low parts, rounded once
+            fx = __fadd_rn(nacc.xh, __fadd_rn(nacc.xl, fx));
+            fy = __fadd_rn(nacc.yh, __fadd_rn(nacc.yl, fy));
+            fz = __fadd_rn(nacc.zh, __fadd_rn(nacc.zl, fz));
+        } else {
+            // slice `part` of the far entries (part, part + TPA, ..., in that
+            // order): four indices loaded ahead while the previous four are computed
+            int32_t li[4] = {0, 0, 0, 0};
+            auto load4 = [&](int32_t s0) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const bool nr = (k & 1) ? accum_pair<COUL, true>(ri, rj[k], pk, gx, gy, gz, ue)
-                                            : accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue);
-                    if (nr) far_near(s + k);
+                    const int32_t sk = s0 + k * TPA;
+                    li[k] = sk < nf ? LF[-(int64_t)sk * kBlock] : 0;
                 }
-            } else {
-                // two entries per packed instruction
-                const unsigned m0 = accum_pair2<COUL>(ri, rj[0], rj[1], pk, pk2c, fx2, fy2, fz2, fx, fy, fz);
-                const unsigned m1 = accum_pair2<COUL>(ri, rj[2], rj[3], pk, pk2c, fx2, fy2, fz2, fx, fy, fz);
-                if (m0 | m1) {
+            };
+            int32_t s = part;
+            if (s < nf) load4(s);
+            for (; s + 3 * TPA < nf; s += 4 * TPA) {
+                int4 rj[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (((k < 2 ? m0 : m1) >> (k & 1)) & 1u) far_near(s + k);
+                for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
+                load4(s + 4 * TPA);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue))
+                        far_near(s + k * TPA);
+            }
+            // at most three entries left, their indices already loaded
+            for (int k = 0; s < nf && k < 4; s += TPA, ++k)
+                if (accum_pair<COUL, MODE == 1>(ri, fetch(li[k]), pk, fx, fy, fz, ue)) far_near(s);
+            // each slice as a two-float value (its single-precision sum in the low
+            // part); the slices added in a fixed order
+            nacc.xl = __fadd_rn(nacc.xl, fx);
+            nacc.yl = __fadd_rn(nacc.yl, fy);
+            nacc.zl = __fadd_rn(nacc.zl, fz);
+            if (part > 0) {
+                spart[part - 1][0][tid] = nacc.xh;
+                spart[part - 1][1][tid] = nacc.xl;
+                spart[part - 1][2][tid] = nacc.yh;
+                spart[part - 1][3][tid] = nacc.yl;
+                spart[part - 1][4][tid] = nacc.zh;
+                spart[part - 1][5][tid] = nacc.zl;
+                const float uh = (float)ue;
+                spart[part - 1][6][tid] = uh;
+                spart[part - 1][7][tid] = (float)(ue - (double)uh);
+            }
+            __syncthreads();
+            if (own) {
+#pragma unroll
+                for (int p = 0; p < TPA - 1; ++p) {
+                    df_acc(nacc.xh, nacc.xl, spart[p][0][tid], spart[p][1][tid]);
+                    df_acc(nacc.yh, nacc.yl, spart[p][2][tid], spart[p][3][tid]);
+                    df_acc(nacc.zh, nacc.zl, spart[p][4][tid], spart[p][5][tid]);
+                    ue += (double)spart[p][6][tid] + (double)spart[p][7][tid];
                 }
             }
+            fx = __fadd_rn(nacc.xh, nacc.xl);
+            fy = __fadd_rn(nacc.yh, nacc.yl);
+            fz = __fadd_rn(nacc.zh, nacc.zl);
         }
-        if constexpr (MODE != 1) {
-            float a, b;
-            upk2(fx2, a, b); fx += a + b;
-            upk2(fy2, a, b); fy += a + b;
-            upk2(fz2, a, b); fz += a + b;
-        } else {
-            fx += gx;
-            fy += gy;
-            fz += gz;
-        }
-        for (; s < nf; ++s)
-            if (accum_pair<COUL, MODE == 1>(ri, fetch(LF[-(int64_t)s * kBlock]), pk, fx, fy, fz, ue))
-                far_near(s);
-        // the force: two-float near sums with the single-precision sums added
-        // to their low parts, rounded once
-        fx = __fadd_rn(nacc.xh, __fadd_rn(nacc.xl, fx));
-        fy = __fadd_rn(nacc.yh, __fadd_rn(nacc.yl, fy));
-        fz = __fadd_rn(nacc.zh, __fadd_rn(nacc.zl, fz));
-    } else {
-        // slice `part` of the far entries (part, part + TPA, ..., in that
-        // order): four indices loaded ahead while the previous four are computed
-        int32_t li[4] = {0, 0, 0, 0};
-        auto load4 = [&](int32_t s0) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int32_t sk = s0 + k * TPA;
-                li[k] = sk < nf ? LF[-(int64_t)sk * kBlock] : 0;
-            }
-        };
-        int32_t s = part;
-        if (s < nf) load4(s);
-        for (; s + 3 * TPA < nf; s += 4 * TPA) {
-            int4 rj[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) rj[k] = fetch(li[k]);
-            load4(s + 4 * TPA);
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue)) far_near(s + k * TPA);
-        }
-        // at most three entries left, their indices already loaded
-        for (int k = 0; s < nf && k < 4; s += TPA, ++k)
-            if (accum_pair<COUL, MODE == 1>(ri, fetch(li[k]), pk, fx, fy, fz, ue)) far_near(s);
-        // each slice as a two-float value (its single-precision sum in the low
-        // part); the slices added in a fixed order
-        nacc.xl = __fadd_rn(nacc.xl, fx);
-        nacc.yl = __fadd_rn(nacc.yl, fy);
-        nacc.zl = __fadd_rn(nacc.zl, fz);
-        if (part > 0) {
-            spart[part - 1][0][tid] = nacc.xh;
-            spart[part - 1][1][tid] = nacc.xl;
-            spart[part - 1][2][tid] = nacc.yh;
-            spart[part - 1][3][tid] = nacc.yl;
-            spart[part - 1][4][tid] = nacc.zh;
-            spart[part - 1][5][tid] = nacc.zl;
-            const float uh = (float)ue;
-            spart[part - 1][6][tid] = uh;
-            spart[part - 1][7][tid] = (float)(ue - (double)uh);
-        }
-        __syncthreads();
-        if (own) {
-#pragma unroll
-            for (int p = 0; p < TPA - 1; ++p) {
-                df_acc(nacc.xh, nacc.xl, spart[p][0][tid], spart[p][1][tid]);
-                df_acc(nacc.yh, nacc.yl, spart[p][2][tid], spart[p][3][tid]);
-                df_acc(nacc.zh, nacc.zl, spart[p][4][tid], spart[p][5][tid]);
-                ue += (double)spart[p][6][tid] + (double)spart[p][7][tid];
-            }
-        }
-        fx = __fadd_rn(nacc.xh, nacc.xl);
-        fy = __fadd_rn(nacc.yh, nacc.yl);
-        fz = __fadd_rn(nacc.zh, nacc.zl);
-    }
     };
     if (min(__ldg(&a.ucount[blockIdx.x]), a.ucap) * a.apl <= a.smrec)
         pairs(std::true_type{});
@@ -2511,9 +2524,10 @@ nd_status md_create_batch(Ctx* parent, const nd_md_params* p, int32_t nsys, cons
 // host state -- one untimed window, then trial_steps timed with events on the
 // stream, early refits included -- and the settings are tuned one at a time
 // (coordinate descent): skin (the given one and -0.2 .. +0.2 in steps of
-// 0.1, not below kMinTunedSkin: a longer list against fewer early refits), atoms per leaf (the leaf and traversal width),
-// re-sort interval, shared-memory staging policy, union search, early-refit
-// check interval.  Candidates that do not fit
+// 0.1, not below kMinTunedSkin: a longer list against fewer early refits),
+// atoms per leaf (the leaf and traversal width), re-sort interval,
+// shared-memory staging policy, union search, early-refit check interval,
+// threads per atom (single systems).  Candidates that do not fit
 // (shared memory, leaf size not dividing every system) are skipped.
 nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsys,
                       const nd_system* sys, const double* x, const double* v, const double* q,
