@@ -530,18 +530,18 @@ __global__ void __launch_bounds__(kBlock)
     for (int32_t k = tid; k < nu; k += kBlock) dst[k] = su[k];
     if (tid == 0) ucount[blockIdx.x] = nu;
     // Per-leaf candidate lists: for each of its leaves a warp keeps the union
-    // positions whose leaf box overlaps that leaf's box (the leaf-leaf test of
-    // leafneighbor_traverse, BVHTraverse.jl:1282), ballot-compacted in union
-    // order, and whose atoms can be within r_list of that leaf's atoms at all:
-    // leaf boxes are atom boxes -/+ r_list/2, so overlapping boxes only say the
-    // atom boxes are within r_list on each axis; the Euclidean gap of the atom
-    // boxes (sqrt of the summed squared per-axis gaps) must be below r_list too,
-    // which drops the candidates diagonally off the leaf.  A lane loads one
-    // union box per chunk and tests it against up to eight own leaves.  The own
-    // boxes are widened by a few ulps so no pair is lost to rounding; the atom
-    // distance test decides.
+    // positions whose atoms can be within r_list of that leaf's atoms at all,
+    // ballot-compacted in union order: leaf boxes are atom boxes -/+ r_list/2,
+    // and the Euclidean gap of the atom boxes (sqrt of the summed squared
+    // per-axis gaps) must be below r_list -- a tighter test than the overlap of
+    // the leaf boxes (the leaf-leaf test of leafneighbor_traverse,
+    // BVHTraverse.jl:1282), which it implies, as it also drops the candidates
+    // diagonally off the leaf.  A lane loads one union box per chunk and tests
+    // it against up to eight own leaves.  The own boxes are widened by a few
+    // ulps so no pair is lost to rounding; the atom distance test decides.
     __shared__ float s_own[kBlock / 32][8][6];
     const unsigned below = (1u << lane) - 1u;
+    const float rl2g = rl * rl * 1.0002f;
     const int32_t leaves_per_warp = 32 / apl;
     const int64_t first_own = ((int64_t)blockIdx.x * kBlock + warp * 32) / apl;
     for (int32_t k0 = 0; k0 < leaves_per_warp; k0 += 8) {
@@ -571,14 +571,12 @@ __global__ void __launch_bounds__(kBlock)
             for (int kl = 0; kl < 8; ++kl) {
                 if (kl >= nown) break;
                 const float* o = s_own[warp][kl];
-                bool hit = (u < nu) && box_overlap(o[0], o[1], o[2], o[3], o[4], o[5], a, b);
-                if (hit) {
-                    // per-axis gap of the atom boxes = key-box gap + r_list
-                    const float gx = fmaxf(fmaxf(o[0] - a.w, a.x - o[3]) + rl, 0.0f);
-                    const float gy = fmaxf(fmaxf(o[1] - b.x, a.y - o[4]) + rl, 0.0f);
-                    const float gz = fmaxf(fmaxf(o[2] - b.y, a.z - o[5]) + rl, 0.0f);
-                    hit = gx * gx + gy * gy + gz * gz < rl * rl * 1.0002f;
-                }
+                // per-axis gap of the atom boxes = key-box gap + r_list (a
+                // Euclidean gap below r_list implies overlapping key boxes)
+                const float gx = fmaxf(fmaxf(o[0] - a.w, a.x - o[3]) + rl, 0.0f);
+                const float gy = fmaxf(fmaxf(o[1] - b.x, a.y - o[4]) + rl, 0.0f);
+                const float gz = fmaxf(fmaxf(o[2] - b.y, a.z - o[5]) + rl, 0.0f);
+                const bool hit = (u < nu) && gx * gx + gy * gy + gz * gz < rl2g;
                 const unsigned m = __ballot_sync(0xffffffffu, hit);
                 if (hit) {
                     const int32_t pos = lc[kl] + __popc(m & below);
