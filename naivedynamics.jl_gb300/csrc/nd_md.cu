@@ -690,17 +690,16 @@ __global__ void __launch_bounds__(kBlock)
                 }
 #pragma unroll
                 for (int e = 0; e < APL; ++e) {
+                    // branch-free: a predicated store to the near or the far end
                     const float d2 = dist2_ref(p.x, p.y, p.z, q[e].x, q[e].y, q[e].z);
                     const bool hit = d2 < rl2 && __float_as_int(q[e].w) != self;
-                    if (hit) {
-                        if (cnt < lcap) {
-                            const bool near = d2 < nb2;
-                            L[(int64_t)(near ? nn : lcap - 1 - nf) * kBlock] = (uint16_t)(u * APL + e);
-                            nn += near ? 1 : 0;
-                            nf += near ? 0 : 1;
-                        }
-                        ++cnt;
-                    }
+                    const bool put = hit && cnt < lcap;
+                    const bool near = d2 < nb2;
+                    const int32_t slot = near ? nn : lcap - 1 - nf;
+                    if (put) L[slot * kBlock] = (uint16_t)(u * APL + e);
+                    nn += (put && near) ? 1 : 0;
+                    nf += (put && !near) ? 1 : 0;
+                    cnt += hit ? 1 : 0;
                 }
             }
         }
