@@ -537,9 +537,13 @@ __global__ void __launch_bounds__(kBlock)
     // the leaf boxes (the leaf-leaf test of leafneighbor_traverse,
     // BVHTraverse.jl:1282), which it implies, as it also drops the candidates
     // diagonally off the leaf.  A lane loads one union box per chunk and tests
-    // it against up to eight own leaves.  The own boxes are widened by a few
+    // it against the box of up to eight own leaves together; the union leaves
+    // that pass are queued (per warp, in union order) and tested 32 at a time
+    // against each of those own leaves.  The own boxes are widened by a few
     // ulps so no pair is lost to rounding; the atom distance test decides.
     __shared__ float s_own[kBlock / 32][8][6];
+    __shared__ int32_t s_qu[kBlock / 32][64];    // per-warp queue: union index
+    __shared__ float s_qb[kBlock / 32][6][64];   // and its key box
     const unsigned below = (1u << lane) - 1u;
     const float rl2g = rl * rl * 1.0002f;
     const int32_t leaves_per_warp = 32 / apl;
@@ -558,7 +562,49 @@ __global__ void __launch_bounds__(kBlock)
             s_own[warp][lane][5] = ob.y + 1e-5f * fabsf(ob.y) + 1e-6f;
         }
         __syncwarp();
+        // the group box: the union of these own boxes; a union leaf whose
+        // atoms cannot come within r_list of it is dropped for all of them
+        float gb[6];
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+            float v = lane < nown ? s_own[warp][lane][d] : (d < 3 ? INFINITY : -INFINITY);
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const float w = __shfl_xor_sync(0xffffffffu, v, sh);
+                v = d < 3 ? fminf(v, w) : fmaxf(v, w);
+            }
+            gb[d] = v;
+        }
+        // Euclidean gap test of key box (a, b) against box o (6 floats): the
+        // per-axis gap of the atom boxes is the key-box gap + r_list, and a
+        // Euclidean gap below r_list implies overlapping key boxes
+        auto near_box = [&](const float* o, const float4& a, const float4& b) {
+            const float gx = fmaxf(fmaxf(o[0] - a.w, a.x - o[3]) + rl, 0.0f);
+            const float gy = fmaxf(fmaxf(o[1] - b.x, a.y - o[4]) + rl, 0.0f);
+            const float gz = fmaxf(fmaxf(o[2] - b.y, a.z - o[5]) + rl, 0.0f);
+            return gx * gx + gy * gy + gz * gz < rl2g;
+        };
         int32_t lc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        // the passing union leaves go through a per-warp queue (in union
+        // order), tested against the own leaves 32 at a time
+        auto test_queue = [&](int32_t cnt) {
+            const bool live = lane < cnt;
+            const int32_t u = live ? s_qu[warp][lane] : 0;
+            const float4 a = make_float4(s_qb[warp][0][lane], s_qb[warp][1][lane],
+                                         s_qb[warp][2][lane], s_qb[warp][3][lane]);
+            const float4 b = make_float4(s_qb[warp][4][lane], s_qb[warp][5][lane], 0.f, 0.f);
+#pragma unroll
+            for (int kl = 0; kl < 8; ++kl) {
+                if (kl >= nown) break;
+                const bool hit = live && near_box(s_own[warp][kl], a, b);
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                const int32_t pos = lc[kl] + __popc(m & below);
+                if (hit && pos < lcap_leaf)
+                    llist_leaf[(first_own + k0 + kl) * lcap_leaf + pos] = (uint16_t)u;
+                lc[kl] += __popc(m);
+            }
+        };
+        int32_t qn = 0;
         for (int32_t base = 0; base < nu; base += 32) {
             const int32_t u = base + lane;
             float4 a = make_float4(1.f, 1.f, 1.f, -1.f), b = make_float4(-1.f, -1.f, 0.f, 0.f);
@@ -567,24 +613,30 @@ __global__ void __launch_bounds__(kBlock)
                 a = __ldg(&keys[2 * (int64_t)leaf]);
                 b = __ldg(&keys[2 * (int64_t)leaf + 1]);
             }
+            const bool pass = u < nu && near_box(gb, a, b);
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (pass) {
+                const int32_t at = qn + __popc(m & below);  // < 64: qn < 32 here
+                s_qu[warp][at] = u;
+                s_qb[warp][0][at] = a.x; s_qb[warp][1][at] = a.y; s_qb[warp][2][at] = a.z;
+                s_qb[warp][3][at] = a.w; s_qb[warp][4][at] = b.x; s_qb[warp][5][at] = b.y;
+            }
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                test_queue(32);
+                __syncwarp();
+                // the rest to the front (sources at 32.., destinations below)
+                if (lane < qn - 32) {
+                    s_qu[warp][lane] = s_qu[warp][32 + lane];
 #pragma unroll
-            for (int kl = 0; kl < 8; ++kl) {
-                if (kl >= nown) break;
-                const float* o = s_own[warp][kl];
-                // per-axis gap of the atom boxes = key-box gap + r_list (a
-                // Euclidean gap below r_list implies overlapping key boxes)
-                const float gx = fmaxf(fmaxf(o[0] - a.w, a.x - o[3]) + rl, 0.0f);
-                const float gy = fmaxf(fmaxf(o[1] - b.x, a.y - o[4]) + rl, 0.0f);
-                const float gz = fmaxf(fmaxf(o[2] - b.y, a.z - o[5]) + rl, 0.0f);
-                const bool hit = (u < nu) && gx * gx + gy * gy + gz * gz < rl2g;
-                const unsigned m = __ballot_sync(0xffffffffu, hit);
-                if (hit) {
-                    const int32_t pos = lc[kl] + __popc(m & below);
-                    if (pos < lcap_leaf) llist_leaf[(first_own + k0 + kl) * lcap_leaf + pos] = (uint16_t)u;
+                    for (int d = 0; d < 6; ++d) s_qb[warp][d][lane] = s_qb[warp][d][32 + lane];
                 }
-                lc[kl] += __popc(m);
+                qn -= 32;
+                __syncwarp();
             }
         }
+        if (qn > 0) test_queue(qn);
         if (lane < nown) {
             int32_t mine = 0;
 #pragma unroll
