@@ -167,3 +167,24 @@ def test_oracle_session_equals_run(oracle):
     s.close()
     assert na == nb
     assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+
+
+def test_autotune_cache_key_names_the_tuner(nd):
+    """The tuned-settings cache key holds the tuner's version, the device and
+    the untuned parameters, so a result from another candidate set or another
+    cutoff is not reused."""
+    import json
+
+    from naivedynamics import dynamics as dyn
+
+    class FakeCtx:
+        def device_name(self):
+            return "GB300-test"
+
+    p = nd.md_params(cutoff=2.5, skin=0.3, box_hi=(17, 17, 17))
+    key = json.loads(dyn._tune_key(FakeCtx(), p, 4096, None, False, False))
+    assert key["tuner"] == dyn.TUNER_VERSION and key["device"] == "GB300-test"
+    assert key["shape"]["n"] == 4096 and key["fixed"]["cutoff"] == 2.5
+    assert "skin" not in key["fixed"]
+    q = nd.md_params(cutoff=3.0, skin=0.3, box_hi=(17, 17, 17))
+    assert dyn._tune_key(FakeCtx(), q, 4096, None, False, False) != json.dumps(key, sort_keys=True)

@@ -245,7 +245,8 @@ def test_autotune_plain_and_batch(nd, tmp_path, monkeypatch):
     assert not nd.autotune.last_cached
     assert best.atomsperleaf in (2, 4, 8) and best.resort_every in (1, 5, 10)
     assert best.stage_policy in (0, 1) and best.union_search in (0, 1) and sps > 0
-    assert abs(best.skin - p.skin) < 0.25 and best.skin >= p.skin
+    # skin candidates: the given one -0.2 .. +0.2 in steps of 0.1, not below 0.1
+    assert abs(best.skin - p.skin) < 0.25 and best.skin >= max(0.1, p.skin - 0.2) - 1e-9
     assert best.cutoff == p.cutoff and best.rebuild_every == p.rebuild_every
     e = _ensemble(nd, nsys=16, nmax=1024)
     t = _table(nd, e)
