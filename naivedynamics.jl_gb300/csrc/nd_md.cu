@@ -1314,8 +1314,8 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
             // groups of four neighbours; the next group's indices are loaded
             // while the current group is computed
             const PairK2 pk2c(pk);
-            uint64_t fx2 = 0, fy2 = 0, fz2 = 0;  // packed (0.0f, 0.0f)
-            float gx = 0.f, gy = 0.f, gz = 0.f;  // measure pass: the odd entries
+            [[maybe_unused]] uint64_t fx2 = 0, fy2 = 0, fz2 = 0;  // packed (0.0f, 0.0f)
+            [[maybe_unused]] float gx = 0.f, gy = 0.f, gz = 0.f;  // measure pass: odd entries
             int32_t s = 0;
             int32_t li[4];
             if (nf >= 4) {
