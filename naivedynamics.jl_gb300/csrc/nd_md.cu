@@ -1184,7 +1184,7 @@ __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, 
 // TPA: threads per atom.  With TPA > 1 (small systems, whose grid is under a
 // couple of waves) thread p of an atom sums list entries p, p + TPA, ... and
 // the slices are added in a fixed order before the atom's update.
-template <bool COUL, bool MASS, bool FIRST, int MODE, bool BATCH, int TPA = 1>
+template <bool COUL, int MODE, bool BATCH, int TPA = 1>
 __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(StepArgs a) {
     extern __shared__ int4 srec[];
     const int tid = threadIdx.x & (kBlock - 1);  // the atom within the block
@@ -1433,6 +1433,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     else
         pairs(std::false_type{});
     if (valid && own) a.f_out[i] = make_float4(fx, fy, fz, 0.f);
+    const bool MASS = a.has_mass != 0, FIRST = a.first != 0;
     const double imv = MASS ? a.im[i] : 1.0;
     const float fv[3] = {fx, fy, fz};
     if constexpr (MODE == 1) {
@@ -1713,34 +1714,14 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<8>, maxsm);
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<16>, maxsm);
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_block_lists<32>, maxsm);
-#define ND_SMEM(C, M, F, MODE)                                                                \
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false>, maxsm); \
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, true>, maxsm);
-    ND_SMEM(true, true, true, 0) ND_SMEM(true, true, false, 0) ND_SMEM(true, false, true, 0)
-    ND_SMEM(true, false, false, 0) ND_SMEM(false, true, true, 0)
-    ND_SMEM(false, true, false, 0) ND_SMEM(false, false, true, 0)
-    ND_SMEM(false, false, false, 0) ND_SMEM(true, true, true, 1)
-    ND_SMEM(true, true, false, 1) ND_SMEM(true, false, true, 1)
-    ND_SMEM(true, false, false, 1) ND_SMEM(false, true, true, 1)
-    ND_SMEM(false, true, false, 1) ND_SMEM(false, false, true, 1)
-    ND_SMEM(false, false, false, 1) ND_SMEM(true, true, true, 2)
-    ND_SMEM(true, true, false, 2) ND_SMEM(true, false, true, 2)
-    ND_SMEM(true, false, false, 2) ND_SMEM(false, true, true, 2)
-    ND_SMEM(false, true, false, 2) ND_SMEM(false, false, true, 2)
-    ND_SMEM(false, false, false, 2)
-#undef ND_SMEM
-#define ND_SMEM(C, M, F, MODE) \
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false, kSmallTPA>, maxsm); \
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, M, F, MODE, false, 2>, maxsm);
-    ND_SMEM(true, true, true, 0) ND_SMEM(true, true, false, 0) ND_SMEM(true, false, true, 0)
-    ND_SMEM(true, false, false, 0) ND_SMEM(false, true, true, 0) ND_SMEM(false, true, false, 0)
-    ND_SMEM(false, false, true, 0) ND_SMEM(false, false, false, 0)
-    ND_SMEM(true, true, true, 1) ND_SMEM(true, true, false, 1) ND_SMEM(true, false, true, 1)
-    ND_SMEM(true, false, false, 1) ND_SMEM(false, true, true, 1) ND_SMEM(false, true, false, 1)
-    ND_SMEM(false, false, true, 1) ND_SMEM(false, false, false, 1)
-    ND_SMEM(true, true, true, 2) ND_SMEM(true, true, false, 2) ND_SMEM(true, false, true, 2)
-    ND_SMEM(true, false, false, 2) ND_SMEM(false, true, true, 2) ND_SMEM(false, true, false, 2)
-    ND_SMEM(false, false, true, 2) ND_SMEM(false, false, false, 2)
+#define ND_SMEM(C, MODE)                                                                        \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, MODE, false>, maxsm);   \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, MODE, true>, maxsm);    \
+    if (e == cudaSuccess)                                                                       \
+        e = raise_smem_limit((const void*)k_md_step<C, MODE, false, kSmallTPA>, maxsm);         \
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, MODE, false, 2>, maxsm);
+    ND_SMEM(true, 0) ND_SMEM(false, 0) ND_SMEM(true, 1) ND_SMEM(false, 1) ND_SMEM(true, 2)
+    ND_SMEM(false, 2)
 #undef ND_SMEM
     if (e != cudaSuccess) return cuda_fail(c, e, "shared memory opt-in");
     return ND_OK;
@@ -1815,60 +1796,23 @@ StepArgs md_step_args(MDEngine* m, int rec_in) {
 }
 
 template <int MODE>
-static void launch_step_impl(MDEngine* m, const StepArgs& a, bool first) {
+static void launch_step_impl(MDEngine* m, const StepArgs& a0, bool first) {
     Ctx* c = &m->sub;
     const unsigned grid = (unsigned)m->nblocks;
     const size_t sm = m->step_smem;
     const bool coul = m->has_q && m->p.coulomb_k != 0.0;
-    const bool mass = m->has_m;
-    if (m->nsys > 0) {
-#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE, true><<<grid, kBlock, sm, c->stream>>>(a)
-        if (coul) {
-            if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
-            else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
-        } else {
-            if (mass) { if (first) ND_STEP(false, true, true); else ND_STEP(false, true, false); }
-            else { if (first) ND_STEP(false, false, true); else ND_STEP(false, false, false); }
-        }
-#undef ND_STEP
-        c->launches++;
-        return;
-    }
-    if (m->tpa == kSmallTPA) {
-#define ND_STEP(C, M, F) \
-    k_md_step<C, M, F, MODE, false, kSmallTPA><<<grid, kBlock * kSmallTPA, sm, c->stream>>>(a)
-        if (coul) {
-            if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
-            else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
-        } else {
-            if (mass) { if (first) ND_STEP(false, true, true); else ND_STEP(false, true, false); }
-            else { if (first) ND_STEP(false, false, true); else ND_STEP(false, false, false); }
-        }
-#undef ND_STEP
-        c->launches++;
-        return;
-    }
-    if (m->tpa == 2) {
-#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE, false, 2><<<grid, kBlock * 2, sm, c->stream>>>(a)
-        if (coul) {
-            if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
-            else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
-        } else {
-            if (mass) { if (first) ND_STEP(false, true, true); else ND_STEP(false, true, false); }
-            else { if (first) ND_STEP(false, false, true); else ND_STEP(false, false, false); }
-        }
-#undef ND_STEP
-        c->launches++;
-        return;
-    }
-#define ND_STEP(C, M, F) k_md_step<C, M, F, MODE, false><<<grid, kBlock, sm, c->stream>>>(a)
-    if (coul) {
-        if (mass) { if (first) ND_STEP(true, true, true); else ND_STEP(true, true, false); }
-        else { if (first) ND_STEP(true, false, true); else ND_STEP(true, false, false); }
-    } else {
-        if (mass) { if (first) ND_STEP(false, true, true); else ND_STEP(false, true, false); }
-        else { if (first) ND_STEP(false, false, true); else ND_STEP(false, false, false); }
-    }
+    StepArgs a = a0;
+    a.first = first ? 1 : 0;
+    a.has_mass = m->has_m ? 1 : 0;
+#define ND_STEP(BATCH, TPA)                                                                     \
+    do {                                                                                        \
+        if (coul) k_md_step<true, MODE, BATCH, TPA><<<grid, kBlock * TPA, sm, c->stream>>>(a);  \
+        else k_md_step<false, MODE, BATCH, TPA><<<grid, kBlock * TPA, sm, c->stream>>>(a);      \
+    } while (0)
+    if (m->nsys > 0) ND_STEP(true, 1);
+    else if (m->tpa == kSmallTPA) ND_STEP(false, kSmallTPA);
+    else if (m->tpa == 2) ND_STEP(false, 2);
+    else ND_STEP(false, 1);
 #undef ND_STEP
     c->launches++;
 }

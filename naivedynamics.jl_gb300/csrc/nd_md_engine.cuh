@@ -96,6 +96,8 @@ __device__ __forceinline__ uint2 pack_fine(uint32_t fx, uint32_t fy, uint32_t fz
 
 struct StepArgs {
     int32_t n, apl, ucap, lcap;
+    int32_t first;     // the first step after an upload (a half kick only)
+    int32_t has_mass;  // im holds inverse masses (else all masses are 1)
     int32_t smrec;  // union records staged in shared memory (the rest read from global)
     const int32_t* __restrict__ ulist;
     const int32_t* __restrict__ ucount;
