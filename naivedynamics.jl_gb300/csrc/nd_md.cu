@@ -1143,8 +1143,9 @@ __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, 
         m |= accum_pair<COUL, false>(ri, rb, k1, sx, sy, sz, ue) ? 2u : 0u;
         return m;
     }
+    // no early return when both lie beyond the cutoff: the zeroed terms cost
+    // less than the divergent branch
     const bool ina = r2a < k1.rc2u, inb = r2b < k1.rc2u;
-    if (!(ina | inb)) return 0u;
     uint64_t inv_r = 0, inv_r2;
     if (COUL) {
         inv_r = pk2(rsqrtf(r2a), rsqrtf(r2b));
