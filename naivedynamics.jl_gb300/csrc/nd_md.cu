@@ -1179,7 +1179,9 @@ __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, 
 // drift, reflect, next record).  MODE 2: the same step inside a captured
 // window, whose last block also sets the early-refit condition of the graph
 // node after it.  MODE 1: measure (force, integer-step velocity and
-// energies; state untouched).
+// energies; state untouched).  MODE 3: measure without the potential energy
+// (forces and velocities for a read-back or a thermostat: the double-precision
+// pair energies are most of a measure pass's time).
 // BATCH: atoms of several systems; pair constants, walls and the fixed-point
 // origin come from the atom's system (a pair never crosses systems).
 // TPA: threads per atom.  With TPA > 1 (small systems, whose grid is under a
@@ -1188,6 +1190,8 @@ __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, 
 template <bool COUL, int MODE, bool BATCH, int TPA = 1>
 __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(StepArgs a) {
     extern __shared__ int4 srec[];
+    // MODE 1 and 3 measure (3: without the potential energy)
+    constexpr bool MEASURE = MODE == 1 || MODE == 3;
     const int tid = threadIdx.x & (kBlock - 1);  // the atom within the block
     const int part = threadIdx.x / kBlock;       // its list slice
     int64_t i = (int64_t)blockIdx.x * kBlock + tid;
@@ -1278,7 +1282,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
         auto fine = [&](int32_t li) -> uint2 {
             return __ldg(&a.recf_in[((int64_t)__ldg(&U[li >> lsh]) << lsh) + (li & emask)]);
         };
-        if constexpr (MODE == 1 || BATCH) {
+        if constexpr (MEASURE || BATCH) {
             // near entries of this thread's slice, the next index loaded ahead
             // (the measure pass, and ensembles, whose per-system constants leave
             // no registers for the packed form)
@@ -1331,13 +1335,13 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
 #pragma unroll
                     for (int k = 0; k < 4; ++k) li[k] = LF[-(int64_t)(s + 4 + k) * kBlock];
                 }
-                if constexpr (MODE == 1) {
+                if constexpr (MEASURE) {
                     // even entries into (fx, fy, fz), odd ones into (gx, gy, gz),
                     // as the two halves of the packed form
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        const bool nr = (k & 1) ? accum_pair<COUL, true>(ri, rj[k], pk, gx, gy, gz, ue)
-                                                : accum_pair<COUL, true>(ri, rj[k], pk, fx, fy, fz, ue);
+                        const bool nr = (k & 1) ? accum_pair<COUL, MODE == 1>(ri, rj[k], pk, gx, gy, gz, ue)
+                                                : accum_pair<COUL, MODE == 1>(ri, rj[k], pk, fx, fy, fz, ue);
                         if (nr) far_near(s + k);
                     }
                 } else {
@@ -1353,7 +1357,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
                     }
                 }
             }
-            if constexpr (MODE != 1) {
+            if constexpr (!MEASURE) {
                 float a, b;
                 upk2(fx2, a, b); fx += a + b;
                 upk2(fy2, a, b); fy += a + b;
@@ -1437,7 +1441,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     const bool MASS = a.has_mass != 0, FIRST = a.first != 0;
     const double imv = MASS ? a.im[i] : 1.0;
     const float fv[3] = {fx, fy, fz};
-    if constexpr (MODE == 1) {
+    if constexpr (MEASURE) {
         double ke = 0.0;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -1722,7 +1726,7 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
         e = raise_smem_limit((const void*)k_md_step<C, MODE, false, kSmallTPA>, maxsm);         \
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, MODE, false, 2>, maxsm);
     ND_SMEM(true, 0) ND_SMEM(false, 0) ND_SMEM(true, 1) ND_SMEM(false, 1) ND_SMEM(true, 2)
-    ND_SMEM(false, 2)
+    ND_SMEM(false, 2) ND_SMEM(true, 3) ND_SMEM(false, 3)
 #undef ND_SMEM
     if (e != cudaSuccess) return cuda_fail(c, e, "shared memory opt-in");
     return ND_OK;
@@ -2059,7 +2063,7 @@ static nd_status md_thermo_body(MDEngine* m) {
     Ctx* c = &m->sub;
     const unsigned g = (unsigned)cdiv(m->n, 256);
     StepArgs a = md_step_args(m, m->rc);
-    launch_step<1>(m, a, false);  // integer-step velocities and forces
+    launch_step<3>(m, a, false);  // integer-step velocities and forces
     const double* vt = (const double*)m->vtmp.p;
     SetPtrs& s = m->set[0];
     k_md_thermo_part<<<g, 256, 0, c->stream>>>(vt, s.im, m->n, (double*)m->obs_part.p);
@@ -2753,17 +2757,18 @@ nd_status md_step_times(MDEngine* m, int32_t steps, float* ms) {
     return st;
 }
 
-nd_status md_measure(MDEngine* m) {
+nd_status md_measure(MDEngine* m, bool energy) {
     Ctx* c = &m->sub;
     cudaMemsetAsync(m->acc.p, 0, 2 * sizeof(double) * (size_t)std::max(m->nsys, 1), c->stream);
     StepArgs a = md_step_args(m, m->rc);
-    launch_step<1>(m, a, m->first);
+    if (energy) launch_step<1>(m, a, m->first);
+    else launch_step<3>(m, a, m->first);
     return check_launch(c, "md measure");
 }
 
 nd_status md_get(MDEngine* m, double* x, double* v, float* f, bool host) {
     Ctx* c = &m->sub;
-    nd_status st = md_measure(m);
+    nd_status st = md_measure(m, false);
     if (st) return st;
     const size_t bytes = 3 * sizeof(double) * (size_t)m->n;
     double *dx = nullptr, *dv = nullptr;
@@ -2798,7 +2803,7 @@ nd_status md_get(MDEngine* m, double* x, double* v, float* f, bool host) {
 
 nd_status md_energy(MDEngine* m, double* pot, double* kin) {
     Ctx* c = &m->sub;
-    nd_status st = md_measure(m);
+    nd_status st = md_measure(m, true);
     if (st) return st;
     const int32_t ns = std::max(m->nsys, 1);
     std::vector<double> h(2 * (size_t)ns);
@@ -2818,7 +2823,7 @@ nd_status md_energy(MDEngine* m, double* pot, double* kin) {
 nd_status md_energies(MDEngine* m, double* pot, double* kin) {
     Ctx* c = &m->sub;
     if (m->nsys <= 0) return ND_ERR_ARG;
-    nd_status st = md_measure(m);
+    nd_status st = md_measure(m, true);
     if (st) return st;
     std::vector<double> h(2 * (size_t)m->nsys);
     cudaError_t e = cudaMemcpyAsync(h.data(), m->acc.p, sizeof(double) * h.size(),
