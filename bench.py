@@ -466,7 +466,7 @@ def plain_leg(nd, ctx, ext, flush):
                      "resort_every": p.resort_every, "stage_policy": p.stage_policy,
                      "union_search": UNION_NAMES[p.union_search],
                      "refit_check_every": max(p.refit_check_every, 1),
-                     "threads_per_atom": p.threads_per_atom,
+                     "threads_per_atom": p.threads_per_atom, "cta_split": p.cta_split,
                      "autotune_s": round(tune_s, 3), "autotune_from_cache": tune_cached,
                      "second_call_s": round(again_s, 4),
                      "second_call_from_cache": again_cached},

@@ -113,7 +113,10 @@ typedef struct {
     int32_t threads_per_atom; /* threads sharing one atom's neighbour list in the step
                               kernel: 1, 2 or 4; 0 = 4 for a single system whose blocks of
                               256 atoms are fewer than two per SM, else 1 (ensembles: 1) */
-    int32_t reserved;      /* 0 */
+    int32_t cta_split;     /* thread blocks of the step kernel per block of 256 atoms with
+                              4 threads per atom: 1, 2 or 4 (blocks of 1024, 512 or 256
+                              threads, for small systems: more SMs busy); 0 = 1; ignored
+                              with fewer threads per atom and for ensembles */
 } nd_md_params;
 
 #define ND_UNION_BLOCKS 0
@@ -522,8 +525,9 @@ nd_status nd_batch_energies(nd_md* md, double* potential, double* kinetic);
  * into *best (skin -- p->skin - 0.2 to p->skin + 0.2 in steps of 0.1, not below
  * 0.1 --, atomsperleaf -- the leaf/traversal width --, resort_every,
  * stage_policy, union_search, refit_check_every -- 1, 2 or 3 -- and, for a
- * plain engine, threads_per_atom -- 1, 2 or 4; every other field copied from
- * *p), tuning one setting at a time.  nsys == 0 tunes a plain engine (sys ignored).  Candidates
+ * plain engine, threads_per_atom -- 1, 2 or 4 -- and cta_split -- 1, 2 or 4 with
+ * 4 threads per atom; every other field copied from *p), tuning one setting at
+ * a time.  nsys == 0 tunes a plain engine (sys ignored).  Candidates
  * change only the summation order of the forces and the steps at which early
  * refits may run, not which pairs interact.  trial_steps: timed steps per candidate
  * (rounded up to whole rebuild windows).  seconds_per_step (may be NULL)

@@ -1187,26 +1187,30 @@ __device__ __forceinline__ unsigned accum_pair2(const int4& ri, const int4& ra, 
 // TPA: threads per atom.  With TPA > 1 (small systems, whose grid is under a
 // couple of waves) thread p of an atom sums list entries p, p + TPA, ... and
 // the slices are added in a fixed order before the atom's update.
-template <bool COUL, int MODE, bool BATCH, int TPA = 1>
-__global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(StepArgs a) {
+template <bool COUL, int MODE, bool BATCH, int TPA = 1, int SPLIT = 1>
+__global__ void __launch_bounds__(kBlock * TPA / SPLIT, TPA == 1 ? 4 : 1) k_md_step(StepArgs a) {
     extern __shared__ int4 srec[];
     // MODE 1 and 3 measure (3: without the potential energy)
     constexpr bool MEASURE = MODE == 1 || MODE == 3;
-    const int tid = threadIdx.x & (kBlock - 1);  // the atom within the block
-    const int part = threadIdx.x / kBlock;       // its list slice
-    int64_t i = (int64_t)blockIdx.x * kBlock + tid;
+    // SPLIT thread blocks share a block of kBlock atoms (and its lists), each
+    // taking kBlock / SPLIT of them
+    constexpr int APB = kBlock / SPLIT;
+    const int32_t blk = (int32_t)(blockIdx.x / SPLIT);
+    const int tid = (int)(blockIdx.x % SPLIT) * APB + (int)(threadIdx.x & (APB - 1));  // the atom
+    const int part = threadIdx.x / APB;  // its list slice
+    int64_t i = (int64_t)blk * kBlock + tid;
     const bool valid = i < a.n;
     const bool own = part == 0;  // the thread that updates the atom
-    const int32_t* __restrict__ U = a.ulist + (int64_t)blockIdx.x * a.ucap;
+    const int32_t* __restrict__ U = a.ulist + (int64_t)blk * a.ucap;
     // stage the block's union: record of atom (leaf * apl + e) at u * apl + e,
     // up to the shared-memory capacity; larger unions read the rest from L2
     {
         // four records per thread in flight: their leaf indices, then the
         // records (apl is a power of two)
-        const int32_t nu = min(__ldg(&a.ucount[blockIdx.x]), a.ucap);
+        const int32_t nu = min(__ldg(&a.ucount[blk]), a.ucap);
         const int32_t m = min(nu * a.apl, a.smrec);
         const int32_t lsh = __ffs(a.apl) - 1, emask = a.apl - 1;
-        constexpr int32_t NT = kBlock * TPA;
+        constexpr int32_t NT = APB * TPA;
         for (int32_t k = threadIdx.x; k < m; k += 4 * NT) {
             int32_t lf[4];
 #pragma unroll
@@ -1260,7 +1264,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
     // near entries (slots 0, 1, ...) and the others (slots lcap - 1, lcap - 2, ...)
     const int32_t cpk = valid ? __ldg(&a.ncount[i]) : 0;
     const int32_t nn = list_near(cpk), nf = cpk >> 16;
-    const uint16_t* __restrict__ L = a.llist + (int64_t)blockIdx.x * a.lcap * kBlock + tid;
+    const uint16_t* __restrict__ L = a.llist + (int64_t)blk * a.lcap * kBlock + tid;
     const uint16_t* __restrict__ LF = L + (int64_t)(a.lcap - 1) * kBlock;
     const int32_t lsh = __ffs(a.apl) - 1, emask = a.apl - 1;
     const uint2 fi = __ldg(&a.recf_in[i]);
@@ -1433,7 +1437,7 @@ __global__ void __launch_bounds__(kBlock * TPA, TPA == 1 ? 4 : 1) k_md_step(Step
             fz = __fadd_rn(nacc.zh, nacc.zl);
         }
     };
-    if (min(__ldg(&a.ucount[blockIdx.x]), a.ucap) * a.apl <= a.smrec)
+    if (min(__ldg(&a.ucount[blk]), a.ucap) * a.apl <= a.smrec)
         pairs(std::true_type{});
     else
         pairs(std::false_type{});
@@ -1703,6 +1707,7 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
         if (m->nsys > 0) m->tpa = 1;
         else if (req > 0) m->tpa = fits(req) ? req : 1;
         else m->tpa = (m->nblocks < 2 * nsm && fits(kSmallTPA)) ? kSmallTPA : 1;
+        m->split = (m->tpa == kSmallTPA && m->p.cta_split > 0) ? m->p.cta_split : 1;
     }
     if ((int)m->union_smem + 1024 > maxsm || (lcap > 0 && (int)m->step_smem + 1024 > maxsm)) {
         c->last_error = "neighbour union too large for shared memory";
@@ -1724,7 +1729,11 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
     if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, MODE, true>, maxsm);    \
     if (e == cudaSuccess)                                                                       \
         e = raise_smem_limit((const void*)k_md_step<C, MODE, false, kSmallTPA>, maxsm);         \
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, MODE, false, 2>, maxsm);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_md_step<C, MODE, false, 2>, maxsm);  \
+    if (e == cudaSuccess)                                                                       \
+        e = raise_smem_limit((const void*)k_md_step<C, MODE, false, kSmallTPA, 2>, maxsm);      \
+    if (e == cudaSuccess)                                                                       \
+        e = raise_smem_limit((const void*)k_md_step<C, MODE, false, kSmallTPA, 4>, maxsm);
     ND_SMEM(true, 0) ND_SMEM(false, 0) ND_SMEM(true, 1) ND_SMEM(false, 1) ND_SMEM(true, 2)
     ND_SMEM(false, 2) ND_SMEM(true, 3) ND_SMEM(false, 3)
 #undef ND_SMEM
@@ -1809,15 +1818,18 @@ static void launch_step_impl(MDEngine* m, const StepArgs& a0, bool first) {
     StepArgs a = a0;
     a.first = first ? 1 : 0;
     a.has_mass = m->has_m ? 1 : 0;
-#define ND_STEP(BATCH, TPA)                                                                     \
+#define ND_STEP(BATCH, TPA, SPLIT)                                                              \
     do {                                                                                        \
-        if (coul) k_md_step<true, MODE, BATCH, TPA><<<grid, kBlock * TPA, sm, c->stream>>>(a);  \
-        else k_md_step<false, MODE, BATCH, TPA><<<grid, kBlock * TPA, sm, c->stream>>>(a);      \
+        const unsigned gs = grid * SPLIT, bs = kBlock * TPA / SPLIT;                            \
+        if (coul) k_md_step<true, MODE, BATCH, TPA, SPLIT><<<gs, bs, sm, c->stream>>>(a);       \
+        else k_md_step<false, MODE, BATCH, TPA, SPLIT><<<gs, bs, sm, c->stream>>>(a);           \
     } while (0)
-    if (m->nsys > 0) ND_STEP(true, 1);
-    else if (m->tpa == kSmallTPA) ND_STEP(false, kSmallTPA);
-    else if (m->tpa == 2) ND_STEP(false, 2);
-    else ND_STEP(false, 1);
+    if (m->nsys > 0) ND_STEP(true, 1, 1);
+    else if (m->tpa == kSmallTPA && m->split == 4) ND_STEP(false, kSmallTPA, 4);
+    else if (m->tpa == kSmallTPA && m->split == 2) ND_STEP(false, kSmallTPA, 2);
+    else if (m->tpa == kSmallTPA) ND_STEP(false, kSmallTPA, 1);
+    else if (m->tpa == 2) ND_STEP(false, 2, 1);
+    else ND_STEP(false, 1, 1);
 #undef ND_STEP
     c->launches++;
 }
@@ -2448,7 +2460,8 @@ static nd_status md_create_common(Ctx* parent, const nd_md_params* p, int32_t n,
         (p->union_search != ND_UNION_BLOCKS && p->union_search != ND_UNION_TREE) ||
         p->refit_check_every < 0 ||
         (p->threads_per_atom != 0 && p->threads_per_atom != 1 && p->threads_per_atom != 2 &&
-         p->threads_per_atom != kSmallTPA))
+         p->threads_per_atom != kSmallTPA) ||
+        (p->cta_split != 0 && p->cta_split != 1 && p->cta_split != 2 && p->cta_split != 4))
         return ND_ERR_ARG;
     if (nsys < 0 || (nsys > 0 && !sys)) return ND_ERR_ARG;
     if (nsys > 0) {
@@ -2525,7 +2538,8 @@ nd_status md_create_batch(Ctx* parent, const nd_md_params* p, int32_t nsys, cons
 // 0.1, not below kMinTunedSkin: a longer list against fewer early refits),
 // atoms per leaf (the leaf and traversal width), re-sort interval,
 // shared-memory staging policy, union search, early-refit check interval,
-// threads per atom (single systems).  Candidates that do not fit
+// threads per atom and thread blocks per block of atoms (single systems).
+// Candidates that do not fit
 // (shared memory, leaf size not dividing every system) are skipped.
 nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsys,
                       const nd_system* sys, const double* x, const double* v, const double* q,
@@ -2632,9 +2646,21 @@ nd_status md_autotune(Ctx* parent, const nd_md_params* p, int32_t n, int32_t nsy
             for (int32_t t : {1, 2, kSmallTPA}) {
                 c = s6;
                 c.threads_per_atom = t;
+                c.cta_split = 1;
                 double tt = -1.0;
                 if ((result = trial(c, &tt))) goto done;
                 if (tt > 0.0 && (tbest < 0.0 || tt < tbest)) { tbest = tt; win = c; }
+            }
+            // with 4 threads per atom, the thread blocks per block of atoms
+            if (win.threads_per_atom == kSmallTPA) {
+                const nd_md_params s7 = win;
+                for (int32_t sp : {2, 4}) {
+                    c = s7;
+                    c.cta_split = sp;
+                    double tt = -1.0;
+                    if ((result = trial(c, &tt))) goto done;
+                    if (tt > 0.0 && (tbest < 0.0 || tt < tbest)) { tbest = tt; win = c; }
+                }
             }
             if (tbest > 0.0) best_t = tbest;
         }

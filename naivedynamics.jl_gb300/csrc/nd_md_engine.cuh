@@ -187,6 +187,7 @@ struct MDEngine {
     int64_t eager_bodies = 0;         // kernels of rebuild bodies run eagerly (counted by the host)
     size_t step_smem = 0, union_smem = 0, lists_smem = 0;
     int32_t lists_smpos = 0;  // positions the list kernel stages in shared memory
+    int32_t split = 1;  // thread blocks of the step kernel per block of kBlock atoms
     int32_t tpa = 1;  // threads per atom of the step kernel
     // observers of the step loop: thermostat (rescale_velocity!) and position log
     double thermo_T = 0.0, thermo_gamma = 0.0;

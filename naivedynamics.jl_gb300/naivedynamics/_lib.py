@@ -73,7 +73,7 @@ class MDParams(ctypes.Structure):
                 ("order", ctypes.c_int32), ("max_neighbors", ctypes.c_int32),
                 ("resort_every", ctypes.c_int32), ("stage_policy", ctypes.c_int32),
                 ("union_search", ctypes.c_int32), ("refit_check_every", ctypes.c_int32),
-                ("threads_per_atom", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("threads_per_atom", ctypes.c_int32), ("cta_split", ctypes.c_int32)]
 
 
 class CompatSim(ctypes.Structure):

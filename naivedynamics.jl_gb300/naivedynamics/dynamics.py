@@ -46,7 +46,7 @@ def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e
               box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), atomsperleaf=4, rebuild_every=10,
               order=ND_ORDER_SPATIAL, max_neighbors=0, resort_every=0,
               stage_policy=0, union_search=ND_UNION_BLOCKS, refit_check_every=1,
-              threads_per_atom=0) -> MDParams:
+              threads_per_atom=0, cta_split=0) -> MDParams:
     p = MDParams()
     p.sigma, p.epsilon, p.coulomb_k, p.cutoff, p.skin, p.dt = (float(sigma), float(epsilon),
                                                                float(coulomb_k), float(cutoff),
@@ -59,7 +59,7 @@ def md_params(sigma=1.0, epsilon=1.0, coulomb_k=0.0, cutoff=2.5, skin=0.3, dt=1e
                                                                  int(max_neighbors))
     p.resort_every, p.stage_policy = int(resort_every), int(stage_policy)
     p.union_search, p.refit_check_every = int(union_search), int(refit_check_every)
-    p.threads_per_atom = int(threads_per_atom)
+    p.threads_per_atom, p.cta_split = int(threads_per_atom), int(cta_split)
     return p
 
 
@@ -541,7 +541,7 @@ class Ensemble(MDEngine):
 
 
 TUNED_FIELDS = ("skin", "atomsperleaf", "resort_every", "stage_policy", "union_search",
-                "refit_check_every", "threads_per_atom")
+                "refit_check_every", "threads_per_atom", "cta_split")
 
 
 def autotune_cache_path() -> str:
@@ -552,7 +552,7 @@ def autotune_cache_path() -> str:
 
 
 # the tuner's candidate set: a cached result from another set is not reused
-TUNER_VERSION = 2
+TUNER_VERSION = 3
 
 
 def _tune_key(ctx, params: MDParams, n: int, systems, has_q: bool, has_m: bool) -> str:
@@ -562,7 +562,7 @@ def _tune_key(ctx, params: MDParams, n: int, systems, has_q: bool, has_m: bool) 
     epsilons and walls."""
     fixed = {name: (list(getattr(params, name)) if name in ("box_lo", "box_hi")
                     else getattr(params, name))
-             for name, _ in params._fields_ if name not in TUNED_FIELDS and name != "reserved"}
+             for name, _ in params._fields_ if name not in TUNED_FIELDS}
     if systems is None:
         vol = float(np.prod(np.asarray(params.box_hi) - np.asarray(params.box_lo)))
         shape = {"n": n, "density": float(f"{n / vol:.4g}")}
@@ -579,7 +579,7 @@ def _tune_key(ctx, params: MDParams, n: int, systems, has_q: bool, has_m: bool) 
 def autotune(params: MDParams, x, v, q=None, m=None, systems=None, trial_steps=20, ctx=None,
              use_cache=True):
     """nd_md_autotune: the fastest (skin, atomsperleaf, resort_every,
-    stage_policy, union_search, refit_check_every, threads_per_atom) for this
+    stage_policy, union_search, refit_check_every, threads_per_atom, cta_split) for this
     state, as a new MDParams, and its time per MD step in seconds.
     systems=None tunes a plain engine.  With use_cache, the result is kept in
     a JSON file (autotune_cache_path()) keyed by device, atom count, density

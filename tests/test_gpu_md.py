@@ -333,6 +333,27 @@ def test_md_graph_equals_eager_and_deterministic(nd):
     assert np.array_equal(xa, xc) and np.array_equal(va, vc)
 
 
+@pytest.mark.parametrize("split", [2, 4])
+def test_md_cta_split_same_bits(nd, split):
+    """Four threads per atom with each block of 256 atoms spread over 2 or 4
+    thread blocks: every atom sums the same slices in the same order, so
+    positions, velocities and forces equal the unsplit engine's bit for bit
+    (through rebuild windows, graphs and the measure pass)."""
+    x0, v0, q = _config1(nd, charges=True, n=4096, side=17.0)
+    a = nd.MDEngine(_params(nd, 17.0, coulomb=1.0, threads_per_atom=4, cta_split=1), x0, v0, q)
+    a.run(35)
+    xa, va, fa = a.get()
+    pa, ka = a.energy()
+    b = nd.MDEngine(_params(nd, 17.0, coulomb=1.0, threads_per_atom=4, cta_split=split),
+                    x0, v0, q)
+    b.run(35)
+    xb, vb, fb = b.get()
+    pb, kb = b.energy()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+    # energies are summed with atomics (any order): equal to rounding
+    assert abs(pa - pb) <= 1e-12 * abs(pa) and abs(ka - kb) <= 1e-12 * abs(ka)
+
+
 def test_md_reference_order_matches_spatial(nd):
     # The order mode changes only the atom order, not the physics.
     x0, v0, _ = _config1(nd, n=2048, side=13.5)
