@@ -115,8 +115,9 @@ typedef struct {
                               256 atoms are fewer than two per SM, else 1 (ensembles: 1) */
     int32_t cta_split;     /* thread blocks of the step kernel per block of 256 atoms with
                               4 threads per atom: 1, 2 or 4 (blocks of 1024, 512 or 256
-                              threads, for small systems: more SMs busy); 0 = 1; ignored
-                              with fewer threads per atom and for ensembles */
+                              threads, for small systems: more SMs busy); 0 = the most that
+                              keep the grid within one thread block per SM; ignored with
+                              fewer threads per atom and for ensembles */
 } nd_md_params;
 
 #define ND_UNION_BLOCKS 0

@@ -1707,7 +1707,15 @@ static nd_status md_alloc_lists(MDEngine* m, int32_t fcap, int32_t ucap, int32_t
         if (m->nsys > 0) m->tpa = 1;
         else if (req > 0) m->tpa = fits(req) ? req : 1;
         else m->tpa = (m->nblocks < 2 * nsm && fits(kSmallTPA)) ? kSmallTPA : 1;
-        m->split = (m->tpa == kSmallTPA && m->p.cta_split > 0) ? m->p.cta_split : 1;
+        // thread blocks per block of atoms with 4 threads per atom: the given
+        // number, or (0) the most that keep the grid within one block per SM
+        // (32,768 atoms: 128 blocks of 1,024 threads ran faster than 256 of 512)
+        m->split = 1;
+        if (m->tpa == kSmallTPA) {
+            if (m->p.cta_split > 0) m->split = m->p.cta_split;
+            else if (4 * m->nblocks <= nsm) m->split = 4;
+            else if (2 * m->nblocks <= nsm) m->split = 2;
+        }
     }
     if ((int)m->union_smem + 1024 > maxsm || (lcap > 0 && (int)m->step_smem + 1024 > maxsm)) {
         c->last_error = "neighbour union too large for shared memory";
