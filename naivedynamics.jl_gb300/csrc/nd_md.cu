@@ -976,13 +976,25 @@ __device__ __forceinline__ bool accum_pair(const int4& ri, const int4& rj, const
             // bias of a fraction of an ulp, which ten million pairs add up)
             const double xd = (double)idiff(ri.x, rj.x), yd = (double)idiff(ri.y, rj.y),
                          zd = (double)idiff(ri.z, rj.z);
+            // 1/r^2 and 1/r by two Newton-Raphson steps each in double
+            // precision (y <- y (2 - r^2 y), y <- y (3 - r^2 y^2) / 2) from the
+            // single-precision reciprocal and reciprocal square root: a double
+            // division or square root costs several times more on GB300's FP64
+            // pipe, and these terms run for every pair of the pass
             const double r2d = xd * xd + yd * yd + zd * zd;
-            const double s2d = ((double)a.sig2u + (double)a.sig2lo) / r2d;
+            double ir2d = (double)__frcp_rn((float)r2d);
+            ir2d = ir2d * (2.0 - r2d * ir2d);
+            ir2d = ir2d * (2.0 - r2d * ir2d);
+            const double s2d = ((double)a.sig2u + (double)a.sig2lo) * ir2d;
             const double s6d = s2d * s2d * s2d;
             double ud = (double)a.eps4 * s6d * (s6d - 1.0);
-            if (COUL)
-                ud += (double)a.kceu * ((double)__int_as_float(ri.w) * (double)__int_as_float(rj.w)) /
-                      sqrt(r2d);
+            if (COUL) {
+                double ird = (double)rsqrtf((float)r2d);
+                ird = ird * (1.5 - 0.5 * r2d * ird * ird);
+                ird = ird * (1.5 - 0.5 * r2d * ird * ird);
+                ud += (double)a.kceu * ((double)__int_as_float(ri.w) * (double)__int_as_float(rj.w)) *
+                      ird;
+            }
             ue += ud;
         }
     }
